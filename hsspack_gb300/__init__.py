@@ -1,0 +1,261 @@
+"""hsspack_gb300 -- GB300 (sm_103a) HSS-accelerated divide-and-conquer eigensolver.
+
+Python mirror of HSSPACK's Fortran interface for the DC merge path, over the
+C ABI of ``_lib/libhsspack_gb300.so`` (declared in include/hsspack_gb300.h).
+The compute runs in hand-written CUDA kernels; there is no CPU fallback: if the
+library cannot be loaded every entry point raises.
+
+Host-array entry points follow the Fortran argument meaning and LAPACK error
+convention (INFO = -i for a bad i-th argument, INFO > 0 for a numerical
+failure):
+
+* :func:`mdstedc` -- ``MDSTEDC(COMPZ,N,D,E,Z,LDZ,WORK,LWORK,IWORK,LIWORK,INFO)``
+  (SRC/mdstedc.f90:139).
+* :func:`cauchylike` -- ``Cauchylike(A,D,F,u,v,M,N)`` (SRC/Cauchylike.f90:1).
+
+Device entry points take torch CUDA tensors (torch is used only to hold device
+memory and streams): :func:`mdstedc_dev`, :func:`secular_dev`,
+:func:`lowner_dev`, :func:`dhssevc_dev`, :func:`cauchy_eig_dev`.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "Config", "Stats", "load", "get_config", "set_config", "get_stats", "finalize",
+    "mdstedc", "eigh_tridiagonal", "cauchylike", "mdstedc_dev", "secular_dev",
+    "lowner_dev", "dhssevc_dev", "cauchy_eig_dev", "HssError",
+]
+
+
+class HssError(RuntimeError):
+    pass
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("hss_leaf", ctypes.c_int), ("bsmlz", ctypes.c_int), ("tol", ctypes.c_double),
+                ("smlsiz", ctypes.c_int), ("precision", ctypes.c_int),
+                ("predictor", ctypes.c_int), ("batched", ctypes.c_int),
+                ("reserved", ctypes.c_int * 9)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_levels", ctypes.c_int), ("n_merges", ctypes.c_int),
+                ("n_hss_merges", ctypes.c_int), ("n_dense_merges", ctypes.c_int),
+                ("max_k", ctypes.c_int), ("max_rank", ctypes.c_int),
+                ("total_k", ctypes.c_longlong), ("secular_iters", ctypes.c_longlong),
+                ("secular_roots", ctypes.c_longlong), ("predictor_fallbacks", ctypes.c_longlong),
+                ("kernel_launches", ctypes.c_longlong), ("ms_total", ctypes.c_double),
+                ("reserved", ctypes.c_int * 8)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+_lib = None
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_V = ctypes.c_void_p
+
+# exported symbol -> (restype, argtypes); must match include/hsspack_gb300.h
+SIGNATURES = {
+    "hss_default_config": (None, [ctypes.POINTER(Config)]),
+    "hss_set_config": (None, [ctypes.POINTER(Config)]),
+    "hss_get_config": (None, [ctypes.POINTER(Config)]),
+    "hss_get_stats": (None, [ctypes.POINTER(Stats)]),
+    "hss_last_error": (ctypes.c_char_p, []),
+    "hss_finalize": (ctypes.c_int, []),
+    "mdstedc_": (None, [ctypes.c_char_p, _I, _D, _D, _D, _I, _D, _I, _I, _I, _I, ctypes.c_size_t]),
+    "cauchylike_": (None, [_D, _D, _D, _D, _D, _I, _I]),
+    "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
+    "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
+    "hss_lowner_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V]),
+    "hss_dhssevc_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, _V, _V, _V, _V,
+                                       _V, _V, ctypes.c_int, ctypes.c_int, _V]),
+    "hss_cauchy_eig_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V, _V]),
+}
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) the CUDA library; raises if unavailable."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise HssError("libhsspack_gb300.so is not built: run hsspack_gb300/build.py")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _err():
+    return load().hss_last_error().decode(errors="replace")
+
+
+def get_config():
+    c = Config()
+    load().hss_get_config(ctypes.byref(c))
+    return c
+
+
+def set_config(**kw):
+    """Update the process-wide configuration; returns the previous one."""
+    old = get_config()
+    c = Config()
+    ctypes.memmove(ctypes.byref(c), ctypes.byref(old), ctypes.sizeof(Config))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    load().hss_set_config(ctypes.byref(c))
+    return old
+
+
+def restore_config(c):
+    load().hss_set_config(ctypes.byref(c))
+
+
+def get_stats():
+    s = Stats()
+    load().hss_get_stats(ctypes.byref(s))
+    return s.as_dict()
+
+
+def finalize():
+    return load().hss_finalize()
+
+
+def _pd(a):
+    return a.ctypes.data_as(_D)
+
+
+def mdstedc(compz, n, d, e, z, ldz, work, lwork, iwork, liwork):
+    """MDSTEDC with the Fortran argument list; arrays are numpy, modified in
+    place (d: eigenvalues, z: eigenvectors in Fortran order).  Returns INFO."""
+    L = load()
+    info = ctypes.c_int(0)
+    n_, ldz_, lw_, liw_ = (ctypes.c_int(int(x)) for x in (n, ldz, lwork, liwork))
+    for a, dt in ((d, np.float64), (e, np.float64), (z, np.float64), (work, np.float64),
+                  (iwork, np.int32)):
+        if a.dtype != dt:
+            raise TypeError("array dtype must be %s" % dt)
+    if z.ndim == 2 and not z.flags.f_contiguous:
+        raise ValueError("z must be Fortran ordered")
+    L.mdstedc_(compz.encode() if isinstance(compz, str) else compz, ctypes.byref(n_), _pd(d), _pd(e),
+               _pd(z), ctypes.byref(ldz_), _pd(work), ctypes.byref(lw_),
+               iwork.ctypes.data_as(_I), ctypes.byref(liw_), ctypes.byref(info), 1)
+    return info.value
+
+
+def eigh_tridiagonal(d, e):
+    """Eigenvalues (ascending) and eigenvectors of the symmetric tridiagonal
+    (d, e) through MDSTEDC('I').  Returns (w, Z) with Z Fortran ordered."""
+    n = len(d)
+    dd = np.array(d, dtype=np.float64, copy=True)
+    ee = np.zeros(max(n, 1), dtype=np.float64)
+    ee[: max(n - 1, 0)] = np.asarray(e, dtype=np.float64)[: max(n - 1, 0)]
+    Z = np.zeros((n, n), dtype=np.float64, order="F")
+    work = np.zeros(1)
+    iwork = np.zeros(1, dtype=np.int32)
+    info = mdstedc("I", n, dd, ee, Z, max(1, n), work, -1, iwork, -1)
+    if info != 0:
+        raise HssError("MDSTEDC workspace query: INFO=%d" % info)
+    lw, liw = int(work[0]), int(iwork[0])
+    # The GPU implementation keeps its workspace in device memory and touches
+    # only WORK(1) and IWORK(1), so one-element arrays declared with the
+    # queried sizes are passed instead of LWORK = 1 + 4N + N^2 doubles.
+    info = mdstedc("I", n, dd, ee, Z, max(1, n), work, lw, iwork, liw)
+    if info != 0:
+        raise HssError("MDSTEDC INFO=%d: %s" % (info, _err()))
+    return dd, Z
+
+
+def cauchylike(D, F, u, v):
+    """A(i,j) = u_i v_j / (D_i - F_j) computed on the GPU (Cauchylike.f90:1)."""
+    D, F, u, v = (np.ascontiguousarray(x, dtype=np.float64) for x in (D, F, u, v))
+    m, n = len(D), len(F)
+    A = np.zeros((m, n), dtype=np.float64, order="F")
+    load().cauchylike_(_pd(A), _pd(D), _pd(F), _pd(u), _pd(v), ctypes.byref(ctypes.c_int(m)),
+                       ctypes.byref(ctypes.c_int(n)))
+    return A
+
+
+# ------------------------------------------------------------ device API ----
+def _ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise HssError("device entry points take CUDA tensors")
+    if not t.is_contiguous():
+        raise HssError("tensor must be contiguous")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def mdstedc_dev(d, e, z, stream=None):
+    """Device MDSTEDC('I'): d (n,) -> eigenvalues, z (n, n) column-major
+    storage, i.e. a tensor whose memory is Fortran order (use z.T for rows)."""
+    n = d.numel()
+    info = load().hss_mdstedc_dev(n, _ptr(d), _ptr(e), _ptr(z), max(1, n), _stream(stream))
+    if info != 0:
+        raise HssError("hss_mdstedc_dev INFO=%d: %s" % (info, _err()))
+    return info
+
+
+def secular_dev(dlamda, z, rho, lam, difl, difr, iters=None, stream=None):
+    k = dlamda.numel()
+    rc = load().hss_secular_dev(k, _ptr(dlamda), _ptr(z), float(rho), _ptr(lam), _ptr(difl),
+                                _ptr(difr), _ptr(iters), _stream(stream))
+    if rc != 0:
+        raise HssError("hss_secular_dev rc=%d: %s" % (rc, _err()))
+    return rc
+
+
+def lowner_dev(dlamda, difl, difr, z, alpha, stream=None):
+    k = dlamda.numel()
+    rc = load().hss_lowner_dev(k, _ptr(dlamda), _ptr(difl), _ptr(difr), _ptr(z), _ptr(alpha),
+                               _stream(stream))
+    if rc != 0:
+        raise HssError("hss_lowner_dev rc=%d: %s" % (rc, _err()))
+    return rc
+
+
+def cauchy_eig_dev(F, u, v, difl, difr, C, stream=None):
+    k = F.numel()
+    rc = load().hss_cauchy_eig_dev(k, _ptr(F), _ptr(u), _ptr(v), _ptr(difl), _ptr(difr), _ptr(C),
+                                   _stream(stream))
+    if rc != 0:
+        raise HssError("hss_cauchy_eig_dev rc=%d: %s" % (rc, _err()))
+    return rc
+
+
+def dhssevc_dev(F, u, v, difl, difr, Q, ldq, nrows, ni=200, tol=1e-17, stream=None):
+    """Q(0:nrows, 0:K) <- Q @ C in place (Q column-major, leading dim ldq)."""
+    k = F.numel()
+    rc = load().hss_dhssevc_dev(k, int(ni), float(tol), _ptr(F), _ptr(u), _ptr(v), _ptr(difl),
+                                _ptr(difr), _ptr(Q), int(ldq), int(nrows), _stream(stream))
+    if rc != 0:
+        raise HssError("hss_dhssevc_dev rc=%d: %s" % (rc, _err()))
+    return rc

@@ -1,0 +1,697 @@
+// driver.cu -- host side of the GB300 divide-and-conquer eigensolver and the
+// C ABI (include/hsspack_gb300.h).
+//
+// MDSTEDC (SRC/mdstedc.f90:139-436): split at negligible off-diagonals, scale
+// each block, run the DC tree, unscale, order.  MDLAED0 (SRC/mdlaed0.f90:
+// 121-380): halving tree down to SMLSIZ, batched leaf eigensolves, then one
+// pass per level over all merges of the level.  Per level the host reads back
+// only the merge sizes K (one small copy), plans workspaces, and launches each
+// stage once for every merge of the level (cfg.batched = 1) or once per merge
+// (cfg.batched = 0, the "plain" mode).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/hsspack_gb300.h"
+#include "hss_common.cuh"
+#include "hss_gemm.h"
+#include "hss_hss.h"
+#include "hss_kernels.h"
+#include "hss_pool.h"
+
+namespace hss {
+
+// ------------------------------------------------------------ device pool --
+struct Buf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+struct Ctx {
+  std::recursive_mutex mu;
+  hss_config cfg;
+  hss_stats stats;
+  std::string err;
+  std::map<std::string, Buf> bufs;
+  void *pinned = nullptr;
+  size_t pinned_cap = 0;
+  long long launches = 0;
+  Ctx() {
+    hss_default_config(&cfg);
+    memset(&stats, 0, sizeof stats);
+  }
+};
+
+static Ctx &ctx() {
+  static Ctx *c = new Ctx();
+  return *c;
+}
+
+struct CudaError {
+  std::string msg;
+};
+
+#define CK(x)                                                                       \
+  do {                                                                              \
+    cudaError_t e_ = (x);                                                           \
+    if (e_ != cudaSuccess) {                                                        \
+      char b_[256];                                                                 \
+      snprintf(b_, sizeof b_, "%s:%d %s: %s", __FILE__, __LINE__, #x,               \
+               cudaGetErrorString(e_));                                             \
+      throw CudaError{b_};                                                          \
+    }                                                                               \
+  } while (0)
+
+template <class T>
+static T *buf(Ctx &c, const char *name, size_t count) {
+  Buf &b = c.bufs[name];
+  size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+  if (b.cap < bytes) {
+    if (b.p) {
+      CK(cudaDeviceSynchronize());
+      CK(cudaFree(b.p));
+      b.p = nullptr;
+      b.cap = 0;
+    }
+    size_t cap = bytes + bytes / 8;
+    CK(cudaMalloc(&b.p, cap));
+    b.cap = cap;
+  }
+  return (T *)b.p;
+}
+
+static void *pinned(Ctx &c, size_t bytes) {
+  if (c.pinned_cap < bytes) {
+    if (c.pinned) CK(cudaFreeHost(c.pinned));
+    c.pinned = nullptr;
+    size_t cap = std::max<size_t>(bytes * 2, 1 << 16);
+    CK(cudaMallocHost(&c.pinned, cap));
+    c.pinned_cap = cap;
+  }
+  return c.pinned;
+}
+
+void *pool_get(const char *name, size_t bytes) { return buf<char>(ctx(), name, bytes); }
+
+template <class T>
+static void h2d(T *dst, const std::vector<T> &src, cudaStream_t st) {
+  if (!src.empty()) CK(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+// ------------------------------------------------------------- DC block --
+struct MergeLevel {
+  std::vector<int> s, n, n1;
+};
+
+// Level arrays shared by all stages of one level (length = block size n).
+struct LevelArrays {
+  LevelScratch w;
+  double *lam, *difl, *difr, *zhat, *alpha;
+  int *iters;
+};
+
+static LevelArrays level_arrays(Ctx &c, int n) {
+  LevelArrays a;
+  a.w.srt = buf<int>(c, "srt", n);
+  a.w.ds = buf<double>(c, "ds", n);
+  a.w.zs = buf<double>(c, "zs", n);
+  a.w.typ = buf<unsigned char>(c, "typ", n);
+  a.w.cand = buf<int>(c, "cand", n);
+  a.w.dl = buf<double>(c, "dl", n);
+  a.w.zw = buf<double>(c, "zw", n);
+  a.w.ndslot = buf<int>(c, "ndslot", n);
+  a.w.grp = buf<int>(c, "grp", n);
+  a.w.dfslot = buf<int>(c, "dfslot", n);
+  a.w.dfval = buf<double>(c, "dfval", n);
+  a.w.gvp = buf<int>(c, "gvp", n);
+  a.w.gvq = buf<int>(c, "gvq", n);
+  a.w.gvc = buf<double>(c, "gvc", n);
+  a.w.gvs = buf<double>(c, "gvs", n);
+  a.w.l1slot = buf<int>(c, "l1slot", n);
+  a.w.l2slot = buf<int>(c, "l2slot", n);
+  a.w.l1val = buf<double>(c, "l1val", n);
+  a.w.l2val = buf<double>(c, "l2val", n);
+  a.lam = buf<double>(c, "lam", n);
+  a.difl = buf<double>(c, "difl", n);
+  a.difr = buf<double>(c, "difr", n);
+  a.zhat = buf<double>(c, "zhat", n);
+  a.alpha = buf<double>(c, "alpha", n);
+  a.iters = buf<int>(c, "iters", n);
+  return a;
+}
+
+// Process a group of merges of one level (all of them when batched, one when
+// not).  Arrays ms/mn/mn1 describe the group.
+static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int> &mn,
+                       const std::vector<int> &mn1, const double *e, double *Q, long long ldq,
+                       double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st) {
+  const int P = (int)ms.size();
+  if (P == 0) return;
+  // ---- upload the group and prepare (deflation)
+  int *dms = buf<int>(c, "g_ms", P), *dmn = buf<int>(c, "g_mn", P), *dmn1 = buf<int>(c, "g_mn1", P);
+  h2d(dms, ms, st); h2d(dmn, mn, st); h2d(dmn1, mn1, st);
+  int *dout = buf<int>(c, "g_out", 5 * P);
+  double *drho = buf<double>(c, "g_rho", P);
+  launch_merge_prepare(P, dms, dmn, dmn1, e, Q, ldq, Dp, perm, L.w, dout, drho, st);
+  c.launches++;
+  char *hp = (char *)pinned(c, (size_t)P * (5 * sizeof(int) + sizeof(double)));
+  int *hout = (int *)hp;
+  double *hrho = (double *)(hp + (size_t)P * 5 * sizeof(int));
+  CK(cudaMemcpyAsync(hout, dout, (size_t)P * 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hrho, drho, (size_t)P * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  // ---- plan
+  std::vector<int> as, an, aK, aoff(1, 0), gs, gn, gng;
+  std::vector<double> arho;
+  std::vector<int> ds_, dn_, dK_, doff(1, 0);
+  std::vector<double> drho_;
+  std::vector<long long> q2off, soff, toff;
+  std::vector<int> hsel;  // HSS merges (index into active arrays)
+  long long q2tot = 0, stot = 0;
+  int maxn = 0, maxn_g = 0;
+  for (int m = 0; m < P; ++m) {
+    const int K = hout[5 * m], ng = hout[5 * m + 1];
+    c.stats.n_merges++;
+    c.stats.total_k += K;
+    c.stats.max_k = std::max(c.stats.max_k, K);
+    if (ng > 0) { gs.push_back(ms[m]); gn.push_back(mn[m]); gng.push_back(ng); maxn_g = std::max(maxn_g, mn[m]); }
+    if (K == 0) continue;
+    as.push_back(ms[m]); an.push_back(mn[m]); aK.push_back(K); arho.push_back(hrho[m]);
+    aoff.push_back(aoff.back() + K);
+    maxn = std::max(maxn, mn[m]);
+    const bool use_hss = K >= c.cfg.bsmlz;
+    if (use_hss) {
+      hsel.push_back((int)as.size() - 1);
+      c.stats.n_hss_merges++;
+      continue;
+    }
+    c.stats.n_dense_merges++;
+    ds_.push_back(ms[m]); dn_.push_back(mn[m]); dK_.push_back(K); drho_.push_back(hrho[m]);
+    doff.push_back(doff.back() + K);
+    q2off.push_back(q2tot);
+    q2tot += (long long)mn[m] * K;
+    soff.push_back(stot);
+    stot += (long long)K * K;
+  }
+  const int PA = (int)as.size();
+  // ---- Givens rotations of deflation
+  if (!gs.empty()) {
+    int *g1 = buf<int>(c, "gv_s", gs.size()), *g2 = buf<int>(c, "gv_n", gs.size()),
+        *g3 = buf<int>(c, "gv_g", gs.size());
+    h2d(g1, gs, st); h2d(g2, gn, st); h2d(g3, gng, st);
+    launch_givens((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, st);
+    c.launches++;
+  }
+  if (PA == 0) return;
+  // ---- secular equation + Loewner for every active merge
+  int *vs = buf<int>(c, "a_s", PA), *vK = buf<int>(c, "a_K", PA), *voff = buf<int>(c, "a_off", PA + 1),
+      *vn = buf<int>(c, "a_n", PA);
+  double *vrho = buf<double>(c, "a_rho", PA);
+  h2d(vs, as, st); h2d(vK, aK, st); h2d(voff, aoff, st); h2d(vrho, arho, st); h2d(vn, an, st);
+  LevelView lv{vs, vK, vrho, voff, PA};
+  const int total = aoff.back();
+  c.stats.secular_roots += total;
+  launch_secular(lv, total, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
+                 (unsigned long long *)(status + 2), nullptr, st);
+  launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st);
+  c.launches += 2;
+  // ---- dense merges: S, gather, GEMM (block structured), scatter
+  const int PD = (int)ds_.size();
+  if (PD > 0) {
+    int *xs = buf<int>(c, "d_s", PD), *xK = buf<int>(c, "d_K", PD), *xoff = buf<int>(c, "d_off", PD + 1),
+        *xn = buf<int>(c, "d_n", PD);
+    double *xrho = buf<double>(c, "d_rho", PD);
+    long long *xq2 = buf<long long>(c, "d_q2off", PD), *xso = buf<long long>(c, "d_soff", PD);
+    h2d(xs, ds_, st); h2d(xK, dK_, st); h2d(xoff, doff, st); h2d(xrho, drho_, st); h2d(xn, dn_, st);
+    h2d(xq2, q2off, st); h2d(xso, soff, st);
+    LevelView dv{xs, xK, xrho, xoff, PD};
+    const int dtot = doff.back();
+    double *Q2 = buf<double>(c, "Q2", q2tot), *T = buf<double>(c, "T", q2tot);
+    double *S = buf<double>(c, "S", stot);
+    launch_build_S(dv, dtot, L.w.dl, L.difl, L.difr, L.zhat, L.w.grp, xso, S, st);
+    int maxnd = *std::max_element(dn_.begin(), dn_.end());
+    launch_gather(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, L.w.grp, xq2, Q, ldq, Q2, st);
+    // GEMM problems: top rows use type 1,2 columns, bottom rows type 2,3
+    std::vector<GemmDesc> probs;
+    int tiles = 0;
+    int di = 0;
+    for (int m = 0; m < P; ++m) {
+      const int K = hout[5 * m];
+      if (K == 0 || K >= c.cfg.bsmlz) continue;
+      const int c1 = hout[5 * m + 2], c2 = hout[5 * m + 3];
+      const int n = mn[m], n1 = mn1[m];
+      double *q2 = Q2 + q2off[di], *t = T + q2off[di], *sm = S + soff[di];
+      GemmDesc top{q2, sm, t, n, K, n, n1, K, c1 + c2, 0, tiles};
+      tiles += gemm_tiles(n1, K);
+      probs.push_back(top);
+      GemmDesc bot{q2 + n1 + (long long)c1 * n, sm + c1, t + n1, n, K, n, n - n1, K, K - c1, 0, tiles};
+      tiles += gemm_tiles(n - n1, K);
+      probs.push_back(bot);
+      ++di;
+    }
+    GemmDesc *dprobs = buf<GemmDesc>(c, "gemm_probs", probs.size());
+    h2d(dprobs, probs, st);
+    launch_gemm_f64((int)probs.size(), tiles, dprobs, st);
+    launch_scatter(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, xq2, T, Q, ldq, st);
+    c.launches += 4;
+  }
+  // ---- HSS merges: one at a time (each has its own HSS tree)
+  for (int a : hsel) {
+    HssMergeArgs h;
+    h.s = as[a]; h.n = an[a]; h.K = aK[a];
+    h.leaf = c.cfg.hss_leaf; h.tol = c.cfg.tol; h.precision = c.cfg.precision;
+    h.dl = L.w.dl + h.s; h.difl = L.difl + h.s; h.difr = L.difr + h.s; h.zhat = L.zhat + h.s;
+    h.alpha = L.alpha + h.s; h.ndslot = L.w.ndslot + h.s;
+    h.Q = Q; h.ldq = ldq;
+    int rank = 0;
+    c.launches += hss_merge(h, &rank, st);
+    c.stats.max_rank = std::max(c.stats.max_rank, rank);
+  }
+  // ---- new ascending order and eigenvalues of the rewritten slots
+  launch_merge_finish(PA, vs, vn, vK, L.lam, L.w, perm, Dp, st);
+  c.launches++;
+}
+
+// Eigen-decomposition of one unreduced, scaled block of size n (> smlsiz):
+// d, e on the device (block-relative), Q block-relative with leading dim ldq.
+static void dc_block(Ctx &c, int n, const double *d, const double *e, double *Q, long long ldq,
+                     double *Dp, int *perm, int *status, cudaStream_t st) {
+  const int smlsiz = std::max(1, std::min(c.cfg.smlsiz, 32));
+  std::vector<int> sz(1, n);
+  while (sz.back() > smlsiz) {
+    std::vector<int> nx;
+    for (int s : sz) { nx.push_back(s / 2); nx.push_back((s + 1) / 2); }
+    sz.swap(nx);
+  }
+  const int nl = (int)sz.size();
+  std::vector<int> ls(nl), ends(nl);
+  for (int i = 0, acc = 0; i < nl; ++i) { ls[i] = acc; acc += sz[i]; ends[i] = acc; }
+  int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl);
+  h2d(dls, ls, st); h2d(dlz, sz, st);
+  launch_leaf(nl, dls, dlz, n, d, e, Q, ldq, Dp, perm, status, st);
+  c.launches++;
+  LevelArrays L = level_arrays(c, n);
+  while ((int)ends.size() > 1) {
+    MergeLevel lvl;
+    std::vector<int> nx;
+    for (size_t i = 0; i + 1 < ends.size(); i += 2) {
+      const int s = i == 0 ? 0 : ends[i - 1];
+      const int matsiz = ends[i + 1] - s;
+      const int msd2 = i == 0 ? ends[0] : matsiz / 2;
+      lvl.s.push_back(s); lvl.n.push_back(matsiz); lvl.n1.push_back(msd2);
+      nx.push_back(ends[i + 1]);
+    }
+    c.stats.n_levels++;
+    if (c.cfg.batched) {
+      run_merges(c, lvl.s, lvl.n, lvl.n1, e, Q, ldq, Dp, perm, L, status, st);
+    } else {
+      for (size_t m = 0; m < lvl.s.size(); ++m)
+        run_merges(c, {lvl.s[m]}, {lvl.n[m]}, {lvl.n1[m]}, e, Q, ldq, Dp, perm, L, status, st);
+    }
+    ends.swap(nx);
+  }
+}
+
+__global__ void k_scale(int n, double *x, double a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] *= a;
+}
+__global__ void k_iota(int n, int *p, int base) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = base + i;
+}
+// a 1x1 block: eigenvector e_i, block-relative order 0
+__global__ void k_put1(double *Q, long long ldq, int i, double *Dp, double v, int *perm) {
+  Q[(long long)i * ldq + i] = 1.0;
+  Dp[i] = v;
+  perm[i] = 0;
+}
+
+// Full MDSTEDC('I') on device arrays.  hd/he: host copies of d/e (n, n-1).
+static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<double> he,
+                        double *dz, long long ldz, double *dw, cudaStream_t st) {
+  memset(&c.stats, 0, sizeof c.stats);
+  c.launches = 0;
+  cudaEvent_t ev0, ev1;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  CK(cudaEventRecord(ev0, st));
+  const double EPS = 1.1102230246251565e-16;
+  he.resize(std::max(n, 1), 0.0);
+  double *Q = buf<double>(c, "Q", (size_t)n * n);
+  double *Dp = buf<double>(c, "Dp", n);
+  int *perm = buf<int>(c, "perm", n);
+  double *d = buf<double>(c, "d_in", n), *e = buf<double>(c, "e_in", std::max(n, 1));
+  // status[0]: error code, status[2..3]: 64-bit sum of secular iterations
+  int *status = buf<int>(c, "status", 4);
+  CK(cudaMemsetAsync(status, 0, 4 * sizeof(int), st));
+  CK(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)n * n, st));
+  // split into unreduced blocks and scale each (mdstedc.f90:305-345)
+  std::vector<int> bstart, bend;
+  std::vector<double> bscale;
+  const int smlsiz = std::max(1, std::min(c.cfg.smlsiz, 32));
+  int start = 0;
+  while (start < n) {
+    int finish = start;
+    while (finish < n - 1) {
+      const double tiny = EPS * std::sqrt(std::fabs(hd[finish])) * std::sqrt(std::fabs(hd[finish + 1]));
+      if (std::fabs(he[finish]) > tiny) ++finish; else break;
+    }
+    double nrm = 0.0;
+    for (int i = start; i <= finish; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
+    for (int i = start; i < finish; ++i) nrm = std::max(nrm, std::fabs(he[i]));
+    const int m = finish - start + 1;
+    double scl = 1.0;
+    if (m > smlsiz && nrm > 0.0) {
+      scl = nrm;
+      const double mul = 1.0 / nrm;
+      for (int i = start; i <= finish; ++i) hd[i] *= mul;
+      for (int i = start; i < finish; ++i) he[i] *= mul;
+    }
+    bstart.push_back(start); bend.push_back(finish); bscale.push_back(scl);
+    start = finish + 1;
+  }
+  CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e, he.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  for (size_t b = 0; b < bstart.size(); ++b) {
+    const int s0 = bstart[b], m = bend[b] - s0 + 1;
+    double *Qb = Q + (long long)s0 * n + s0;
+    if (m == 1) {
+      k_put1<<<1, 1, 0, st>>>(Q, n, s0, Dp, hd[s0], perm);
+      continue;
+    }
+    if (m <= smlsiz) {
+      std::vector<int> ls(1, 0), lz(1, m);
+      int *dls = buf<int>(c, "leaf_s", 1), *dlz = buf<int>(c, "leaf_z", 1);
+      h2d(dls, ls, st); h2d(dlz, lz, st);
+      launch_leaf(1, dls, dlz, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
+      c.launches++;
+    } else {
+      dc_block(c, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
+    }
+    if (bscale[b] != 1.0) k_scale<<<(m + 255) / 256, 256, 0, st>>>(m, Dp + s0, bscale[b]);
+  }
+  // block-relative slots/perm -> absolute order
+  int *fperm = perm;
+  if (bstart.size() > 1) {
+    std::vector<int> hp(n);
+    std::vector<double> hv(n);
+    CK(cudaMemcpyAsync(hp.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hv.data(), Dp, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<std::pair<double, int>> all;
+    all.reserve(n);
+    // perm entries are block-relative slots; Dp is indexed block-relative too
+    for (size_t b = 0; b < bstart.size(); ++b)
+      for (int i = bstart[b]; i <= bend[b]; ++i) {
+        const int slot = bstart[b] + hp[i];
+        all.push_back({hv[slot], slot});
+      }
+    std::stable_sort(all.begin(), all.end(),
+                     [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+                       return a.first < b.first;
+                     });
+    std::vector<int> fp(n);
+    for (int i = 0; i < n; ++i) fp[i] = all[i].second;
+    fperm = buf<int>(c, "fperm", n);
+    h2d(fperm, fp, st);
+  }
+  launch_final_gather(n, fperm, Dp, Q, n, dz, ldz, dw, st);
+  c.launches++;
+  CK(cudaEventRecord(ev1, st));
+  int hst[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const int hstatus = hst[0];
+  unsigned long long its;
+  memcpy(&its, hst + 2, sizeof its);
+  c.stats.secular_iters = (long long)its;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  c.stats.ms_total = ms;
+  c.stats.kernel_launches = c.launches;
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  CK(cudaGetLastError());
+  if (hstatus != 0) {
+    c.err = hstatus == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
+                                           : "leaf QL iteration did not converge";
+    return 1;
+  }
+  return 0;
+}
+
+}  // namespace hss
+
+// ================================================================== C ABI ==
+using namespace hss;
+
+extern "C" {
+
+void hss_default_config(hss_config *cfg) {
+  memset(cfg, 0, sizeof *cfg);
+  cfg->hss_leaf = 200;
+  cfg->bsmlz = 1500;
+  cfg->tol = 1e-17;
+  cfg->smlsiz = 25;
+  cfg->precision = 0;
+  cfg->predictor = 0;
+  cfg->batched = 1;
+}
+
+void hss_set_config(const hss_config *cfg) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  c.cfg = *cfg;
+}
+void hss_get_config(hss_config *cfg) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  *cfg = c.cfg;
+}
+void hss_get_stats(hss_stats *st) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  *st = c.stats;
+}
+const char *hss_last_error(void) { return ctx().err.c_str(); }
+
+int hss_finalize(void) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  cudaDeviceSynchronize();
+  for (auto &kv : c.bufs)
+    if (kv.second.p) cudaFree(kv.second.p);
+  c.bufs.clear();
+  if (c.pinned) cudaFreeHost(c.pinned);
+  c.pinned = nullptr;
+  c.pinned_cap = 0;
+  return 0;
+}
+
+int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -2;
+  if (ldz < std::max(1, n)) return -6;
+  if (n == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    std::vector<double> hd(n), he(std::max(n, 1), 0.0);
+    CK(cudaMemcpyAsync(hd.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (n > 1) CK(cudaMemcpyAsync(he.data(), e, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double *dw = buf<double>(c, "w_out", n);
+    int info = mdstedc_core(c, n, hd, he, z, ldz, dw, st);
+    CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return info;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+void mdstedc_(const char *compz, const int *n_, double *d, double *e, double *z, const int *ldz_,
+              double *work, const int *lwork_, int *iwork, const int *liwork_, int *info,
+              size_t /*compz_len*/) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  const int n = *n_, ldz = *ldz_, lwork = *lwork_, liwork = *liwork_;
+  const char cz = compz[0];
+  int icompz = (cz == 'N' || cz == 'n') ? 0 : (cz == 'V' || cz == 'v') ? 1 : (cz == 'I' || cz == 'i') ? 2 : -1;
+  *info = 0;
+  const bool lquery = (lwork == -1 || liwork == -1);
+  if (icompz < 0 || icompz == 1) *info = -1;
+  else if (n < 0) *info = -2;
+  else if (ldz < 1 || (icompz > 0 && ldz < std::max(1, n))) *info = -6;
+  long long lwmin = 1, liwmin = 1;
+  if (*info == 0) {
+    const int smlsiz = c.cfg.smlsiz;
+    if (n <= 1 || icompz == 0) { lwmin = 1; liwmin = 1; }
+    else if (n <= smlsiz) { lwmin = 2LL * (n - 1); liwmin = 1; }
+    else { lwmin = 1 + 4LL * n + (long long)n * n; liwmin = 3 + 5LL * n; }
+    if (work) work[0] = (double)lwmin;
+    if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
+    if (lwork < lwmin && !lquery) *info = -8;
+    else if (liwork < liwmin && !lquery) *info = -10;
+  }
+  if (*info != 0) {
+    c.err = "MDSTEDC: illegal argument " + std::to_string(-*info);
+    return;
+  }
+  if (lquery || n == 0) return;
+  if (n == 1) {
+    if (icompz != 0) z[0] = 1.0;
+    return;
+  }
+  try {
+    cudaStream_t st = nullptr;
+    std::vector<double> hd(d, d + n), he(e, e + (n - 1));
+    double *dz = buf<double>(c, "z_out", (size_t)n * n);
+    double *dw = buf<double>(c, "w_out", n);
+    if (icompz == 0) {
+      // eigenvalues only: the same solve, vectors discarded (the reference
+      // calls DSTERF here, mdstedc.f90:264-267)
+      *info = mdstedc_core(c, n, hd, he, dz, n, dw, st);
+    } else {
+      *info = mdstedc_core(c, n, hd, he, dz, n, dw, st);
+      CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n, n,
+                           cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (work) work[0] = (double)lwmin;
+    if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
+  }
+}
+
+int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, double *lam,
+                    double *difl, double *difr, int *iters, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k <= 0) return k < 0 ? -1 : 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    std::vector<int> s(1, 0), K(1, k), off{0, k};
+    std::vector<double> r(1, rho);
+    int *vs = buf<int>(c, "x_s", 1), *vK = buf<int>(c, "x_K", 1), *vo = buf<int>(c, "x_off", 2);
+    double *vr = buf<double>(c, "x_rho", 1);
+    int *status = buf<int>(c, "x_status", 1);
+    h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
+    CK(cudaMemsetAsync(status, 0, sizeof(int), st));
+    LevelView lv{vs, vK, vr, vo, 1};
+    launch_secular(lv, k, dlamda, z, lam, difl, difr, iters, status, nullptr, nullptr, st);
+    int hs = 0;
+    CK(cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    return hs ? 1 : 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_lowner_dev(int k, const double *dlamda, const double *difl, const double *difr, double *z,
+                   double *alpha, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k <= 0) return k < 0 ? -1 : 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    std::vector<int> s(1, 0), K(1, k), off{0, k};
+    std::vector<double> r(1, 1.0);
+    int *vs = buf<int>(c, "x_s", 1), *vK = buf<int>(c, "x_K", 1), *vo = buf<int>(c, "x_off", 2);
+    double *vr = buf<double>(c, "x_rho", 1);
+    h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
+    LevelView lv{vs, vK, vr, vo, 1};
+    double *zh = buf<double>(c, "x_zhat", k);
+    launch_lowner(lv, k, dlamda, difl, difr, z, zh, st);
+    launch_alpha(lv, k, dlamda, difl, difr, zh, alpha, st);
+    CK(cudaMemcpyAsync(z, zh, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_cauchy_eig_dev(int k, const double *F, const double *u, const double *v,
+                       const double *difl, const double *difr, double *C, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k < 0) return -1;
+  try {
+    launch_cauchy_eig(k, F, u, v, difl, difr, C, (cudaStream_t)stream);
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u, const double *v,
+                    const double *difl, const double *difr, double *Q, int ldq, int nrows,
+                    void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k < 0) return -1;
+  if (ni < 1) return -2;
+  if (ldq < std::max(1, nrows)) return -10;
+  if (k == 0 || nrows == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    int rank = 0;
+    hss_dhssevc_core(k, ni, tol, c.cfg.precision, F, u, v, difl, difr, Q, ldq, nrows, &rank, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    c.stats.max_rank = rank;
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+void cauchylike_(double *A, const double *D, const double *F, const double *u, const double *v,
+                 const int *m_, const int *n_) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  const int m = *m_, n = *n_;
+  if (m <= 0 || n <= 0) return;
+  try {
+    cudaStream_t st = nullptr;
+    double *dD = buf<double>(c, "cl_D", m), *dF = buf<double>(c, "cl_F", n), *du = buf<double>(c, "cl_u", m),
+           *dv = buf<double>(c, "cl_v", n), *dA = buf<double>(c, "cl_A", (size_t)m * n);
+    CK(cudaMemcpyAsync(dD, D, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dF, F, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(du, u, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv, v, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    launch_cauchylike(m, n, dD, dF, du, dv, dA, st);
+    CK(cudaMemcpyAsync(A, dA, sizeof(double) * (size_t)m * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// gemm_f64.cu -- grouped FP64 GEMM: C_p = A_p * B_p (+ C_p) for a list of
+// problems launched together (the dense merge update Q2*S of LAPACK DLAED3 and
+// the per-level products of the HSS multiply, SRC/ConstructHssd.f90:1394-1630).
+//
+// 64x64 output tile per CTA, 16-deep K slices double-buffered in shared
+// memory, 256 threads with a 4x4 register tile each (DFMA).  Problems and
+// their tiles are flattened; a CTA finds its problem by binary search on the
+// tile prefix.  All operands column-major.
+#include "hss_common.cuh"
+#include "hss_gemm.h"
+
+namespace hss {
+
+constexpr int BM = 64, BN = 64, BK = 16, GT = 256;
+
+__global__ void __launch_bounds__(GT)
+k_gemm_f64(int nprob, const GemmDesc *__restrict__ probs) {
+  __shared__ double As[2][BK][BM + 2];
+  __shared__ double Bs[2][BK][BN + 2];
+  // locate problem
+  int lo = 0, hi = nprob;
+  const int b = blockIdx.x;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (probs[mid].tile0 <= b) lo = mid; else hi = mid;
+  }
+  const GemmDesc P = probs[lo];
+  const int t = b - P.tile0;
+  const int tm = (P.M + BM - 1) / BM;
+  const int m0 = (t % tm) * BM, n0 = (t / tm) * BN;
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;  // thread owns rows tx*4.., cols ty*4..
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  const int nk = (P.K + BK - 1) / BK;
+  auto load = [&](int buf, int kb) {
+    const int k0 = kb * BK;
+    // A tile: BM x BK, 1024 values, 4 per thread (column-major: row fastest)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * GT;
+      const int row = idx % BM, kk = idx / BM;
+      const int gr = m0 + row, gk = k0 + kk;
+      As[buf][kk][row] = (gr < P.M && gk < P.K) ? P.A[(long long)gk * P.lda + gr] : 0.0;
+    }
+    // B tile: BK x BN
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + r * GT;
+      const int kk = idx % BK, col = idx / BK;
+      const int gk = k0 + kk, gc = n0 + col;
+      Bs[buf][kk][col] = (gk < P.K && gc < P.N) ? P.B[(long long)gc * P.ldb + gk] : 0.0;
+    }
+  };
+  if (nk > 0) load(0, 0);
+  __syncthreads();
+  for (int kb = 0; kb < nk; ++kb) {
+    const int cur = kb & 1;
+    if (kb + 1 < nk) load(cur ^ 1, kb + 1);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], bb[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[cur][kk][tx * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bb[j] = Bs[cur][kk][ty * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int gc = n0 + ty * 4 + j;
+    if (gc >= P.N) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int gr = m0 + tx * 4 + i;
+      if (gr >= P.M) continue;
+      double *c = P.C + (long long)gc * P.ldc + gr;
+      *c = P.beta ? *c + acc[i][j] : acc[i][j];
+    }
+  }
+}
+
+int gemm_tiles(int M, int N) { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN); }
+
+void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaStream_t st) {
+  if (nprob <= 0 || total_tiles <= 0) return;
+  k_gemm_f64<<<total_tiles, GT, 0, st>>>(nprob, d_probs);
+}
+
+}  // namespace hss

@@ -1,0 +1,71 @@
+// hss_common.cuh -- shared device helpers for the sm_103a HSS merge kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define HSS_EPS 1.1102230246251565e-16   /* 2^-53, LAPACK DLAMCH('Epsilon') */
+#define HSS_WARP 32
+#define HSS_FULL 0xffffffffu
+
+// ---- warp all-reduce (butterfly: every lane ends with the same bits) --------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(HSS_FULL, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(HSS_FULL, v, o));
+  return v;
+}
+__device__ __forceinline__ int warp_sum_int(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(HSS_FULL, v, o);
+  return v;
+}
+
+// (value, index) argmax with "first index wins" ties -- Fortran MAXLOC order.
+struct ArgMax {
+  double v;
+  int i;
+};
+__device__ __forceinline__ ArgMax argmax_merge(ArgMax a, ArgMax b) {
+  if (b.v > a.v || (b.v == a.v && b.i < a.i)) return b;
+  return a;
+}
+__device__ __forceinline__ ArgMax warp_argmax(ArgMax a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ArgMax b;
+    b.v = __shfl_xor_sync(HSS_FULL, a.v, o);
+    b.i = __shfl_xor_sync(HSS_FULL, a.i, o);
+    a = argmax_merge(a, b);
+  }
+  return a;
+}
+
+// Differences of the old poles F and new roots lam = F + DIFL, formed from
+// DIFL/DIFR so that no cancellation occurs near the poles
+// (SRC/CauchyHssEig.f90:470-568, computfd / computdd).
+//   fd(p, q) = F_p - lam_q ;  dd(p, q) = lam_p - lam_q
+struct PoleDiff {
+  const double *__restrict__ F;
+  const double *__restrict__ difl;
+  const double *__restrict__ difr;
+  __device__ __forceinline__ double fd(int p, int q) const {
+    return p <= q ? (__ldg(F + p) - __ldg(F + q)) - __ldg(difl + q)
+                  : (__ldg(F + p) - __ldg(F + q + 1)) - __ldg(difr + q);
+  }
+  __device__ __forceinline__ double dd(int p, int q) const {
+    return p < q ? (__ldg(F + p + 1) - __ldg(F + q)) + __ldg(difr + p) - __ldg(difl + q)
+                 : (__ldg(F + p) - __ldg(F + q + 1)) + __ldg(difl + p) - __ldg(difr + q);
+  }
+};
+
+// Device status words written by kernels; the host maps them to INFO > 0.
+enum HssStatus : int {
+  HSS_OK = 0,
+  HSS_SECULAR_NOCONV = 1,   // a secular root hit the iteration cap
+  HSS_LEAF_NOCONV = 2,      // a leaf QL iteration hit its cap
+  HSS_BAD_INPUT = 3,        // NaN / non-increasing poles
+};

@@ -1,0 +1,38 @@
+// hss_hss.h -- the HSS path of one merge (MDLAED3 + DHSSEVC, SRC/mdlaed3.f90:124-261,
+// SRC/CauchyHssEig.f90:2444-2598).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+namespace hss {
+
+struct HssError {
+  std::string msg;
+};
+
+// One HSS merge of a DC level.  Poles/roots/weights are the merge's slices of
+// the level arrays (already offset); ndslot lists the Q slots of the K
+// non-deflated columns; Q is block-relative with leading dimension ldq and the
+// merge's rows/columns start at s.
+struct HssMergeArgs {
+  int s, n, K;
+  int leaf;
+  double tol;
+  int precision;
+  const double *dl, *difl, *difr, *zhat;
+  double *alpha;
+  const int *ndslot;
+  double *Q;
+  long long ldq;
+};
+
+// Returns the number of kernels launched; *rank receives the largest HSS rank.
+int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st);
+
+// DHSSEVC on caller arrays: Q(0:nrows, 0:K) <- Q * C.
+int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
+                     const double *v, const double *difl, const double *difr, double *Q,
+                     long long ldq, int nrows, int *rank, cudaStream_t st);
+
+}  // namespace hss

@@ -1,0 +1,73 @@
+// hss_kernels.h -- host-side launch wrappers of the device kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace hss {
+
+// Merges of one DC level that have K > 0, compacted: merge m owns positions
+// [s[m], s[m] + K[m]) of the level arrays; rootoff = prefix sum of K (P + 1).
+struct LevelView {
+  const int *s;
+  const int *K;
+  const double *rho;
+  const int *rootoff;
+  int P;
+};
+
+struct LevelScratch {
+  int *srt;
+  double *ds;
+  double *zs;
+  unsigned char *typ;
+  int *cand;
+  double *dl;
+  double *zw;
+  int *ndslot;
+  int *grp;
+  int *dfslot;
+  double *dfval;
+  int *gvp, *gvq;
+  double *gvc, *gvs;
+  int *l1slot, *l2slot;  // deflated by small z / by rotation, before merging
+  double *l1val, *l2val;
+};
+
+// secular.cu
+void launch_secular(const LevelView &lv, int total, const double *dl, const double *zw,
+                    double *lam, double *difl, double *difr, int *iters, int *status,
+                    unsigned long long *itsum, const float *guess, cudaStream_t st);
+void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
+                   const double *difr, const double *zw, double *zhat, cudaStream_t st);
+void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
+                  const double *difr, const double *zhat, double *alpha, cudaStream_t st);
+void launch_build_S(const LevelView &lv, int total, const double *dl, const double *difl,
+                    const double *difr, const double *zhat, const int *grp,
+                    const long long *soff, double *Sws, cudaStream_t st);
+void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
+                       const double *difl, const double *difr, double *C, cudaStream_t st);
+void launch_cauchylike(int M, int N, const double *D, const double *F, const double *u,
+                       const double *v, double *A, cudaStream_t st);
+
+// leaf.cu
+void launch_leaf(int nleaf, const int *lstart, const int *lsize, int nblk, const double *d,
+                 const double *e, double *Q, long long ldq, double *Dp, int *perm, int *status,
+                 cudaStream_t st);
+
+// merge.cu
+void launch_merge_prepare(int P, const int *ms, const int *mn, const int *mn1, const double *e,
+                          const double *Q, long long ldq, double *Dp, int *perm,
+                          const LevelScratch &w, int *out, double *orho, cudaStream_t st);
+void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
+                   const LevelScratch &w, double *Q, long long ldq, cudaStream_t st);
+void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
+                   const int *ndslot, const int *grp, const long long *boff, const double *Q,
+                   long long ldq, double *B, cudaStream_t st);
+void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
+                    const int *ndslot, const long long *toff, const double *T, double *Q,
+                    long long ldq, cudaStream_t st);
+void launch_merge_finish(int P, const int *ms, const int *mn, const int *mK, const double *lam,
+                         const LevelScratch &w, int *perm, double *Dp, cudaStream_t st);
+void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
+                         double *Z, long long ldz, double *wout, cudaStream_t st);
+
+}  // namespace hss

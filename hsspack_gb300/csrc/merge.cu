@@ -1,0 +1,407 @@
+// merge.cu -- per-level bookkeeping of the DC merges (MDLAED1/MDLAED2 of
+// SRC/mdlaed1.f90:109-233 and SRC/mdlaed2.f90:149-528), batched one CTA per merge.
+//
+// Storage model ("physical slots").  The eigenvector matrix Q (n x n, column-
+// major) is block diagonal at every level.  A column never moves: slot p keeps
+// its storage, Dp[p] its eigenvalue, and perm[] lists the slots of each block
+// in ascending eigenvalue order.  A merge rewrites only the K slots whose
+// eigenvectors change (the non-deflated ones); deflated columns stay where
+// they are, modified in place only by deflating Givens rotations.  This is the
+// reference's INDXQ indirection (mdlaed0.f90:221, mdlaed2.f90:229-233) carried
+// through to the end, so no level copies the whole n x n block.
+#include "hss_common.cuh"
+#include "hss_kernels.h"
+
+namespace hss {
+
+constexpr int MT = 512;  // threads per merge CTA
+
+// Block-wide exclusive scan of one 64-bit value per thread.
+__device__ __forceinline__ unsigned long long block_scan64(unsigned long long v,
+                                                           unsigned long long *tot) {
+  __shared__ unsigned long long ws[MT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long y = __shfl_up_sync(HSS_FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long t = (lane < MT / 32) ? ws[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(HSS_FULL, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < MT / 32) ws[lane] = t;
+  }
+  __syncthreads();
+  const unsigned long long base = (w > 0) ? ws[w - 1] : 0ull;
+  if (tot) *tot = ws[MT / 32 - 1];
+  const unsigned long long r = base + x - v;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v) {
+  __shared__ double ws[MT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_max(v);
+  if (lane == 0) ws[w] = v;
+  __syncthreads();
+  double r = ws[0];
+  for (int i = 1; i < MT / 32; ++i) r = fmax(r, ws[i]);
+  __syncthreads();
+  return r;
+}
+
+// Stable bottom-up merge sort of (v, p) pairs of length len by one CTA, with
+// scratch (tv, tp) of the same length; each pass places every element by a
+// binary search in the partner run (merge path).
+__device__ void block_sort_pairs(double *v, int *p, double *tv, int *tp, int len) {
+  bool in_tmp = false;
+  for (int width = 1; width < len; width <<= 1) {
+    const double *sv = in_tmp ? tv : v;
+    const int *sp = in_tmp ? tp : p;
+    double *dv = in_tmp ? v : tv;
+    int *dp = in_tmp ? p : tp;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      const int run = i / width, start = (run & ~1) * width;
+      const int mid = min(start + width, len), end = min(start + 2 * width, len);
+      const double x = sv[i];
+      int pos;
+      if ((run & 1) == 0) {
+        int lo = mid, hi = end;
+        while (lo < hi) { int md = (lo + hi) >> 1; if (sv[md] < x) lo = md + 1; else hi = md; }
+        pos = (i - start) + (lo - mid);
+      } else {
+        int lo = start, hi = mid;
+        while (lo < hi) { int md = (lo + hi) >> 1; if (sv[md] <= x) lo = md + 1; else hi = md; }
+        pos = (i - mid) + (lo - start);
+      }
+      dv[start + pos] = x;
+      dp[start + pos] = sp[i];
+    }
+    __syncthreads();
+    in_tmp = !in_tmp;
+  }
+  if (in_tmp) {
+    for (int i = threadIdx.x; i < len; i += blockDim.x) { v[i] = tv[i]; p[i] = tp[i]; }
+    __syncthreads();
+  }
+}
+
+// out[5*m + {0..4}] = K, #rotations, #type1, #type2, #type3 ; orho[m] = |2 rho|
+__global__ void __launch_bounds__(MT)
+k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+                const int *__restrict__ mn1, const double *__restrict__ e,
+                const double *__restrict__ Q, long long ldq, double *__restrict__ Dp,
+                int *__restrict__ perm, LevelScratch w, int *__restrict__ out,
+                double *__restrict__ orho) {
+  const int m = blockIdx.x;
+  if (m >= P) return;
+  const int s = ms[m], n = mn[m], n1 = mn1[m], n2 = n - n1;
+  const int tid = threadIdx.x;
+  const double rho_in = e[s + n1 - 1];
+  // ---- merge the two ascending halves (DLAMRG, ties to the first list)
+  for (int i = tid; i < n1; i += MT) {
+    const int slot = perm[s + i];
+    const double a = Dp[slot];
+    int lo = 0, hi = n2;  // count right values < a
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (Dp[perm[s + n1 + mid]] < a) lo = mid + 1; else hi = mid;
+    }
+    w.srt[s + i + lo] = slot;
+  }
+  for (int j = tid; j < n2; j += MT) {
+    const int slot = perm[s + n1 + j];
+    const double b = Dp[slot];
+    int lo = 0, hi = n1;  // count left values <= b
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (Dp[perm[s + mid]] <= b) lo = mid + 1; else hi = mid;
+    }
+    w.srt[s + j + lo] = slot;
+  }
+  __syncthreads();
+  // ---- z = [last row of Q1, first row of Q2] / sqrt(2) (mdlaed1.f90:178-180,
+  //      mdlaed2.f90:203-211) in merged order
+  const double sc = 1.0 / sqrt(2.0);
+  double dmax = 0.0, zmax = 0.0;
+  for (int i = tid; i < n; i += MT) {
+    const int slot = w.srt[s + i];
+    const bool top = slot < s + n1;
+    double z = Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
+    if (!top && rho_in < 0.0) z = -z;
+    z *= sc;
+    const double dv = Dp[slot];
+    w.ds[s + i] = dv;
+    w.zs[s + i] = z;
+    w.typ[s + i] = top ? 1 : 3;
+    dmax = fmax(dmax, fabs(dv));
+    zmax = fmax(zmax, fabs(z));
+  }
+  dmax = block_max(dmax);
+  zmax = block_max(zmax);
+  const double rho = fabs(2.0 * rho_in);
+  const double tol = 8.0 * HSS_EPS * fmax(dmax, zmax);  // mdlaed2.f90:265-267
+  if (rho * zmax <= tol) {  // nothing couples the halves
+    for (int i = tid; i < n; i += MT) perm[s + i] = w.srt[s + i];
+    if (tid == 0) {
+      out[5 * m] = 0; out[5 * m + 1] = 0; out[5 * m + 2] = 0; out[5 * m + 3] = 0;
+      out[5 * m + 4] = 0;
+      orho[m] = rho;
+    }
+    return;
+  }
+  // ---- candidates: z large enough (deflation by small z, mdlaed2.f90:304-313)
+  const int chunk = (n + MT - 1) / MT;
+  const int b0 = min(n, tid * chunk), b1 = min(n, b0 + chunk);
+  int cnt = 0;
+  for (int i = b0; i < b1; ++i) {
+    const bool big = rho * fabs(w.zs[s + i]) > tol;  // typ 4: deflated, small z
+    cnt += big;
+    if (!big) w.typ[s + i] = 4;
+  }
+  unsigned long long tot;
+  int pos = (int)block_scan64((unsigned long long)cnt, &tot);
+  const int nc = (int)tot;
+  for (int i = b0; i < b1; ++i)
+    if (w.typ[s + i] != 4) w.cand[s + pos++] = i;
+  __syncthreads();
+  // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371): a
+  //      sequential chain over the candidates, run by one thread
+  __shared__ int s_ng;
+  if (tid == 0) {
+    int ng = 0;
+    int pj = w.cand[s];
+    for (int t = 1; t < nc; ++t) {
+      const int nj = w.cand[s + t];
+      const double zp = w.zs[s + pj], zn = w.zs[s + nj];
+      const double tau = hypot(zn, zp);
+      const double tt = w.ds[s + nj] - w.ds[s + pj];
+      const double c = zn / tau, sn = -zp / tau;
+      if (fabs(tt * c * sn) <= tol) {
+        w.zs[s + nj] = tau;
+        w.zs[s + pj] = 0.0;
+        if (w.typ[s + nj] != w.typ[s + pj]) w.typ[s + nj] = 2;
+        w.typ[s + pj] = 5;  // deflated by rotation: value changes, order fixed below
+        w.gvp[s + ng] = w.srt[s + pj];
+        w.gvq[s + ng] = w.srt[s + nj];
+        w.gvc[s + ng] = c;
+        w.gvs[s + ng] = sn;
+        ++ng;
+        const double dp = w.ds[s + pj], dn = w.ds[s + nj];
+        w.ds[s + pj] = dp * c * c + dn * sn * sn;
+        w.ds[s + nj] = dp * sn * sn + dn * c * c;
+      }
+      pj = nj;
+    }
+    s_ng = ng;
+  }
+  __syncthreads();
+  // ---- compact non-deflated (poles, weights, slots, block-structure groups)
+  //      and deflated (slots, values) lists
+  unsigned long long pk = 0;
+  int n5 = 0;
+  for (int i = b0; i < b1; ++i) {
+    const int t = w.typ[s + i];
+    if (t <= 3) pk += 1ull << (21 * (t == 1 ? 0 : t == 2 ? 1 : 2));
+    n5 += (t == 5);
+  }
+  unsigned long long ptot, t5;
+  unsigned long long pre = block_scan64(pk, &ptot);
+  int r5 = (int)block_scan64((unsigned long long)n5, &t5);
+  const int c1 = (int)(ptot & 0x1fffff), c2 = (int)((ptot >> 21) & 0x1fffff),
+            c3 = (int)((ptot >> 42) & 0x1fffff);
+  const int K = c1 + c2 + c3;
+  const int nrot = (int)t5;
+  int r1 = (int)(pre & 0x1fffff), r2 = (int)((pre >> 21) & 0x1fffff),
+      r3 = (int)((pre >> 42) & 0x1fffff);
+  for (int i = b0; i < b1; ++i) {
+    const int t = w.typ[s + i];
+    const int j = r1 + r2 + r3;  // non-deflated before position i
+    if (t <= 3) {
+      w.dl[s + j] = w.ds[s + i];
+      w.zw[s + j] = w.zs[s + i];
+      w.ndslot[s + j] = w.srt[s + i];
+      w.grp[s + j] = (t == 1) ? r1 : (t == 2) ? c1 + r2 : c1 + c2 + r3;
+      if (t == 1) ++r1; else if (t == 2) ++r2; else ++r3;
+    } else {
+      const int a = i - j;  // deflated before position i
+      const int slot = w.srt[s + i];
+      const double v = w.ds[s + i];
+      Dp[slot] = v;
+      if (t == 5) {
+        w.l2slot[s + r5] = slot; w.l2val[s + r5] = v; ++r5;
+      } else {
+        const int a1 = a - r5;  // small-z deflated before position i
+        w.l1slot[s + a1] = slot; w.l1val[s + a1] = v;
+      }
+    }
+  }
+  __syncthreads();
+  // The small-z list is ascending; rotated poles moved inside their gap
+  // (mdlaed2.f90:340-356 inserts them in order), so sort those and merge.
+  if (nrot > 1) block_sort_pairs(w.l2val + s, w.l2slot + s, w.ds + s, w.cand + s, nrot);
+  const int n1l = (n - K) - nrot;
+  for (int i = tid; i < n1l; i += MT) {  // L1 element: count L2 < v
+    const double v = w.l1val[s + i];
+    int lo = 0, hi = nrot;
+    while (lo < hi) { int md = (lo + hi) >> 1; if (w.l2val[s + md] < v) lo = md + 1; else hi = md; }
+    w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = w.l1slot[s + i];
+  }
+  for (int i = tid; i < nrot; i += MT) {  // L2 element: count L1 <= v
+    const double v = w.l2val[s + i];
+    int lo = 0, hi = n1l;
+    while (lo < hi) { int md = (lo + hi) >> 1; if (w.l1val[s + md] <= v) lo = md + 1; else hi = md; }
+    w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = w.l2slot[s + i];
+  }
+  if (tid == 0) {
+    out[5 * m] = K; out[5 * m + 1] = s_ng; out[5 * m + 2] = c1; out[5 * m + 3] = c2;
+    out[5 * m + 4] = c3;
+    orho[m] = rho;
+  }
+}
+
+// Apply each merge's Givens rotations, in order, to its slot pairs: one thread
+// per row (rows of a block are independent; columns are read coalesced).
+__global__ void k_givens(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+                         const int *__restrict__ ng, const LevelScratch w, double *Q,
+                         long long ldq) {
+  const int m = blockIdx.y;
+  const int s = ms[m], n = mn[m], g = ng[m];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n || g == 0) return;
+  const long long row = s + r;
+  for (int t = 0; t < g; ++t) {
+    const long long p = w.gvp[s + t], q = w.gvq[s + t];
+    const double c = w.gvc[s + t], sn = w.gvs[s + t];
+    const double x = Q[p * ldq + row], y = Q[q * ldq + row];
+    Q[p * ldq + row] = c * x + sn * y;
+    Q[q * ldq + row] = c * y - sn * x;
+  }
+}
+
+// Copy the K non-deflated columns of merge m into a dense n_m x K buffer
+// (column `grp` when grouped, else column j).  One CTA per (column, row chunk).
+__global__ void k_gather(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+                         const int *__restrict__ rootoff, const int *__restrict__ ndslot,
+                         const int *__restrict__ grp, const long long *__restrict__ boff,
+                         const double *__restrict__ Q, long long ldq, double *__restrict__ B) {
+  const int r = blockIdx.x;
+  if (r >= rootoff[P]) return;
+  int lo = 0, hi = P;
+  while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (rootoff[mid] <= r) lo = mid; else hi = mid; }
+  const int m = lo, j = r - rootoff[m];
+  const int s = ms[m], n = mn[m];
+  const int col = grp ? grp[s + j] : j;
+  const double *src = Q + (long long)ndslot[s + j] * ldq + s;
+  double *dst = B + boff[m] + (long long)col * n;
+  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x)
+    dst[i] = src[i];
+}
+
+// Write the new eigenvectors (columns of T, n_m x K) into the non-deflated slots.
+__global__ void k_scatter(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+                          const int *__restrict__ rootoff, const int *__restrict__ ndslot,
+                          const long long *__restrict__ toff, const double *__restrict__ T,
+                          double *__restrict__ Q, long long ldq) {
+  const int r = blockIdx.x;
+  if (r >= rootoff[P]) return;
+  int lo = 0, hi = P;
+  while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (rootoff[mid] <= r) lo = mid; else hi = mid; }
+  const int m = lo, j = r - rootoff[m];
+  const int s = ms[m], n = mn[m];
+  const double *src = T + toff[m] + (long long)j * n;
+  double *dst = Q + (long long)ndslot[s + j] * ldq + s;
+  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x)
+    dst[i] = src[i];
+}
+
+// New ascending order of each merged block: roots (ascending) merged with the
+// deflated eigenvalues (ascending), roots first on ties (DLAMRG at
+// mdlaed1.f90:221); eigenvalues of the rewritten slots are set to the roots.
+__global__ void __launch_bounds__(MT)
+k_merge_finish(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+               const int *__restrict__ mK, const double *__restrict__ lam,
+               const LevelScratch w, int *__restrict__ perm, double *__restrict__ Dp) {
+  const int m = blockIdx.x;
+  const int s = ms[m], n = mn[m], K = mK[m];
+  const int nd = n - K;
+  for (int j = threadIdx.x; j < K; j += MT) {
+    const double a = lam[s + j];
+    int lo = 0, hi = nd;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (w.dfval[s + mid] < a) lo = mid + 1; else hi = mid; }
+    const int slot = w.ndslot[s + j];
+    perm[s + j + lo] = slot;
+    Dp[slot] = a;
+  }
+  for (int a_ = threadIdx.x; a_ < nd; a_ += MT) {
+    const double b = w.dfval[s + a_];
+    int lo = 0, hi = K;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (lam[s + mid] <= b) lo = mid + 1; else hi = mid; }
+    perm[s + a_ + lo] = w.dfslot[s + a_];
+  }
+}
+
+// Final column permutation (mdlaed0.f90:355-362): Z(:, i) = Q(:, perm(i)),
+// w(i) = Dp(perm(i)).  One CTA per column.
+__global__ void k_final_gather(int n, const int *__restrict__ perm, const double *__restrict__ Dp,
+                               const double *__restrict__ Q, long long ldq, double *__restrict__ Z,
+                               long long ldz, double *__restrict__ wout) {
+  const int c = blockIdx.x;
+  if (c >= n) return;
+  const long long p = perm[c];
+  const double2 *src = reinterpret_cast<const double2 *>(Q + p * ldq);
+  double *dst = Z + (long long)c * ldz;
+  if ((ldq % 2 == 0) && (ldz % 2 == 0) && (n % 2 == 0)) {
+    double2 *d2 = reinterpret_cast<double2 *>(dst);
+    for (int i = threadIdx.x; i < n / 2; i += blockDim.x) d2[i] = src[i];
+  } else {
+    const double *s1 = Q + p * ldq;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = s1[i];
+  }
+  if (threadIdx.x == 0) wout[c] = Dp[p];
+}
+
+// ---------------------------------------------------------------- launch --
+void launch_merge_prepare(int P, const int *ms, const int *mn, const int *mn1, const double *e,
+                          const double *Q, long long ldq, double *Dp, int *perm,
+                          const LevelScratch &w, int *out, double *orho, cudaStream_t st) {
+  if (P > 0) k_merge_prepare<<<P, MT, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho);
+}
+void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
+                   const LevelScratch &w, double *Q, long long ldq, cudaStream_t st) {
+  if (P <= 0) return;
+  dim3 grid((maxn + 255) / 256, P);
+  k_givens<<<grid, 256, 0, st>>>(P, ms, mn, ng, w, Q, ldq);
+}
+void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
+                   const int *ndslot, const int *grp, const long long *boff, const double *Q,
+                   long long ldq, double *B, cudaStream_t st) {
+  if (total <= 0) return;
+  dim3 grid(total, (maxn + 1023) / 1024);
+  k_gather<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, grp, boff, Q, ldq, B);
+}
+void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
+                    const int *ndslot, const long long *toff, const double *T, double *Q,
+                    long long ldq, cudaStream_t st) {
+  if (total <= 0) return;
+  dim3 grid(total, (maxn + 1023) / 1024);
+  k_scatter<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, toff, T, Q, ldq);
+}
+void launch_merge_finish(int P, const int *ms, const int *mn, const int *mK, const double *lam,
+                         const LevelScratch &w, int *perm, double *Dp, cudaStream_t st) {
+  if (P > 0) k_merge_finish<<<P, MT, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp);
+}
+void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
+                         double *Z, long long ldz, double *wout, cudaStream_t st) {
+  if (n > 0) k_final_gather<<<n, 256, 0, st>>>(n, perm, Dp, Q, ldq, Z, ldz, wout);
+}
+
+}  // namespace hss

@@ -1,0 +1,405 @@
+// secular.cu -- secular equation, Loewner z-hat and eigenvector scalings on sm_103a.
+//
+// One warp solves one root of
+//     f(x) = 1/rho + sum_i z_i^2 / (d_i - x) = 0 ,   d_0 < d_1 < ... < d_{K-1},
+// (the DLAED4 calls of SRC/mdlaed3.f90:207-225).  The method is the "middle
+// way" rational iteration of R.-C. Li (1993) as analysed by Gu & Eisenstat
+// (1995): the sums left and right of the root are each replaced by a one-pole
+// rational model matching value and slope at the current iterate, and the
+// two-pole model equation is solved in closed form.  A bracket keeps every
+// iterate inside the pole interval; a step that leaves it is replaced by
+// bisection.  All arithmetic is FP64.  Lanes split the pole sums; the five
+// partial sums are combined by butterfly shuffles, so every lane holds
+// identical values and the scalar control flow is uniform across the warp.
+//
+// Positions are measured from the nearer pole ("origin") so that the gaps
+// d_i - x near the root keep full relative accuracy; DIFL/DIFR are formed from
+// those gaps exactly as LAPACK's DELTA output is used at mdlaed3.f90:215-216.
+#include "hss_common.cuh"
+#include "hss_kernels.h"
+
+namespace hss {
+
+struct SecSums {
+  double psi, dpsi, phi, dphi, eabs;
+};
+
+// Sums over i of z_i^2/(d_i - x) split at jl (psi: i <= jl, phi: i > jl),
+// their derivatives, and sum |z_i^2/(d_i - x)| for the rounding-error bound.
+// x = o + tau; every gap is formed as (d_i - o) - tau.
+__device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
+                                            const double *__restrict__ z, int K,
+                                            double o, double tau, int jl, int lane) {
+  double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0, e = 0.0;
+  for (int i = lane; i < K; i += HSS_WARP) {
+    const double zi = __ldg(z + i);
+    const double del = (__ldg(d + i) - o) - tau;
+    const double t = zi / del;
+    const double v = zi * t;
+    const double dv = t * t;
+    if (i <= jl) { a0 += v; a1 += dv; } else { b0 += v; b1 += dv; }
+    e += fabs(v);
+  }
+  SecSums s;
+  s.psi = warp_sum(a0); s.dpsi = warp_sum(a1);
+  s.phi = warp_sum(b0); s.dphi = warp_sum(b1);
+  s.eabs = warp_sum(e);
+  return s;
+}
+
+// Root of  c + A/(da - t) + B/(db - t) = 0  inside (lo, hi); returns false if
+// neither root of the equivalent quadratic lies there.
+__device__ __forceinline__ bool two_pole_root(double c, double A, double B, double da,
+                                              double db, double lo, double hi,
+                                              double &t) {
+  const double a2 = c;
+  const double a1 = -(c * (da + db) + A + B);
+  const double a0 = c * da * db + A * db + B * da;
+  double r1, r2;
+  if (a2 == 0.0) {
+    if (a1 == 0.0) return false;
+    r1 = r2 = -a0 / a1;
+  } else {
+    double disc = a1 * a1 - 4.0 * a2 * a0;
+    if (disc < 0.0) disc = 0.0;
+    const double q = -0.5 * (a1 + copysign(sqrt(disc), a1));
+    r1 = q / a2;
+    r2 = (q != 0.0) ? a0 / q : r1;
+  }
+  const bool ok1 = r1 > lo && r1 < hi, ok2 = r2 > lo && r2 < hi;
+  if (ok1 && ok2) {  // both inside: take the one nearer the bracket middle
+    const double m = 0.5 * (lo + hi);
+    t = fabs(r1 - m) <= fabs(r2 - m) ? r1 : r2;
+    return true;
+  }
+  if (ok1) { t = r1; return true; }
+  if (ok2) { t = r2; return true; }
+  return false;
+}
+
+struct RootOut {
+  double lam, difl, difr;
+  int iters;
+  int status;
+};
+
+// Solve root j of the secular equation with a full warp.  `guess` (>= 0 and
+// < 1 when valid) is a learned estimate of (lam_j - d_j)/(d_{j+1} - d_j); it only
+// replaces the initial iterate, the FP64 iteration always runs to convergence.
+__device__ RootOut secular_root(const double *__restrict__ d, const double *__restrict__ z,
+                                int K, double rho, int j, float guess, int lane) {
+  RootOut out;
+  out.iters = 0;
+  out.status = HSS_OK;
+  const double rhoinv = 1.0 / rho;
+  if (K == 1) {
+    const double zz = __ldg(z) * __ldg(z);
+    out.lam = __ldg(d) + rho * zz;
+    out.difl = rho * zz;
+    out.difr = 0.0;
+    return out;
+  }
+  const bool last = (j == K - 1);
+  const int jl = last ? K - 2 : j;  // left model pole
+  const int jr = jl + 1;            // right model pole
+  double o, tau, lo, hi, delta = 0.0;
+  bool have = false;
+  const double zl = __ldg(z + jl), zr = __ldg(z + jr);
+  if (!last) {
+    delta = __ldg(d + j + 1) - __ldg(d + j);
+    if (guess > 0.0f && guess < 1.0f) {
+      // learned position: origin at the nearer pole, bracket = whole interval
+      const double x = (double)guess * delta;
+      if (guess <= 0.5f) { o = __ldg(d + j); tau = x; lo = 0.0; hi = delta; }
+      else { o = __ldg(d + j + 1); tau = x - delta; lo = -delta; hi = 0.0; }
+      have = true;
+    } else {
+      o = __ldg(d + j);
+      const double tm = 0.5 * delta;
+      SecSums s = sec_eval(d, z, K, o, tm, jl, lane);
+      ++out.iters;
+      const double w = rhoinv + s.psi + s.phi;
+      const double gl = (__ldg(d + jl) - o) - tm, gr = (__ldg(d + jr) - o) - tm;
+      const double c = w - zl * (zl / gl) - zr * (zr / gr);
+      if (w >= 0.0) {  // root in (d_j, midpoint]
+        lo = 0.0; hi = tm;
+        have = two_pole_root(c, zl * zl, zr * zr, 0.0, delta, lo, hi, tau);
+        if (!have) tau = 0.5 * tm;
+      } else {         // root in (midpoint, d_{j+1}): measure from d_{j+1}
+        o = __ldg(d + j + 1);
+        lo = tm - delta; hi = 0.0;
+        have = two_pole_root(c, zl * zl, zr * zr, -delta, 0.0, lo, hi, tau);
+        if (!have) tau = 0.5 * lo;
+      }
+    }
+  } else {
+    // last root lies in (d_{K-1}, d_{K-1} + rho * |z|^2]
+    o = __ldg(d + K - 1);
+    double zs = 0.0;
+    for (int i = lane; i < K; i += HSS_WARP) zs += __ldg(z + i) * __ldg(z + i);
+    zs = warp_sum(zs);
+    const double top = rho * zs;
+    const double tm = 0.5 * top;
+    SecSums s = sec_eval(d, z, K, o, tm, jl, lane);
+    ++out.iters;
+    const double w = rhoinv + s.psi + s.phi;
+    const double gl = (__ldg(d + jl) - o) - tm, gr = (__ldg(d + jr) - o) - tm;
+    const double c = w - zl * (zl / gl) - zr * (zr / gr);
+    const double da = __ldg(d + jl) - o;
+    if (w >= 0.0) { lo = 0.0; hi = tm; } else { lo = tm; hi = top * (1.0 + 4.0 * HSS_EPS); }
+    have = two_pole_root(c, zl * zl, zr * zr, da, 0.0, lo, hi, tau);
+    if (!have) tau = 0.5 * (lo + hi);
+  }
+  // ---- middle-way iteration
+  const int MAXIT = 40;
+  bool conv = false;
+  for (int it = 0; it < MAXIT; ++it) {
+    SecSums s = sec_eval(d, z, K, o, tau, jl, lane);
+    ++out.iters;
+    const double w = rhoinv + s.psi + s.phi;
+    const double dw = s.dpsi + s.dphi;
+    const double erretm = 8.0 * s.eabs + 2.0 * rhoinv + 3.0 * fabs(tau) * dw;
+    if (fabs(w) <= HSS_EPS * erretm) { conv = true; break; }
+    if (w < 0.0) lo = fmax(lo, tau); else hi = fmin(hi, tau);
+    const double gl = (__ldg(d + jl) - o) - tau;
+    const double gr = (__ldg(d + jr) - o) - tau;
+    const double a = (gl + gr) * w - gl * gr * dw;
+    const double b = gl * gr * w;
+    const double c = w - gl * s.dpsi - gr * s.dphi;
+    double eta;
+    if (c == 0.0) {
+      eta = (a != 0.0) ? b / a : -w / dw;
+    } else {
+      double disc = a * a - 4.0 * b * c;
+      if (disc < 0.0) disc = 0.0;
+      eta = (a <= 0.0) ? (a - sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a + sqrt(disc));
+    }
+    if (w * eta >= 0.0) eta = -w / dw;  // model went the wrong way: Newton step
+    double tn = tau + eta;
+    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
+    const double step = tn - tau;
+    tau = tn;
+    if (!last) {  // keep the origin at the pole nearer the iterate
+      if (o == __ldg(d + j) && tau > 0.5 * delta) {
+        o = __ldg(d + j + 1); tau -= delta; lo -= delta; hi -= delta;
+      } else if (o == __ldg(d + j + 1) && tau < -0.5 * delta) {
+        o = __ldg(d + j); tau += delta; lo += delta; hi += delta;
+      }
+    }
+    if (fabs(step) <= 2.0 * HSS_EPS * fabs(tau) || hi - lo <= 2.0 * HSS_EPS * fabs(tau)) {
+      conv = true;
+      break;
+    }
+  }
+  if (!conv) out.status = HSS_SECULAR_NOCONV;
+  out.lam = o + tau;
+  out.difl = -((__ldg(d + j) - o) - tau);
+  out.difr = last ? 0.0 : -((__ldg(d + j + 1) - o) - tau);
+  return out;
+}
+
+// ------------------------------------------------------------- kernels -----
+// Batched over the merges of one DC level.  Merge m owns positions
+// [s[m], s[m] + K[m]) of the level arrays; rootoff is the prefix sum of K.
+__device__ __forceinline__ int find_merge(const int *__restrict__ off, int P, int r) {
+  int lo = 0, hi = P;  // off[lo] <= r < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= r) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_secular(LevelView lv, const double *__restrict__ dl,
+                          const double *__restrict__ zw, double *__restrict__ lam,
+                          double *__restrict__ difl, double *__restrict__ difr,
+                          int *__restrict__ iters, int *__restrict__ status,
+                          unsigned long long *__restrict__ itsum,
+                          const float *__restrict__ guess) {
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= __ldg(lv.rootoff + lv.P)) return;
+  const int m = find_merge(lv.rootoff, lv.P, r);
+  const int j = r - __ldg(lv.rootoff + m);
+  const int s = __ldg(lv.s + m);
+  const int K = __ldg(lv.K + m);
+  const float g = guess ? __ldg(guess + s + j) : -1.0f;
+  RootOut o = secular_root(dl + s, zw + s, K, __ldg(lv.rho + m), j, g, lane);
+  if (lane == 0) {
+    lam[s + j] = o.lam;
+    difl[s + j] = o.difl;
+    difr[s + j] = o.difr;
+    if (iters) iters[s + j] = o.iters;
+    if (itsum) atomicAdd(itsum, (unsigned long long)o.iters);
+    if (o.status) atomicMax(status, o.status);
+  }
+}
+
+// Loewner: z_hat_i^2 = prod_j (d_i - lam_j) / prod_{j != i} (d_i - d_j)
+// (SRC/mdlaed3.f90:217-230).  Numerators and denominators are multiplied
+// separately and renormalised by their binary exponents every 8 factors, so
+// there is one multiply per factor and no division in the O(K^2) loop.
+__global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
+                         const double *__restrict__ difl, const double *__restrict__ difr,
+                         const double *__restrict__ zw, double *__restrict__ zhat) {
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= __ldg(lv.rootoff + lv.P)) return;
+  const int m = find_merge(lv.rootoff, lv.P, r);
+  const int i = r - __ldg(lv.rootoff + m);
+  const int s = __ldg(lv.s + m);
+  const int K = __ldg(lv.K + m);
+  PoleDiff P{dl + s, difl + s, difr + s};
+  const double di = __ldg(dl + s + i);
+  double num = 1.0, den = 1.0;
+  int en = 0, ed = 0, cnt = 0;
+  for (int j = lane; j < K; j += HSS_WARP) {
+    num *= P.fd(i, j);
+    if (j != i) den *= (di - __ldg(dl + s + j));
+    if (++cnt == 8) {
+      int e;
+      num = frexp(num, &e); en += e;
+      den = frexp(den, &e); ed += e;
+      cnt = 0;
+    }
+  }
+  {
+    int e;
+    num = frexp(num, &e); en += e;
+    den = frexp(den, &e); ed += e;
+  }
+#pragma unroll
+  for (int ofs = 16; ofs > 0; ofs >>= 1) {
+    double on = __shfl_xor_sync(HSS_FULL, num, ofs);
+    double od = __shfl_xor_sync(HSS_FULL, den, ofs);
+    int oen = __shfl_xor_sync(HSS_FULL, en, ofs);
+    int oed = __shfl_xor_sync(HSS_FULL, ed, ofs);
+    int e;
+    num = frexp(num * on, &e); en += oen + e;
+    den = frexp(den * od, &e); ed += oed + e;
+  }
+  if (lane == 0) {
+    const double q = ldexp(fabs(num / den), en - ed);
+    zhat[s + i] = copysign(sqrt(q), __ldg(zw + s + i));
+  }
+}
+
+// alpha_j = 1 / || (z_hat_i / (d_i - lam_j))_i ||_2  (SRC/mdlaed3.f90:233-249).
+__global__ void k_alpha(LevelView lv, const double *__restrict__ dl,
+                        const double *__restrict__ difl, const double *__restrict__ difr,
+                        const double *__restrict__ zhat, double *__restrict__ alpha) {
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= __ldg(lv.rootoff + lv.P)) return;
+  const int m = find_merge(lv.rootoff, lv.P, r);
+  const int j = r - __ldg(lv.rootoff + m);
+  const int s = __ldg(lv.s + m);
+  const int K = __ldg(lv.K + m);
+  PoleDiff P{dl + s, difl + s, difr + s};
+  double acc = 0.0;
+  for (int i = lane; i < K; i += HSS_WARP) {
+    const double w = __ldg(zhat + s + i) / P.fd(i, j);
+    acc += w * w;
+  }
+  acc = warp_sum(acc);
+  if (lane == 0) alpha[s + j] = 1.0 / sqrt(acc);
+}
+
+// Dense eigenvector block of the rank-one update for the small-K merges
+// (LAPACK DLAED3's S, used at SRC/mdlaed1.f90:198-201): column j holds
+// z_hat_i / (d_i - lam_j) normalised to unit length.  Row i is written at
+// group position grp[s+i] (columns of Q2 grouped by block structure) of a
+// per-merge K x K column-major buffer starting at Sws + soff[m].
+__global__ void k_build_S(LevelView lv, const double *__restrict__ dl,
+                          const double *__restrict__ difl, const double *__restrict__ difr,
+                          const double *__restrict__ zhat, const int *__restrict__ grp,
+                          const long long *__restrict__ soff, double *__restrict__ Sws) {
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= __ldg(lv.rootoff + lv.P)) return;
+  const int m = find_merge(lv.rootoff, lv.P, r);
+  const int j = r - __ldg(lv.rootoff + m);
+  const int s = __ldg(lv.s + m);
+  const int K = __ldg(lv.K + m);
+  double *S = Sws + __ldg(soff + m) + (long long)j * K;
+  if (K == 1) {
+    if (lane == 0) S[0] = 1.0;
+    return;
+  }
+  PoleDiff P{dl + s, difl + s, difr + s};
+  double acc = 0.0;
+  for (int i = lane; i < K; i += HSS_WARP) {
+    const double w = __ldg(zhat + s + i) / P.fd(i, j);
+    S[__ldg(grp + s + i)] = w;
+    acc += w * w;
+  }
+  acc = warp_sum(acc);
+  const double a = 1.0 / sqrt(acc);
+  __syncwarp();
+  for (int i = lane; i < K; i += HSS_WARP) {
+    const int g = __ldg(grp + s + i);
+    S[g] *= a;
+  }
+}
+
+// Dense Cauchy-like block for the standalone API.
+__global__ void k_cauchy_eig(int K, const double *__restrict__ F, const double *__restrict__ u,
+                             const double *__restrict__ v, const double *__restrict__ difl,
+                             const double *__restrict__ difr, double *__restrict__ C) {
+  PoleDiff P{F, difl, difr};
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)K * K) return;
+  const int i = (int)(idx % K), j = (int)(idx / K);
+  C[idx] = __ldg(u + i) * __ldg(v + j) / P.fd(i, j);
+}
+
+__global__ void k_cauchylike(int M, int N, const double *__restrict__ D,
+                             const double *__restrict__ F, const double *__restrict__ u,
+                             const double *__restrict__ v, double *__restrict__ A) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)M * N) return;
+  const int i = (int)(idx % M), j = (int)(idx / M);
+  A[idx] = __ldg(u + i) * __ldg(v + j) / (__ldg(D + i) - __ldg(F + j));
+}
+
+// ---------------------------------------------------------------- launch --
+static inline int warp_grid(int total, int threads) {
+  return (int)(((long long)total * 32 + threads - 1) / threads);
+}
+void launch_secular(const LevelView &lv, int total, const double *dl, const double *zw,
+                    double *lam, double *difl, double *difr, int *iters, int *status,
+                    unsigned long long *itsum, const float *guess, cudaStream_t st) {
+  if (total <= 0) return;
+  k_secular<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,
+                                                   itsum, guess);
+}
+void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
+                   const double *difr, const double *zw, double *zhat, cudaStream_t st) {
+  if (total <= 0) return;
+  k_lowner<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zw, zhat);
+}
+void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
+                  const double *difr, const double *zhat, double *alpha, cudaStream_t st) {
+  if (total <= 0) return;
+  k_alpha<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, alpha);
+}
+void launch_build_S(const LevelView &lv, int total, const double *dl, const double *difl,
+                    const double *difr, const double *zhat, const int *grp,
+                    const long long *soff, double *Sws, cudaStream_t st) {
+  if (total <= 0) return;
+  k_build_S<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, grp, soff, Sws);
+}
+void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
+                       const double *difl, const double *difr, double *C, cudaStream_t st) {
+  const long long tot = (long long)K * K;
+  if (tot <= 0) return;
+  k_cauchy_eig<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(K, F, u, v, difl, difr, C);
+}
+void launch_cauchylike(int M, int N, const double *D, const double *F, const double *u,
+                       const double *v, double *A, cudaStream_t st) {
+  const long long tot = (long long)M * N;
+  if (tot <= 0) return;
+  k_cauchylike<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(M, N, D, F, u, v, A);
+}
+
+}  // namespace hss

@@ -1,0 +1,106 @@
+/*
+ * hsspack_gb300.h -- C ABI of the GB300 (sm_103a) HSS divide-and-conquer merge.
+ *
+ * Two layers:
+ *  1. Fortran drop-ins with the reference's argument lists (gfortran/ifort ABI:
+ *     lower-case name + '_', every argument by reference, a hidden size_t
+ *     length after the visible arguments for each CHARACTER argument).  All
+ *     arrays are host memory, column-major.  A Fortran caller links
+ *     libhsspack_gb300.so in place of libhsspack.a for these routines.
+ *  2. Device entry points (hss_*_dev) taking device pointers and a CUDA stream,
+ *     for C/C++ callers whose data already lives in HBM.
+ *
+ * Status convention (LAPACK): 0 = success, -i = bad i-th argument,
+ * > 0 = numerical failure; device-side failures are mapped into > 0 ranges and
+ * reported through hss_last_error().  Nothing here aborts the process.
+ */
+#ifndef HSSPACK_GB300_H
+#define HSSPACK_GB300_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ config ---- */
+typedef struct hss_config {
+  int hss_leaf;   /* HSS leaf block Ni (reference: 200, SRC/mdlaed3.f90:253)        */
+  int bsmlz;      /* merges with K >= bsmlz use HSS, else dense (mdlaed2.f90:175)    */
+  double tol;     /* HSS low-rank tolerance (reference: 1e-17, CauchyHssEig.f90:2523) */
+  int smlsiz;     /* DC leaf size, ILAENV(9) = 25 (mdlaed0.f90:188)                  */
+  int precision;  /* 0: FP64 products; 1: split-BF16 tensor-core products           */
+  int predictor;  /* 0: standard secular initial guess; 1: learned initial guess    */
+  int batched;    /* 1: one launch per stage per DC level; 0: launches per merge    */
+  int reserved[9];
+} hss_config;
+
+typedef struct hss_stats {
+  int n_levels, n_merges, n_hss_merges, n_dense_merges;
+  int max_k, max_rank;
+  long long total_k;            /* sum of secular sizes                     */
+  long long secular_iters;      /* sum over roots of iterations             */
+  long long secular_roots;      /* number of roots solved                   */
+  long long predictor_fallbacks;/* roots whose learned guess was rejected   */
+  long long kernel_launches;    /* kernels launched by the last call        */
+  double ms_total;              /* device time of the last call (events)    */
+  int reserved[8];
+} hss_stats;
+
+void hss_default_config(hss_config *cfg);
+void hss_set_config(const hss_config *cfg);      /* process-wide default */
+void hss_get_config(hss_config *cfg);
+void hss_get_stats(hss_stats *st);
+const char *hss_last_error(void);
+int hss_finalize(void);                           /* frees the device pool */
+
+/* ------------------------------------------ Fortran drop-ins (host) ---- */
+/* MDSTEDC(COMPZ,N,D,E,Z,LDZ,WORK,LWORK,IWORK,LIWORK,INFO)
+ * replaces SRC/mdstedc.f90:139.  COMPZ = 'I' runs the GPU merge; 'N' returns
+ * eigenvalues only; 'V' is rejected with INFO = -1 (the reference routes it
+ * through LAPACK DLAED7, outside the HSS path).  LWORK = -1 or LIWORK = -1 is
+ * a workspace query returning WORK(1) = 1+4N+N^2 and IWORK(1) = 3+5N as the
+ * reference does (mdstedc.f90:226-227). */
+void mdstedc_(const char *compz, const int *n, double *d, double *e, double *z,
+              const int *ldz, double *work, const int *lwork, int *iwork,
+              const int *liwork, int *info, size_t compz_len);
+
+/* Cauchylike(A,D,F,u,v,M,N): A(i,j) = u(i) v(j) / (D(i) - F(j)),
+ * replaces SRC/Cauchylike.f90:1 (computed on the GPU). */
+void cauchylike_(double *A, const double *D, const double *F, const double *u,
+                 const double *v, const int *m, const int *n);
+
+/* ------------------------------------------------ device entry points ---- */
+/* Whole tridiagonal eigensolve, COMPZ='I' semantics, all pointers in HBM.
+ * d(n) in: diagonal, out: eigenvalues ascending; e(n-1) off-diagonal
+ * (destroyed); z(ldz, n) out: eigenvectors.  stream may be NULL. */
+int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *stream);
+
+/* K secular roots of 1 + rho * sum_i z_i^2 / (dlamda_i - x) (the DLAED4 loop of
+ * SRC/mdlaed3.f90:207-225).  Outputs lam(K), difl(K) = lam_j - dlamda_j,
+ * difr(K) = lam_j - dlamda_{j+1} (difr(K-1) = 0), iters(K) (may be NULL).
+ * Returns 0 or the 1-based index of the first root that failed. */
+int hss_secular_dev(int k, const double *dlamda, const double *z, double rho,
+                    double *lam, double *difl, double *difr, int *iters,
+                    void *stream);
+
+/* Loewner rebuild of z and the column scalings alpha (SRC/mdlaed3.f90:228-249):
+ * z(K) in/out, alpha(K) out. */
+int hss_lowner_dev(int k, const double *dlamda, const double *difl,
+                   const double *difr, double *z, double *alpha, void *stream);
+
+/* DHSSEVC (SRC/CauchyHssEig.f90:2444): Q(0:nrows, 0:K) <- Q * C where
+ * C(i,j) = u_i v_j / (F_i - lam_j), lam_j = F_j + difl_j, compressed to HSS
+ * with leaf ni and tolerance tol.  Q is column-major with leading dim ldq. */
+int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u,
+                    const double *v, const double *difl, const double *difr,
+                    double *Q, int ldq, int nrows, void *stream);
+
+/* Dense Cauchy-like eigenvector block C(i,j) = u_i v_j / (F_i - lam_j) through
+ * DIFL/DIFR (SRC/CauchyHssEig.f90:1688, CauchylikeEig), k-by-k column-major. */
+int hss_cauchy_eig_dev(int k, const double *F, const double *u, const double *v,
+                       const double *difl, const double *difr, double *C,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -773,8 +773,14 @@ int secular_lowner(int K, const double *dlamda, double *z, double rho,
 #pragma omp atomic write
         err = jj;
       }
-      difl[j] = -delta[j];
-      difr[j] = (j + 1 < K) ? -delta[j + 1] : 0.0;
+      if (K > 2) {
+        difl[j] = -delta[j];
+        difr[j] = (j + 1 < K) ? -delta[j + 1] : 0.0;
+      } else {
+        // for N <= 2 LAPACK's DELTA holds eigenvector data, not d_i - lam
+        difl[j] = lam[j] - dlamda[j];
+        difr[j] = (j + 1 < K) ? lam[j] - dlamda[j + 1] : 0.0;
+      }
       lprod[j] *= delta[j];
       for (int i = 0; i < K; ++i)
         if (i != j) lprod[i] *= delta[i] / (dlamda[i] - dlamda[j]);

@@ -1,0 +1,93 @@
+"""Generate the golden fixtures in this directory (run from the repo root:
+``python tests/golden/make_golden.py``).
+
+* secular_mp.npz -- secular problems with roots computed to 50 digits by
+  bisection in mpmath (independent of LAPACK); the parity tests pin both the
+  oracle (LAPACK DLAED4) and the GPU solver against them.
+* dc_small.npz -- eigenvalues (and for n = 64 the eigenvectors) of seeded
+  tridiagonals from the oracle's restated MDSTEDC, cross-checked here against
+  LAPACK DSTEDC before they are written.
+* hss_grid.npz -- the interlacing Cauchy grid of TEST/testCauchyHss_serial.f90
+  (F_i = 0.1 + (2i-1)g, D_i = F_i + g) with random generators and a dense
+  product C @ B computed in numpy, for the standalone Cauchy/HSS APIs.
+
+The reference ships no golden vectors of its own (its test drivers only print
+errors against LAPACK), so these are the pins.
+"""
+import os
+import sys
+
+import mpmath as mp
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+import oracle  # noqa: E402
+from helpers import (eig_metrics, interlace_grid, rand_tridiag, secular_problem,  # noqa: E402
+                     toeplitz_tridiag)
+
+
+def mp_roots(d, z, rho, dps=50):
+    mp.mp.dps = dps
+    dm = [mp.mpf(float(x)) for x in d]
+    z2 = [mp.mpf(float(x)) ** 2 for x in z]
+    r = mp.mpf(float(rho))
+    K = len(d)
+
+    def f(x):
+        return 1 / r + mp.fsum(zz / (di - x) for di, zz in zip(dm, z2))
+
+    lam, difl, difr = [], [], []
+    for j in range(K):
+        lo = dm[j]
+        hi = dm[j + 1] if j + 1 < K else dm[j] + r * mp.fsum(z2)
+        for _ in range(190):
+            mid = (lo + hi) / 2
+            if f(mid) < 0:
+                lo = mid
+            else:
+                hi = mid
+        x = (lo + hi) / 2
+        lam.append(float(x))
+        difl.append(float(x - dm[j]))
+        difr.append(float(x - dm[j + 1]) if j + 1 < K else 0.0)
+    return np.array(lam), np.array(difl), np.array(difr)
+
+
+def main():
+    out = {}
+    for k, seed in [(3, 11), (40, 12), (200, 13)]:
+        d, z, rho = secular_problem(k, seed)
+        lam, difl, difr = mp_roots(d, z, rho)
+        out["k%d_d" % k], out["k%d_z" % k], out["k%d_rho" % k] = d, z, np.array(rho)
+        out["k%d_lam" % k], out["k%d_difl" % k], out["k%d_difr" % k] = lam, difl, difr
+    np.savez_compressed(os.path.join(HERE, "secular_mp.npz"), **out)
+
+    dc = {}
+    cases = [("rand64", rand_tridiag(64, seed=64)), ("rand200", rand_tridiag(200, seed=200)),
+             ("rand512", rand_tridiag(512, seed=512)), ("toep100", toeplitz_tridiag(100))]
+    for name, (d, e) in cases:
+        w, Q = oracle.eigh_tridiagonal(d, e, hss_leaf=64, bsmlz=40, tol=1e-14)
+        wl, _ = oracle.dstedc_lapack(d, e)
+        ev, res, orth = eig_metrics(d, e, w, Q, wl)
+        assert ev <= 1e-13 and res <= 1e-12 and orth <= 1e-12, (name, ev, res, orth)
+        dc[name + "_d"], dc[name + "_e"], dc[name + "_w"] = d, e, w
+        if len(d) == 64:
+            dc[name + "_Q"] = Q
+    np.savez_compressed(os.path.join(HERE, "dc_small.npz"), **dc)
+
+    n = 300
+    F, D = interlace_grid(n)
+    rng = np.random.default_rng(300)
+    u, v = rng.uniform(0, 1, n), rng.uniform(0, 1, n)
+    B = rng.uniform(0, 1, (n, 8))
+    C = u[:, None] * v[None, :] / (D[:, None] - F[None, :])
+    np.savez_compressed(os.path.join(HERE, "hss_grid.npz"), F=F, D=D, u=u, v=v, B=B, CB=C @ B)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,70 @@
+"""The C-ABI library: loads without a GPU, exports every function declared in
+include/hsspack_gb300.h, and handles argument checks and workspace queries
+(LAPACK conventions of SRC/mdstedc.f90:186-245) on the host."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+import hsspack_gb300 as hp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "hsspack_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b([a-z_][a-z0-9_]*)\s*\([^;{]*\)\s*;", src)
+    return sorted(set(n for n in names if n not in ("if", "sizeof")))
+
+
+def test_library_exports_every_declared_symbol():
+    L = hp.load()
+    names = declared_functions()
+    assert "mdstedc_" in names and "hss_mdstedc_dev" in names
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in hp.SIGNATURES, n
+
+
+def test_config_roundtrip():
+    old = hp.set_config(hss_leaf=64, tol=1e-14)
+    try:
+        c = hp.get_config()
+        assert c.hss_leaf == 64 and c.tol == 1e-14
+    finally:
+        hp.restore_config(old)
+    assert hp.get_config().hss_leaf == old.hss_leaf
+
+
+def _call(compz, n, ldz, lwork, liwork):
+    d = np.zeros(max(n, 1)); e = np.zeros(max(n, 1)); z = np.zeros((max(ldz, 1), max(n, 1)), order="F")
+    work = np.zeros(1); iwork = np.zeros(1, dtype=np.int32)
+    info = hp.mdstedc(compz, n, d, e, z, ldz, work, lwork, iwork, liwork)
+    return info, work[0], iwork[0]
+
+
+def test_mdstedc_workspace_query():
+    n = 1000
+    info, lw, liw = _call("I", n, n, -1, -1)
+    assert info == 0
+    assert lw == 1 + 4 * n + n * n and liw == 3 + 5 * n
+    info, lw, liw = _call("I", 20, 20, -1, -1)  # N <= SMLSIZ
+    assert info == 0 and lw == 2 * 19 and liw == 1
+
+
+def test_mdstedc_argument_errors():
+    assert _call("X", 10, 10, 1000, 1000)[0] == -1
+    assert _call("V", 10, 10, 1000, 1000)[0] == -1  # COMPZ='V' is outside the HSS path
+    assert _call("I", -1, 10, 1000, 1000)[0] == -2
+    assert _call("I", 10, 5, 1000, 1000)[0] == -6
+    assert _call("I", 100, 100, 10, 10000)[0] == -8
+    assert _call("I", 100, 100, 100000, 10)[0] == -10
+
+
+def test_mdstedc_quick_returns_without_gpu():
+    assert _call("I", 0, 1, 1, 1)[0] == 0
+    d = np.array([3.0]); e = np.zeros(1); z = np.zeros((1, 1), order="F")
+    info = hp.mdstedc("I", 1, d, e, z, 1, np.zeros(1), 1, np.zeros(1, dtype=np.int32), 1)
+    assert info == 0 and z[0, 0] == 1.0 and d[0] == 3.0

@@ -1,0 +1,87 @@
+"""GPU secular solver, Loewner formula and Cauchy blocks vs the CPU oracle
+(LAPACK DLAED4 and the restated MDLAED3 steps)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import hsspack_gb300 as hp
+from helpers import secular_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _solve(d, z, rho):
+    k = len(d)
+    lam, difl, difr = (torch.zeros(k, dtype=torch.float64, device="cuda") for _ in range(3))
+    it = torch.zeros(k, dtype=torch.int32, device="cuda")
+    hp.secular_dev(_dev(d), _dev(z), rho, lam, difl, difr, it)
+    return lam.cpu().numpy(), difl.cpu().numpy(), difr.cpu().numpy(), it.cpu().numpy()
+
+
+@pytest.mark.parametrize("k", [3, 40, 200])
+def test_secular_vs_50_digit_roots(k):
+    g = np.load(os.path.join(GOLD, "secular_mp.npz"))
+    d, z, rho = g["k%d_d" % k], g["k%d_z" % k], float(g["k%d_rho" % k])
+    lam, difl, difr, it = _solve(d, z, rho)
+    assert np.max(np.abs(lam - g["k%d_lam" % k])) <= 4e-16 * max(1.0, np.abs(d).max())
+    assert np.max(np.abs(difl - g["k%d_difl" % k]) / np.abs(g["k%d_difl" % k])) <= 1e-13
+    dr = g["k%d_difr" % k][:-1]
+    assert np.max(np.abs(difr[:-1] - dr) / np.abs(dr)) <= 1e-13
+
+
+@pytest.mark.parametrize("k,seed", [(1, 0), (2, 1), (3, 2), (50, 3), (1000, 4), (5000, 5)])
+def test_secular_vs_dlaed4(k, seed):
+    d, z, rho = secular_problem(k, seed)
+    lam_o, difl_o, difr_o = oracle.secular(d, z, rho)
+    lam, difl, difr, it = _solve(d, z, rho)
+    # parity bar: roots within 1e-13 * ||d||; DLAED4 itself is only that
+    # accurate on the last root (its stopping test is looser)
+    assert np.max(np.abs(lam - lam_o)) <= 1e-13 * max(1.0, np.abs(d).max())
+    rel = np.abs(difl - difl_o) / np.abs(difl_o)
+    assert np.max(rel) <= 1e-11, np.max(rel)
+    if k > 1:
+        rr = np.abs(difr[:-1] - difr_o[:-1]) / np.abs(difr_o[:-1])
+        assert np.max(rr) <= 1e-11, np.max(rr)
+    assert it.max() < 40
+
+
+@pytest.mark.parametrize("k", [10, 700])
+def test_lowner_alpha(k):
+    d, z, rho = secular_problem(k, 7)
+    lam, difl, difr = oracle.secular(d, z, rho)
+    zo, ao = oracle.lowner(d, difl, difr, z)
+    zz, al = _dev(z), torch.zeros(k, dtype=torch.float64, device="cuda")
+    hp.lowner_dev(_dev(d), _dev(difl), _dev(difr), zz, al)
+    assert np.max(np.abs(zz.cpu().numpy() - zo) / np.abs(zo)) <= 1e-12
+    assert np.max(np.abs(al.cpu().numpy() - ao) / np.abs(ao)) <= 1e-12
+
+
+def test_cauchy_eig_block_orthogonal():
+    k = 300
+    d, z, rho = secular_problem(k, 9)
+    lam, difl, difr = oracle.secular(d, z, rho)
+    zo, ao = oracle.lowner(d, difl, difr, z)
+    C = torch.zeros(k * k, dtype=torch.float64, device="cuda")
+    hp.cauchy_eig_dev(_dev(d), _dev(zo), _dev(ao), _dev(difl), _dev(difr), C)
+    Cg = C.cpu().numpy().reshape(k, k).T  # column-major storage
+    Co = oracle.cauchy_eig_dense(d, zo, ao, difl, difr)
+    assert np.max(np.abs(Cg - Co)) <= 1e-14
+    assert np.linalg.norm(Cg.T @ Cg - np.eye(k)) / k <= 1e-14
+
+
+def test_cauchylike_host_entry():
+    rng = np.random.default_rng(0)
+    D, F = rng.uniform(0, 1, 40), rng.uniform(2, 3, 30)
+    u, v = rng.standard_normal(40), rng.standard_normal(30)
+    A = hp.cauchylike(D, F, u, v)
+    assert np.allclose(A, u[:, None] * v[None, :] / (D[:, None] - F[None, :]), rtol=1e-15, atol=0)

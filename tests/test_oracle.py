@@ -1,0 +1,82 @@
+"""CPU tests of the oracle (the checker): pinned against LAPACK DSTEDC, the
+closed-form spectrum of TEST/Testedc.f90 (D = 2, E = 1), 50-digit secular
+roots and the committed golden fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import (eig_metrics, interlace_grid, rand_tridiag, secular_problem, toeplitz_eigs,
+                     toeplitz_tridiag)
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+EV_TOL, RES_TOL, ORTH_TOL = 1e-13, 1e-12, 1e-12
+
+
+@pytest.mark.parametrize("n,bsmlz,leaf", [(30, 1500, 200), (300, 1500, 200), (700, 60, 32),
+                                          (1024, 100, 64)])
+def test_oracle_vs_lapack_random(n, bsmlz, leaf):
+    d, e = rand_tridiag(n, seed=n)
+    w, Q = oracle.eigh_tridiagonal(d, e, hss_leaf=leaf, bsmlz=bsmlz, tol=1e-14)
+    wl, _ = oracle.dstedc_lapack(d, e)
+    ev, res, orth = eig_metrics(d, e, w, Q, wl)
+    assert ev <= EV_TOL and res <= RES_TOL and orth <= ORTH_TOL, (ev, res, orth)
+
+
+@pytest.mark.parametrize("n,bsmlz", [(500, 1500), (1000, 200), (2048, 600)])
+def test_oracle_toeplitz_closed_form(n, bsmlz):
+    d, e = toeplitz_tridiag(n)
+    w, Q = oracle.eigh_tridiagonal(d, e, hss_leaf=64, bsmlz=bsmlz, tol=1e-14)
+    assert np.max(np.abs(w - toeplitz_eigs(n))) <= 4 * EV_TOL
+    ev, res, orth = eig_metrics(d, e, w, Q, toeplitz_eigs(n))
+    assert res <= RES_TOL and orth <= ORTH_TOL
+    if bsmlz < n // 2:
+        assert oracle.stats()["n_hss_merges"] > 0
+
+
+def test_oracle_secular_vs_mp_roots():
+    g = np.load(os.path.join(GOLD, "secular_mp.npz"))
+    for k in (3, 40, 200):
+        d, z, rho = g["k%d_d" % k], g["k%d_z" % k], float(g["k%d_rho" % k])
+        lam, difl, difr = oracle.secular(d, z, rho)
+        assert np.max(np.abs(lam - g["k%d_lam" % k])) <= 1e-13
+        assert np.max(np.abs(difl - g["k%d_difl" % k]) / np.abs(g["k%d_difl" % k])) <= 1e-10
+
+
+def test_oracle_matches_golden_dc():
+    g = np.load(os.path.join(GOLD, "dc_small.npz"))
+    for name in ("rand64", "rand200", "rand512", "toep100"):
+        d, e = g[name + "_d"], g[name + "_e"]
+        w, Q = oracle.eigh_tridiagonal(d, e, hss_leaf=64, bsmlz=40, tol=1e-14)
+        assert np.max(np.abs(w - g[name + "_w"])) <= 1e-13
+        if name + "_Q" in g:
+            # eigenvectors up to sign
+            Qg = g[name + "_Q"]
+            s = np.sign(np.sum(Q * Qg, axis=0))
+            assert np.max(np.abs(Q * s - Qg)) <= 1e-12
+
+
+@pytest.mark.parametrize("k,ni,tol", [(600, 64, 1e-14), (1500, 128, 1e-17), (2000, 200, 1e-17)])
+def test_oracle_dhssevc_vs_dense(k, ni, tol):
+    d, z, rho = secular_problem(k, seed=k)
+    lam, difl, difr = oracle.secular(d, z, rho)
+    zh, alpha = oracle.lowner(d, difl, difr, z)
+    C = oracle.cauchy_eig_dense(d, zh, alpha, difl, difr)
+    assert np.linalg.norm(C.T @ C - np.eye(k)) / k <= 1e-14
+    rng = np.random.default_rng(k)
+    X = np.asfortranarray(rng.standard_normal((97, k)))
+    Y, rank = oracle.dhssevc(d, zh, alpha, difl, difr, X, ni=ni, tol=tol)
+    err = np.max(np.abs(Y - X @ C)) / np.max(np.abs(X @ C))
+    assert err <= 1e-12, err
+    assert 0 < rank <= 2 * ni  # parents compress the union of two child skeletons
+
+
+def test_cauchylike_grid_fixture():
+    g = np.load(os.path.join(GOLD, "hss_grid.npz"))
+    A = np.zeros((len(g["D"]), len(g["F"])))
+    F, D = interlace_grid(len(g["F"]))
+    assert np.array_equal(F, g["F"]) and np.array_equal(D, g["D"])
+    C = g["u"][:, None] * g["v"][None, :] / (g["D"][:, None] - g["F"][None, :])
+    assert np.allclose(C @ g["B"], g["CB"], rtol=1e-13, atol=0)
+    del A
