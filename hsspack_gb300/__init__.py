@@ -39,7 +39,7 @@ class Config(ctypes.Structure):
     _fields_ = [("hss_leaf", ctypes.c_int), ("bsmlz", ctypes.c_int), ("tol", ctypes.c_double),
                 ("smlsiz", ctypes.c_int), ("precision", ctypes.c_int),
                 ("predictor", ctypes.c_int), ("batched", ctypes.c_int),
-                ("reserved", ctypes.c_int * 9)]
+                ("profile", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -52,10 +52,19 @@ class Stats(ctypes.Structure):
                 ("total_k", ctypes.c_longlong), ("secular_iters", ctypes.c_longlong),
                 ("secular_roots", ctypes.c_longlong), ("predictor_fallbacks", ctypes.c_longlong),
                 ("kernel_launches", ctypes.c_longlong), ("ms_total", ctypes.c_double),
+                ("stage_ms", ctypes.c_double * 16), ("stage_calls", ctypes.c_longlong * 16),
+                ("stage_bytes", ctypes.c_longlong * 16), ("stage_flops", ctypes.c_double * 16),
                 ("reserved", ctypes.c_int * 8)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        for k in ("stage_ms", "stage_calls", "stage_bytes", "stage_flops"):
+            d[k] = {STAGES[i]: d[k][i] for i in range(len(STAGES))}
+        return d
+
+
+STAGES = ["leaf", "prepare", "givens", "secular", "lowner", "build_S", "gather", "gemm",
+          "scatter", "finish", "final_gather", "hss_build", "hss_multiply", "other"]
 
 
 _lib = None

@@ -35,8 +35,19 @@ struct Buf {
   size_t cap = 0;
 };
 
+struct TimedRange {
+  int stage;
+  cudaEvent_t a, b;
+  long long bytes;
+  double flops;
+};
+
 struct Ctx {
   std::recursive_mutex mu;
+  std::vector<cudaEvent_t> evpool;
+  size_t evused = 0;
+  std::vector<TimedRange> ranges;
+  cudaEvent_t open_ev[HSS_NSTAGE] = {};
   hss_config cfg;
   hss_stats stats;
   std::string err;
@@ -101,6 +112,45 @@ static void *pinned(Ctx &c, size_t bytes) {
 
 void *pool_get(const char *name, size_t bytes) { return buf<char>(ctx(), name, bytes); }
 
+static cudaEvent_t next_event(Ctx &c) {
+  if (c.evused == c.evpool.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c.evpool.push_back(e);
+  }
+  return c.evpool[c.evused++];
+}
+
+void stage_begin(int stage, void *st) {
+  Ctx &c = ctx();
+  if (!c.cfg.profile) return;
+  cudaEvent_t a = next_event(c);
+  CK(cudaEventRecord(a, (cudaStream_t)st));
+  c.open_ev[stage] = a;
+}
+
+void stage_end(int stage, void *st, long long bytes, double flops) {
+  Ctx &c = ctx();
+  c.stats.stage_bytes[stage] += bytes;
+  c.stats.stage_flops[stage] += flops;
+  if (!c.cfg.profile || !c.open_ev[stage]) return;
+  cudaEvent_t b = next_event(c);
+  CK(cudaEventRecord(b, (cudaStream_t)st));
+  c.ranges.push_back({stage, c.open_ev[stage], b, bytes, flops});
+  c.open_ev[stage] = nullptr;
+}
+
+static void collect_stage_times(Ctx &c) {
+  for (auto &r : c.ranges) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, r.a, r.b));
+    c.stats.stage_ms[r.stage] += ms;
+    c.stats.stage_calls[r.stage] += 1;
+  }
+  c.ranges.clear();
+  c.evused = 0;
+}
+
 template <class T>
 static void h2d(T *dst, const std::vector<T> &src, cudaStream_t st) {
   if (!src.empty()) CK(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st));
@@ -160,7 +210,14 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   h2d(dms, ms, st); h2d(dmn, mn, st); h2d(dmn1, mn1, st);
   int *dout = buf<int>(c, "g_out", 5 * P);
   double *drho = buf<double>(c, "g_rho", P);
+  stage_begin(HSS_ST_PREPARE, st);
   launch_merge_prepare(P, dms, dmn, dmn1, e, Q, ldq, Dp, perm, L.w, dout, drho, st);
+  {
+    long long nn = 0;
+    for (int x : mn) nn += x;
+    // merged order + z row gather + compaction: ~64 bytes per position
+    stage_end(HSS_ST_PREPARE, st, 64 * nn, 0.0);
+  }
   c.launches++;
   char *hp = (char *)pinned(c, (size_t)P * (5 * sizeof(int) + sizeof(double)));
   int *hout = (int *)hp;
@@ -207,7 +264,11 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     int *g1 = buf<int>(c, "gv_s", gs.size()), *g2 = buf<int>(c, "gv_n", gs.size()),
         *g3 = buf<int>(c, "gv_g", gs.size());
     h2d(g1, gs, st); h2d(g2, gn, st); h2d(g3, gng, st);
+    stage_begin(HSS_ST_GIVENS, st);
     launch_givens((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, st);
+    long long gb = 0;
+    for (size_t i = 0; i < gs.size(); ++i) gb += 32LL * gn[i] * gng[i];
+    stage_end(HSS_ST_GIVENS, st, gb, 0.0);
     c.launches++;
   }
   if (PA == 0) return;
@@ -219,9 +280,16 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   LevelView lv{vs, vK, vrho, voff, PA};
   const int total = aoff.back();
   c.stats.secular_roots += total;
+  double k2 = 0.0;
+  for (int K : aK) k2 += (double)K * K;
+  stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
                  (unsigned long long *)(status + 2), nullptr, st);
+  // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
+  stage_end(HSS_ST_SECULAR, st, 40LL * total, 8.0 * 4.0 * k2);
+  stage_begin(HSS_ST_LOWNER, st);
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st);
+  stage_end(HSS_ST_LOWNER, st, 40LL * total, 5.0 * k2);
   c.launches += 2;
   // ---- dense merges: S, gather, GEMM (block structured), scatter
   const int PD = (int)ds_.size();
@@ -236,9 +304,13 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     const int dtot = doff.back();
     double *Q2 = buf<double>(c, "Q2", q2tot), *T = buf<double>(c, "T", q2tot);
     double *S = buf<double>(c, "S", stot);
+    stage_begin(HSS_ST_BUILD_S, st);
     launch_build_S(dv, dtot, L.w.dl, L.difl, L.difr, L.zhat, L.w.grp, xso, S, st);
+    stage_end(HSS_ST_BUILD_S, st, 8LL * stot * 2, 0.0);
     int maxnd = *std::max_element(dn_.begin(), dn_.end());
+    stage_begin(HSS_ST_GATHER, st);
     launch_gather(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, L.w.grp, xq2, Q, ldq, Q2, st);
+    stage_end(HSS_ST_GATHER, st, 16LL * q2tot, 0.0);
     // GEMM problems: top rows use type 1,2 columns, bottom rows type 2,3
     std::vector<GemmDesc> probs;
     int tiles = 0;
@@ -259,8 +331,18 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     }
     GemmDesc *dprobs = buf<GemmDesc>(c, "gemm_probs", probs.size());
     h2d(dprobs, probs, st);
+    double fl = 0.0;
+    long long gbytes = 0;
+    for (auto &p : probs) {
+      fl += 2.0 * p.M * p.N * p.K;
+      gbytes += 8LL * ((long long)p.M * p.K + (long long)p.K * p.N + (long long)p.M * p.N);
+    }
+    stage_begin(HSS_ST_GEMM, st);
     launch_gemm_f64((int)probs.size(), tiles, dprobs, st);
+    stage_end(HSS_ST_GEMM, st, gbytes, fl);
+    stage_begin(HSS_ST_SCATTER, st);
     launch_scatter(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, xq2, T, Q, ldq, st);
+    stage_end(HSS_ST_SCATTER, st, 16LL * q2tot, 0.0);
     c.launches += 4;
   }
   // ---- HSS merges: one at a time (each has its own HSS tree)
@@ -272,11 +354,17 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     h.alpha = L.alpha + h.s; h.ndslot = L.w.ndslot + h.s;
     h.Q = Q; h.ldq = ldq;
     int rank = 0;
-    c.launches += hss_merge(h, &rank, st);
+    c.launches += hss_merge(h, &rank, st);  // times its own stages
     c.stats.max_rank = std::max(c.stats.max_rank, rank);
   }
   // ---- new ascending order and eigenvalues of the rewritten slots
+  stage_begin(HSS_ST_FINISH, st);
   launch_merge_finish(PA, vs, vn, vK, L.lam, L.w, perm, Dp, st);
+  {
+    long long nn = 0;
+    for (int x : an) nn += x;
+    stage_end(HSS_ST_FINISH, st, 24 * nn, 0.0);
+  }
   c.launches++;
 }
 
@@ -296,7 +384,13 @@ static void dc_block(Ctx &c, int n, const double *d, const double *e, double *Q,
   for (int i = 0, acc = 0; i < nl; ++i) { ls[i] = acc; acc += sz[i]; ends[i] = acc; }
   int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl);
   h2d(dls, ls, st); h2d(dlz, sz, st);
+  stage_begin(HSS_ST_LEAF, st);
   launch_leaf(nl, dls, dlz, n, d, e, Q, ldq, Dp, perm, status, st);
+  {
+    double fl = 0.0;
+    for (int x : sz) fl += 30.0 * x * x * x;
+    stage_end(HSS_ST_LEAF, st, 8LL * n * smlsiz, fl);
+  }
   c.launches++;
   LevelArrays L = level_arrays(c, n);
   while ((int)ends.size() > 1) {
@@ -424,7 +518,9 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
     fperm = buf<int>(c, "fperm", n);
     h2d(fperm, fp, st);
   }
+  stage_begin(HSS_ST_FINAL, st);
   launch_final_gather(n, fperm, Dp, Q, n, dz, ldz, dw, st);
+  stage_end(HSS_ST_FINAL, st, 16LL * n * n + 20LL * n, 0.0);
   c.launches++;
   CK(cudaEventRecord(ev1, st));
   int hst[4] = {0, 0, 0, 0};
@@ -438,6 +534,7 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   c.stats.ms_total = ms;
   c.stats.kernel_launches = c.launches;
+  collect_stage_times(c);
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   CK(cudaGetLastError());

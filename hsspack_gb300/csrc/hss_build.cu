@@ -1,4 +1,26 @@
-// hss_build.cu -- HSS path of a merge (interim: dense Cauchy-like product).
+// hss_build.cu -- HSS compression of the Cauchy-like eigenvector matrix and the
+// fast HSS multiply on sm_103a (DHSSEVC, SRC/CauchyHssEig.f90:2444-2598).
+//
+//   C(i,j) = u_i v_j / (F_i - lam_j),  lam_j = F_j + DIFL_j,   K x K
+//
+// Construction (Cauchy2hssEig_omp, :1945-2250) walks the HSS tree bottom-up.
+// At each level every node compresses its block row against all other
+// current columns, then its block column against all other current rows, by
+// a structured strong rank-revealing LU that only touches the O(M + N)
+// generators (rrluCauchyEig{row,col}, :7-467).  One CTA owns one node; all
+// nodes of a level run in one launch.  The node's own generators live in
+// shared memory, the "other side" generators (length up to K) in a private
+// global scratch slice that stays L2-resident.  Pivot searches are block-wide
+// argmax reductions with Fortran MAXLOC tie-breaking; every pivot decision is
+// FP64.  After each half-level a single-CTA kernel compacts the surviving
+// skeleton generators in the reference's order (:2140-2166, :2196-2227).
+//
+// Multiply (fastHssmmL_omp, SRC/ConstructHssd.f90:1394-1630): X (n x K) times
+// the HSS matrix, as grouped GEMMs per tree level: upsweep G = X U, sibling
+// products F = G B, downsweep F V, leaves Y = X D + F V.
+#include <algorithm>
+#include <climits>
+#include <cstring>
 #include <vector>
 
 #include "hss_common.cuh"
@@ -6,24 +28,749 @@
 #include "hss_hss.h"
 #include "hss_kernels.h"
 #include "hss_pool.h"
+#include "../../include/hsspack_gb300.h"
 
 namespace hss {
 
-#define HCK(x)                                                             \
-  do {                                                                     \
-    cudaError_t e_ = (x);                                                  \
+#define HCK(x)                                                                              \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
     if (e_ != cudaSuccess) throw HssError{std::string(#x) + ": " + cudaGetErrorString(e_)}; \
   } while (0)
 
-static LevelView single_view(int K, cudaStream_t st) {
-  int *v = pool<int>("hss_view", 4);
-  double *r = pool<double>("hss_view_rho", 1);
-  int hv[4] = {0, K, 0, K};
-  HCK(cudaMemcpyAsync(v, hv, sizeof hv, cudaMemcpyHostToDevice, st));
-  double one = 1.0;
-  HCK(cudaMemcpyAsync(r, &one, sizeof one, cudaMemcpyHostToDevice, st));
-  // s = v[0], K = v[1], rootoff = v[2..3]
-  return LevelView{v, v + 1, r, v + 2, 1};
+constexpr int HT = 256;        // threads per node CTA
+constexpr int HSS_RMIN = 256;  // rank capacity floor
+
+// ------------------------------------------------------------- host tree --
+// npart / n2tree / GetTreeInfo (SRC/aux_hss.f90:238-307, :737-827): nodes
+// 1..ltr in post order, parent[root] = 0, depth[root] = 0.
+struct HostTree {
+  int lm = 0, ltr = 0, lvl = 0, mmax = 0;
+  std::vector<int> m, parent, c1, c2, depth, leafstart;
+  std::vector<std::vector<int>> ttr;
+  bool leaf(int i) const { return c1[i] == 0 && c2[i] == 0; }
+  int sibling(int i) const { int p = parent[i]; return c1[p] == i ? c2[p] : c1[p]; }
+};
+
+static void perfect_tree(int n, int off, std::vector<int> &par) {
+  if (n == 1) { par[off + 1] = 0; return; }
+  int h = (n - 1) / 2;
+  perfect_tree(h, off, par);
+  perfect_tree(h, off + h, par);
+  par[off + h] = off + n; par[off + 2 * h] = off + n; par[off + n] = 0;
+}
+static void n2tree(int n, int off, std::vector<int> &par) {
+  if (n == 1) { par[off + 1] = 0; return; }
+  int p2 = 1;
+  while (p2 * 2 <= n) p2 *= 2;
+  int n1 = p2 - 1;
+  perfect_tree(n1, off, par);
+  n2tree(n - n1 - 1, off + n1, par);
+  par[off + n1] = off + n; par[off + n - 1] = off + n; par[off + n] = 0;
+}
+
+static HostTree make_tree(int K, int ni) {
+  HostTree t;
+  int lm = K / ni, mr = K % ni;
+  if (lm == 0) { lm = 1; t.m.assign(1, K); }
+  else {
+    t.m.assign(lm, ni);
+    if (mr >= ni / 2) { t.m.push_back(mr); ++lm; } else t.m[lm - 1] += mr;
+  }
+  t.lm = lm;
+  t.ltr = 2 * lm - 1;
+  t.parent.assign(t.ltr + 1, 0);
+  n2tree(t.ltr, 0, t.parent);
+  t.c1.assign(t.ltr + 1, 0); t.c2.assign(t.ltr + 1, 0);
+  for (int i = 1; i < t.ltr; ++i) {
+    int p = t.parent[i];
+    if (t.c1[p] == 0) t.c1[p] = i; else t.c2[p] = i;
+  }
+  t.depth.assign(t.ltr + 1, 0);
+  for (int i = t.ltr - 1; i >= 1; --i) t.depth[i] = t.depth[t.parent[i]] + 1;
+  int lvl = 0, p = 1;
+  while (p < t.ltr + 1) { p *= 2; ++lvl; }
+  t.lvl = lvl - 1;
+  t.ttr.assign(t.lvl + 1, {});
+  for (int j = 1; j < t.ltr; ++j) t.ttr[t.depth[j]].push_back(j);
+  t.leafstart.assign(t.ltr + 1, 0);
+  for (int i = 1, acc = 0, it = 0; i <= t.ltr; ++i)
+    if (t.leaf(i)) { t.leafstart[i] = acc; acc += t.m[it++]; }
+  t.mmax = *std::max_element(t.m.begin(), t.m.end());
+  return t;
+}
+
+// ------------------------------------------------------- device helpers --
+__device__ __forceinline__ ArgMax block_argmax(ArgMax a, ArgMax *red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  a = warp_argmax(a);
+  __syncthreads();
+  if (lane == 0) red[w] = a;
+  __syncthreads();
+  ArgMax r = red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = argmax_merge(r, red[i]);
+  return r;
+}
+
+__device__ __forceinline__ double warp_prod(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v *= __shfl_xor_sync(HSS_FULL, v, o);
+  return v;
+}
+
+// Node state shared by the row and column kernels.
+struct HssDev {
+  const double *FF, *DIFL, *DIFR;  // poles and root gaps (length K)
+  int K, ltr, rmax;
+  // current compressed generators (row side: U, PL; column side: V, PU)
+  double *U, *V;
+  int *PL, *PU;
+  double *Ut, *Vt;  // compaction temporaries
+  int *PLt, *PUt;
+  int *lr0, *lr1, *lc0, *lc1;    // per node ranges in the current arrays
+  int *Ur, *Uc, *Vr, *Vc, *Br, *Bc, *Dm;
+  double *Ug, *Vg, *Bg, *Dg;     // generator storage
+  long long ucap, vcap, bcap;    // per node capacity (doubles)
+  const long long *doff;         // leaf diagonal block offsets
+  double *oval;                  // per node "other side" scratch (values)
+  int *oidx;                     //                              (pole indices)
+  int *lda, *lca;                // current row / column counts
+  int *flag;                     // [0]: rank overflow, [1]: swap count
+};
+
+// Structured strong RRLU of one node (row or column case).  Node side (length
+// M) in shared memory, other side (length N) in global scratch.
+//   ROW:  C(i,j) = A_i V_j / (F_{PL_i} - lam_{PU_j})
+//   COL:  C(i,j) = A_i V_j / (lam_{PL_i} - F_{PU_j})
+// Returns Rk; on exit A/PL/F are permuted, Z holds the Schur row generators,
+// W the column generators of the interpolation block, PQ the row permutation.
+template <bool ROW>
+__device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, double *W, int *PL,
+                         int *PQ, double *V, int *PU, int M, int N, double tol, int rmax,
+                         int *overflow, int *nswap) {
+  __shared__ ArgMax red[HT / 32];
+  __shared__ int s_rk;
+  const int tid = threadIdx.x;
+  // row poles: ROW -> F values (old poles); COL -> lam values (index PL)
+  auto den = [&](int pl, int pu) -> double {  // C denominator for pole indices
+    return ROW ? P.fd(pl, pu) : -P.fd(pu, pl);
+  };
+  auto rowdiff = [&](int i, int j) -> double {  // row pole i minus row pole j
+    return ROW ? (F[i] - F[j]) : P.dd(PL[i], PL[j]);
+  };
+  for (int i = tid; i < M; i += HT) { Z[i] = A[i]; PQ[i] = i; }
+  if (tid == 0) s_rk = -1;
+  __syncthreads();
+  const int mn = min(M, N);
+  double Amax = 0.0;
+  auto colmax = [&](int k) -> int {
+    ArgMax a{-1.0, INT_MAX};
+    for (int i = k + tid; i < M; i += HT) {
+      const double t = fabs(Z[i] / den(PL[i], PU[k]));
+      if (t > a.v) { a.v = t; a.i = i; }
+    }
+    a = block_argmax(a, red);
+    return a.i == INT_MAX ? k : a.i;
+  };
+  auto colmax_v = [&](int k, int &arg) -> double {
+    ArgMax a{-1.0, INT_MAX};
+    for (int i = k + tid; i < M; i += HT) {
+      const double t = fabs(Z[i] / den(PL[i], PU[k]));
+      if (t > a.v) { a.v = t; a.i = i; }
+    }
+    a = block_argmax(a, red);
+    arg = a.i == INT_MAX ? k : a.i;
+    return a.v;
+  };
+  auto rowmax_v = [&](int k, int &arg) -> double {
+    ArgMax a{-1.0, INT_MAX};
+    for (int j = k + tid; j < N; j += HT) {
+      const double t = fabs(V[j] / den(PL[k], PU[j]));
+      if (t > a.v) { a.v = t; a.i = j; }
+    }
+    a = block_argmax(a, red);
+    arg = a.i == INT_MAX ? k : a.i;
+    return a.v;
+  };
+  auto swap_row = [&](int a, int b) {
+    __syncthreads();
+    if (tid == 0 && a != b) {
+      double t; int ti;
+      t = F[a]; F[a] = F[b]; F[b] = t;
+      t = Z[a]; Z[a] = Z[b]; Z[b] = t;
+      t = A[a]; A[a] = A[b]; A[b] = t;
+      ti = PL[a]; PL[a] = PL[b]; PL[b] = ti;
+      ti = PQ[a]; PQ[a] = PQ[b]; PQ[b] = ti;
+    }
+    __syncthreads();
+  };
+  auto swap_col = [&](int a, int b) {
+    __syncthreads();
+    if (tid == 0 && a != b) {
+      double t = V[a]; V[a] = V[b]; V[b] = t;
+      int ti = PU[a]; PU[a] = PU[b]; PU[b] = ti;
+    }
+    __syncthreads();
+  };
+  int Rk = mn;
+  for (int k = 0; k < mn; ++k) {
+    if (k >= rmax) {  // would exceed the generator capacity
+      if (tid == 0) atomicOr(overflow, 1);
+      Rk = k;
+      break;
+    }
+    {  // Gu's variant of complete pivoting (CauchyPivtEig, :571-680)
+      int jl, ju;
+      double jkL = colmax_v(k, jl);
+      double jkU = rowmax_v(k, ju);
+      jkL *= fabs(V[k]);
+      jkU *= fabs(Z[k]);
+      const double piv = fabs(Z[k] * V[k] / den(PL[k], PU[k]));
+      if (!(jkL <= piv && jkU <= piv)) {
+        bool fromcol = jkL > jkU;
+        for (int guard = 0; guard < 4 * (M + N) + 8; ++guard) {
+          if (fromcol) {
+            swap_row(k, jl);
+            rowmax_v(k, ju);
+            if (ju == k) break;
+            fromcol = false;
+          }
+          swap_col(k, ju);
+          jl = colmax(k);
+          if (jl == k) break;
+          fromcol = true;
+        }
+      }
+    }
+    __syncthreads();
+    double Ukk = Z[k] * V[k] / den(PL[k], PU[k]);
+    Amax = fmax(Amax, fabs(Ukk));
+    if (fabs(Ukk) < tol * Amax) {
+      // complete pivoting over the Schur complement (CauchyPivtEig_CP)
+      ArgMax best{-1.0, INT_MAX};
+      int bi_loc = k;
+      for (int j = k + tid; j < N; j += HT) {
+        double cm = -1.0;
+        int a = k;
+        for (int i = k; i < M; ++i) {
+          const double t = fabs(Z[i] / den(PL[i], PU[j]));
+          if (t > cm) { cm = t; a = i; }
+        }
+        const double t = fabs(cm * V[j]);
+        if (t > best.v) { best.v = t; best.i = j; bi_loc = a; }
+      }
+      __shared__ int s_bi;
+      ArgMax r = block_argmax(best, red);
+      const int bj = r.i == INT_MAX ? k : r.i;
+      if (tid == 0 && r.i == INT_MAX) s_bi = k;
+      __syncthreads();
+      if (r.i != INT_MAX && best.i == r.i && best.v == r.v) s_bi = bi_loc;
+      __syncthreads();
+      const int bi = s_bi;
+      swap_row(k, bi);
+      swap_col(k, bj);
+      Ukk = Z[k] * V[k] / den(PL[k], PU[k]);
+      Amax = fmax(Amax, fabs(Ukk));
+      if (fabs(Ukk) < tol * Amax) { Rk = k; break; }
+    }
+    // Schur-complement generator updates
+    const double Fk = ROW ? F[k] : 0.0;
+    for (int j = k + 1 + tid; j < M; j += HT)
+      Z[j] *= rowdiff(j, k) / den(PL[j], PU[k]);
+    for (int j = k + 1 + tid; j < N; j += HT)
+      V[j] *= ROW ? P.dd(PU[j], PU[k]) / (-P.fd(PL[k], PU[j]))
+                  : (__ldg(P.F + PU[j]) - __ldg(P.F + PU[k])) / P.fd(PU[j], PL[k]);
+    for (int j = tid; j < k; j += HT)
+      W[j] *= ROW ? (-P.fd(PL[j], PU[k])) / (Fk - F[j]) : P.fd(PU[k], PL[j]) / P.dd(PL[k], PL[j]);
+    if (tid < 32) {  // W[k] = den(k,k)/A[k] * prod_{j<k} ...
+      double pr = 1.0;
+      for (int j = tid; j < k; j += 32)
+        pr *= ROW ? (-P.fd(PL[k], PU[j])) / (F[j] - Fk) : P.fd(PU[j], PL[k]) / P.dd(PL[j], PL[k]);
+      pr = warp_prod(pr);
+      if (tid == 0) W[k] = (den(PL[k], PU[k]) / A[k]) * pr;
+    }
+    __syncthreads();
+    // strong swaps every 10 steps (searchMax2Eig[m], rho = 1.5)
+    if ((k + 1) % 10 == 0) {
+      for (int guard = 0; guard < M + 8; ++guard) {
+        ArgMax best{-1.0, INT_MAX};
+        int ii_loc = 0;
+        for (int j = tid; j <= k; j += HT) {
+          double cm = -1.0;
+          int a = k + 1;
+          for (int i = k + 1; i < M; ++i) {
+            const double t = fabs(Z[i] / rowdiff(i, j));
+            if (t > cm) { cm = t; a = i; }
+          }
+          const double t = cm * fabs(W[j]);
+          if (t > best.v) { best.v = t; best.i = j; ii_loc = a; }
+        }
+        __shared__ int s_jj;
+        ArgMax r = block_argmax(best, red);
+        if (tid == 0) s_jj = (r.i == INT_MAX) ? M : -1;
+        __syncthreads();
+        if (r.i != INT_MAX && best.i == r.i && best.v == r.v) s_jj = ii_loc;
+        __syncthreads();
+        const int ii = r.i == INT_MAX ? 0 : r.i, jj = s_jj;
+        if (!(r.v > 1.5) || jj >= M) break;
+        if (tid == 0) atomicAdd(nswap, 1);
+        for (int j = k + 1 + tid; j < N; j += HT)
+          V[j] *= ROW ? (-P.fd(PL[ii], PU[j])) / (-P.fd(PL[jj], PU[j]))
+                      : P.fd(PU[j], PL[ii]) / P.fd(PU[j], PL[jj]);
+        double ujj = 0.0, wii = 0.0;
+        if (tid < 32) {
+          double pu = 1.0, pw = 1.0;
+          for (int j = tid; j <= k; j += 32) {
+            if (j == ii) continue;
+            if (ROW) {
+              pu *= (F[ii] - F[j]) / P.fd(PL[ii], PU[j]);
+              pw *= (-P.fd(PL[jj], PU[j])) / (F[j] - F[jj]);
+            } else {
+              pu *= P.dd(PL[ii], PL[j]) / (-P.fd(PU[j], PL[ii]));
+              pw *= P.fd(PU[j], PL[jj]) / P.dd(PL[j], PL[jj]);
+            }
+          }
+          pu = warp_prod(pu);
+          pw = warp_prod(pw);
+          ujj = A[ii] * (rowdiff(ii, jj) / den(PL[ii], PU[ii])) * pu;
+          wii = (ROW ? P.fd(PL[jj], PU[ii]) : -P.fd(PU[ii], PL[jj])) / A[jj] * pw;
+        }
+        __syncthreads();
+        // Z, W updates use the pre-swap poles
+        double zn[(512 + HT - 1) / HT];
+        int cnt = 0;
+        for (int j = k + 1 + tid; j < M; j += HT, ++cnt)
+          zn[cnt] = (j != jj) ? Z[j] * (rowdiff(j, jj) / rowdiff(j, ii)) : Z[j];
+        double wn = 0.0;
+        if (tid <= k && tid != ii) wn = W[tid] * (rowdiff(tid, ii) / rowdiff(tid, jj));
+        double wn2[(256 + HT - 1) / HT];
+        int c2 = 0;
+        for (int j = tid + HT; j <= k; j += HT, ++c2)
+          wn2[c2] = (j != ii) ? W[j] * (rowdiff(j, ii) / rowdiff(j, jj)) : W[j];
+        __syncthreads();
+        cnt = 0;
+        for (int j = k + 1 + tid; j < M; j += HT, ++cnt) Z[j] = zn[cnt];
+        if (tid <= k && tid != ii) W[tid] = wn;
+        c2 = 0;
+        for (int j = tid + HT; j <= k; j += HT, ++c2) W[j] = wn2[c2];
+        if (tid == 0) {
+          Z[jj] = ujj;
+          W[ii] = wii;
+          int ti = PL[ii]; PL[ii] = PL[jj]; PL[jj] = ti;
+          ti = PQ[ii]; PQ[ii] = PQ[jj]; PQ[jj] = ti;
+          double t = F[ii]; F[ii] = F[jj]; F[jj] = t;
+          t = A[ii]; A[ii] = A[jj]; A[jj] = t;
+        }
+        __syncthreads();
+      }
+    }
+  }
+  return Rk;
+}
+
+// Row compression of every node of one level: node block row against all
+// other current columns (ComprcauchyEig 'r', :2338-2380).
+constexpr int MMAXS = 512;  // max rows of a node handled in shared memory
+
+__global__ void __launch_bounds__(HT)
+k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
+  __shared__ double F[MMAXS], A[MMAXS], Z[MMAXS], W[MMAXS];
+  __shared__ int PL[MMAXS], PQ[MMAXS], INV[MMAXS];
+  const int a = blockIdx.x;
+  if (a >= nn) return;
+  const int node = nodes[a];
+  const int tid = threadIdx.x;
+  const int r0 = h.lr0[node], M = h.lr1[node] - r0 + 1;
+  const int c0 = h.lc0[node], nc = h.lc1[node] - c0 + 1;
+  const int lca = *h.lca, N = lca - nc;
+  if (M > MMAXS) { if (tid == 0) atomicOr(h.flag, 2); return; }
+  double *V = h.oval + (long long)a * h.K;
+  int *PU = h.oidx + (long long)a * h.K;
+  for (int j = tid; j < lca; j += HT) {
+    if (j < c0) { V[j] = h.V[j]; PU[j] = h.PU[j]; }
+    else if (j > h.lc1[node]) { V[j - nc] = h.V[j]; PU[j - nc] = h.PU[j]; }
+  }
+  for (int i = tid; i < M; i += HT) {
+    A[i] = h.U[r0 + i];
+    PL[i] = h.PL[r0 + i];
+    F[i] = h.FF[PL[i]];
+    W[i] = 0.0;
+  }
+  __syncthreads();
+  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  int Rk = rrlu_node<true>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1);
+  __syncthreads();
+  for (int i = tid; i < M; i += HT) { h.U[r0 + i] = A[i]; h.PL[r0 + i] = PL[i]; INV[PQ[i]] = i; }
+  __syncthreads();
+  const int mn = min(M, N);
+  double *G = h.Ug + (long long)node * h.ucap;
+  if (Rk < mn) {
+    for (int idx = tid; idx < M * Rk; idx += HT) {
+      const int r = idx % M, j = idx / M, p = INV[r];
+      G[idx] = (p < Rk) ? (p == j ? 1.0 : 0.0) : Z[p] * W[j] / (F[p] - F[j]);
+    }
+  } else {
+    Rk = M;
+    if ((long long)M * M > h.ucap) { if (tid == 0) atomicOr(h.flag, 1); Rk = 0; }
+    else
+      for (int idx = tid; idx < M * M; idx += HT) {
+        const int r = idx % M, j = idx / M;
+        G[idx] = (INV[r] == j) ? 1.0 : 0.0;
+      }
+  }
+  if (tid == 0) { h.Ur[node] = M; h.Uc[node] = Rk; }
+}
+
+// Column compression: node block column against all other current rows
+// (ComprcauchyEig 'c', :2382-2430).  The transposed block has the node's
+// roots as row poles.
+__global__ void __launch_bounds__(HT)
+k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
+  __shared__ double F[MMAXS], A[MMAXS], Z[MMAXS], W[MMAXS];
+  __shared__ int PL[MMAXS], PQ[MMAXS], INV[MMAXS];
+  const int a = blockIdx.x;
+  if (a >= nn) return;
+  const int node = nodes[a];
+  const int tid = threadIdx.x;
+  const int c0 = h.lc0[node], M = h.lc1[node] - c0 + 1;  // node columns
+  const int r0 = h.lr0[node], nr = h.lr1[node] - r0 + 1;
+  const int lda = *h.lda, N = lda - nr;
+  if (M > MMAXS) { if (tid == 0) atomicOr(h.flag, 2); return; }
+  double *V = h.oval + (long long)a * h.K;
+  int *PU = h.oidx + (long long)a * h.K;
+  for (int j = tid; j < lda; j += HT) {
+    if (j < r0) { V[j] = h.U[j]; PU[j] = h.PL[j]; }
+    else if (j > h.lr1[node]) { V[j - nr] = h.U[j]; PU[j - nr] = h.PL[j]; }
+  }
+  for (int i = tid; i < M; i += HT) {
+    A[i] = h.V[c0 + i];
+    PL[i] = h.PU[c0 + i];
+    F[i] = 0.0;
+    W[i] = 0.0;
+  }
+  __syncthreads();
+  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  int Rk = rrlu_node<false>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1);
+  __syncthreads();
+  for (int i = tid; i < M; i += HT) { h.V[c0 + i] = A[i]; h.PU[c0 + i] = PL[i]; INV[PQ[i]] = i; }
+  __syncthreads();
+  const int mn = min(M, N);
+  double *G = h.Vg + (long long)node * h.vcap;
+  if (Rk < mn) {
+    for (int idx = tid; idx < Rk * M; idx += HT) {
+      const int i = idx % Rk, c = idx / Rk, p = INV[c];
+      G[idx] = (p < Rk) ? (p == i ? 1.0 : 0.0) : -W[i] * Z[p] / P.dd(PL[i], PL[p]);
+    }
+  } else {
+    Rk = M;
+    if ((long long)M * M > h.vcap) { if (tid == 0) atomicOr(h.flag, 1); Rk = 0; }
+    else
+      for (int idx = tid; idx < M * M; idx += HT) {
+        const int i = idx % M, c = idx / M;
+        G[idx] = (INV[c] == i) ? 1.0 : 0.0;
+      }
+  }
+  if (tid == 0) { h.Vr[node] = Rk; h.Vc[node] = M; }
+}
+
+// Compact the surviving generators: skeletons of this level's nodes (in level
+// order), then the untouched leaves of the levels above (deepest first).
+// rows = true: U/PL/lr, else V/PU/lc.  Also sets the ranges of the parents at
+// the next level up once both halves are compacted.
+__global__ void k_hss_compact(HssDev h, const int *__restrict__ nodes, int nn,
+                              const int *__restrict__ above, int na,
+                              const int *__restrict__ parents, int np, int rows) {
+  __shared__ int off[1024 + 1];
+  const int tid = threadIdx.x;
+  int *r0 = rows ? h.lr0 : h.lc0, *r1 = rows ? h.lr1 : h.lc1;
+  const int *rk = rows ? h.Uc : h.Vr;
+  double *val = rows ? h.U : h.V, *tval = rows ? h.Ut : h.Vt;
+  int *idx = rows ? h.PL : h.PU, *tidx = rows ? h.PLt : h.PUt;
+  const int tot = nn + na;
+  if (tid == 0) {
+    int acc = 0;
+    for (int a = 0; a < tot; ++a) {
+      off[a] = acc;
+      const int node = a < nn ? nodes[a] : above[a - nn];
+      acc += a < nn ? rk[node] : (r1[node] - r0[node] + 1);
+    }
+    off[tot] = acc;
+  }
+  __syncthreads();
+  for (int a = 0; a < tot; ++a) {
+    const int node = a < nn ? nodes[a] : above[a - nn];
+    const int len = off[a + 1] - off[a], src = r0[node];
+    for (int i = tid; i < len; i += blockDim.x) {
+      tval[off[a] + i] = val[src + i];
+      tidx[off[a] + i] = idx[src + i];
+    }
+  }
+  __syncthreads();
+  const int total = off[tot];
+  for (int i = tid; i < total; i += blockDim.x) { val[i] = tval[i]; idx[i] = tidx[i]; }
+  __syncthreads();
+  if (tid == 0) {
+    for (int a = 0; a < tot; ++a) {
+      const int node = a < nn ? nodes[a] : above[a - nn];
+      r0[node] = off[a];
+      r1[node] = off[a + 1] - 1;
+    }
+    if (rows) *h.lda = total; else *h.lca = total;
+  }
+  __syncthreads();
+  if (!rows && tid == 0) {  // parents of the next level up: union of children
+    for (int a = 0; a < np; ++a) {
+      // parents[] lists (parent, child1, child2) triples
+      const int p = parents[3 * a], x = parents[3 * a + 1], y = parents[3 * a + 2];
+      h.lr0[p] = h.lr0[x]; h.lr1[p] = h.lr1[y];
+      h.lc0[p] = h.lc0[x]; h.lc1[p] = h.lc1[y];
+    }
+  }
+}
+
+// B generator of each node: skeleton rows of the node x skeleton columns of
+// its sibling (CauchyHssEig.f90:2230-2244).
+__global__ void k_hss_B(HssDev h, const int *__restrict__ pairs, int nn) {
+  const int a = blockIdx.x;
+  if (a >= nn) return;
+  const int node = pairs[2 * a], sib = pairs[2 * a + 1];
+  const int r0 = h.lr0[node], m = h.lr1[node] - r0 + 1;
+  const int c0 = h.lc0[sib], n = h.lc1[sib] - c0 + 1;
+  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  double *B = h.Bg + (long long)node * h.bcap;
+  if ((long long)m * n > h.bcap) { if (threadIdx.x == 0) atomicOr(h.flag, 1); return; }
+  for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
+    const int i = idx % m, j = idx / m;
+    B[idx] = h.U[r0 + i] * h.V[c0 + j] / P.fd(h.PL[r0 + i], h.PU[c0 + j]);
+  }
+  if (threadIdx.x == 0) { h.Br[node] = m; h.Bc[node] = n; }
+}
+
+// Leaf diagonal blocks from the original generators (CauchylikeEig, :2089-2100).
+__global__ void k_hss_leafD(HssDev h, const int *__restrict__ leaves, const int *__restrict__ lstart,
+                            const int *__restrict__ lsize, int nl, const double *__restrict__ u,
+                            const double *__restrict__ v) {
+  const int a = blockIdx.y;
+  if (a >= nl) return;
+  const int node = leaves[a], s = lstart[a], m = lsize[a];
+  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  double *D = h.Dg + h.doff[a];
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m * m; idx += gridDim.x * blockDim.x) {
+    const int i = idx % m, j = idx / m;
+    D[idx] = u[s + i] * v[s + j] / P.fd(s + i, s + j);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) h.Dm[node] = m;
+}
+
+__global__ void k_init_gens(int K, const double *__restrict__ u, const double *__restrict__ v,
+                            double *U, double *V, int *PL, int *PU) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < K) { U[i] = u[i]; V[i] = v[i]; PL[i] = i; PU[i] = i; }
+}
+
+// --------------------------------------------------------------- host ----
+template <class T>
+static T *up(const char *name, const std::vector<T> &v, cudaStream_t st) {
+  T *d = pool<T>(name, std::max<size_t>(v.size(), 1));
+  if (!v.empty()) HCK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  return d;
+}
+
+struct HssPlan {
+  HostTree t;
+  HssDev h;
+  std::vector<int> Uc, Ur, Vr, Vc, Br, Bc, Dm;
+  std::vector<long long> doff;
+  bool ok = true;
+  int max_rank = 0;
+};
+
+// Build the HSS generators on the device; on return the ranks are on the host.
+static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F, const double *u,
+                         const double *v, const double *difl, const double *difr, cudaStream_t st) {
+  int launches = 0;
+  pl.t = make_tree(K, ni);
+  const HostTree &t = pl.t;
+  const int ltr = t.ltr;
+  const int rmax = std::max(HSS_RMIN, t.mmax);
+  HssDev &h = pl.h;
+  h.FF = F; h.DIFL = difl; h.DIFR = difr;
+  h.K = K; h.ltr = ltr; h.rmax = rmax;
+  h.U = pool<double>("hs_U", K); h.V = pool<double>("hs_V", K);
+  h.PL = pool<int>("hs_PL", K); h.PU = pool<int>("hs_PU", K);
+  h.Ut = pool<double>("hs_Ut", K); h.Vt = pool<double>("hs_Vt", K);
+  h.PLt = pool<int>("hs_PLt", K); h.PUt = pool<int>("hs_PUt", K);
+  int *ints = pool<int>("hs_ints", (size_t)11 * (ltr + 1) + 8);
+  HCK(cudaMemsetAsync(ints, 0, sizeof(int) * ((size_t)11 * (ltr + 1) + 8), st));
+  int *q = ints;
+  h.lr0 = q; q += ltr + 1; h.lr1 = q; q += ltr + 1; h.lc0 = q; q += ltr + 1; h.lc1 = q; q += ltr + 1;
+  h.Ur = q; q += ltr + 1; h.Uc = q; q += ltr + 1; h.Vr = q; q += ltr + 1; h.Vc = q; q += ltr + 1;
+  h.Br = q; q += ltr + 1; h.Bc = q; q += ltr + 1; h.Dm = q; q += ltr + 1;
+  h.lda = q; h.lca = q + 1; h.flag = q + 2;
+  const long long rows_cap = std::max(t.mmax, 2 * rmax);
+  h.ucap = rows_cap * rmax;
+  h.vcap = rows_cap * rmax;
+  h.bcap = (long long)rmax * rmax;
+  h.Ug = pool<double>("hs_Ug", (size_t)(ltr + 1) * h.ucap);
+  h.Vg = pool<double>("hs_Vg", (size_t)(ltr + 1) * h.vcap);
+  h.Bg = pool<double>("hs_Bg", (size_t)(ltr + 1) * h.bcap);
+  size_t maxlev = 1;
+  for (int L = 1; L <= t.lvl; ++L) maxlev = std::max(maxlev, t.ttr[L].size());
+  h.oval = pool<double>("hs_oval", maxlev * K);
+  h.oidx = pool<int>("hs_oidx", maxlev * K);
+  // leaf ranges, diagonal blocks
+  std::vector<int> lr0(ltr + 1, 0), lr1(ltr + 1, -1), leaves, lstart, lsize;
+  std::vector<long long> doff;
+  long long dtot = 0;
+  for (int i = 1, it = 0; i <= ltr; ++i)
+    if (t.leaf(i)) {
+      lr0[i] = t.leafstart[i]; lr1[i] = t.leafstart[i] + t.m[it] - 1;
+      leaves.push_back(i); lstart.push_back(t.leafstart[i]); lsize.push_back(t.m[it]);
+      doff.push_back(dtot); dtot += (long long)t.m[it] * t.m[it];
+      ++it;
+    }
+  pl.doff = doff;
+  h.Dg = pool<double>("hs_Dg", dtot);
+  h.doff = up("hs_doff", doff, st);
+  HCK(cudaMemcpyAsync(h.lr0, lr0.data(), sizeof(int) * (ltr + 1), cudaMemcpyHostToDevice, st));
+  HCK(cudaMemcpyAsync(h.lr1, lr1.data(), sizeof(int) * (ltr + 1), cudaMemcpyHostToDevice, st));
+  HCK(cudaMemcpyAsync(h.lc0, lr0.data(), sizeof(int) * (ltr + 1), cudaMemcpyHostToDevice, st));
+  HCK(cudaMemcpyAsync(h.lc1, lr1.data(), sizeof(int) * (ltr + 1), cudaMemcpyHostToDevice, st));
+  int kk[2] = {K, K};
+  HCK(cudaMemcpyAsync(h.lda, kk, sizeof kk, cudaMemcpyHostToDevice, st));
+  k_init_gens<<<(K + 255) / 256, 256, 0, st>>>(K, u, v, h.U, h.V, h.PL, h.PU);
+  int *dleaves = up("hs_leaves", leaves, st), *dls = up("hs_ls", lstart, st),
+      *dlz = up("hs_lz", lsize, st);
+  {
+    dim3 g((t.mmax * t.mmax + 255) / 256, (unsigned)leaves.size());
+    k_hss_leafD<<<g, 256, 0, st>>>(h, dleaves, dls, dlz, (int)leaves.size(), u, v);
+  }
+  launches += 2;
+  // per level node lists (processing order)
+  for (int LL = t.lvl; LL >= 1; --LL) {
+    const std::vector<int> &nodes = t.ttr[LL];
+    std::vector<int> above, parents, pairs;
+    for (int LLt = LL - 1; LLt >= 1; --LLt)
+      for (int nd : t.ttr[LLt])
+        if (t.leaf(nd)) above.push_back(nd);
+    if (LL > 1)
+      for (int nd : t.ttr[LL - 1])
+        if (!t.leaf(nd)) { parents.push_back(nd); parents.push_back(t.c1[nd]); parents.push_back(t.c2[nd]); }
+    for (int nd : nodes) { pairs.push_back(nd); pairs.push_back(t.sibling(nd)); }
+    if (nodes.size() + above.size() > 1024) throw HssError{"HSS tree too wide"};
+    char nm[32];
+    snprintf(nm, sizeof nm, "hs_nodes%d", LL);
+    int *dn = up(nm, nodes, st);
+    snprintf(nm, sizeof nm, "hs_above%d", LL);
+    int *da = up(nm, above, st);
+    snprintf(nm, sizeof nm, "hs_par%d", LL);
+    int *dp = up(nm, parents, st);
+    snprintf(nm, sizeof nm, "hs_pairs%d", LL);
+    int *dpr = up(nm, pairs, st);
+    const int nn = (int)nodes.size();
+    k_hss_rows<<<nn, HT, 0, st>>>(h, dn, nn, tol);
+    k_hss_compact<<<1, 512, 0, st>>>(h, dn, nn, da, (int)above.size(), dp, 0, 1);
+    k_hss_cols<<<nn, HT, 0, st>>>(h, dn, nn, tol);
+    k_hss_compact<<<1, 512, 0, st>>>(h, dn, nn, da, (int)above.size(), dp, (int)parents.size() / 3, 0);
+    k_hss_B<<<nn, 256, 0, st>>>(h, dpr, nn);
+    launches += 5;
+  }
+  // ranks and dims to the host (one sync per HSS merge)
+  std::vector<int> hint((size_t)11 * (ltr + 1) + 8);
+  HCK(cudaMemcpyAsync(hint.data(), ints, sizeof(int) * hint.size(), cudaMemcpyDeviceToHost, st));
+  HCK(cudaStreamSynchronize(st));
+  auto seg = [&](int k) { return std::vector<int>(hint.begin() + (size_t)k * (ltr + 1), hint.begin() + (size_t)(k + 1) * (ltr + 1)); };
+  pl.Ur = seg(4); pl.Uc = seg(5); pl.Vr = seg(6); pl.Vc = seg(7); pl.Br = seg(8); pl.Bc = seg(9); pl.Dm = seg(10);
+  const int flag = hint[(size_t)11 * (ltr + 1) + 2];
+  pl.ok = (flag == 0);
+  for (int i = 1; i < ltr; ++i) pl.max_rank = std::max(pl.max_rank, std::max(pl.Uc[i], pl.Vr[i]));
+  return launches;
+}
+
+// Y (nrows x K, ldy) = X (nrows x K, ldx) * H, FP64 grouped GEMMs per level.
+static int hss_multiply(const HssPlan &pl, const double *X, long long ldx, int nrows, double *Y,
+                        long long ldy, cudaStream_t st, double *flops = nullptr,
+                        long long *bytes = nullptr) {
+  const HostTree &t = pl.t;
+  const HssDev &h = pl.h;
+  const int ltr = t.ltr;
+  int launches = 0;
+  auto launch = [&](std::vector<GemmDesc> &probs, const char *name) {
+    if (probs.empty()) return;
+    int tiles = 0;
+    for (auto &p : probs) {
+      p.tile0 = tiles;
+      tiles += gemm_tiles(p.M, p.N);
+      if (flops) *flops += 2.0 * p.M * p.N * p.K;
+      if (bytes) *bytes += 8LL * ((long long)p.M * p.K + (long long)p.K * p.N + (long long)p.M * p.N);
+    }
+    GemmDesc *d = up(name, probs, st);
+    launch_gemm_f64((int)probs.size(), tiles, d, st);
+    ++launches;
+  };
+  if (t.lm == 1) {
+    std::vector<GemmDesc> p{{X, h.Dg, Y, (int)ldx, pl.Dm[ltr], (int)ldy, nrows, pl.Dm[ltr], pl.Dm[ltr], 0, 0}};
+    launch(p, "hm_p0");
+    return launches;
+  }
+  std::vector<long long> lg(ltr + 1, 0), lf(ltr + 1, 0);
+  long long ncg = 0, ncf = 0;
+  for (int LL = t.lvl; LL >= 1; --LL)
+    for (int nd : t.ttr[LL]) { lg[nd] = ncg; ncg += pl.Uc[nd]; }
+  for (int LL = 1; LL <= t.lvl; ++LL)
+    for (int nd : t.ttr[LL]) { lf[nd] = ncf; ncf += pl.Bc[t.sibling(nd)]; }
+  double *G = pool<double>("hm_G", (size_t)nrows * std::max<long long>(ncg, 1));
+  double *Fm = pool<double>("hm_F", (size_t)nrows * std::max<long long>(ncf, 1));
+  auto Ug = [&](int nd) { return h.Ug + (long long)nd * h.ucap; };
+  auto Vg = [&](int nd) { return h.Vg + (long long)nd * h.vcap; };
+  auto Bg = [&](int nd) { return h.Bg + (long long)nd * h.bcap; };
+  // upsweep
+  for (int LL = t.lvl; LL >= 1; --LL) {
+    std::vector<GemmDesc> probs;
+    for (int nd : t.ttr[LL]) {
+      if (pl.Uc[nd] == 0) continue;
+      const double *A = t.leaf(nd) ? X + (long long)t.leafstart[nd] * ldx : G + lg[t.c1[nd]] * nrows;
+      const int lda = t.leaf(nd) ? (int)ldx : nrows;
+      probs.push_back({A, Ug(nd), G + lg[nd] * nrows, lda, pl.Ur[nd], nrows, nrows, pl.Uc[nd],
+                       pl.Ur[nd], 0, 0});
+    }
+    char nm[24];
+    snprintf(nm, sizeof nm, "hm_up%d", LL);
+    launch(probs, nm);
+  }
+  // downsweep: F_i (+)= G_sib B_sib ; F_children = F_i V_i
+  for (int LL = 1; LL <= t.lvl; ++LL) {
+    std::vector<GemmDesc> pb, pv;
+    for (int nd : t.ttr[LL]) {
+      const int sb = t.sibling(nd);
+      pb.push_back({G + lg[sb] * nrows, Bg(sb), Fm + lf[nd] * nrows, nrows, std::max(pl.Br[sb], 1),
+                    nrows, nrows, pl.Bc[sb], pl.Br[sb], LL == 1 ? 0 : 1, 0});
+      if (!t.leaf(nd))
+        pv.push_back({Fm + lf[nd] * nrows, Vg(nd), Fm + lf[t.c1[nd]] * nrows, nrows,
+                      std::max(pl.Vr[nd], 1), nrows, nrows, pl.Vc[nd], pl.Vr[nd], 0, 0});
+    }
+    char nm[24];
+    snprintf(nm, sizeof nm, "hm_b%d", LL);
+    launch(pb, nm);
+    snprintf(nm, sizeof nm, "hm_v%d", LL);
+    launch(pv, nm);
+  }
+  // leaves: Y_i = X_i D_i, then Y_i += F_i V_i
+  std::vector<GemmDesc> pd, pf;
+  int li = 0;
+  for (int nd = 1; nd < ltr; ++nd) {
+    if (!t.leaf(nd)) continue;
+    const int m = pl.Dm[nd];
+    const long long c0 = t.leafstart[nd];
+    pd.push_back({X + c0 * ldx, h.Dg + pl.doff[li], Y + c0 * ldy, (int)ldx, m, (int)ldy, nrows, m, m,
+                  0, 0});
+    pf.push_back({Fm + lf[nd] * nrows, Vg(nd), Y + c0 * ldy, nrows, std::max(pl.Vr[nd], 1), (int)ldy,
+                  nrows, pl.Vc[nd], pl.Vr[nd], 1, 0});
+    ++li;
+  }
+  launch(pd, "hm_d");
+  launch(pf, "hm_f");
+  return launches;
 }
 
 static void dense_product(int K, const double *F, const double *u, const double *v,
@@ -31,42 +778,68 @@ static void dense_product(int K, const double *F, const double *u, const double 
                           int nrows, double *Y, long long ldy, cudaStream_t st) {
   double *C = pool<double>("hss_denseC", (size_t)K * K);
   launch_cauchy_eig(K, F, u, v, difl, difr, C, st);
-  GemmDesc g{X, C, Y, (int)ldx, K, (int)ldy, nrows, K, K, 0, 0};
-  GemmDesc *dg = pool<GemmDesc>("hss_gemm1", 1);
-  HCK(cudaMemcpyAsync(dg, &g, sizeof g, cudaMemcpyHostToDevice, st));
+  std::vector<GemmDesc> g{{X, C, Y, (int)ldx, K, (int)ldy, nrows, K, K, 0, 0}};
+  GemmDesc *dg = up("hss_gemm1", g, st);
   launch_gemm_f64(1, gemm_tiles(nrows, K), dg, st);
 }
 
+static LevelView single_view(int K, cudaStream_t st) {
+  std::vector<int> hv{0, K, 0, K};
+  int *v = up("hss_view", hv, st);
+  std::vector<double> r{1.0};
+  double *rr = up("hss_view_rho", r, st);
+  return LevelView{v, v + 1, rr, v + 2, 1};
+}
+
 int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st) {
+  int launches = 0;
   LevelView lv = single_view(a.K, st);
   launch_alpha(lv, a.K, a.dl, a.difl, a.difr, a.zhat, a.alpha, st);
-  // gather the non-deflated columns into X (n x K)
   double *X = pool<double>("hss_X", (size_t)a.n * a.K);
   double *T = pool<double>("hss_T", (size_t)a.n * a.K);
-  int *dv = pool<int>("hss_gview", 4);
-  int hv[4] = {a.s, a.n, 0, a.K};
-  HCK(cudaMemcpyAsync(dv, hv, sizeof hv, cudaMemcpyHostToDevice, st));
-  long long *boff = pool<long long>("hss_boff", 1);
-  long long zero = 0;
-  HCK(cudaMemcpyAsync(boff, &zero, sizeof zero, cudaMemcpyHostToDevice, st));
-  // the gather/scatter kernels index the level arrays with s; pass ndslot - s
+  std::vector<int> hv{a.s, a.n, 0, a.K};
+  int *dv = up("hss_gview", hv, st);
+  std::vector<long long> z0{0};
+  long long *boff = up("hss_boff", z0, st);
   launch_gather(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, nullptr, boff, a.Q, a.ldq, X, st);
-  dense_product(a.K, a.dl, a.zhat, a.alpha, a.difl, a.difr, X, a.n, a.n, T, a.n, st);
+  launches += 2;
+  HssPlan pl;
+  stage_begin(HSS_ST_HSS_BUILD, st);
+  launches += hss_construct(pl, a.K, a.leaf, a.tol, a.dl, a.zhat, a.alpha, a.difl, a.difr, st);
+  stage_end(HSS_ST_HSS_BUILD, st, 0, 0.0);
+  if (pl.ok) {
+    stage_begin(HSS_ST_HSS_MM, st);
+    double fl = 0.0;
+    long long by = 0;
+    launches += hss_multiply(pl, X, a.n, a.n, T, a.n, st, &fl, &by);
+    stage_end(HSS_ST_HSS_MM, st, by, fl);
+    *rank = pl.max_rank;
+  } else {  // rank capacity exceeded: exact dense product
+    dense_product(a.K, a.dl, a.zhat, a.alpha, a.difl, a.difr, X, a.n, a.n, T, a.n, st);
+    launches += 2;
+    *rank = a.K;
+  }
   launch_scatter(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, boff, T, a.Q, a.ldq, st);
-  *rank = a.K;
-  return 5;
+  return launches + 1;
 }
 
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
                      long long ldq, int nrows, int *rank, cudaStream_t st) {
-  (void)ni; (void)tol; (void)precision;
+  (void)precision;
   double *T = pool<double>("hss_T", (size_t)nrows * K);
-  dense_product(K, F, u, v, difl, difr, Q, ldq, nrows, T, nrows, st);
+  HssPlan pl;
+  int launches = hss_construct(pl, K, ni, tol, F, u, v, difl, difr, st);
+  if (pl.ok) {
+    launches += hss_multiply(pl, Q, ldq, nrows, T, nrows, st);
+    *rank = pl.max_rank;
+  } else {
+    dense_product(K, F, u, v, difl, difr, Q, ldq, nrows, T, nrows, st);
+    *rank = K;
+  }
   HCK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), T, nrows * sizeof(double), nrows * sizeof(double), K,
                         cudaMemcpyDeviceToDevice, st));
-  *rank = K;
-  return 0;
+  return launches + 1;
 }
 
 }  // namespace hss

@@ -10,4 +10,8 @@ template <class T>
 inline T *pool(const char *name, size_t count) {
   return (T *)pool_get(name, count * sizeof(T));
 }
+// Stage timing hooks (active when hss_config.profile = 1): begin/end record
+// CUDA events on `st`; bytes/flops are the stage's algorithmic work.
+void stage_begin(int stage, void *st);
+void stage_end(int stage, void *st, long long bytes, double flops);
 }  // namespace hss

@@ -30,8 +30,16 @@ typedef struct hss_config {
   int precision;  /* 0: FP64 products; 1: split-BF16 tensor-core products           */
   int predictor;  /* 0: standard secular initial guess; 1: learned initial guess    */
   int batched;    /* 1: one launch per stage per DC level; 0: launches per merge    */
-  int reserved[9];
+  int profile;    /* 1: time every stage with CUDA events (hss_stats.stage_ms)      */
+  int reserved[8];
 } hss_config;
+
+/* stages timed when hss_config.profile = 1 */
+enum hss_stage {
+  HSS_ST_LEAF = 0, HSS_ST_PREPARE, HSS_ST_GIVENS, HSS_ST_SECULAR, HSS_ST_LOWNER,
+  HSS_ST_BUILD_S, HSS_ST_GATHER, HSS_ST_GEMM, HSS_ST_SCATTER, HSS_ST_FINISH,
+  HSS_ST_FINAL, HSS_ST_HSS_BUILD, HSS_ST_HSS_MM, HSS_ST_OTHER, HSS_NSTAGE = 16
+};
 
 typedef struct hss_stats {
   int n_levels, n_merges, n_hss_merges, n_dense_merges;
@@ -42,6 +50,10 @@ typedef struct hss_stats {
   long long predictor_fallbacks;/* roots whose learned guess was rejected   */
   long long kernel_launches;    /* kernels launched by the last call        */
   double ms_total;              /* device time of the last call (events)    */
+  double stage_ms[16];          /* per hss_stage device time (profile = 1)  */
+  long long stage_calls[16];    /* timed launches per stage                 */
+  long long stage_bytes[16];    /* algorithmic bytes moved per stage        */
+  double stage_flops[16];       /* algorithmic flops per stage              */
   int reserved[8];
 } hss_stats;
 
