@@ -224,6 +224,11 @@ def run_ours(args):
     clocks.start()
     ms, acc, launches, st = timed(args.steps, args.warmup, True, full_cfg)
     clk = clocks.stop()
+    if args.profile_only:  # solves only: the command the ncu launch list wraps
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "ms_per_step": ms, "launches": launches,
+                              "stages_ms": {k: v for k, v in acc["ms"].items() if v > 0}}))
+        return
     # plain GPU merge (per-merge launches), fewer steps
     ms_plain, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, plain_cfg)
     acc_chk = check_accuracy(torch, d, e, dw, Z, n)
@@ -319,6 +324,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run only the warmup + timed solves (for ncu launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
