@@ -88,6 +88,9 @@ SIGNATURES = {
     "hss_dhssevc_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, _V, _V, _V, _V,
                                        _V, _V, ctypes.c_int, ctypes.c_int, _V]),
     "hss_cauchy_eig_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V, _V]),
+    "hss_gemm_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _V, ctypes.c_int,
+                                    _V, ctypes.c_int, _V, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, _V]),
 }
 
 
@@ -257,6 +260,15 @@ def cauchy_eig_dev(F, u, v, difl, difr, C, stream=None):
                                    _stream(stream))
     if rc != 0:
         raise HssError("hss_cauchy_eig_dev rc=%d: %s" % (rc, _err()))
+    return rc
+
+
+def gemm_dev(A, B, C, m, n, k, lda, ldb, ldc, beta=0, precision=0, stream=None):
+    """C = A @ B (+ C) on column-major device buffers (FP64 or split-BF16)."""
+    rc = load().hss_gemm_dev(int(m), int(n), int(k), _ptr(A), int(lda), _ptr(B), int(ldb), _ptr(C),
+                             int(ldc), int(beta), int(precision), _stream(stream))
+    if rc != 0:
+        raise HssError("hss_gemm_dev rc=%d: %s" % (rc, _err()))
     return rc
 
 

@@ -329,8 +329,6 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
       probs.push_back(bot);
       ++di;
     }
-    GemmDesc *dprobs = buf<GemmDesc>(c, "gemm_probs", probs.size());
-    h2d(dprobs, probs, st);
     double fl = 0.0;
     long long gbytes = 0;
     for (auto &p : probs) {
@@ -338,7 +336,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
       gbytes += 8LL * ((long long)p.M * p.K + (long long)p.K * p.N + (long long)p.M * p.N);
     }
     stage_begin(HSS_ST_GEMM, st);
-    launch_gemm_f64((int)probs.size(), tiles, dprobs, st);
+    launch_gemm(probs, c.cfg.precision, st);
     stage_end(HSS_ST_GEMM, st, gbytes, fl);
     stage_begin(HSS_ST_SCATTER, st);
     launch_scatter(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, xq2, T, Q, ldq, st);
@@ -766,6 +764,39 @@ int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u,
   } catch (HssError &ex) {
     c.err = ex.msg;
     return 1000001;
+  }
+}
+
+int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B, int ldb,
+                 double *C, int ldc, int beta, int precision, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (k < 0) return -3;
+  if (lda < std::max(1, m)) return -5;
+  if (ldb < std::max(1, k)) return -7;
+  if (ldc < std::max(1, m)) return -9;
+  if (precision < 0 || precision > 1) return -11;
+  if (m == 0 || n == 0) return 0;
+  try {
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<GemmDesc> p{{A, B, C, lda, ldb, ldc, m, n, k, beta ? 1 : 0, 0}};
+    int *err = buf<int>(c, "gemm_err", 1);
+    CK(cudaMemsetAsync(err, 0, sizeof(int), st));
+    launch_gemm(p, precision, st);
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    if (herr) {
+      c.err = "tensor-core GEMM: bounded wait timed out";
+      return 1;
+    }
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
   }
 }
 

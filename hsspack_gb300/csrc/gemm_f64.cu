@@ -8,6 +8,7 @@
 // tile prefix.  All operands column-major.
 #include "hss_common.cuh"
 #include "hss_gemm.h"
+#include "hss_pool.h"
 
 namespace hss {
 
@@ -93,6 +94,21 @@ int gemm_tiles(int M, int N) { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
 void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaStream_t st) {
   if (nprob <= 0 || total_tiles <= 0) return;
   k_gemm_f64<<<total_tiles, GT, 0, st>>>(nprob, d_probs);
+}
+
+void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStream_t st) {
+  if (probs_in.empty()) return;
+  if (precision == 1) {
+    int *err = pool<int>("gemm_err", 1);
+    launch_gemm_split(probs_in, err, st);
+    return;
+  }
+  std::vector<GemmDesc> probs(probs_in);
+  int tiles = 0;
+  for (auto &p : probs) { p.tile0 = tiles; tiles += gemm_tiles(p.M, p.N); }
+  GemmDesc *d = pool<GemmDesc>("gemm_f64_probs", probs.size());
+  cudaMemcpyAsync(d, probs.data(), probs.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice, st);
+  launch_gemm_f64((int)probs.size(), tiles, d, st);
 }
 
 }  // namespace hss

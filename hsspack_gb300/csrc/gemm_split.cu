@@ -1,0 +1,454 @@
+// gemm_split.cu -- FP64-accurate GEMM on the BF16 tensor cores of sm_103a.
+//
+// C (M x N) = A (M x K) * B (K x N), all FP64 column-major, computed by error-
+// free splitting (Ozaki, Ogita, Oishi & Rump, "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59, 2012):
+//
+//   A_ik = 2^{e_i} sum_{s<S} a^s_ik 2^{-8(s+1)},  B_kj = 2^{f_j} sum_{t<S} b^t_kj 2^{-8(t+1)}
+//
+// with integer digits |a^s|, |b^t| <= 256 (exact in BF16), e_i / f_j the row /
+// column exponents.  Digit products are integers; for a group g = s + t the
+// partial sums over a K window of 128 stay below 2^24 for g <= 2, so the FP32
+// tensor-core accumulation is exact there; groups g >= 3 weigh <= 2^-24
+// relative and their FP32 rounding is below FP64 resolution.  The S(S+1)/2
+// digit-plane products with s + t < S are accumulated per group in TMEM and
+// folded into FP64 registers after each window:
+//
+//   C_ij = 2^{e_i + f_j} sum_g acc_g 2^{-8(g+2)}
+//
+// S = 6 digit planes give 48 significant bits (relative error ~2^-48 of
+// sum_k |A_ik||B_kj| bounds, i.e. ~3.5e-15).
+//
+// Kernels: k_split_a / k_split_b write the digit planes pre-tiled in the
+// tcgen05 shared-memory image (K-major, no swizzle, 8x16-byte core matrices),
+// so the GEMM stages each tile with one cp.async.bulk (TMA) copy.  k_gemm_tc:
+// one CTA per 128 x 64 output tile; one elected thread issues
+// tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) into TMEM, 4 warps drain TMEM
+// with tcgen05.ld and accumulate in FP64.  Every mbarrier wait is bounded; a
+// timeout sets an error flag and the CTA still frees its TMEM before exiting.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "hss_common.cuh"
+#include "hss_gemm.h"
+#include "hss_pool.h"
+
+namespace hss {
+
+constexpr int SP = 6;        // digit planes
+constexpr int TM = 128;      // output tile rows (tcgen05 M)
+constexpr int TN = 64;       // output tile cols (tcgen05 N)
+constexpr int TK = 64;       // K per staged chunk
+constexpr int KWIN = 128;    // exactness window for groups 0..2
+constexpr int ATILE = TM * TK * 2;  // bytes of one A digit-plane tile (16 KB)
+constexpr int BTILE = TN * TK * 2;  // bytes of one B digit-plane tile (8 KB)
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
+
+// ------------------------------------------------------------ splitting ---
+// byte offset of element (r, k) inside a K-major no-swizzle tile with R rows:
+// core matrix (r/8, k/8) is 128 contiguous bytes, rows of 16 bytes; core
+// matrices adjacent in K are R*16 bytes apart (LBO), in R 128 bytes (SBO).
+__device__ __forceinline__ int tile_off(int r, int k, int R) {
+  return ((k >> 3) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ void split_digits(double x, double scale, __nv_bfloat16 *dig) {
+  long long q = __double2ll_rn(x * scale);  // |q| < 2^62
+#pragma unroll
+  for (int s = 0; s < SP; ++s) {
+    const int sh = 54 - 8 * s;
+    const long long d = (q + (1ll << (sh - 1))) >> sh;
+    q -= d << sh;
+    dig[s] = __float2bfloat16_rn((float)d);
+  }
+}
+
+// exponent e with max|x| <= 2^e (frexp convention), 0 for an all-zero vector
+__device__ __forceinline__ int exp_of(double amax) {
+  if (amax == 0.0) return 0;
+  int e;
+  frexp(amax, &e);
+  return e;
+}
+
+// A: M x K (lda) -> planes [tile_m][tile_k][s] of TM x TK, row exponents.
+// One CTA per 128-row panel; pass 1 row max, pass 2 digits.
+__global__ void __launch_bounds__(256)
+k_split_a(const SplitProb *__restrict__ probs, int nprob) {
+  const SplitProb P = probs[blockIdx.y];
+  const int tm = blockIdx.x;
+  if (tm * TM >= P.rows) return;
+  __shared__ double smax[8][TM];
+  __shared__ double sscale[TM];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  // pass 1: each warp takes columns k = w, w+8, ...; lanes cover 4 x 32 rows
+  double mx[4] = {0, 0, 0, 0};
+  for (int k = w; k < P.inner; k += 8)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = tm * TM + q * 32 + lane;
+      if (r < P.rows) mx[q] = fmax(mx[q], fabs(P.src[(long long)k * P.ld + r]));
+    }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) smax[w][q * 32 + lane] = mx[q];
+  __syncthreads();
+  if (tid < TM) {
+    double m = 0.0;
+    for (int i = 0; i < 8; ++i) m = fmax(m, smax[i][tid]);
+    const int e = exp_of(m);
+    const int r = tm * TM + tid;
+    if (r < P.rows) P.expo[r] = e;
+    sscale[tid] = ldexp(1.0, 62 - e);
+  }
+  __syncthreads();
+  // pass 2: thread handles (row, 8 consecutive k) -> 16-byte rows of core matrices
+  const int nkt = (P.inner + TK - 1) / TK;
+  for (int kt = 0; kt < nkt; ++kt) {
+    char *tile = (char *)P.dst + ((long long)tm * P.ktiles + kt) * SP * ATILE;
+    for (int u = tid; u < TM * (TK / 8); u += 256) {
+      const int r = u % TM, k8 = u / TM;
+      const int gr = tm * TM + r;
+      __align__(16) __nv_bfloat16 dg[SP][8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int gk = kt * TK + k8 * 8 + c;
+        const double x = (gr < P.rows && gk < P.inner) ? P.src[(long long)gk * P.ld + gr] : 0.0;
+        __nv_bfloat16 d[SP];
+        split_digits(x, sscale[r], d);
+#pragma unroll
+        for (int s = 0; s < SP; ++s) dg[s][c] = d[s];
+      }
+#pragma unroll
+      for (int s = 0; s < SP; ++s)
+        *reinterpret_cast<uint4 *>(tile + s * ATILE + tile_off(r, k8 * 8, TM)) =
+            *reinterpret_cast<uint4 *>(dg[s]);
+    }
+  }
+}
+
+// B: K x N (ldb) -> planes [tile_n][tile_k][s] of TN x TK (K-major), column
+// exponents.  One CTA per 64-column panel.
+__global__ void __launch_bounds__(256)
+k_split_b(const SplitProb *__restrict__ probs, int nprob) {
+  const SplitProb P = probs[blockIdx.y];
+  const int tn = blockIdx.x;
+  if (tn * TN >= P.rows) return;
+  __shared__ double sscale[TN];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int c = w; c < TN; c += 8) {  // warp per column: max over k
+    const int gc = tn * TN + c;
+    double m = 0.0;
+    if (gc < P.rows)
+      for (int k = lane; k < P.inner; k += 32) m = fmax(m, fabs(P.src[(long long)gc * P.ld + k]));
+    m = warp_max(m);
+    if (lane == 0) {
+      const int e = exp_of(m);
+      if (gc < P.rows) P.expo[gc] = e;
+      sscale[c] = ldexp(1.0, 62 - e);
+    }
+  }
+  __syncthreads();
+  const int nkt = (P.inner + TK - 1) / TK;
+  for (int kt = 0; kt < nkt; ++kt) {
+    char *tile = (char *)P.dst + ((long long)tn * P.ktiles + kt) * SP * BTILE;
+    for (int u = tid; u < TN * (TK / 8); u += 256) {
+      const int c = u / (TK / 8), k8 = u % (TK / 8);
+      const int gc = tn * TN + c;
+      __align__(16) __nv_bfloat16 dg[SP][8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int gk = kt * TK + k8 * 8 + q;
+        const double x = (gc < P.rows && gk < P.inner) ? P.src[(long long)gc * P.ld + gk] : 0.0;
+        __nv_bfloat16 d[SP];
+        split_digits(x, sscale[c], d);
+#pragma unroll
+        for (int s = 0; s < SP; ++s) dg[s][q] = d[s];
+      }
+#pragma unroll
+      for (int s = 0; s < SP; ++s)
+        *reinterpret_cast<uint4 *>(tile + s * BTILE + tile_off(c, k8 * 8, TN)) =
+            *reinterpret_cast<uint4 *>(dg[s]);
+    }
+  }
+}
+
+// ------------------------------------------------------- PTX wrappers -----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  // base offset 0, relative LBO, swizzle none (bits 61-63 = 0)
+  return d;
+}
+
+// kind::f16 instruction descriptor: D FP32, A/B BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4)                     // D format FP32
+         | (1u << 7)                   // A format BF16
+         | (1u << 10)                  // B format BF16
+         | ((uint32_t)(N >> 3) << 17)  // N / 8
+         | ((uint32_t)(M >> 4) << 24); // M / 16
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// wait on phase parity, bounded by WAIT_NS of wall time; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  const uint64_t t0 = globaltimer_ns();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity));
+    if (done) return true;
+    if (globaltimer_ns() - t0 > WAIT_NS) return false;
+  }
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes));
+}
+
+// bulk (non-tensor) TMA copy global -> shared, completion on an mbarrier
+__device__ __forceinline__ void tma_load(void *sdst, const void *gsrc, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(sdst)),
+      "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                     uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------- GEMM ----
+struct TcProb {
+  const char *a_planes;  // [tm][kt][s] ATILE
+  const char *b_planes;  // [tn][kt][s] BTILE
+  const int *ea, *eb;    // row / column exponents
+  double *C;
+  int ldc, M, N, ktiles, beta;
+  int tile0;             // first flattened tile index
+};
+
+constexpr int GTH = 128;  // 4 warps: TMEM lanes 0..127
+// 16 KB of slack keeps every descriptor-addressed byte inside the allocation
+constexpr int SMEM_TC = SP * ATILE + SP * BTILE + 16384;
+
+__global__ void __launch_bounds__(GTH, 1)
+k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t bar_tma, bar_mma;
+  __shared__ uint32_t tmem_base;
+  // locate problem and tile
+  int lo = 0, hi = nprob;
+  const int b = blockIdx.x;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (probs[mid].tile0 <= b) lo = mid; else hi = mid;
+  }
+  const TcProb P = probs[lo];
+  const int t = b - P.tile0;
+  const int ntm = (P.M + TM - 1) / TM;
+  const int tm = t % ntm, tn = t / ntm;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *sa = smem;                   // SP A planes
+  unsigned char *sb = smem + SP * ATILE;      // SP B planes
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    mbar_init(&bar_tma, 1);
+    mbar_init(&bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tbase = tmem_base;
+  const uint32_t idesc = make_idesc(TM, TN);
+  double acc[TN];
+#pragma unroll
+  for (int j = 0; j < TN; ++j) acc[j] = 0.0;
+  uint32_t ph_tma = 0, ph_mma = 0;
+  bool ok = true;
+  const int kwin = KWIN / TK;  // chunks per exactness window
+  for (int kt0 = 0; kt0 < P.ktiles && ok; kt0 += kwin) {
+    const int kt1 = min(P.ktiles, kt0 + kwin);
+    for (int kt = kt0; kt < kt1; ++kt) {
+      // stage the SP A and SP B digit-plane tiles of this K chunk (TMA)
+      if (tid == 0) {
+        mbar_expect_tx(&bar_tma, SP * (ATILE + BTILE));
+        const char *ga = P.a_planes + ((long long)tm * P.ktiles + kt) * SP * ATILE;
+        const char *gb = P.b_planes + ((long long)tn * P.ktiles + kt) * SP * BTILE;
+        tma_load(sa, ga, SP * ATILE, &bar_tma);
+        tma_load(sb, gb, SP * BTILE, &bar_tma);
+      }
+      ok = __syncthreads_and(mbar_wait(&bar_tma, ph_tma));  // block-uniform
+      ph_tma ^= 1;
+      if (!ok) { if (tid == 0) atomicOr(err, 1); break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        // digit-plane products with s + t < SP into group accumulator g
+#pragma unroll 1
+        for (int kk = 0; kk < TK / 16; ++kk) {
+#pragma unroll 1
+          for (int s = 0; s < SP; ++s)
+#pragma unroll 1
+            for (int q = 0; q + s < SP; ++q) {
+              const int g = s + q;
+              const uint32_t aaddr = smem_u32(sa + s * ATILE) + kk * 2 * (TM * 16);
+              const uint32_t baddr = smem_u32(sb + q * BTILE) + kk * 2 * (TN * 16);
+              const uint64_t ad = make_desc(aaddr, TM * 16, 128);
+              const uint64_t bd = make_desc(baddr, TN * 16, 128);
+              // first product of this group in the window overwrites
+              const uint32_t accum = (kt > kt0 || kk > 0 || s > 0) ? 1u : 0u;
+              umma(tbase + g * TN, ad, bd, idesc, accum);
+            }
+        }
+        umma_commit(&bar_mma);
+      }
+      __syncwarp();
+      ok = __syncthreads_and(mbar_wait(&bar_mma, ph_mma));
+      ph_mma ^= 1;
+      if (!ok) { if (tid == 0) atomicOr(err, 2); break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (!ok) break;
+    // drain the group accumulators of this window into FP64
+    const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int g = 0; g < SP; ++g) {
+      const double w = ldexp(1.0, -8 * (g + 2));
+#pragma unroll
+      for (int c = 0; c < TN; c += 16) {
+        float v[16];
+        tmem_ld16(lane_addr + g * TN + c, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc[c + i] = fma((double)v[i], w, acc[c + i]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  // epilogue: C = 2^{e_i + f_j} acc (+ C)
+  const int r = tm * TM + tid;
+  if (ok && r < P.M) {
+    const int ei = P.ea[r];
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int c = tn * TN + j;
+      if (c < P.N) {
+        const double v = ldexp(acc[j], ei + P.eb[c]);
+        double *dst = P.C + (long long)c * P.ldc + r;
+        *dst = P.beta ? *dst + v : v;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512));
+}
+
+// ----------------------------------------------------------------- host ---
+void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStream_t st) {
+  if (probs.empty()) return;
+  // split every A and B operand
+  std::vector<SplitProb> sa, sb;
+  std::vector<TcProb> tc;
+  long long abytes = 0, bbytes = 0, ea = 0, eb = 0;
+  int maxtm = 0, maxtn = 0, tiles = 0;
+  for (const auto &p : probs) {
+    const int kt = (p.K + TK - 1) / TK;
+    const int ntm = (p.M + TM - 1) / TM, ntn = (p.N + TN - 1) / TN;
+    SplitProb a{p.A, p.lda, p.M, p.K, kt, nullptr, nullptr};
+    SplitProb bb{p.B, p.ldb, p.N, p.K, kt, nullptr, nullptr};
+    a.dst = (void *)abytes; a.expo = (int *)ea;
+    bb.dst = (void *)bbytes; bb.expo = (int *)eb;
+    abytes += (long long)ntm * kt * SP * ATILE;
+    bbytes += (long long)ntn * kt * SP * BTILE;
+    ea += ntm * TM;
+    eb += ntn * TN;
+    sa.push_back(a); sb.push_back(bb);
+    maxtm = std::max(maxtm, ntm); maxtn = std::max(maxtn, ntn);
+    TcProb t{nullptr, nullptr, nullptr, nullptr, p.C, p.ldc, p.M, p.N, kt, p.beta, tiles};
+    tiles += ntm * ntn;
+    tc.push_back(t);
+  }
+  char *A = pool<char>("gs_A", abytes + 1024), *B = pool<char>("gs_B", bbytes + 1024);
+  int *EA = pool<int>("gs_ea", ea + 1), *EB = pool<int>("gs_eb", eb + 1);
+  for (size_t i = 0; i < probs.size(); ++i) {
+    sa[i].dst = A + (long long)sa[i].dst; sa[i].expo = EA + (long long)sa[i].expo;
+    sb[i].dst = B + (long long)sb[i].dst; sb[i].expo = EB + (long long)sb[i].expo;
+    tc[i].a_planes = (const char *)sa[i].dst; tc[i].b_planes = (const char *)sb[i].dst;
+    tc[i].ea = sa[i].expo; tc[i].eb = sb[i].expo;
+  }
+  SplitProb *dsa = pool<SplitProb>("gs_sa", sa.size()), *dsb = pool<SplitProb>("gs_sb", sb.size());
+  TcProb *dtc = pool<TcProb>("gs_tc", tc.size());
+  cudaMemcpyAsync(dsa, sa.data(), sa.size() * sizeof(SplitProb), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dsb, sb.data(), sb.size() * sizeof(SplitProb), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dtc, tc.data(), tc.size() * sizeof(TcProb), cudaMemcpyHostToDevice, st);
+  k_split_a<<<dim3(maxtm, (unsigned)sa.size()), 256, 0, st>>>(dsa, (int)sa.size());
+  k_split_b<<<dim3(maxtn, (unsigned)sb.size()), 256, 0, st>>>(dsb, (int)sb.size());
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);
+    attr = true;
+  }
+  k_gemm_tc<<<tiles, GTH, SMEM_TC, st>>>(dtc, (int)tc.size(), d_err);
+}
+
+}  // namespace hss

@@ -689,24 +689,21 @@ static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F
 
 // Y (nrows x K, ldy) = X (nrows x K, ldx) * H, FP64 grouped GEMMs per level.
 static int hss_multiply(const HssPlan &pl, const double *X, long long ldx, int nrows, double *Y,
-                        long long ldy, cudaStream_t st, double *flops = nullptr,
+                        long long ldy, int precision, cudaStream_t st, double *flops = nullptr,
                         long long *bytes = nullptr) {
   const HostTree &t = pl.t;
   const HssDev &h = pl.h;
   const int ltr = t.ltr;
   int launches = 0;
   auto launch = [&](std::vector<GemmDesc> &probs, const char *name) {
+    (void)name;
     if (probs.empty()) return;
-    int tiles = 0;
     for (auto &p : probs) {
-      p.tile0 = tiles;
-      tiles += gemm_tiles(p.M, p.N);
       if (flops) *flops += 2.0 * p.M * p.N * p.K;
       if (bytes) *bytes += 8LL * ((long long)p.M * p.K + (long long)p.K * p.N + (long long)p.M * p.N);
     }
-    GemmDesc *d = up(name, probs, st);
-    launch_gemm_f64((int)probs.size(), tiles, d, st);
-    ++launches;
+    launch_gemm(probs, precision, st);
+    launches += precision ? 3 : 1;
   };
   if (t.lm == 1) {
     std::vector<GemmDesc> p{{X, h.Dg, Y, (int)ldx, pl.Dm[ltr], (int)ldy, nrows, pl.Dm[ltr], pl.Dm[ltr], 0, 0}};
@@ -779,8 +776,7 @@ static void dense_product(int K, const double *F, const double *u, const double 
   double *C = pool<double>("hss_denseC", (size_t)K * K);
   launch_cauchy_eig(K, F, u, v, difl, difr, C, st);
   std::vector<GemmDesc> g{{X, C, Y, (int)ldx, K, (int)ldy, nrows, K, K, 0, 0}};
-  GemmDesc *dg = up("hss_gemm1", g, st);
-  launch_gemm_f64(1, gemm_tiles(nrows, K), dg, st);
+  launch_gemm(g, 0, st);
 }
 
 static LevelView single_view(int K, cudaStream_t st) {
@@ -811,7 +807,7 @@ int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st) {
     stage_begin(HSS_ST_HSS_MM, st);
     double fl = 0.0;
     long long by = 0;
-    launches += hss_multiply(pl, X, a.n, a.n, T, a.n, st, &fl, &by);
+    launches += hss_multiply(pl, X, a.n, a.n, T, a.n, a.precision, st, &fl, &by);
     stage_end(HSS_ST_HSS_MM, st, by, fl);
     *rank = pl.max_rank;
   } else {  // rank capacity exceeded: exact dense product
@@ -826,12 +822,11 @@ int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st) {
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
                      long long ldq, int nrows, int *rank, cudaStream_t st) {
-  (void)precision;
   double *T = pool<double>("hss_T", (size_t)nrows * K);
   HssPlan pl;
   int launches = hss_construct(pl, K, ni, tol, F, u, v, difl, difr, st);
   if (pl.ok) {
-    launches += hss_multiply(pl, Q, ldq, nrows, T, nrows, st);
+    launches += hss_multiply(pl, Q, ldq, nrows, T, nrows, precision, st);
     *rank = pl.max_rank;
   } else {
     dense_product(K, F, u, v, difl, difr, Q, ldq, nrows, T, nrows, st);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace hss {
 
 // C (M x N, ldc) = A (M x K, lda) * B (K x N, ldb) [+ C if beta]; column-major.
@@ -15,7 +17,21 @@ struct GemmDesc {
   int tile0;  // first flattened tile index of this problem
 };
 
+// one operand of the split-BF16 GEMM: `rows` vectors of length `inner`
+// (A: rows of an M x K column-major matrix; B: columns of a K x N matrix)
+struct SplitProb {
+  const double *src;
+  int ld, rows, inner, ktiles;
+  void *dst;   // digit planes, pre-tiled
+  int *expo;   // per row / column exponent
+};
+
 int gemm_tiles(int M, int N);
 void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaStream_t st);
+// FP64-accurate products on the BF16 tensor cores (digit-plane splitting);
+// d_err receives 1/2 if a bounded wait timed out.
+void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStream_t st);
+// precision 0: FP64 CUDA cores, 1: split BF16 tensor cores
+void launch_gemm(const std::vector<GemmDesc> &probs, int precision, cudaStream_t st);
 
 }  // namespace hss

@@ -112,6 +112,14 @@ int hss_cauchy_eig_dev(int k, const double *F, const double *u, const double *v,
                        const double *difl, const double *difr, double *C,
                        void *stream);
 
+/* C(m x n, ldc) = A(m x k, lda) * B(k x n, ldb) [+ C if beta != 0], FP64
+ * column-major device arrays; precision 0 = FP64 CUDA cores, 1 = split-BF16
+ * tensor cores (6 digit planes, FP64-accurate to ~3.5e-15 relative).  The
+ * grouped GEMM behind the dense merge update of LAPACK DLAED3 (called at
+ * SRC/mdlaed1.f90:199) and the HSS multiply (SRC/ConstructHssd.f90:1394). */
+int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B, int ldb,
+                 double *C, int ldc, int beta, int precision, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,61 @@
+"""Grouped GEMM: FP64 CUDA-core path and the split-BF16 tensor-core path
+(6 digit planes) against numpy FP64 products.  Tolerance for the split path:
+|C - AB| <= 2^-44 * (|A| |B|)_ij elementwise bound scale (S = 6 planes give
+48 bits; 16x slack for the FP32 group accumulation and FP64 recombination)."""
+import numpy as np
+import pytest
+import torch
+
+import hsspack_gb300 as hp
+
+pytestmark = pytest.mark.gpu
+
+
+def _colmajor(a):
+    """device buffer holding a in column-major order"""
+    return torch.tensor(np.asfortranarray(a).T.copy(), dtype=torch.float64, device="cuda")
+
+
+def _run(A, B, C0=None, beta=0, precision=1):
+    m, k = A.shape
+    n = B.shape[1]
+    dA, dB = _colmajor(A), _colmajor(B)
+    dC = _colmajor(C0 if C0 is not None else np.zeros((m, n)))
+    hp.gemm_dev(dA, dB, dC, m, n, k, m, k, m, beta=beta, precision=precision)
+    return dC.cpu().numpy().T
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 64, 64), (300, 70, 150), (1000, 115, 60), (257, 33, 257),
+                                   (64, 200, 700), (5, 3, 1)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_gemm_vs_numpy(m, n, k, precision):
+    rng = np.random.default_rng(m * 7 + n * 3 + k)
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    C = _run(A, B, precision=precision)
+    ref = A @ B
+    bound = np.abs(A) @ np.abs(B)
+    tol = 2.0 ** -44 if precision == 1 else 1e-15 * k
+    assert np.max(np.abs(C - ref) / bound) <= tol, np.max(np.abs(C - ref) / bound)
+
+
+def test_split_row_col_scales_and_beta():
+    rng = np.random.default_rng(5)
+    m, n, k = 384, 128, 200
+    A = rng.standard_normal((m, k)) * (2.0 ** rng.integers(-40, 40, size=(m, 1)))
+    B = rng.standard_normal((k, n)) * (2.0 ** rng.integers(-40, 40, size=(1, n)))
+    A[3, :] = 0.0  # an all-zero row
+    C0 = rng.standard_normal((m, n))
+    C = _run(A, B, C0=C0, beta=1, precision=1)
+    ref = C0 + A @ B
+    bound = np.abs(A) @ np.abs(B) + np.abs(C0) * 2.0 ** -50
+    assert np.max(np.abs(C - ref) / bound) <= 2.0 ** -44
+
+
+def test_split_orthogonal_update_accuracy():
+    # the use in the eigensolver: Q (orthogonal) times an orthogonal S
+    rng = np.random.default_rng(9)
+    Q, _ = np.linalg.qr(rng.standard_normal((512, 512)))
+    S, _ = np.linalg.qr(rng.standard_normal((512, 512)))
+    C = _run(Q, S, precision=1)
+    assert np.linalg.norm(C.T @ C - np.eye(512)) / 512 <= 1e-14
