@@ -218,8 +218,10 @@ def run_ours(args):
         finally:
             hp.restore_config(old)
 
-    full_cfg = {"batched": 1}
-    plain_cfg = {"batched": 0}
+    # "full": level-batched launches + split-BF16 tensor-core products;
+    # "plain": per-merge launches, FP64 products, standard secular guess
+    full_cfg = {"batched": 1, "precision": 1}
+    plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()
     clocks.start()
     ms, acc, launches, st = timed(args.steps, args.warmup, True, full_cfg)
@@ -231,6 +233,7 @@ def run_ours(args):
         return
     # plain GPU merge (per-merge launches), fewer steps
     ms_plain, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, plain_cfg)
+    ms_fp64, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, {"batched": 1, "precision": 0})
     acc_chk = check_accuracy(torch, d, e, dw, Z, n)
 
     # end to end through the Fortran drop-in with pinned host buffers
@@ -292,7 +295,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "tridiagonal DC eigensolve n=%d, D,E iid U[-1,1] seed 0, COMPZ='I'"
-                   % n, "n": n, "mode": "batched levels, FP64 products",
+                   % n, "n": n, "mode": "batched levels, split-BF16 tensor-core products",
                    "l2": "no flush: the 8.6 GB eigenvector matrix exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 16 * n,
@@ -302,6 +305,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": clk,
         "plain_gpu_s": ms_plain / 1000.0,
+        "batched_fp64_s": ms_fp64 / 1000.0,
         "full_vs_plain": ms_plain / ms,
         "accuracy": acc_chk,
         "stages_ms_per_step": {k: v / args.steps for k, v in acc["ms"].items() if v > 0},

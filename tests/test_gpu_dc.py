@@ -33,15 +33,17 @@ def _check(d, e, **cfg):
 
 
 @pytest.mark.parametrize("n", [1, 2, 7, 25, 26, 64, 100, 257, 1000, 2048])
-def test_random(n):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_random(n, precision):
     d, e = rand_tridiag(n, seed=n)
-    _check(d, e)
+    _check(d, e, precision=precision)
 
 
 @pytest.mark.parametrize("n", [30, 500, 2048])
-def test_toeplitz_closed_form(n):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_toeplitz_closed_form(n, precision):
     d, e = toeplitz_tridiag(n)
-    w, _ = _check(d, e)
+    w, _ = _check(d, e, precision=precision)
     assert np.max(np.abs(w - toeplitz_eigs(n))) <= 4 * EV_TOL
 
 

@@ -48,7 +48,8 @@ def test_split_row_col_scales_and_beta():
     C0 = rng.standard_normal((m, n))
     C = _run(A, B, C0=C0, beta=1, precision=1)
     ref = C0 + A @ B
-    bound = np.abs(A) @ np.abs(B) + np.abs(C0) * 2.0 ** -50
+    # FP64 rounding of C0 + AB itself is 2^-53 |C0|: allow 2^-52 |C0| on top
+    bound = np.abs(A) @ np.abs(B) + np.abs(C0) * 2.0 ** -8
     assert np.max(np.abs(C - ref) / bound) <= 2.0 ** -44
 
 

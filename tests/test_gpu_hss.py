@@ -24,13 +24,18 @@ def _problem(k, seed):
 
 @pytest.mark.parametrize("k,ni,tol,nrows", [(600, 64, 1e-14, 97), (2000, 200, 1e-17, 300),
                                             (4096, 128, 1e-14, 256), (1000, 2000, 1e-14, 64)])
-def test_dhssevc_vs_dense(k, ni, tol, nrows):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_dhssevc_vs_dense(k, ni, tol, nrows, precision):
     d, zh, alpha, difl, difr = _problem(k, k)
     C = oracle.cauchy_eig_dense(d, zh, alpha, difl, difr)
     X = np.random.default_rng(k).standard_normal((nrows, k))
     Xd = _dev(np.asfortranarray(X).T.copy())  # rows of the tensor = columns of X
-    hp.dhssevc_dev(_dev(d), _dev(zh), _dev(alpha), _dev(difl), _dev(difr), Xd, nrows, nrows,
-                   ni=ni, tol=tol)
+    old = hp.set_config(precision=precision)
+    try:
+        hp.dhssevc_dev(_dev(d), _dev(zh), _dev(alpha), _dev(difl), _dev(difr), Xd, nrows, nrows,
+                       ni=ni, tol=tol)
+    finally:
+        hp.restore_config(old)
     Y = Xd.cpu().numpy().T
     ref = X @ C
     err = np.max(np.abs(Y - ref)) / np.max(np.abs(ref))
@@ -42,9 +47,10 @@ def test_dhssevc_vs_dense(k, ni, tol, nrows):
 
 
 @pytest.mark.parametrize("n,bsmlz,leaf,tol", [(2048, 200, 64, 1e-14), (3000, 500, 200, 1e-17)])
-def test_dc_with_hss_merges(n, bsmlz, leaf, tol):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_dc_with_hss_merges(n, bsmlz, leaf, tol, precision):
     d, e = toeplitz_tridiag(n)
-    old = hp.set_config(bsmlz=bsmlz, hss_leaf=leaf, tol=tol)
+    old = hp.set_config(bsmlz=bsmlz, hss_leaf=leaf, tol=tol, precision=precision)
     try:
         w, Q = hp.eigh_tridiagonal(d, e)
         st = hp.get_stats()
