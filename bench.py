@@ -221,6 +221,10 @@ def run_ours(args):
     # "full": level-batched launches + split-BF16 tensor-core products;
     # "plain": per-merge launches, FP64 products, standard secular guess
     full_cfg = {"batched": 1, "precision": 1}
+    # DC leaf size from the project's autotuner (timed outside the measured region)
+    from hsspack_gb300 import autotune
+    tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg)
+    full_cfg.update(tuned)
     plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()
     clocks.start()
@@ -296,6 +300,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "tridiagonal DC eigensolve n=%d, D,E iid U[-1,1] seed 0, COMPZ='I'"
                    % n, "n": n, "mode": "batched levels, split-BF16 tensor-core products",
+                   "smlsiz": full_cfg.get("smlsiz"), "autotune_ms": tune_ms,
                    "l2": "no flush: the 8.6 GB eigenvector matrix exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 16 * n,

@@ -211,7 +211,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   int *dout = buf<int>(c, "g_out", 5 * P);
   double *drho = buf<double>(c, "g_rho", P);
   stage_begin(HSS_ST_PREPARE, st);
-  launch_merge_prepare(P, dms, dmn, dmn1, e, Q, ldq, Dp, perm, L.w, dout, drho, st);
+  launch_merge_prepare(P, *std::max_element(mn.begin(), mn.end()), dms, dmn, dmn1, e, Q, ldq, Dp,
+                       perm, L.w, dout, drho, st);
   {
     long long nn = 0;
     for (int x : mn) nn += x;
@@ -283,7 +284,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   double k2 = 0.0;
   for (int K : aK) k2 += (double)K * K;
   stage_begin(HSS_ST_SECULAR, st);
-  launch_secular(lv, total, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
+  launch_secular(lv, total, *std::max_element(aK.begin(), aK.end()), L.w.dl, L.w.zw, L.lam, L.difl,
+                 L.difr, L.iters, status,
                  (unsigned long long *)(status + 2), nullptr, st);
   // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 8.0 * 4.0 * k2);
@@ -357,7 +359,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   }
   // ---- new ascending order and eigenvalues of the rewritten slots
   stage_begin(HSS_ST_FINISH, st);
-  launch_merge_finish(PA, vs, vn, vK, L.lam, L.w, perm, Dp, st);
+  launch_merge_finish(PA, maxn, vs, vn, vK, L.lam, L.w, perm, Dp, st);
   {
     long long nn = 0;
     for (int x : an) nn += x;
@@ -383,7 +385,8 @@ static void dc_block(Ctx &c, int n, const double *d, const double *e, double *Q,
   int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl);
   h2d(dls, ls, st); h2d(dlz, sz, st);
   stage_begin(HSS_ST_LEAF, st);
-  launch_leaf(nl, dls, dlz, n, d, e, Q, ldq, Dp, perm, status, st);
+  launch_leaf(nl, dls, dlz, *std::max_element(sz.begin(), sz.end()), n, d, e, Q, ldq, Dp, perm,
+              status, st);
   {
     double fl = 0.0;
     for (int x : sz) fl += 30.0 * x * x * x;
@@ -484,7 +487,7 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
       std::vector<int> ls(1, 0), lz(1, m);
       int *dls = buf<int>(c, "leaf_s", 1), *dlz = buf<int>(c, "leaf_z", 1);
       h2d(dls, ls, st); h2d(dlz, lz, st);
-      launch_leaf(1, dls, dlz, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
+      launch_leaf(1, dls, dlz, m, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
       c.launches++;
     } else {
       dc_block(c, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
@@ -687,7 +690,7 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
     CK(cudaMemsetAsync(status, 0, sizeof(int), st));
     LevelView lv{vs, vK, vr, vo, 1};
-    launch_secular(lv, k, dlamda, z, lam, difl, difr, iters, status, nullptr, nullptr, st);
+    launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, nullptr, nullptr, st);
     int hs = 0;
     CK(cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

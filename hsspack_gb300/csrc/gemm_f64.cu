@@ -98,12 +98,21 @@ void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaSt
 
 void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStream_t st) {
   if (probs_in.empty()) return;
+  std::vector<GemmDesc> probs;
   if (precision == 1) {
+    // tensor-core splitting pays off once a product has enough MACs per
+    // operand byte; small products stay on the FP64 pipe
+    std::vector<GemmDesc> big;
+    for (const auto &p : probs_in) {
+      if ((double)p.M * p.N * p.K >= (double)(1 << 20) && p.M >= 256) big.push_back(p);
+      else probs.push_back(p);
+    }
     int *err = pool<int>("gemm_err", 1);
-    launch_gemm_split(probs_in, err, st);
-    return;
+    if (!big.empty()) launch_gemm_split(big, err, st);
+    if (probs.empty()) return;
+  } else {
+    probs = probs_in;
   }
-  std::vector<GemmDesc> probs(probs_in);
   int tiles = 0;
   for (auto &p : probs) { p.tile0 = tiles; tiles += gemm_tiles(p.M, p.N); }
   GemmDesc *d = pool<GemmDesc>("gemm_f64_probs", probs.size());

@@ -366,18 +366,29 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
     if (!ok) break;
-    // drain the group accumulators of this window into FP64
+    // drain the group accumulators of this window.  Groups 0..2 hold exact
+    // integers (< 2^24): combine them exactly in int64; groups 3..5 weigh
+    // <= 2^-24 and are combined in FP32; one FP64 add per element:
+    //   window sum * 2^32 = (a0 2^16 + a1 2^8 + a2) + (a3 + a4 2^-8 + a5 2^-16) 2^-8
     const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-    for (int g = 0; g < SP; ++g) {
-      const double w = ldexp(1.0, -8 * (g + 2));
 #pragma unroll
-      for (int c = 0; c < TN; c += 16) {
+    for (int c = 0; c < TN; c += 16) {
+      long long hi[16];
+      float lo[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) { hi[i] = 0; lo[i] = 0.0f; }
+#pragma unroll
+      for (int g = 0; g < SP; ++g) {
         float v[16];
         tmem_ld16(lane_addr + g * TN + c, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) acc[c + i] = fma((double)v[i], w, acc[c + i]);
+        for (int i = 0; i < 16; ++i) {
+          if (g < 3) hi[i] += (long long)__float2int_rn(v[i]) << (8 * (2 - g));
+          else lo[i] = fmaf(v[i], g == 3 ? 1.0f : g == 4 ? 0x1p-8f : 0x1p-16f, lo[i]);
+        }
       }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) acc[c + i] += fma((double)lo[i], 0x1p-8, (double)hi[i]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -391,7 +402,7 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
     for (int j = 0; j < TN; ++j) {
       const int c = tn * TN + j;
       if (c < P.N) {
-        const double v = ldexp(acc[j], ei + P.eb[c]);
+        const double v = ldexp(acc[j], ei + P.eb[c] - 32);
         double *dst = P.C + (long long)c * P.ldc + r;
         *dst = P.beta ? *dst + v : v;
       }

@@ -33,7 +33,7 @@ struct LevelScratch {
 };
 
 // secular.cu
-void launch_secular(const LevelView &lv, int total, const double *dl, const double *zw,
+void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st);
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
@@ -49,12 +49,12 @@ void launch_cauchylike(int M, int N, const double *D, const double *F, const dou
                        const double *v, double *A, cudaStream_t st);
 
 // leaf.cu
-void launch_leaf(int nleaf, const int *lstart, const int *lsize, int nblk, const double *d,
-                 const double *e, double *Q, long long ldq, double *Dp, int *perm, int *status,
-                 cudaStream_t st);
+void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int nblk,
+                 const double *d, const double *e, double *Q, long long ldq, double *Dp, int *perm,
+                 int *status, cudaStream_t st);
 
 // merge.cu
-void launch_merge_prepare(int P, const int *ms, const int *mn, const int *mn1, const double *e,
+void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1, const double *e,
                           const double *Q, long long ldq, double *Dp, int *perm,
                           const LevelScratch &w, int *out, double *orho, cudaStream_t st);
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
@@ -65,7 +65,7 @@ void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, con
 void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                     const int *ndslot, const long long *toff, const double *T, double *Q,
                     long long ldq, cudaStream_t st);
-void launch_merge_finish(int P, const int *ms, const int *mn, const int *mK, const double *lam,
+void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const int *mK, const double *lam,
                          const LevelScratch &w, int *perm, double *Dp, cudaStream_t st);
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st);

@@ -1,129 +1,152 @@
 // leaf.cu -- batched eigensolver for the DC leaves (the DSTEQR('I') calls of
 // SRC/mdlaed0.f90:262-266).
 //
-// One warp per leaf of size m <= 32.  The implicit QL iteration with a
-// Wilkinson shift (Golub & Van Loan, Matrix Computations, sec. 8.3) runs its
-// scalar recurrence identically on every lane from shared memory; lane k owns
-// row k of the eigenvector block and applies each Givens rotation to it.
-// Eigenpairs are finally sorted ascending (selection sort, as DSTEQR ends).
-// The rank-one cuts of the divide step (mdlaed0.f90:213-219) are applied on
-// load: d(first) -= |e(left cut)|, d(last) -= |e(right cut)|.
+// One thread per leaf of size m <= 32, up to 32 leaves per CTA.  Each thread runs the
+// implicit QL iteration with a Wilkinson shift (Golub & Van Loan, Matrix
+// Computations, sec. 8.3) on its own leaf, rotating the columns of its
+// eigenvector block, then sorts the eigenpairs ascending (selection sort, as
+// DSTEQR ends).  GB300's FP64 pipe is narrow, so no FP64 instruction is
+// replicated across lanes: every lane does distinct work.  Per-leaf storage
+// lives in shared memory interleaved by lane ([row][col][lane]), so the 32
+// lanes of a warp always touch 32 consecutive words (no bank conflicts).  The
+// rank-one cuts of the divide step (mdlaed0.f90:213-219) are applied on load:
+// d(first) -= |e(left cut)|, d(last) -= |e(right cut)|.
 #include "hss_common.cuh"
 #include "hss_kernels.h"
+
+#include <algorithm>
 
 namespace hss {
 
 constexpr int LEAF_MAX = 32;
-constexpr int LEAF_WARPS = 4;
 
-__global__ void __launch_bounds__(LEAF_WARPS * 32)
-k_leaf_ql(int nleaf, const int *__restrict__ lstart, const int *__restrict__ lsize,
+__global__ void __launch_bounds__(32)
+k_leaf_ql(int nleaf, const int *__restrict__ lstart, const int *__restrict__ lsize, int mmax,
           int nblk, const double *__restrict__ d, const double *__restrict__ e,
           double *__restrict__ Q, long long ldq, double *__restrict__ Dp,
           int *__restrict__ perm, int *__restrict__ status) {
-  __shared__ double sd[LEAF_WARPS][LEAF_MAX + 1];
-  __shared__ double se[LEAF_WARPS][LEAF_MAX + 1];
-  __shared__ double sz[LEAF_WARPS][LEAF_MAX][LEAF_MAX + 1];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int leaf = blockIdx.x * LEAF_WARPS + w;
-  if (leaf >= nleaf) return;
-  const int s = __ldg(lstart + leaf), m = __ldg(lsize + leaf);
-  double *D = sd[w], *E = se[w];
-  double(*Z)[LEAF_MAX + 1] = sz[w];
-  if (lane < m) {
-    double dv = __ldg(d + s + lane);
-    if (lane == 0 && s > 0) dv -= fabs(__ldg(e + s - 1));
-    if (lane == m - 1 && s + m < nblk) dv -= fabs(__ldg(e + s + m - 1));
-    D[lane] = dv;
-    E[lane] = (lane < m - 1) ? __ldg(e + s + lane) : 0.0;
-    for (int c = 0; c < m; ++c) Z[lane][c] = (c == lane) ? 1.0 : 0.0;
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x, LW = blockDim.x;
+  const int leaf = blockIdx.x * LW + lane;
+  const bool active = leaf < nleaf;
+  double *D = sm;                    // D[i*LW + lane]
+  double *E = sm + mmax * LW;        // E[i*LW + lane]
+  double *Z = sm + 2 * mmax * LW;    // Z[(r*mmax + c)*LW + lane]
+#define DD(i) D[(i) * LW + lane]
+#define EE(i) E[(i) * LW + lane]
+#define ZZ(r, c) Z[((r) * mmax + (c)) * LW + lane]
+  int s = 0, m = 0;
+  if (active) {
+    s = lstart[leaf];
+    m = lsize[leaf];
+    for (int i = 0; i < m; ++i) {
+      double dv = d[s + i];
+      if (i == 0 && s > 0) dv -= fabs(e[s - 1]);
+      if (i == m - 1 && s + m < nblk) dv -= fabs(e[s + m - 1]);
+      DD(i) = dv;
+      EE(i) = (i < m - 1) ? e[s + i] : 0.0;
+      for (int c = 0; c < m; ++c) ZZ(i, c) = (i == c) ? 1.0 : 0.0;
+    }
   }
-  __syncwarp();
   int bad = 0;
-  for (int l = 0; l < m; ++l) {
+  for (int l = 0; l < m && !bad; ++l) {
     int iter = 0;
     while (true) {
       int mm = l;
-      for (; mm < m - 1; ++mm) {
-        const double dd = fabs(D[mm]) + fabs(D[mm + 1]);
-        if (fabs(E[mm]) <= HSS_EPS * dd) break;
-      }
+      for (; mm < m - 1; ++mm)
+        if (fabs(EE(mm)) <= HSS_EPS * (fabs(DD(mm)) + fabs(DD(mm + 1)))) break;
       if (mm == l) break;
       if (++iter > 30 * m) { bad = 1; break; }
-      // Wilkinson-type shift from the leading 2x2 block
-      double g = (D[l + 1] - D[l]) / (2.0 * E[l]);
-      double r = hypot(g, 1.0);
-      g = D[mm] - D[l] + E[l] / (g + copysign(r, g));
+      // operands are O(||T||) after the block scaling, so plain sqrt is safe
+      double g = (DD(l + 1) - DD(l)) / (2.0 * EE(l));
+      double r = sqrt(fma(g, g, 1.0));
+      g = DD(mm) - DD(l) + EE(l) / (g + copysign(r, g));
       double sn = 1.0, cs = 1.0, p = 0.0;
-      int i = mm - 1;
       bool early = false;
-      for (; i >= l; --i) {
-        const double f = sn * E[i], b = cs * E[i];
-        r = hypot(f, g);
-        if (lane == 0) E[i + 1] = r;
+      for (int i = mm - 1; i >= l; --i) {
+        const double f = sn * EE(i), b = cs * EE(i);
+        r = sqrt(fma(f, f, g * g));
+        EE(i + 1) = r;
         if (r == 0.0) {
-          __syncwarp();
-          if (lane == 0) { D[i + 1] -= p; E[mm] = 0.0; }
+          DD(i + 1) -= p;
+          EE(mm) = 0.0;
           early = true;
           break;
         }
-        sn = f / r;
-        cs = g / r;
-        g = D[i + 1] - p;
-        r = (D[i] - g) * sn + 2.0 * cs * b;
+        const double rinv = 1.0 / r;
+        sn = f * rinv;
+        cs = g * rinv;
+        g = DD(i + 1) - p;
+        r = (DD(i) - g) * sn + 2.0 * cs * b;
         p = sn * r;
-        __syncwarp();
-        if (lane == 0) D[i + 1] = g + p;
+        DD(i + 1) = g + p;
         g = cs * r - b;
-        if (lane < m) {  // rotate columns i, i+1 of row `lane`
-          const double zi = Z[lane][i], zi1 = Z[lane][i + 1];
-          Z[lane][i + 1] = sn * zi + cs * zi1;
-          Z[lane][i] = cs * zi - sn * zi1;
+        for (int k = 0; k < m; ++k) {  // rotate columns i, i+1
+          const double zi = ZZ(k, i), zi1 = ZZ(k, i + 1);
+          ZZ(k, i + 1) = sn * zi + cs * zi1;
+          ZZ(k, i) = cs * zi - sn * zi1;
         }
-        __syncwarp();
       }
-      __syncwarp();
       if (early) continue;
-      if (lane == 0) { D[l] -= p; E[l] = g; E[mm] = 0.0; }
-      __syncwarp();
+      DD(l) -= p;
+      EE(l) = g;
+      EE(mm) = 0.0;
     }
-    if (bad) break;
   }
-  __syncwarp();
   // selection sort ascending, moving columns
   for (int i = 0; i < m - 1; ++i) {
     int k = i;
-    double pmin = D[i];
+    double pmin = DD(i);
     for (int j = i + 1; j < m; ++j)
-      if (D[j] < pmin) { k = j; pmin = D[j]; }
-    __syncwarp();
+      if (DD(j) < pmin) { k = j; pmin = DD(j); }
     if (k != i) {
-      if (lane == 0) { D[k] = D[i]; D[i] = pmin; }
-      if (lane < m) {
-        const double t = Z[lane][i];
-        Z[lane][i] = Z[lane][k];
-        Z[lane][k] = t;
+      DD(k) = DD(i);
+      DD(i) = pmin;
+      for (int r = 0; r < m; ++r) {
+        const double t = ZZ(r, i);
+        ZZ(r, i) = ZZ(r, k);
+        ZZ(r, k) = t;
       }
     }
-    __syncwarp();
   }
-  // write the m x m block at Q(s, s), eigenvalues and identity order
-  for (int c = 0; c < m; ++c)
-    if (lane < m) Q[(long long)(s + c) * ldq + s + lane] = Z[lane][c];
-  if (lane < m) {
-    Dp[s + lane] = D[lane];
-    perm[s + lane] = s + lane;
+  if (active) {
+    for (int i = 0; i < m; ++i) {
+      Dp[s + i] = DD(i);
+      perm[s + i] = s + i;
+    }
+    if (bad) atomicMax(status, HSS_LEAF_NOCONV);
   }
-  if (bad && lane == 0) atomicMax(status, HSS_LEAF_NOCONV);
+  __syncthreads();
+  // write the blocks: lanes over rows, one leaf at a time (coalesced columns)
+  for (int q = 0; q < LW; ++q) {
+    const int lf = blockIdx.x * LW + q;
+    if (lf >= nleaf) break;
+    const int s2 = lstart[lf], m2 = lsize[lf];
+    for (int c = 0; c < m2; ++c)
+      for (int r = lane; r < m2; r += LW) Q[(long long)(s2 + c) * ldq + s2 + r] = Z[(r * mmax + c) * LW + q];
+  }
+#undef DD
+#undef EE
+#undef ZZ
 }
 
-void launch_leaf(int nleaf, const int *lstart, const int *lsize, int nblk, const double *d,
-                 const double *e, double *Q, long long ldq, double *Dp, int *perm, int *status,
-                 cudaStream_t st) {
+void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int nblk,
+                 const double *d, const double *e, double *Q, long long ldq, double *Dp, int *perm,
+                 int *status, cudaStream_t st) {
   if (nleaf <= 0) return;
-  dim3 grid((nleaf + LEAF_WARPS - 1) / LEAF_WARPS);
-  k_leaf_ql<<<grid, LEAF_WARPS * 32, 0, st>>>(nleaf, lstart, lsize, nblk, d, e, Q, ldq, Dp, perm,
-                                              status);
+  mmax = std::max(1, std::min(mmax, LEAF_MAX));
+  // leaves per CTA: enough CTAs to cover the SMs, and the block within smem
+  int lw = 32;
+  while (lw > 8 && (nleaf + lw - 1) / lw < 2 * 148) lw /= 2;
+  while (lw > 1 && (size_t)(mmax * mmax + 2 * mmax) * lw * sizeof(double) > 200 * 1024) lw /= 2;
+  const size_t smem = (size_t)(mmax * mmax + 2 * mmax) * lw * sizeof(double);
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    cudaFuncSetAttribute(k_leaf_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = smem;
+  }
+  k_leaf_ql<<<(nleaf + lw - 1) / lw, lw, smem, st>>>(nleaf, lstart, lsize, mmax, nblk, d, e, Q, ldq,
+                                                      Dp, perm, status);
 }
 
 }  // namespace hss

@@ -14,9 +14,8 @@
 
 namespace hss {
 
-constexpr int MT = 512;  // threads per merge CTA
-
-// Block-wide exclusive scan of one 64-bit value per thread.
+// Block-wide exclusive scan of one 64-bit value per thread (MT threads).
+template <int MT>
 __device__ __forceinline__ unsigned long long block_scan64(unsigned long long v,
                                                            unsigned long long *tot) {
   __shared__ unsigned long long ws[MT / 32];
@@ -46,6 +45,7 @@ __device__ __forceinline__ unsigned long long block_scan64(unsigned long long v,
   return r;
 }
 
+template <int MT>
 __device__ __forceinline__ double block_max(double v) {
   __shared__ double ws[MT / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -95,6 +95,7 @@ __device__ void block_sort_pairs(double *v, int *p, double *tv, int *tp, int len
 }
 
 // out[5*m + {0..4}] = K, #rotations, #type1, #type2, #type3 ; orho[m] = |2 rho|
+template <int MT>
 __global__ void __launch_bounds__(MT)
 k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                 const int *__restrict__ mn1, const double *__restrict__ e,
@@ -106,26 +107,30 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   const int s = ms[m], n = mn[m], n1 = mn1[m], n2 = n - n1;
   const int tid = threadIdx.x;
   const double rho_in = e[s + n1 - 1];
-  // ---- merge the two ascending halves (DLAMRG, ties to the first list)
+  // ---- merge the two ascending halves (DLAMRG, ties to the first list) by
+  //      merge path on contiguous copies of their eigenvalues (zs as scratch)
+  for (int i = tid; i < n; i += MT) w.zs[s + i] = Dp[perm[s + i]];
+  __syncthreads();
+  const double *hv = w.zs + s;
   for (int i = tid; i < n1; i += MT) {
-    const int slot = perm[s + i];
-    const double a = Dp[slot];
+    const double a = hv[i];
     int lo = 0, hi = n2;  // count right values < a
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
-      if (Dp[perm[s + n1 + mid]] < a) lo = mid + 1; else hi = mid;
+      if (hv[n1 + mid] < a) lo = mid + 1; else hi = mid;
     }
-    w.srt[s + i + lo] = slot;
+    w.srt[s + i + lo] = perm[s + i];
+    w.ds[s + i + lo] = a;
   }
   for (int j = tid; j < n2; j += MT) {
-    const int slot = perm[s + n1 + j];
-    const double b = Dp[slot];
+    const double b = hv[n1 + j];
     int lo = 0, hi = n1;  // count left values <= b
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
-      if (Dp[perm[s + mid]] <= b) lo = mid + 1; else hi = mid;
+      if (hv[mid] <= b) lo = mid + 1; else hi = mid;
     }
-    w.srt[s + j + lo] = slot;
+    w.srt[s + j + lo] = perm[s + n1 + j];
+    w.ds[s + j + lo] = b;
   }
   __syncthreads();
   // ---- z = [last row of Q1, first row of Q2] / sqrt(2) (mdlaed1.f90:178-180,
@@ -138,15 +143,14 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     double z = Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
     if (!top && rho_in < 0.0) z = -z;
     z *= sc;
-    const double dv = Dp[slot];
-    w.ds[s + i] = dv;
+    const double dv = w.ds[s + i];
     w.zs[s + i] = z;
     w.typ[s + i] = top ? 1 : 3;
     dmax = fmax(dmax, fabs(dv));
     zmax = fmax(zmax, fabs(z));
   }
-  dmax = block_max(dmax);
-  zmax = block_max(zmax);
+  dmax = block_max<MT>(dmax);
+  zmax = block_max<MT>(zmax);
   const double rho = fabs(2.0 * rho_in);
   const double tol = 8.0 * HSS_EPS * fmax(dmax, zmax);  // mdlaed2.f90:265-267
   if (rho * zmax <= tol) {  // nothing couples the halves
@@ -168,7 +172,7 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     if (!big) w.typ[s + i] = 4;
   }
   unsigned long long tot;
-  int pos = (int)block_scan64((unsigned long long)cnt, &tot);
+  int pos = (int)block_scan64<MT>((unsigned long long)cnt, &tot);
   const int nc = (int)tot;
   for (int i = b0; i < b1; ++i)
     if (w.typ[s + i] != 4) w.cand[s + pos++] = i;
@@ -214,8 +218,8 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     n5 += (t == 5);
   }
   unsigned long long ptot, t5;
-  unsigned long long pre = block_scan64(pk, &ptot);
-  int r5 = (int)block_scan64((unsigned long long)n5, &t5);
+  unsigned long long pre = block_scan64<MT>(pk, &ptot);
+  int r5 = (int)block_scan64<MT>((unsigned long long)n5, &t5);
   const int c1 = (int)(ptot & 0x1fffff), c2 = (int)((ptot >> 21) & 0x1fffff),
             c3 = (int)((ptot >> 42) & 0x1fffff);
   const int K = c1 + c2 + c3;
@@ -326,6 +330,7 @@ __global__ void k_scatter(int P, const int *__restrict__ ms, const int *__restri
 // New ascending order of each merged block: roots (ascending) merged with the
 // deflated eigenvalues (ascending), roots first on ties (DLAMRG at
 // mdlaed1.f90:221); eigenvalues of the rewritten slots are set to the roots.
+template <int MT>
 __global__ void __launch_bounds__(MT)
 k_merge_finish(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                const int *__restrict__ mK, const double *__restrict__ lam,
@@ -370,10 +375,20 @@ __global__ void k_final_gather(int n, const int *__restrict__ perm, const double
 }
 
 // ---------------------------------------------------------------- launch --
-void launch_merge_prepare(int P, const int *ms, const int *mn, const int *mn1, const double *e,
-                          const double *Q, long long ldq, double *Dp, int *perm,
+static int merge_threads(int maxn) {
+  return maxn <= 64 ? 64 : maxn <= 256 ? 128 : maxn <= 2048 ? 256 : 512;
+}
+
+void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1,
+                          const double *e, const double *Q, long long ldq, double *Dp, int *perm,
                           const LevelScratch &w, int *out, double *orho, cudaStream_t st) {
-  if (P > 0) k_merge_prepare<<<P, MT, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho);
+  if (P <= 0) return;
+  switch (merge_threads(maxn)) {
+    case 64: k_merge_prepare<64><<<P, 64, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
+    case 128: k_merge_prepare<128><<<P, 128, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
+    case 256: k_merge_prepare<256><<<P, 256, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
+    default: k_merge_prepare<512><<<P, 512, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
+  }
 }
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
                    const LevelScratch &w, double *Q, long long ldq, cudaStream_t st) {
@@ -395,9 +410,16 @@ void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, co
   dim3 grid(total, (maxn + 1023) / 1024);
   k_scatter<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, toff, T, Q, ldq);
 }
-void launch_merge_finish(int P, const int *ms, const int *mn, const int *mK, const double *lam,
-                         const LevelScratch &w, int *perm, double *Dp, cudaStream_t st) {
-  if (P > 0) k_merge_finish<<<P, MT, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp);
+void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const int *mK,
+                         const double *lam, const LevelScratch &w, int *perm, double *Dp,
+                         cudaStream_t st) {
+  if (P <= 0) return;
+  switch (merge_threads(maxn)) {
+    case 64: k_merge_finish<64><<<P, 64, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp); break;
+    case 128: k_merge_finish<128><<<P, 128, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp); break;
+    case 256: k_merge_finish<256><<<P, 256, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp); break;
+    default: k_merge_finish<512><<<P, 512, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp); break;
+  }
 }
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st) {

@@ -24,14 +24,25 @@ struct SecSums {
   double psi, dpsi, phi, dphi, eabs;
 };
 
+// Sum over the L lanes of one root group (xor offsets < L stay in the group;
+// every lane of the warp takes part, so the shuffles are never divergent).
+template <int L>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(HSS_FULL, v, o);
+  return v;
+}
+
 // Sums over i of z_i^2/(d_i - x) split at jl (psi: i <= jl, phi: i > jl),
 // their derivatives, and sum |z_i^2/(d_i - x)| for the rounding-error bound.
-// x = o + tau; every gap is formed as (d_i - o) - tau.
+// x = o + tau; every gap is formed as (d_i - o) - tau.  Lane gl of the group
+// takes terms gl, gl + L, ...
+template <int L>
 __device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
-                                            const double *__restrict__ z, int K,
-                                            double o, double tau, int jl, int lane) {
+                                            const double *__restrict__ z, int K, double o,
+                                            double tau, int jl, int gl) {
   double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0, e = 0.0;
-  for (int i = lane; i < K; i += HSS_WARP) {
+  for (int i = gl; i < K; i += L) {
     const double zi = __ldg(z + i);
     const double del = (__ldg(d + i) - o) - tau;
     const double t = zi / del;
@@ -41,9 +52,9 @@ __device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
     e += fabs(v);
   }
   SecSums s;
-  s.psi = warp_sum(a0); s.dpsi = warp_sum(a1);
-  s.phi = warp_sum(b0); s.dphi = warp_sum(b1);
-  s.eabs = warp_sum(e);
+  s.psi = group_sum<L>(a0); s.dpsi = group_sum<L>(a1);
+  s.phi = group_sum<L>(b0); s.dphi = group_sum<L>(b1);
+  s.eabs = group_sum<L>(e);
   return s;
 }
 
@@ -77,125 +88,112 @@ __device__ __forceinline__ bool two_pole_root(double c, double A, double B, doub
   return false;
 }
 
-struct RootOut {
-  double lam, difl, difr;
-  int iters;
-  int status;
+// Per-root iteration state.  A group of L lanes owns one root; all lanes of a
+// group hold identical copies.  The warp loops until every group converged;
+// finished groups keep taking part in the (harmless) shuffles.
+struct RootState {
+  const double *d, *z;
+  int K, j, jl, jr;
+  double rho, rhoinv, o, tau, lo, hi, delta, top;
+  int phase;  // 0: first evaluation (midpoint), 1: iterating, 2: done
+  int iters, status;
+  bool last;
 };
 
-// Solve root j of the secular equation with a full warp.  `guess` (>= 0 and
-// < 1 when valid) is a learned estimate of (lam_j - d_j)/(d_{j+1} - d_j); it only
-// replaces the initial iterate, the FP64 iteration always runs to convergence.
-__device__ RootOut secular_root(const double *__restrict__ d, const double *__restrict__ z,
-                                int K, double rho, int j, float guess, int lane) {
-  RootOut out;
-  out.iters = 0;
-  out.status = HSS_OK;
-  const double rhoinv = 1.0 / rho;
-  if (K == 1) {
-    const double zz = __ldg(z) * __ldg(z);
-    out.lam = __ldg(d) + rho * zz;
-    out.difl = rho * zz;
-    out.difr = 0.0;
-    return out;
-  }
-  const bool last = (j == K - 1);
-  const int jl = last ? K - 2 : j;  // left model pole
-  const int jr = jl + 1;            // right model pole
-  double o, tau, lo, hi, delta = 0.0;
-  bool have = false;
-  const double zl = __ldg(z + jl), zr = __ldg(z + jr);
-  if (!last) {
-    delta = __ldg(d + j + 1) - __ldg(d + j);
-    if (guess > 0.0f && guess < 1.0f) {
-      // learned position: origin at the nearer pole, bracket = whole interval
-      const double x = (double)guess * delta;
-      if (guess <= 0.5f) { o = __ldg(d + j); tau = x; lo = 0.0; hi = delta; }
-      else { o = __ldg(d + j + 1); tau = x - delta; lo = -delta; hi = 0.0; }
-      have = true;
-    } else {
-      o = __ldg(d + j);
-      const double tm = 0.5 * delta;
-      SecSums s = sec_eval(d, z, K, o, tm, jl, lane);
-      ++out.iters;
-      const double w = rhoinv + s.psi + s.phi;
-      const double gl = (__ldg(d + jl) - o) - tm, gr = (__ldg(d + jr) - o) - tm;
-      const double c = w - zl * (zl / gl) - zr * (zr / gr);
-      if (w >= 0.0) {  // root in (d_j, midpoint]
-        lo = 0.0; hi = tm;
-        have = two_pole_root(c, zl * zl, zr * zr, 0.0, delta, lo, hi, tau);
-        if (!have) tau = 0.5 * tm;
-      } else {         // root in (midpoint, d_{j+1}): measure from d_{j+1}
-        o = __ldg(d + j + 1);
-        lo = tm - delta; hi = 0.0;
-        have = two_pole_root(c, zl * zl, zr * zr, -delta, 0.0, lo, hi, tau);
-        if (!have) tau = 0.5 * lo;
-      }
+__device__ __forceinline__ double pole(const RootState &r, int i) { return __ldg(r.d + i); }
+
+// First evaluation point: the midpoint of the pole interval (standard guess),
+// or the learned position (phase 1 directly).
+__device__ __forceinline__ void root_init(RootState &r, float guess, double zsq) {
+  r.rhoinv = 1.0 / r.rho;
+  r.iters = 0;
+  r.status = HSS_OK;
+  r.last = (r.j == r.K - 1);
+  r.jl = r.last ? r.K - 2 : r.j;
+  r.jr = r.jl + 1;
+  r.delta = r.last ? 0.0 : pole(r, r.j + 1) - pole(r, r.j);
+  r.top = r.rho * zsq;
+  r.phase = 0;
+  if (!r.last) {
+    r.o = pole(r, r.j);
+    r.tau = 0.5 * r.delta;
+    if (guess > 0.0f && guess < 1.0f) {  // learned position inside (d_j, d_{j+1})
+      const double x = (double)guess * r.delta;
+      if (guess <= 0.5f) { r.o = pole(r, r.j); r.tau = x; r.lo = 0.0; r.hi = r.delta; }
+      else { r.o = pole(r, r.j + 1); r.tau = x - r.delta; r.lo = -r.delta; r.hi = 0.0; }
+      r.phase = 1;
     }
   } else {
-    // last root lies in (d_{K-1}, d_{K-1} + rho * |z|^2]
-    o = __ldg(d + K - 1);
-    double zs = 0.0;
-    for (int i = lane; i < K; i += HSS_WARP) zs += __ldg(z + i) * __ldg(z + i);
-    zs = warp_sum(zs);
-    const double top = rho * zs;
-    const double tm = 0.5 * top;
-    SecSums s = sec_eval(d, z, K, o, tm, jl, lane);
-    ++out.iters;
-    const double w = rhoinv + s.psi + s.phi;
-    const double gl = (__ldg(d + jl) - o) - tm, gr = (__ldg(d + jr) - o) - tm;
+    r.o = pole(r, r.K - 1);
+    r.tau = 0.5 * r.top;
+  }
+}
+
+// Consume one evaluation at (o, tau).
+__device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
+  if (r.phase == 2) return;
+  ++r.iters;
+  const double zl = __ldg(r.z + r.jl), zr = __ldg(r.z + r.jr);
+  const double w = r.rhoinv + s.psi + s.phi;
+  if (r.phase == 0) {
+    // two-pole model with the far poles frozen at the midpoint value
+    const double gl = (pole(r, r.jl) - r.o) - r.tau, gr = (pole(r, r.jr) - r.o) - r.tau;
     const double c = w - zl * (zl / gl) - zr * (zr / gr);
-    const double da = __ldg(d + jl) - o;
-    if (w >= 0.0) { lo = 0.0; hi = tm; } else { lo = tm; hi = top * (1.0 + 4.0 * HSS_EPS); }
-    have = two_pole_root(c, zl * zl, zr * zr, da, 0.0, lo, hi, tau);
-    if (!have) tau = 0.5 * (lo + hi);
-  }
-  // ---- middle-way iteration
-  const int MAXIT = 40;
-  bool conv = false;
-  for (int it = 0; it < MAXIT; ++it) {
-    SecSums s = sec_eval(d, z, K, o, tau, jl, lane);
-    ++out.iters;
-    const double w = rhoinv + s.psi + s.phi;
-    const double dw = s.dpsi + s.dphi;
-    const double erretm = 8.0 * s.eabs + 2.0 * rhoinv + 3.0 * fabs(tau) * dw;
-    if (fabs(w) <= HSS_EPS * erretm) { conv = true; break; }
-    if (w < 0.0) lo = fmax(lo, tau); else hi = fmin(hi, tau);
-    const double gl = (__ldg(d + jl) - o) - tau;
-    const double gr = (__ldg(d + jr) - o) - tau;
-    const double a = (gl + gr) * w - gl * gr * dw;
-    const double b = gl * gr * w;
-    const double c = w - gl * s.dpsi - gr * s.dphi;
-    double eta;
-    if (c == 0.0) {
-      eta = (a != 0.0) ? b / a : -w / dw;
-    } else {
-      double disc = a * a - 4.0 * b * c;
-      if (disc < 0.0) disc = 0.0;
-      eta = (a <= 0.0) ? (a - sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a + sqrt(disc));
-    }
-    if (w * eta >= 0.0) eta = -w / dw;  // model went the wrong way: Newton step
-    double tn = tau + eta;
-    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
-    const double step = tn - tau;
-    tau = tn;
-    if (!last) {  // keep the origin at the pole nearer the iterate
-      if (o == __ldg(d + j) && tau > 0.5 * delta) {
-        o = __ldg(d + j + 1); tau -= delta; lo -= delta; hi -= delta;
-      } else if (o == __ldg(d + j + 1) && tau < -0.5 * delta) {
-        o = __ldg(d + j); tau += delta; lo += delta; hi += delta;
+    double t;
+    if (!r.last) {
+      const double tm = r.tau;
+      if (w >= 0.0) {  // root in (d_j, midpoint]
+        r.lo = 0.0; r.hi = tm;
+        if (!two_pole_root(c, zl * zl, zr * zr, 0.0, r.delta, r.lo, r.hi, t)) t = 0.5 * tm;
+      } else {         // root in (midpoint, d_{j+1}): measure from d_{j+1}
+        r.o = pole(r, r.j + 1);
+        r.lo = tm - r.delta; r.hi = 0.0;
+        if (!two_pole_root(c, zl * zl, zr * zr, -r.delta, 0.0, r.lo, r.hi, t)) t = 0.5 * r.lo;
       }
+    } else {
+      const double tm = r.tau;
+      const double da = pole(r, r.jl) - r.o;
+      if (w >= 0.0) { r.lo = 0.0; r.hi = tm; }
+      else { r.lo = tm; r.hi = r.top * (1.0 + 4.0 * HSS_EPS); }
+      if (!two_pole_root(c, zl * zl, zr * zr, da, 0.0, r.lo, r.hi, t)) t = 0.5 * (r.lo + r.hi);
     }
-    if (fabs(step) <= 2.0 * HSS_EPS * fabs(tau) || hi - lo <= 2.0 * HSS_EPS * fabs(tau)) {
-      conv = true;
-      break;
+    r.tau = t;
+    r.phase = 1;
+    return;
+  }
+  // middle-way step
+  const double dw = s.dpsi + s.dphi;
+  const double erretm = 8.0 * s.eabs + 2.0 * r.rhoinv + 3.0 * fabs(r.tau) * dw;
+  if (fabs(w) <= HSS_EPS * erretm) { r.phase = 2; return; }
+  if (r.iters > 41) { r.status = HSS_SECULAR_NOCONV; r.phase = 2; return; }
+  if (w < 0.0) r.lo = fmax(r.lo, r.tau); else r.hi = fmin(r.hi, r.tau);
+  const double gl = (pole(r, r.jl) - r.o) - r.tau;
+  const double gr = (pole(r, r.jr) - r.o) - r.tau;
+  const double a = (gl + gr) * w - gl * gr * dw;
+  const double b = gl * gr * w;
+  const double c = w - gl * s.dpsi - gr * s.dphi;
+  double eta;
+  if (c == 0.0) {
+    eta = (a != 0.0) ? b / a : -w / dw;
+  } else {
+    double disc = a * a - 4.0 * b * c;
+    if (disc < 0.0) disc = 0.0;
+    eta = (a <= 0.0) ? (a - sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a + sqrt(disc));
+  }
+  if (w * eta >= 0.0) eta = -w / dw;  // model went the wrong way: Newton step
+  double tn = r.tau + eta;
+  if (!(tn > r.lo && tn < r.hi)) tn = 0.5 * (r.lo + r.hi);
+  const double step = tn - r.tau;
+  r.tau = tn;
+  if (!r.last) {  // keep the origin at the pole nearer the iterate
+    if (r.o == pole(r, r.j) && r.tau > 0.5 * r.delta) {
+      r.o = pole(r, r.j + 1); r.tau -= r.delta; r.lo -= r.delta; r.hi -= r.delta;
+    } else if (r.o == pole(r, r.j + 1) && r.tau < -0.5 * r.delta) {
+      r.o = pole(r, r.j); r.tau += r.delta; r.lo += r.delta; r.hi += r.delta;
     }
   }
-  if (!conv) out.status = HSS_SECULAR_NOCONV;
-  out.lam = o + tau;
-  out.difl = -((__ldg(d + j) - o) - tau);
-  out.difr = last ? 0.0 : -((__ldg(d + j + 1) - o) - tau);
-  return out;
+  if (fabs(step) <= 2.0 * HSS_EPS * fabs(r.tau) || r.hi - r.lo <= 2.0 * HSS_EPS * fabs(r.tau))
+    r.phase = 2;
 }
 
 // ------------------------------------------------------------- kernels -----
@@ -210,28 +208,58 @@ __device__ __forceinline__ int find_merge(const int *__restrict__ off, int P, in
   return lo;
 }
 
-__global__ void k_secular(LevelView lv, const double *__restrict__ dl,
-                          const double *__restrict__ zw, double *__restrict__ lam,
-                          double *__restrict__ difl, double *__restrict__ difr,
-                          int *__restrict__ iters, int *__restrict__ status,
-                          unsigned long long *__restrict__ itsum,
-                          const float *__restrict__ guess) {
-  const int lane = threadIdx.x & 31;
-  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= __ldg(lv.rootoff + lv.P)) return;
-  const int m = find_merge(lv.rootoff, lv.P, r);
-  const int j = r - __ldg(lv.rootoff + m);
-  const int s = __ldg(lv.s + m);
-  const int K = __ldg(lv.K + m);
-  const float g = guess ? __ldg(guess + s + j) : -1.0f;
-  RootOut o = secular_root(dl + s, zw + s, K, __ldg(lv.rho + m), j, g, lane);
-  if (lane == 0) {
-    lam[s + j] = o.lam;
-    difl[s + j] = o.difl;
-    difr[s + j] = o.difr;
-    if (iters) iters[s + j] = o.iters;
-    if (itsum) atomicAdd(itsum, (unsigned long long)o.iters);
-    if (o.status) atomicMax(status, o.status);
+// One root per group of L lanes (L = 1..32 chosen from the level's largest
+// K so that each lane sums ~8 pole terms and the group reductions stay cheap).
+template <int L>
+__global__ void __launch_bounds__(256)
+k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
+          double *__restrict__ lam, double *__restrict__ difl, double *__restrict__ difr,
+          int *__restrict__ iters, int *__restrict__ status, unsigned long long *__restrict__ itsum,
+          const float *__restrict__ guess) {
+  const int lane = threadIdx.x & 31, gl = lane & (L - 1);
+  const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
+  const int total = __ldg(lv.rootoff + lv.P);
+  RootState st;
+  int s = 0;
+  const bool valid = r < total;
+  if (valid) {
+    const int m = find_merge(lv.rootoff, lv.P, r);
+    s = __ldg(lv.s + m);
+    st.j = r - __ldg(lv.rootoff + m);
+    st.K = __ldg(lv.K + m);
+    st.rho = __ldg(lv.rho + m);
+  } else {
+    st.j = 0; st.K = 0; st.rho = 1.0;
+  }
+  st.d = dl + s;
+  st.z = zw + s;
+  double zsq = 0.0;
+  for (int i = gl; i < st.K; i += L) zsq += __ldg(st.z + i) * __ldg(st.z + i);
+  zsq = group_sum<L>(zsq);
+  const bool trivial = !valid || st.K == 1;
+  if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : -1.0f, zsq);
+  else st.phase = 2;
+  while (__any_sync(HSS_FULL, st.phase != 2)) {
+    const SecSums sm = sec_eval<L>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.o, st.tau, st.jl, gl);
+    root_step(st, sm);
+  }
+  if (valid && gl == 0) {
+    double lm, dfl, dfr;
+    if (st.K == 1) {
+      const double zz = __ldg(st.z) * __ldg(st.z);
+      lm = __ldg(st.d) + st.rho * zz; dfl = st.rho * zz; dfr = 0.0;
+      st.iters = 0; st.status = HSS_OK;
+    } else {
+      lm = st.o + st.tau;
+      dfl = -((pole(st, st.j) - st.o) - st.tau);
+      dfr = st.last ? 0.0 : -((pole(st, st.j + 1) - st.o) - st.tau);
+    }
+    lam[s + st.j] = lm;
+    difl[s + st.j] = dfl;
+    difr[s + st.j] = dfr;
+    if (iters) iters[s + st.j] = st.iters;
+    if (itsum) atomicAdd(itsum, (unsigned long long)st.iters);
+    if (st.status) atomicMax(status, st.status);
   }
 }
 
@@ -366,12 +394,22 @@ __global__ void k_cauchylike(int M, int N, const double *__restrict__ D,
 static inline int warp_grid(int total, int threads) {
   return (int)(((long long)total * 32 + threads - 1) / threads);
 }
-void launch_secular(const LevelView &lv, int total, const double *dl, const double *zw,
+void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st) {
   if (total <= 0) return;
-  k_secular<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,
-                                                   itsum, guess);
+  int L = 1;
+  while (L < 32 && L * 8 < maxk) L *= 2;  // ~8 pole terms per lane
+  const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
+  switch (L) {
+#define SEC_CASE(LL)                                                                         \
+  case LL:                                                                                   \
+    k_secular<LL><<<grid, 256, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status, itsum, \
+                                        guess);                                              \
+    break;
+    SEC_CASE(1) SEC_CASE(2) SEC_CASE(4) SEC_CASE(8) SEC_CASE(16) SEC_CASE(32)
+#undef SEC_CASE
+  }
 }
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
                    const double *difr, const double *zw, double *zhat, cudaStream_t st) {

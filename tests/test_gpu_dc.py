@@ -47,12 +47,15 @@ def test_toeplitz_closed_form(n, precision):
     assert np.max(np.abs(w - toeplitz_eigs(n))) <= 4 * EV_TOL
 
 
-def test_plain_vs_batched_identical():
+def test_plain_vs_batched_agree():
+    # the lane-group width of the secular solver follows the largest K in a
+    # launch, so per-merge and per-level launches sum in different orders
     d, e = rand_tridiag(1500, seed=3)
     w1, Q1 = _check(d, e, batched=1)
     w2, Q2 = _check(d, e, batched=0)
-    assert np.array_equal(w1, w2)
-    assert np.array_equal(Q1, Q2)
+    assert np.max(np.abs(w1 - w2)) <= 1e-14 * np.max(np.abs(w1))
+    s = np.sign(np.sum(Q1 * Q2, axis=0))
+    assert np.max(np.abs(Q1 * s - Q2)) <= 1e-10
 
 
 def test_split_blocks():
