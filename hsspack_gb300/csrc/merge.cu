@@ -178,36 +178,85 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     if (w.typ[s + i] != 4) w.cand[s + pos++] = i;
   __syncthreads();
   // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371): a
-  //      sequential chain over the candidates, run by one thread
+  //      sequential chain over the candidates, run by one thread on a shared-
+  //      memory copy of their z, d, type (global memory when there are many)
+  constexpr int NCS = 1536;
+  __shared__ double c_z[NCS], c_d[NCS];
+  __shared__ unsigned char c_t[NCS];
   __shared__ int s_ng;
+  const bool in_smem = nc <= NCS;
+  if (in_smem) {
+    for (int t = tid; t < nc; t += MT) {
+      const int pos_t = w.cand[s + t];
+      c_z[t] = w.zs[s + pos_t];
+      c_d[t] = w.ds[s + pos_t];
+      c_t[t] = w.typ[s + pos_t];
+    }
+    __syncthreads();
+  }
   if (tid == 0) {
     int ng = 0;
-    int pj = w.cand[s];
-    for (int t = 1; t < nc; ++t) {
-      const int nj = w.cand[s + t];
-      const double zp = w.zs[s + pj], zn = w.zs[s + nj];
-      const double tau = hypot(zn, zp);
-      const double tt = w.ds[s + nj] - w.ds[s + pj];
-      const double c = zn / tau, sn = -zp / tau;
-      if (fabs(tt * c * sn) <= tol) {
-        w.zs[s + nj] = tau;
-        w.zs[s + pj] = 0.0;
-        if (w.typ[s + nj] != w.typ[s + pj]) w.typ[s + nj] = 2;
-        w.typ[s + pj] = 5;  // deflated by rotation: value changes, order fixed below
-        w.gvp[s + ng] = w.srt[s + pj];
-        w.gvq[s + ng] = w.srt[s + nj];
-        w.gvc[s + ng] = c;
-        w.gvs[s + ng] = sn;
-        ++ng;
-        const double dp = w.ds[s + pj], dn = w.ds[s + nj];
-        w.ds[s + pj] = dp * c * c + dn * sn * sn;
-        w.ds[s + nj] = dp * sn * sn + dn * c * c;
+    if (in_smem) {
+      int pj = 0;
+      for (int t = 1; t < nc; ++t) {
+        const int nj = t;
+        const double zp = c_z[pj], zn = c_z[nj];
+        const double tau = hypot(zn, zp);
+        const double tt = c_d[nj] - c_d[pj];
+        const double c = zn / tau, sn = -zp / tau;
+        if (fabs(tt * c * sn) <= tol) {
+          c_z[nj] = tau;
+          c_z[pj] = 0.0;
+          if (c_t[nj] != c_t[pj]) c_t[nj] = 2;
+          c_t[pj] = 5;  // deflated by rotation: value changes, order fixed below
+          w.gvp[s + ng] = w.srt[s + w.cand[s + pj]];
+          w.gvq[s + ng] = w.srt[s + w.cand[s + nj]];
+          w.gvc[s + ng] = c;
+          w.gvs[s + ng] = sn;
+          ++ng;
+          const double dp = c_d[pj], dn = c_d[nj];
+          c_d[pj] = dp * c * c + dn * sn * sn;
+          c_d[nj] = dp * sn * sn + dn * c * c;
+        }
+        pj = nj;
       }
-      pj = nj;
+    } else {
+      int pj = w.cand[s];
+      for (int t = 1; t < nc; ++t) {
+        const int nj = w.cand[s + t];
+        const double zp = w.zs[s + pj], zn = w.zs[s + nj];
+        const double tau = hypot(zn, zp);
+        const double tt = w.ds[s + nj] - w.ds[s + pj];
+        const double c = zn / tau, sn = -zp / tau;
+        if (fabs(tt * c * sn) <= tol) {
+          w.zs[s + nj] = tau;
+          w.zs[s + pj] = 0.0;
+          if (w.typ[s + nj] != w.typ[s + pj]) w.typ[s + nj] = 2;
+          w.typ[s + pj] = 5;
+          w.gvp[s + ng] = w.srt[s + pj];
+          w.gvq[s + ng] = w.srt[s + nj];
+          w.gvc[s + ng] = c;
+          w.gvs[s + ng] = sn;
+          ++ng;
+          const double dp = w.ds[s + pj], dn = w.ds[s + nj];
+          w.ds[s + pj] = dp * c * c + dn * sn * sn;
+          w.ds[s + nj] = dp * sn * sn + dn * c * c;
+        }
+        pj = nj;
+      }
     }
     s_ng = ng;
   }
   __syncthreads();
+  if (in_smem) {  // scatter the chain's results back
+    for (int t = tid; t < nc; t += MT) {
+      const int pos_t = w.cand[s + t];
+      w.zs[s + pos_t] = c_z[t];
+      w.ds[s + pos_t] = c_d[t];
+      w.typ[s + pos_t] = c_t[t];
+    }
+    __syncthreads();
+  }
   // ---- compact non-deflated (poles, weights, slots, block-structure groups)
   //      and deflated (slots, values) lists
   unsigned long long pk = 0;
