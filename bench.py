@@ -221,6 +221,9 @@ def run_ours(args):
     # "full": level-batched launches + split-BF16 tensor-core products;
     # "plain": per-merge launches, FP64 products, standard secular guess
     full_cfg = {"batched": 1, "precision": 1}
+    from hsspack_gb300 import predictor as _pred
+    if _pred.install():  # committed weights trained by hsspack_gb300/predictor.py
+        full_cfg["predictor"] = 1
     # DC leaf size from the project's autotuner (timed outside the measured region)
     from hsspack_gb300 import autotune
     tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg)
@@ -299,7 +302,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "tridiagonal DC eigensolve n=%d, D,E iid U[-1,1] seed 0, COMPZ='I'"
-                   % n, "n": n, "mode": "batched levels, split-BF16 tensor-core products",
+                   % n, "n": n, "mode": "batched levels, split-BF16 tensor-core products" +
+                           (", learned secular start" if full_cfg.get("predictor") else ""),
                    "smlsiz": full_cfg.get("smlsiz"), "autotune_ms": tune_ms,
                    "l2": "no flush: the 8.6 GB eigenvector matrix exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -317,7 +321,7 @@ def run_ours(args):
         "profiled_stage_share": {k: v / total_ms for k, v in acc["ms"].items() if v > 0},
         "stats": {k: st[k] for k in ("n_levels", "n_merges", "n_hss_merges", "n_dense_merges",
                                      "max_k", "max_rank", "total_k", "secular_iters",
-                                     "secular_roots")},
+                                     "secular_roots", "predictor_fallbacks")},
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -52,6 +52,7 @@ struct Ctx {
   hss_stats stats;
   std::string err;
   std::map<std::string, Buf> bufs;
+  bool pred_ready = false;  // learned secular predictor installed
   void *pinned = nullptr;
   size_t pinned_cap = 0;
   long long launches = 0;
@@ -163,6 +164,7 @@ struct MergeLevel {
 
 // Level arrays shared by all stages of one level (length = block size n).
 struct LevelArrays {
+  int n = 0;
   LevelScratch w;
   double *lam, *difl, *difr, *zhat, *alpha;
   int *iters;
@@ -170,6 +172,7 @@ struct LevelArrays {
 
 static LevelArrays level_arrays(Ctx &c, int n) {
   LevelArrays a;
+  a.n = n;
   a.w.srt = buf<int>(c, "srt", n);
   a.w.ds = buf<double>(c, "ds", n);
   a.w.zs = buf<double>(c, "zs", n);
@@ -283,10 +286,17 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   c.stats.secular_roots += total;
   double k2 = 0.0;
   for (int K : aK) k2 += (double)K * K;
+  float *guess = nullptr;
+  if (c.cfg.predictor && c.pred_ready) {
+    guess = buf<float>(c, "guess", L.n);
+    launch_predict(lv, total, L.w.dl, L.w.zw, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0),
+                   guess, st);
+    c.launches++;
+  }
   stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, *std::max_element(aK.begin(), aK.end()), L.w.dl, L.w.zw, L.lam, L.difl,
                  L.difr, L.iters, status,
-                 (unsigned long long *)(status + 2), nullptr, st);
+                 (unsigned long long *)(status + 2), guess, st);
   // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 8.0 * 4.0 * k2);
   stage_begin(HSS_ST_LOWNER, st);
@@ -445,9 +455,10 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
   double *Dp = buf<double>(c, "Dp", n);
   int *perm = buf<int>(c, "perm", n);
   double *d = buf<double>(c, "d_in", n), *e = buf<double>(c, "e_in", std::max(n, 1));
-  // status[0]: error code, status[2..3]: 64-bit sum of secular iterations
-  int *status = buf<int>(c, "status", 4);
-  CK(cudaMemsetAsync(status, 0, 4 * sizeof(int), st));
+  // status[0]: error code, status[2..3]: 64-bit sum of secular iterations,
+  // status[4..5]: 64-bit count of learned starts that fell back
+  int *status = buf<int>(c, "status", 6);
+  CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
   CK(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)n * n, st));
   // split into unreduced blocks and scale each (mdstedc.f90:305-345)
   std::vector<int> bstart, bend;
@@ -524,13 +535,15 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
   stage_end(HSS_ST_FINAL, st, 16LL * n * n + 20LL * n, 0.0);
   c.launches++;
   CK(cudaEventRecord(ev1, st));
-  int hst[4] = {0, 0, 0, 0};
+  int hst[6] = {0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const int hstatus = hst[0];
-  unsigned long long its;
+  unsigned long long its, fb;
   memcpy(&its, hst + 2, sizeof its);
+  memcpy(&fb, hst + 4, sizeof fb);
   c.stats.secular_iters = (long long)its;
+  c.stats.predictor_fallbacks = (long long)fb;
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   c.stats.ms_total = ms;
@@ -690,11 +703,24 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
     CK(cudaMemsetAsync(status, 0, sizeof(int), st));
     LevelView lv{vs, vK, vr, vo, 1};
-    launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, nullptr, nullptr, st);
+    float *guess = nullptr;
+    if (c.cfg.predictor && c.pred_ready) {
+      guess = buf<float>(c, "x_guess", k);
+      launch_predict(lv, k, dlamda, z, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0),
+                     guess, st);
+    }
+    unsigned long long *cnt = (unsigned long long *)buf<char>(c, "x_counts", 16);
+    CK(cudaMemsetAsync(cnt, 0, 16, st));
+    launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, cnt, guess, st);
+    unsigned long long hc[2];
+    CK(cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
     int hs = 0;
     CK(cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
+    c.stats.secular_iters = (long long)hc[0];
+    c.stats.secular_roots = k;
+    c.stats.predictor_fallbacks = (long long)hc[1];
     return hs ? 1 : 0;
   } catch (CudaError &ex) {
     c.err = ex.msg;
@@ -796,6 +822,106 @@ int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B,
       c.err = "tensor-core GEMM: bounded wait timed out";
       return 1;
     }
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_predictor_nparam(void) { return mlp_nparam(); }
+int hss_predictor_nfeat(void) { return mlp_nfeat(); }
+
+int hss_predictor_set(const float *W, const float *norm) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  try {
+    if (!W || !norm) { c.pred_ready = false; return 0; }
+    const int np = mlp_nparam(), nf = mlp_nfeat();
+    std::vector<unsigned short> wb(np);
+    for (int i = 0; i < np; ++i) {  // round to nearest even BF16
+      unsigned int u;
+      memcpy(&u, &W[i], 4);
+      u += 0x7fff + ((u >> 16) & 1);
+      wb[i] = (unsigned short)(u >> 16);
+    }
+    void *dw = buf<char>(c, "pred_wb", 2 * (size_t)np);
+    float *dn = buf<float>(c, "pred_norm", 2 * (size_t)nf);
+    CK(cudaMemcpy(dw, wb.data(), 2 * (size_t)np, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dn, norm, sizeof(float) * 2 * nf, cudaMemcpyHostToDevice));
+    c.pred_ready = true;
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_predictor_features_dev(int k, const double *d, const double *z, double rho,
+                               const double *difl, float *X, float *T, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k < 0) return -1;
+  try {
+    launch_train_features(k, d, z, rho, difl, X, T, (cudaStream_t)stream);
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_predictor_grad_dev(int n, const float *X, const float *T, const float *norm,
+                           const float *W, float *G, float *loss, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  try {
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemsetAsync(G, 0, sizeof(float) * mlp_nparam(), st));
+    CK(cudaMemsetAsync(loss, 0, sizeof(float), st));
+    launch_mlp_grad(n, X, T, norm, W, G, loss, st);
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_predictor_adam_dev(const float *G, float *W, float *M, float *V, float lr, int step,
+                           void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (step < 1) return -6;
+  try {
+    launch_adam(mlp_nparam(), W, G, M, V, lr, step, nullptr, (cudaStream_t)stream);
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_predict_dev(int k, const double *d, const double *z, double rho, float *guess,
+                    void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k < 0) return -1;
+  if (!c.pred_ready) { c.err = "no predictor installed"; return 1; }
+  try {
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<int> s(1, 0), K(1, k), off{0, k};
+    std::vector<double> r(1, rho);
+    int *vs = buf<int>(c, "x_s", 1), *vK = buf<int>(c, "x_K", 1), *vo = buf<int>(c, "x_off", 2);
+    double *vr = buf<double>(c, "x_rho", 1);
+    h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
+    LevelView lv{vs, vK, vr, vo, 1};
+    launch_predict(lv, k, d, z, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
     return 0;
   } catch (CudaError &ex) {
     c.err = ex.msg;

@@ -70,4 +70,16 @@ void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const in
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st);
 
+// predictor.cu
+int mlp_nparam();
+int mlp_nfeat();
+void launch_predict(const LevelView &lv, int total, const double *dl, const double *zw,
+                    const void *Wb, const float *norm, float *guess, cudaStream_t st);
+void launch_train_features(int K, const double *d, const double *z, double rho,
+                           const double *difl, float *X, float *T, cudaStream_t st);
+void launch_mlp_grad(int n, const float *X, const float *T, const float *norm, const float *W,
+                     float *G, float *L, cudaStream_t st);
+void launch_adam(int np, float *W, const float *G, float *M, float *V, float lr, int step,
+                 void *Wb, cudaStream_t st);
+
 }  // namespace hss

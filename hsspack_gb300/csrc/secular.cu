@@ -98,6 +98,8 @@ struct RootState {
   int phase;  // 0: first evaluation (midpoint), 1: iterating, 2: done
   int iters, status;
   bool last;
+  bool learned;  // started from the learned position; checked at the first step
+  bool fell_back;
 };
 
 __device__ __forceinline__ double pole(const RootState &r, int i) { return __ldg(r.d + i); }
@@ -114,6 +116,8 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq)
   r.delta = r.last ? 0.0 : pole(r, r.j + 1) - pole(r, r.j);
   r.top = r.rho * zsq;
   r.phase = 0;
+  r.learned = false;
+  r.fell_back = false;
   if (!r.last) {
     r.o = pole(r, r.j);
     r.tau = 0.5 * r.delta;
@@ -122,6 +126,7 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq)
       if (guess <= 0.5f) { r.o = pole(r, r.j); r.tau = x; r.lo = 0.0; r.hi = r.delta; }
       else { r.o = pole(r, r.j + 1); r.tau = x - r.delta; r.lo = -r.delta; r.hi = 0.0; }
       r.phase = 1;
+      r.learned = true;
     }
   } else {
     r.o = pole(r, r.K - 1);
@@ -166,6 +171,18 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   const double erretm = 8.0 * s.eabs + 2.0 * r.rhoinv + 3.0 * fabs(r.tau) * dw;
   if (fabs(w) <= HSS_EPS * erretm) { r.phase = 2; return; }
   if (r.iters > 41) { r.status = HSS_SECULAR_NOCONV; r.phase = 2; return; }
+  if (r.learned && r.iters == 1) {
+    // residual check of the learned start: a Newton step longer than a tenth
+    // of the pole gap means the guess is off; restart from the standard guess
+    r.learned = false;
+    if (fabs(w / dw) > 0.1 * r.delta) {
+      r.fell_back = true;
+      r.phase = 0;
+      r.o = pole(r, r.j);
+      r.tau = 0.5 * r.delta;
+      return;
+    }
+  }
   if (w < 0.0) r.lo = fmax(r.lo, r.tau); else r.hi = fmin(r.hi, r.tau);
   const double gl = (pole(r, r.jl) - r.o) - r.tau;
   const double gr = (pole(r, r.jr) - r.o) - r.tau;
@@ -258,7 +275,10 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
     difl[s + st.j] = dfl;
     difr[s + st.j] = dfr;
     if (iters) iters[s + st.j] = st.iters;
-    if (itsum) atomicAdd(itsum, (unsigned long long)st.iters);
+    if (itsum) {
+      atomicAdd(itsum, (unsigned long long)st.iters);
+      if (st.fell_back) atomicAdd(itsum + 1, 1ull);
+    }
     if (st.status) atomicMax(status, st.status);
   }
 }

@@ -120,6 +120,30 @@ int hss_cauchy_eig_dev(int k, const double *F, const double *u, const double *v,
 int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B, int ldb,
                  double *C, int ldc, int beta, int precision, void *stream);
 
+/* ---------------------------------------- learned secular initial iterate ----
+ * No reference counterpart: a 3 x 64 MLP (BF16 weights, FP32 math) predicting
+ * each root's position inside its pole interval from local features; used as
+ * the first iterate of the secular solver when hss_config.predictor = 1.  The
+ * FP64 iteration always finishes (and restarts from the standard guess when
+ * the learned start fails its residual check). */
+int hss_predictor_nparam(void);                 /* parameters (FP32 layout)    */
+int hss_predictor_nfeat(void);                  /* features per root           */
+/* install weights W[nparam] and feature normalisation norm[2*nfeat] (host) */
+int hss_predictor_set(const float *W, const float *norm);
+/* training features X[(k-1) x nfeat] and targets T[k-1] for one solved
+ * secular problem (device arrays) */
+int hss_predictor_features_dev(int k, const double *d, const double *z, double rho,
+                               const double *difl, float *X, float *T, void *stream);
+/* mean squared error and its gradient G[nparam] over n samples (device) */
+int hss_predictor_grad_dev(int n, const float *X, const float *T, const float *norm,
+                           const float *W, float *G, float *loss, void *stream);
+/* one Adam step on W with moments M, V (device arrays of nparam floats) */
+int hss_predictor_adam_dev(const float *G, float *W, float *M, float *V, float lr, int step,
+                           void *stream);
+/* learned start positions guess[k] (in (0,1); -1 where not predicted) */
+int hss_predict_dev(int k, const double *d, const double *z, double rho, float *guess,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif
