@@ -92,7 +92,7 @@ SIGNATURES = {
     "hss_predictor_nfeat": (ctypes.c_int, []),
     "hss_predictor_set": (ctypes.c_int, [_V, _V]),
     "hss_predictor_features_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V,
-                                                  _V, _V]),
+                                                  _V, _V, _V]),
     "hss_predictor_grad_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V, _V]),
     "hss_predictor_adam_dev": (ctypes.c_int, [_V, _V, _V, _V, ctypes.c_float, ctypes.c_int, _V]),
     "hss_predict_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V]),

@@ -288,10 +288,14 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   for (int K : aK) k2 += (double)K * K;
   float *guess = nullptr;
   if (c.cfg.predictor && c.pred_ready) {
+    // features for every position of the level (unused slots carry side = -1)
+    float *feat = buf<float>(c, "pred_feat", (size_t)L.n * (mlp_nfeat() + 1));
     guess = buf<float>(c, "guess", L.n);
-    launch_predict(lv, total, L.w.dl, L.w.zw, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0),
-                   guess, st);
-    c.launches++;
+    stage_begin(HSS_ST_SECULAR, st);
+    launch_secular_mid(lv, total, *std::max_element(aK.begin(), aK.end()), L.w.dl, L.w.zw, feat, st);
+    launch_predict(L.n, feat, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
+    stage_end(HSS_ST_SECULAR, st, 0, 0.0);
+    c.launches += 2;
   }
   stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, *std::max_element(aK.begin(), aK.end()), L.w.dl, L.w.zw, L.lam, L.difl,
@@ -705,9 +709,10 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     LevelView lv{vs, vK, vr, vo, 1};
     float *guess = nullptr;
     if (c.cfg.predictor && c.pred_ready) {
+      float *feat = buf<float>(c, "x_feat", (size_t)k * (mlp_nfeat() + 1));
       guess = buf<float>(c, "x_guess", k);
-      launch_predict(lv, k, dlamda, z, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0),
-                     guess, st);
+      launch_secular_mid(lv, k, k, dlamda, z, feat, st);
+      launch_predict(k, feat, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
     }
     unsigned long long *cnt = (unsigned long long *)buf<char>(c, "x_counts", 16);
     CK(cudaMemsetAsync(cnt, 0, 16, st));
@@ -858,12 +863,23 @@ int hss_predictor_set(const float *W, const float *norm) {
 }
 
 int hss_predictor_features_dev(int k, const double *d, const double *z, double rho,
-                               const double *difl, float *X, float *T, void *stream) {
+                               const double *difl, const double *difr, float *X, float *T,
+                               void *stream) {
   Ctx &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
   if (k < 0) return -1;
+  if (k < 2) return 0;
   try {
-    launch_train_features(k, d, z, rho, difl, X, T, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<int> s(1, 0), K(1, k), off{0, k};
+    std::vector<double> r(1, rho);
+    int *vs = buf<int>(c, "x_s", 1), *vK = buf<int>(c, "x_K", 1), *vo = buf<int>(c, "x_off", 2);
+    double *vr = buf<double>(c, "x_rho", 1);
+    h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
+    LevelView lv{vs, vK, vr, vo, 1};
+    float *feat = buf<float>(c, "x_feat", (size_t)k * (mlp_nfeat() + 1));
+    launch_secular_mid(lv, k, k, d, z, feat, st);
+    launch_train_targets(k, d, difl, difr, feat, X, T, st);
     CK(cudaGetLastError());
     return 0;
   } catch (CudaError &ex) {
@@ -919,7 +935,9 @@ int hss_predict_dev(int k, const double *d, const double *z, double rho, float *
     double *vr = buf<double>(c, "x_rho", 1);
     h2d(vs, s, st); h2d(vK, K, st); h2d(vo, off, st); h2d(vr, r, st);
     LevelView lv{vs, vK, vr, vo, 1};
-    launch_predict(lv, k, d, z, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
+    float *feat = buf<float>(c, "x_feat", (size_t)k * (mlp_nfeat() + 1));
+    launch_secular_mid(lv, k, k, d, z, feat, st);
+    launch_predict(k, feat, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     return 0;

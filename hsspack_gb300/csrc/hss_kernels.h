@@ -73,10 +73,14 @@ void launch_final_gather(int n, const int *perm, const double *Dp, const double 
 // predictor.cu
 int mlp_nparam();
 int mlp_nfeat();
-void launch_predict(const LevelView &lv, int total, const double *dl, const double *zw,
-                    const void *Wb, const float *norm, float *guess, cudaStream_t st);
-void launch_train_features(int K, const double *d, const double *z, double rho,
-                           const double *difl, float *X, float *T, cudaStream_t st);
+void launch_predict(int n, const float *feat, const void *Wb, const float *norm, float *guess,
+                    cudaStream_t st);
+void launch_train_targets(int K, const double *d, const double *difl, const double *difr,
+                          const float *feat, float *X, float *T, cudaStream_t st);
+// secular.cu: midpoint evaluation producing the predictor features, nf + 1
+// floats per root at position s + j (the level layout)
+void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *dl,
+                        const double *zw, float *feat, cudaStream_t st);
 void launch_mlp_grad(int n, const float *X, const float *T, const float *norm, const float *W,
                      float *G, float *L, cudaStream_t st);
 void launch_adam(int np, float *W, const float *G, float *M, float *V, float lr, int step,

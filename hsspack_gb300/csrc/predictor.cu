@@ -1,21 +1,25 @@
 // predictor.cu -- learned initial iterate for the secular solver.
 //
 // For a non-last root j of f(x) = 1/rho + sum_i z_i^2/(d_i - x), with
-// delta = d_{j+1} - d_j, the target is x* = (lam_j - d_j)/delta in (0, 1).
-// Local features (O(W) work per root, W = 6 poles each side):
-//   f0 = log(z_j^2/delta), f1 = log(z_{j+1}^2/delta), f2 = log(delta/rho),
-//   f3/f4 = windowed left/right far sums at the midpoint (times delta),
-//   f5/f6 = log gaps to the next pole on each side (over delta),
-//   f7 = logit of the analytic two-pole guess with the windowed far sum.
-// A 3 x 64 MLP (ReLU) maps the features to a logit correction; the guess is
-// sigmoid(f7 + mlp(f)).  Weights are stored in BF16, all arithmetic in FP32.
-// The FP64 secular iteration starts from this guess and always runs to
-// convergence inside its bracket, so a poor prediction costs iterations only.
+// delta = d_{j+1} - d_j and x = d_j + t*delta, delta*f = c(t) - a/t + b/(1-t)
+// where a = z_j^2, b = z_{j+1}^2 and c(t) collects 1/rho and every far pole.
+// The midpoint pass (k_secular_mid, secular.cu) evaluates the full sums at
+// t = 1/2 -- exactly the first evaluation of the standard method -- and gives
+// c0 = c(1/2), c1 = c'(1/2).  Features:
+//   f0 = log(a/|c0|), f1 = log(b/|c0|), f2 = c1/|c0|, f3 = sign(c0),
+//   f4/f5 = log of the neighbouring pole gaps over delta,
+//   f6 = logit t0 (two-pole root with c = c0, the standard guess),
+//   f7 = logit t1 (two-pole root with c = c0 + c1 (t0 - 1/2)).
+// A 3 x 64 MLP (ReLU) predicts the residual logit(t*) - f7; the learned start
+// is sigmoid(f7 + mlp(f)) kept inside the half interval that the sign of
+// f(midpoint) selects.  Weights are stored in BF16, arithmetic in FP32.  The
+// FP64 secular iteration starts there and always runs to convergence inside
+// its bracket (restarting from the standard guess if the start fails its
+// residual check), so a poor prediction costs iterations only.
 //
-// Training (hand-written): forward / backward of the same network over a batch
-// in FP32 (one thread per sample, gradients reduced per CTA in shared memory,
-// then one atomic per parameter per CTA), mean squared error on the logit,
-// Adam update.
+// Training (hand-written): forward / backward of the same network in FP32
+// (one thread per sample, gradients reduced per CTA in shared memory, then one
+// atomic per parameter per CTA), mean squared error, Adam update.
 #include <cuda_bf16.h>
 
 #include "hss_common.cuh"
@@ -34,48 +38,6 @@ constexpr int P_W1 = 0, P_B1 = P_W1 + NF * NH, P_W2 = P_B1 + NH, P_B2 = P_W2 + N
 
 __device__ __forceinline__ float clampf(float x, float lo, float hi) {
   return fminf(fmaxf(x, lo), hi);
-}
-
-// Features of root j (non-last) of the secular problem (d, z, rho, K).
-__device__ void root_features(const double *__restrict__ d, const double *__restrict__ z, int K,
-                             double rho, int j, float *f) {
-  const double dj = d[j], dj1 = d[j + 1];
-  const double delta = dj1 - dj;
-  const double mid = dj + 0.5 * delta;
-  const double a = z[j] * z[j] / delta, b = z[j + 1] * z[j + 1] / delta;
-  double sl = 0.0, sr = 0.0;
-  for (int i = max(0, j - WIN); i < j; ++i) sl += z[i] * z[i] / (d[i] - mid);
-  for (int i = j + 2; i <= min(K - 1, j + 1 + WIN); ++i) sr += z[i] * z[i] / (d[i] - mid);
-  sl *= delta;
-  sr *= delta;
-  // two-pole model  c - a/x + b/(1-x) = 0  (units of 1/delta), c = delta/rho + sl + sr
-  const double c = delta / rho + sl + sr;
-  // c x (1 - x) - a (1 - x) + b x = 0  ->  -c x^2 + (c + a + b) x - a = 0
-  double x0;
-  {
-    const double A = -c, B = c + a + b, C = -a;
-    if (fabs(A) < 1e-300) {
-      x0 = a / (a + b);
-    } else {
-      double disc = B * B - 4.0 * A * C;
-      disc = disc < 0.0 ? 0.0 : disc;
-      const double q = -0.5 * (B + copysign(sqrt(disc), B));
-      const double r1 = q / A, r2 = (q != 0.0) ? C / q : r1;
-      x0 = (r1 > 0.0 && r1 < 1.0) ? r1 : r2;
-      if (!(x0 > 0.0 && x0 < 1.0)) x0 = 0.5;
-    }
-  }
-  x0 = fmin(fmax(x0, 1e-7), 1.0 - 1e-7);
-  const double gl = (j > 0) ? (dj - d[j - 1]) / delta : 1e3;
-  const double gr = (j + 2 < K) ? (d[j + 2] - dj1) / delta : 1e3;
-  f[0] = clampf((float)log(a + 1e-300), -80.f, 80.f);
-  f[1] = clampf((float)log(b + 1e-300), -80.f, 80.f);
-  f[2] = clampf((float)log(delta / rho + 1e-300), -80.f, 80.f);
-  f[3] = clampf((float)sl, -1e4f, 1e4f);
-  f[4] = clampf((float)sr, -1e4f, 1e4f);
-  f[5] = clampf((float)log(gl), -40.f, 40.f);
-  f[6] = clampf((float)log(gr), -40.f, 40.f);
-  f[7] = (float)log(x0 / (1.0 - x0));
 }
 
 // y = mlp(f) with weights given as FP32 (training) or read from BF16 (inference)
@@ -109,46 +71,48 @@ struct bf16w {
   __device__ operator float() const { return __bfloat162float(v); }
 };
 
-// Inference over the roots of a level: guess[s + j] for j < K-1 of every merge.
-// Features are normalised by (mu, sigma) before the network.
+// Inference: feat[(s+j)*(NF+1) + i] from the midpoint pass (slot NF holds the
+// side: 0 root in (d_j, midpoint], 1 in (midpoint, d_{j+1}), -1 no prediction).
 __global__ void __launch_bounds__(128)
-k_predict(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
-          const __nv_bfloat16 *__restrict__ Wb, const float *__restrict__ norm,
-          float *__restrict__ guess) {
+k_predict(int n, const float *__restrict__ feat, const __nv_bfloat16 *__restrict__ Wb,
+          const float *__restrict__ norm, float *__restrict__ guess) {
   __shared__ __nv_bfloat16 sW[NPARAM];
   for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) sW[i] = Wb[i];
   __syncthreads();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= __ldg(lv.rootoff + lv.P)) return;
-  int lo = 0, hi = lv.P;
-  while (hi - lo > 1) { int md = (lo + hi) >> 1; if (__ldg(lv.rootoff + md) <= r) lo = md; else hi = md; }
-  const int j = r - __ldg(lv.rootoff + lo);
-  const int s = __ldg(lv.s + lo), K = __ldg(lv.K + lo);
-  if (j >= K - 1 || K < 3) { guess[s + j] = -1.0f; return; }
-  float f[NF];
-  root_features(dl + s, zw + s, K, __ldg(lv.rho + lo), j, f);
+  if (r >= n) return;
+  const float *f = feat + (long long)r * (NF + 1);
+  const float side = f[NF];
+  if (side < 0.f) { guess[r] = 2.0f; return; }  // no prediction
   float fn[NF];
 #pragma unroll
   for (int i = 0; i < NF; ++i) fn[i] = (f[i] - norm[i]) / norm[NF + i];
   float h1[NH], h2[NH], h3[NH];
   const float y = mlp_forward(fn, reinterpret_cast<const bf16w *>(sW), h1, h2, h3);
-  const float logit = clampf(f[7] + y, -16.f, 16.f);
-  guess[s + j] = 1.f / (1.f + __expf(-logit));
+  const float l = f[NF - 1] + clampf(y, -1.f, 1.f);
+  // signed distance to the nearer pole: +u (left pole), -u (right pole)
+  float u;
+  if (side == 0.f) u = (l <= 0.f) ? __expf(l) / (1.f + __expf(l)) : 0.5f;
+  else u = (l > 0.f) ? __expf(-l) / (1.f + __expf(-l)) : 0.5f;
+  u = fminf(fmaxf(u, 1e-20f), side == 0.f ? 0.5f : 0.49999f);
+  guess[r] = side == 0.f ? u : -u;
 }
 
-// Training features and targets for one secular problem solved by the plain
-// solver: X[j] = features, T[j] = logit(difl_j / delta_j) - f7 (the correction).
-__global__ void k_train_features(int K, const double *__restrict__ d, const double *__restrict__ z,
-                                 double rho, const double *__restrict__ difl, float *__restrict__ X,
-                                 float *__restrict__ T) {
+// Training targets: T[j] = clamp(logit(difl_j / delta_j) - f7_j), from the
+// midpoint features of one solved secular problem (non-last roots).
+__global__ void k_train_targets(int K, const double *__restrict__ d,
+                                const double *__restrict__ difl, const double *__restrict__ difr,
+                                const float *__restrict__ feat, float *__restrict__ X,
+                                float *__restrict__ T) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= K - 1) return;
-  float f[NF];
-  root_features(d, z, K, rho, j, f);
+  const float *f = feat + (long long)j * (NF + 1);
   for (int i = 0; i < NF; ++i) X[(long long)j * NF + i] = f[i];
-  double x = difl[j] / (d[j + 1] - d[j]);
-  x = fmin(fmax(x, 1e-7), 1.0 - 1e-7);
-  T[j] = (float)log(x / (1.0 - x)) - f[7];
+  // logit of the root's position: log(t / (1 - t)) = log(difl / -difr)
+  const double l = log(fmax(difl[j], 1e-300) / fmax(-difr[j], 1e-300));
+  // only small refinements of the analytic start are learned; larger
+  // residuals are rare and left to the FP64 iteration
+  T[j] = clampf((float)(l - (double)f[NF - 1]), -1.f, 1.f);
 }
 
 // One training pass over n samples: loss = mean (mlp(xn) - t)^2; gradients
@@ -237,17 +201,16 @@ __global__ void k_adam(int np, float *__restrict__ W, const float *__restrict__ 
 int mlp_nparam() { return NPARAM; }
 int mlp_nfeat() { return NF; }
 
-void launch_predict(const LevelView &lv, int total, const double *dl, const double *zw,
-                    const void *Wb, const float *norm, float *guess, cudaStream_t st) {
-  if (total <= 0) return;
-  k_predict<<<(total + 127) / 128, 128, 0, st>>>(lv, dl, zw, (const __nv_bfloat16 *)Wb, norm,
-                                                 guess);
+void launch_predict(int n, const float *feat, const void *Wb, const float *norm, float *guess,
+                    cudaStream_t st) {
+  if (n <= 0) return;
+  k_predict<<<(n + 127) / 128, 128, 0, st>>>(n, feat, (const __nv_bfloat16 *)Wb, norm, guess);
 }
 
-void launch_train_features(int K, const double *d, const double *z, double rho,
-                           const double *difl, float *X, float *T, cudaStream_t st) {
+void launch_train_targets(int K, const double *d, const double *difl, const double *difr,
+                          const float *feat, float *X, float *T, cudaStream_t st) {
   if (K < 2) return;
-  k_train_features<<<(K + 127) / 128, 128, 0, st>>>(K, d, z, rho, difl, X, T);
+  k_train_targets<<<(K + 127) / 128, 128, 0, st>>>(K, d, difl, difr, feat, X, T);
 }
 
 void launch_mlp_grad(int n, const float *X, const float *T, const float *norm, const float *W,

@@ -121,12 +121,13 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq)
   if (!r.last) {
     r.o = pole(r, r.j);
     r.tau = 0.5 * r.delta;
-    if (guess > 0.0f && guess < 1.0f) {  // learned position inside (d_j, d_{j+1})
-      const double x = (double)guess * r.delta;
-      if (guess <= 0.5f) { r.o = pole(r, r.j); r.tau = x; r.lo = 0.0; r.hi = r.delta; }
-      else { r.o = pole(r, r.j + 1); r.tau = x - r.delta; r.lo = -r.delta; r.hi = 0.0; }
+    if (guess != 0.0f && fabsf(guess) <= 0.5f) {  // learned signed distance to the nearer pole
+      // the midpoint pass already fixed the half interval (one evaluation)
+      if (guess > 0.0f) { r.o = pole(r, r.j); r.tau = (double)guess * r.delta; r.lo = 0.0; r.hi = 0.5 * r.delta; }
+      else { r.o = pole(r, r.j + 1); r.tau = (double)guess * r.delta; r.lo = -0.5 * r.delta; r.hi = 0.0; }
       r.phase = 1;
       r.learned = true;
+      r.iters = 1;
     }
   } else {
     r.o = pole(r, r.K - 1);
@@ -168,14 +169,20 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   }
   // middle-way step
   const double dw = s.dpsi + s.dphi;
+  if (!(fabs(w) <= 1.7e308) || !(dw <= 1.7e308)) {  // overflow next to a pole: bisect
+    if (r.iters > 41) { r.status = HSS_SECULAR_NOCONV; r.phase = 2; return; }
+    r.learned = false;
+    r.tau = 0.5 * (r.lo + r.hi);
+    return;
+  }
   const double erretm = 8.0 * s.eabs + 2.0 * r.rhoinv + 3.0 * fabs(r.tau) * dw;
   if (fabs(w) <= HSS_EPS * erretm) { r.phase = 2; return; }
   if (r.iters > 41) { r.status = HSS_SECULAR_NOCONV; r.phase = 2; return; }
-  if (r.learned && r.iters == 1) {
-    // residual check of the learned start: a Newton step longer than a tenth
-    // of the pole gap means the guess is off; restart from the standard guess
+  if (r.learned && r.iters == 2) {
+    // residual check of the learned start: a Newton step across most of the
+    // half interval means the start is unusable; restart from the standard guess
     r.learned = false;
-    if (fabs(w / dw) > 0.1 * r.delta) {
+    if (!(fabs(w / dw) <= 0.45 * r.delta)) {
       r.fell_back = true;
       r.phase = 0;
       r.o = pole(r, r.j);
@@ -254,7 +261,7 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
   for (int i = gl; i < st.K; i += L) zsq += __ldg(st.z + i) * __ldg(st.z + i);
   zsq = group_sum<L>(zsq);
   const bool trivial = !valid || st.K == 1;
-  if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : -1.0f, zsq);
+  if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq);
   else st.phase = 2;
   while (__any_sync(HSS_FULL, st.phase != 2)) {
     const SecSums sm = sec_eval<L>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.o, st.tau, st.jl, gl);
@@ -410,6 +417,89 @@ __global__ void k_cauchylike(int M, int N, const double *__restrict__ D,
   A[idx] = __ldg(u + i) * __ldg(v + j) / (__ldg(D + i) - __ldg(F + j));
 }
 
+// Midpoint pass for the learned start: per non-last root, the full secular
+// sums at the midpoint of (d_j, d_{j+1}) (the standard method's first
+// evaluation) turned into the predictor's features (see predictor.cu).
+// Root of the two-pole model  c - a/t + b/(1-t) = 0  in (0, 1), returned as
+// the distance u to the nearer pole (side 0: t = u, side 1: t = 1 - u), each
+// side solved from its own quadratic so that u keeps full relative accuracy.
+__device__ __forceinline__ double small_root(double A, double B, double C) {
+  // root of A u^2 + B u + C = 0 nearest 0 (stable form)
+  if (fabs(A) < 1e-300) return -C / B;
+  double disc = B * B - 4.0 * A * C;
+  disc = disc < 0.0 ? 0.0 : disc;
+  const double q = -0.5 * (B + copysign(sqrt(disc), B));
+  return (q != 0.0) ? C / q : -B / (2.0 * A);
+}
+__device__ __forceinline__ double pole_root_u(double c, double a, double b, int &side) {
+  // side 0:  c t(1-t) - a(1-t) + b t = 0   ->  -c t^2 + (c+a+b) t - a = 0
+  // side 1 (t = 1-u):  -c u^2 + (c-a-b) u + b = 0
+  const double f_half = c - 2.0 * a + 2.0 * b;  // delta*f at t = 1/2
+  double u;
+  if (f_half >= 0.0) { side = 0; u = small_root(-c, c + a + b, -a); }
+  else { side = 1; u = small_root(-c, c - a - b, b); }
+  if (!(u > 0.0)) u = 1e-300;
+  return fmin(u, 0.5);
+}
+__device__ __forceinline__ double logit_u(double u, int side) {
+  const double l = log(u / (1.0 - u));
+  return side == 0 ? l : -l;
+}
+
+template <int L>
+__global__ void __launch_bounds__(256)
+k_secular_mid(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
+              float *__restrict__ feat) {
+  constexpr int NFP = 9;  // 8 features + side
+  const int lane = threadIdx.x & 31, gl = lane & (L - 1);
+  const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
+  const int total = __ldg(lv.rootoff + lv.P);
+  int s = 0, j = 0, K = 0;
+  double rho = 1.0;
+  if (r < total) {
+    const int m = find_merge(lv.rootoff, lv.P, r);
+    s = __ldg(lv.s + m);
+    j = r - __ldg(lv.rootoff + m);
+    K = __ldg(lv.K + m);
+    rho = __ldg(lv.rho + m);
+  }
+  const bool active = (r < total) && (j < K - 1) && K >= 2;
+  const double *d = dl + s, *z = zw + s;
+  double o = 0.0, tm = 0.0, delta = 1.0;
+  if (active) {
+    o = __ldg(d + j);
+    delta = __ldg(d + j + 1) - o;
+    tm = 0.5 * delta;
+  }
+  const SecSums sm = sec_eval<L>(d, z, active ? K : 0, o, tm, j, gl);
+  if (r >= total || gl != 0) return;
+  float *f = feat + (long long)(s + j) * NFP;
+  if (!active) { f[NFP - 1] = -1.f; return; }
+  const double zj = __ldg(z + j), zj1 = __ldg(z + j + 1);
+  const double gl_ = (__ldg(d + j) - o) - tm, gr_ = (__ldg(d + j + 1) - o) - tm;
+  const double w = 1.0 / rho + sm.psi + sm.phi, dw = sm.dpsi + sm.dphi;
+  const double a = zj * zj, b = zj1 * zj1;
+  const double c0 = delta * (w - zj * (zj / gl_) - zj1 * (zj1 / gr_));
+  const double c1 = delta * delta * (dw - (zj / gl_) * (zj / gl_) - (zj1 / gr_) * (zj1 / gr_));
+  int s0, s1;
+  const double u0 = pole_root_u(c0, a, b, s0);
+  const double t0 = s0 == 0 ? u0 : 1.0 - u0;
+  const double u1 = pole_root_u(c0 + c1 * (t0 - 0.5), a, b, s1);
+  const double ac = fmax(fabs(c0), 1e-300);
+  const double gapl = (j > 0) ? (__ldg(d + j) - __ldg(d + j - 1)) / delta : 1e3;
+  const double gapr = (j + 2 < K) ? (__ldg(d + j + 2) - __ldg(d + j + 1)) / delta : 1e3;
+  auto cl = [](double x, double lo, double hi) { return (float)fmin(fmax(x, lo), hi); };
+  f[0] = cl(log(a / ac + 1e-300), -60, 60);
+  f[1] = cl(log(b / ac + 1e-300), -60, 60);
+  f[2] = cl(c1 / ac, -1e3, 1e3);
+  f[3] = c0 >= 0.0 ? 1.f : -1.f;
+  f[4] = cl(log(gapl), -40, 40);
+  f[5] = cl(log(gapr), -40, 40);
+  f[6] = cl(logit_u(u0, s0), -700, 700);
+  f[7] = cl(logit_u(u1, s1), -700, 700);
+  f[8] = (w >= 0.0) ? 0.f : 1.f;  // root left / right of the midpoint
+}
+
 // ---------------------------------------------------------------- launch --
 static inline int warp_grid(int total, int threads) {
   return (int)(((long long)total * 32 + threads - 1) / threads);
@@ -431,6 +521,20 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
 #undef SEC_CASE
   }
 }
+void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *dl,
+                        const double *zw, float *feat, cudaStream_t st) {
+  if (total <= 0) return;
+  int L = 1;
+  while (L < 32 && L * 8 < maxk) L *= 2;
+  const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
+  switch (L) {
+#define MID_CASE(LL) \
+  case LL: k_secular_mid<LL><<<grid, 256, 0, st>>>(lv, dl, zw, feat); break;
+    MID_CASE(1) MID_CASE(2) MID_CASE(4) MID_CASE(8) MID_CASE(16) MID_CASE(32)
+#undef MID_CASE
+  }
+}
+
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
                    const double *difr, const double *zw, double *zhat, cudaStream_t st) {
   if (total <= 0) return;

@@ -80,7 +80,8 @@ def collect(problems):
             X = torch.zeros((k - 1) * nf, dtype=torch.float32, device="cuda")
             T = torch.zeros(k - 1, dtype=torch.float32, device="cuda")
             rc = L.hss_predictor_features_dev(k, hp._ptr(dd), hp._ptr(zz), float(rho), hp._ptr(difl),
-                                              hp._ptr(X), hp._ptr(T), hp._stream(None))
+                                              hp._ptr(difr), hp._ptr(X), hp._ptr(T),
+                                              hp._stream(None))
             if rc != 0:
                 raise hp.HssError("features rc=%d" % rc)
             Xs.append(X.view(k - 1, nf))
@@ -211,10 +212,16 @@ def main(argv=None):
     base, _, lam0 = iterations(test_p, False)
     pred, fb, lam1 = iterations(test_p, True)
     dmax = max(float(np.max(np.abs(a - b))) for a, b in zip(lam0, lam1))
+    # ablation: the analytic slope-refined start alone (network output 0)
+    zero = np.zeros_like(W)
+    hp.load().hss_predictor_set(zero.ctypes.data, norm.ctypes.data)
+    analytic, fb0, _ = iterations(test_p, True)
+    install(a.out)
     print(json.dumps({"samples": int(T.numel()), "train_loss": loss,
                       "evaluations_per_root_standard": base,
+                      "evaluations_per_root_analytic_start": analytic,
                       "evaluations_per_root_learned": pred, "fallbacks": fb,
-                      "max_root_difference": dmax}))
+                      "fallbacks_analytic": fb0, "max_root_difference": dmax}))
 
 
 if __name__ == "__main__":

