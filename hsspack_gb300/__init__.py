@@ -85,6 +85,7 @@ SIGNATURES = {
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
     "hss_lowner_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V]),
+    "hss_lowner_noalloc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V]),
     "hss_dhssevc_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, _V, _V, _V, _V,
                                        _V, _V, ctypes.c_int, ctypes.c_int, _V]),
     "hss_cauchy_eig_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V, _V]),

@@ -564,6 +564,13 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
   return 0;
 }
 
+// Message for hss_last_error() from entry points that live outside this file.
+void set_last_error(const std::string &msg) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  c.err = msg;
+}
+
 }  // namespace hss
 
 // ================================================================== C ABI ==

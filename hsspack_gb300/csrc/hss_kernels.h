@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
+
 namespace hss {
 
 // Merges of one DC level that have K > 0, compacted: merge m owns positions
@@ -85,5 +87,8 @@ void launch_mlp_grad(int n, const float *X, const float *T, const float *norm, c
                      float *G, float *L, cudaStream_t st);
 void launch_adam(int np, float *W, const float *G, float *M, float *V, float lr, int step,
                  void *Wb, cudaStream_t st);
+
+// driver.cu: set the message hss_last_error() returns
+void set_last_error(const std::string &msg);
 
 }  // namespace hss

@@ -99,6 +99,18 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho,
 int hss_lowner_dev(int k, const double *dlamda, const double *difl,
                    const double *difr, double *z, double *alpha, void *stream);
 
+/* hss_lowner_dev without any device allocation; no counterpart in the
+ * reference.  For callers that cannot let a library allocate device memory
+ * (all of it reserved by their own allocator, or allocation forbidden after
+ * start-up): the scratch is a static device array of 65536 doubles, so
+ * k <= 65536 (larger k returns -1 and sets hss_last_error()).  The first call
+ * on a device resolves the scratch address and should come at set-up, before
+ * any stream capture.  All calls share the scratch; calls are serialised and
+ * wait for their stream, since overlapping ones would race on it. */
+int hss_lowner_noalloc_dev(int k, const double *dlamda, const double *difl,
+                           const double *difr, double *z, double *alpha,
+                           void *stream);
+
 /* DHSSEVC (SRC/CauchyHssEig.f90:2444): Q(0:nrows, 0:K) <- Q * C where
  * C(i,j) = u_i v_j / (F_i - lam_j), lam_j = F_j + difl_j, compressed to HSS
  * with leaf ni and tolerance tol.  Q is column-major with leading dim ldq. */
