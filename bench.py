@@ -7,7 +7,9 @@ eigenvector matrix (8.6 GB) is far larger than L2, so no flush is needed
 between steps.
 
 value: device-resident seconds per solve (inputs already in HBM, CUDA events
-on the launching stream over exactly K steps).  e2e: the same solve through the
+on the launching stream over exactly K steps).  batch: the second half of the
+metric, 512 uneven tridiagonals (n log-uniform in [256, 4096]) solved in one
+batched call, as solves/s, beside one call per problem and the plain GPU merge.  e2e: the same solve through the
 Fortran drop-in ``mdstedc_`` with pinned host buffers (D/E host->device and
 Z/W device->host inside the timed region).  roofline: the stage that takes the
 most device time, its algorithmic bytes (or flops) over its event-timed
@@ -131,6 +133,111 @@ def cpu_reference_sample(n_sample, n_target, threads):
     t = time.perf_counter() - t
     scale = (n_target / n_sample) ** 2 * (np.log2(n_target) / np.log2(n_sample))
     return t, t * scale, scale
+
+
+BATCH_COUNT, BATCH_LO, BATCH_HI = 512, 256, 4096
+
+
+def batch_inputs(seed=2):
+    """512 tridiagonals, n = round(exp(U[ln 256, ln 4096])) (seed 2), D, E iid
+    U[-1, 1] (problem p from seed 1000 + p)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.round(np.exp(rng.uniform(np.log(BATCH_LO), np.log(BATCH_HI), BATCH_COUNT)))
+    sizes = sizes.astype(np.int32)
+    probs = [inputs(int(n), seed=1000 + p) for p, n in enumerate(sizes)]
+    return sizes, probs
+
+
+def batch_cpu_sample(sizes, probs, threads, count=12):
+    """CPU oracle on the first `count` problems of the batch, scaled to all 512
+    by sum n^2 log n."""
+    import oracle
+    oracle.set_threads(threads)
+    t = time.perf_counter()
+    for p in range(count):
+        oracle.eigh_tridiagonal(*probs[p])
+    t = time.perf_counter() - t
+    w = sizes.astype(np.float64) ** 2 * np.log2(sizes.astype(np.float64))
+    scale = float(w.sum() / w[:count].sum())
+    return t, t * scale, scale
+
+
+def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
+    """The uneven batch: solves/s batched (one call), one call per problem, and
+    with the plain GPU merge; residual of every problem on the device."""
+    sizes, probs = batch_inputs()
+    _, D, E = hp.pack_batch(probs)
+    o, oz = hp.batch_offsets(sizes)
+    d0 = torch.tensor(D, device="cuda")
+    e0 = torch.tensor(E, device="cuda")
+    d, e = d0.clone(), e0.clone()
+    z = torch.empty(int(oz[-1]), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def batched():
+        d.copy_(d0)
+        e.copy_(e0)
+        hp.mdstedc_batch_dev(sizes, d, e, z, stream=stream)
+
+    def loop():
+        for p in range(len(sizes)):
+            a, b = int(o[p]), int(o[p + 1])
+            d[a:b].copy_(d0[a:b])
+            e[a:b].copy_(e0[a:b])
+            hp.mdstedc_dev(d[a:b], e[a:b], z[int(oz[p]):int(oz[p + 1])], stream=stream)
+
+    def timed(fn, steps, warmup, cfg):
+        old = hp.set_config(**cfg)
+        launches = 0
+        try:
+            for _ in range(warmup):
+                fn()
+            if world > 1:
+                dist.barrier()
+            torch.cuda.synchronize()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(steps):
+                fn()
+                launches += hp.get_stats()["kernel_launches"]
+            t1.record(stream)
+            torch.cuda.synchronize()
+            return t0.elapsed_time(t1) / steps, launches
+        finally:
+            hp.restore_config(old)
+
+    steps = max(1, min(args.steps, 5))
+    ms, launches = timed(batched, steps, max(3, args.warmup), full_cfg)
+    # every problem's residual ||TQ - QW||_F / (n ||T||) from the last solve
+    res = 0.0
+    for p, n in enumerate(sizes):
+        n = int(n)
+        a, b = int(o[p]), int(o[p + 1])
+        Q = z[int(oz[p]):int(oz[p + 1])].view(n, n).T
+        dd, ee = d0[a:b], e0[a:b - 1]
+        R = dd[:, None] * Q - Q * d[a:b][None, :]
+        R[:-1] += ee[:, None] * Q[1:]
+        R[1:] += ee[:, None] * Q[:-1]
+        tn = float(dd.abs().max() + 2 * ee.abs().max())
+        res = max(res, float(torch.linalg.norm(R)) / (n * tn))
+    ms_loop, _ = timed(loop, 1, 1, full_cfg)
+    ms_plain, _ = timed(batched, 1, 0, plain_cfg)
+    out = {"workload": "512 tridiagonals, n log-uniform in [256, 4096] (seed 2), D,E iid U[-1,1]",
+           "sum_n": int(o[-1]), "sum_n2": int(oz[-1]),
+           "solves_per_s": len(sizes) * 1000.0 / ms, "ms_per_batch": ms,
+           "gpu_launches_per_batch": launches / steps,
+           "loop_solves_per_s": len(sizes) * 1000.0 / ms_loop,
+           "plain_solves_per_s": len(sizes) * 1000.0 / ms_plain,
+           "full_vs_plain": ms_plain / ms, "batched_vs_loop": ms_loop / ms,
+           "resid_max": res}
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        t_s, scaled, scale = batch_cpu_sample(sizes, probs, threads)
+        out["cpu_baseline"] = {"value": len(sizes) / scaled, "unit": "solves/s", "cores": threads,
+                               "kind": "port",
+                               "sample": "first 12 problems (%.2f s), x%.1f (sum n^2 log n) to 512"
+                                         % (t_s, scale)}
+    return out
 
 
 def run_reference(args):
@@ -272,6 +379,10 @@ def run_ours(args):
         dist.all_reduce(x, op=dist.ReduceOp.MAX)
         e2e_s = float(x)
 
+    batch = None
+    if not args.no_batch:
+        batch = run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist)
+
     # dominant stage -> roofline
     pk = peaks()
     top = max(acc["ms"], key=lambda s: acc["ms"][s])
@@ -317,6 +428,7 @@ def run_ours(args):
         "batched_fp64_s": ms_fp64 / 1000.0,
         "full_vs_plain": ms_plain / ms,
         "accuracy": acc_chk,
+        "batch": batch,
         "stages_ms_per_step": {k: v / args.steps for k, v in acc["ms"].items() if v > 0},
         "profiled_stage_share": {k: v / total_ms for k, v in acc["ms"].items() if v > 0},
         "stats": {k: st[k] for k in ("n_levels", "n_merges", "n_hss_merges", "n_dense_merges",
@@ -337,6 +449,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batch figures")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warmup + timed solves (for ncu launch lists)")
     args = ap.parse_args()

@@ -14,7 +14,8 @@ failure):
 * :func:`cauchylike` -- ``Cauchylike(A,D,F,u,v,M,N)`` (SRC/Cauchylike.f90:1).
 
 Device entry points take torch CUDA tensors (torch is used only to hold device
-memory and streams): :func:`mdstedc_dev`, :func:`secular_dev`,
+memory and streams): :func:`mdstedc_dev`, :func:`mdstedc_batch_dev`
+(many problems of uneven sizes in one call), :func:`secular_dev`,
 :func:`lowner_dev`, :func:`dhssevc_dev`, :func:`cauchy_eig_dev`.
 """
 import ctypes
@@ -26,7 +27,8 @@ from . import build as _build
 
 __all__ = [
     "Config", "Stats", "load", "get_config", "set_config", "get_stats", "finalize",
-    "mdstedc", "eigh_tridiagonal", "cauchylike", "mdstedc_dev", "secular_dev",
+    "mdstedc", "eigh_tridiagonal", "cauchylike", "mdstedc_dev", "mdstedc_batch_dev",
+    "batch_offsets", "secular_dev",
     "lowner_dev", "dhssevc_dev", "cauchy_eig_dev", "HssError",
 ]
 
@@ -83,6 +85,7 @@ SIGNATURES = {
     "mdstedc_": (None, [ctypes.c_char_p, _I, _D, _D, _D, _I, _D, _I, _I, _I, _I, ctypes.c_size_t]),
     "cauchylike_": (None, [_D, _D, _D, _D, _D, _I, _I]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
+    "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
     "hss_lowner_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V]),
     "hss_lowner_noalloc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V]),
@@ -243,6 +246,53 @@ def mdstedc_dev(d, e, z, stream=None):
     if info != 0:
         raise HssError("hss_mdstedc_dev INFO=%d: %s" % (info, _err()))
     return info
+
+
+def batch_offsets(sizes):
+    """Offsets of each problem in the packed d/e (sum n) and z (sum n^2) arrays."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    o = np.concatenate([[0], np.cumsum(sizes)])
+    oz = np.concatenate([[0], np.cumsum(sizes * sizes)])
+    return o, oz
+
+
+def mdstedc_batch_dev(sizes, d, e, z, stream=None):
+    """Batched device MDSTEDC('I') over packed problems (see
+    :func:`batch_offsets`): d (sum n) -> eigenvalues, e (sum n; problem p's
+    off-diagonals at its offset), z (sum n^2; problem p column-major n_p x n_p)."""
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    info = load().hss_mdstedc_batch_dev(len(sizes), sizes.ctypes.data_as(ctypes.c_void_p), _ptr(d),
+                                        _ptr(e), _ptr(z), _stream(stream))
+    if info != 0:
+        raise HssError("hss_mdstedc_batch_dev INFO=%d: %s" % (info, _err()))
+    return info
+
+
+def pack_batch(problems):
+    """Packed host arrays (sizes, d, e) of a list of (d, e) numpy pairs."""
+    sizes = np.array([len(d) for d, _ in problems], dtype=np.int32)
+    o, _ = batch_offsets(sizes)
+    D = np.zeros(int(o[-1]))
+    E = np.zeros(int(o[-1]))
+    for p, (d, e) in enumerate(problems):
+        D[o[p]:o[p + 1]] = d
+        E[o[p]:o[p] + len(e)] = e
+    return sizes, D, E
+
+
+def eigh_tridiagonal_batch(problems, stream=None):
+    """[(w, Q)] for a list of (d, e) problems, solved in one batched call."""
+    import torch
+    sizes, D, E = pack_batch(problems)
+    o, oz = batch_offsets(sizes)
+    d = torch.tensor(D, device="cuda")
+    e = torch.tensor(E, device="cuda")
+    z = torch.empty(int(oz[-1]), dtype=torch.float64, device="cuda")
+    mdstedc_batch_dev(sizes, d, e, z, stream)
+    w, zh = d.cpu().numpy(), z.cpu().numpy()
+    return [(w[o[p]:o[p + 1]].copy(),
+             zh[oz[p]:oz[p + 1]].reshape(int(sizes[p]), int(sizes[p])).T.copy())
+            for p in range(len(sizes))]
 
 
 def secular_dev(dlamda, z, rho, lam, difl, difr, iters=None, stream=None):

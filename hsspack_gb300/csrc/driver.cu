@@ -382,41 +382,62 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   c.launches++;
 }
 
-// Eigen-decomposition of one unreduced, scaled block of size n (> smlsiz):
-// d, e on the device (block-relative), Q block-relative with leading dim ldq.
-static void dc_block(Ctx &c, int n, const double *d, const double *e, double *Q, long long ldq,
-                     double *Dp, int *perm, int *status, cudaStream_t st) {
+// Eigen-decomposition of many unreduced, scaled blocks at once.  Block b
+// covers global positions bs[b] .. bs[b] + bm[b] - 1 of d, e, Dp, perm and the
+// same rows and columns of Q (leading dim ldq); e is zero at every block's last
+// position, so no cut crosses two blocks.  Each block is halved down to leaves
+// of at most smlsiz; the leaves of all blocks form one launch and the merges of
+// one tree level of all blocks are processed together.
+static void dc_blocks(Ctx &c, const std::vector<int> &bs, const std::vector<int> &bm, int N,
+                      const double *d, const double *e, double *Q, long long ldq, double *Dp,
+                      int *perm, int *status, cudaStream_t st) {
   const int smlsiz = std::max(1, std::min(c.cfg.smlsiz, 32));
-  std::vector<int> sz(1, n);
-  while (sz.back() > smlsiz) {
-    std::vector<int> nx;
-    for (int s : sz) { nx.push_back(s / 2); nx.push_back((s + 1) / 2); }
-    sz.swap(nx);
+  const int nb = (int)bs.size();
+  std::vector<std::vector<int>> ends(nb);
+  std::vector<int> ls, lz;
+  int mmax = 1;
+  double fl = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    std::vector<int> sz(1, bm[b]);
+    while (*std::max_element(sz.begin(), sz.end()) > smlsiz) {
+      std::vector<int> nx;
+      for (int x : sz) { nx.push_back(x / 2); nx.push_back((x + 1) / 2); }
+      sz.swap(nx);
+    }
+    int acc = bs[b];
+    for (int x : sz) {
+      ls.push_back(acc); lz.push_back(x);
+      acc += x;
+      ends[b].push_back(acc);
+      mmax = std::max(mmax, x);
+      fl += 30.0 * x * x * x;
+    }
   }
-  const int nl = (int)sz.size();
-  std::vector<int> ls(nl), ends(nl);
-  for (int i = 0, acc = 0; i < nl; ++i) { ls[i] = acc; acc += sz[i]; ends[i] = acc; }
+  const int nl = (int)ls.size();
   int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl);
-  h2d(dls, ls, st); h2d(dlz, sz, st);
+  h2d(dls, ls, st); h2d(dlz, lz, st);
   stage_begin(HSS_ST_LEAF, st);
-  launch_leaf(nl, dls, dlz, *std::max_element(sz.begin(), sz.end()), n, d, e, Q, ldq, Dp, perm,
-              status, st);
-  {
-    double fl = 0.0;
-    for (int x : sz) fl += 30.0 * x * x * x;
-    stage_end(HSS_ST_LEAF, st, 8LL * n * smlsiz, fl);
-  }
+  launch_leaf(nl, dls, dlz, mmax, N, d, e, Q, ldq, Dp, perm, status, st);
+  stage_end(HSS_ST_LEAF, st, 8LL * N * smlsiz, fl);
   c.launches++;
-  LevelArrays L = level_arrays(c, n);
-  while ((int)ends.size() > 1) {
+  bool more = false;
+  for (auto &v : ends) more |= v.size() > 1;
+  if (!more) return;
+  LevelArrays L = level_arrays(c, N);
+  while (more) {
     MergeLevel lvl;
-    std::vector<int> nx;
-    for (size_t i = 0; i + 1 < ends.size(); i += 2) {
-      const int s = i == 0 ? 0 : ends[i - 1];
-      const int matsiz = ends[i + 1] - s;
-      const int msd2 = i == 0 ? ends[0] : matsiz / 2;
-      lvl.s.push_back(s); lvl.n.push_back(matsiz); lvl.n1.push_back(msd2);
-      nx.push_back(ends[i + 1]);
+    more = false;
+    for (int b = 0; b < nb; ++b) {
+      std::vector<int> &en = ends[b];
+      if (en.size() < 2) continue;
+      std::vector<int> nx;
+      for (size_t i = 0; i + 1 < en.size(); i += 2) {
+        const int s = i == 0 ? bs[b] : en[i - 1];
+        lvl.s.push_back(s); lvl.n.push_back(en[i + 1] - s); lvl.n1.push_back(en[i] - s);
+        nx.push_back(en[i + 1]);
+      }
+      en.swap(nx);
+      more |= en.size() > 1;
     }
     c.stats.n_levels++;
     if (c.cfg.batched) {
@@ -425,28 +446,26 @@ static void dc_block(Ctx &c, int n, const double *d, const double *e, double *Q,
       for (size_t m = 0; m < lvl.s.size(); ++m)
         run_merges(c, {lvl.s[m]}, {lvl.n[m]}, {lvl.n1[m]}, e, Q, ldq, Dp, perm, L, status, st);
     }
-    ends.swap(nx);
   }
 }
 
-__global__ void k_scale(int n, double *x, double a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] *= a;
-}
-__global__ void k_iota(int n, int *p, int base) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = base + i;
-}
-// a 1x1 block: eigenvector e_i, block-relative order 0
-__global__ void k_put1(double *Q, long long ldq, int i, double *Dp, double v, int *perm) {
-  Q[(long long)i * ldq + i] = 1.0;
-  Dp[i] = v;
-  perm[i] = 0;
-}
+// One tridiagonal of a solve: host copies of d (n) and e (n - 1), device
+// outputs z (leading dim ldz) and w (n eigenvalues, ascending).
+struct Problem {
+  int n;
+  const double *hd, *he;
+  double *z;
+  long long ldz;
+  double *w;
+};
 
-// Full MDSTEDC('I') on device arrays.  hd/he: host copies of d/e (n, n-1).
-static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<double> he,
-                        double *dz, long long ldz, double *dw, cudaStream_t st) {
+// MDSTEDC('I') of every problem in one pass over the DC tree levels.  Problem
+// p occupies global positions P[p] .. P[p+1] - 1; all problems share one Q of
+// leading dimension L = max n_p, problem p's block starting at Q + P[p](L + 1).
+// Within a problem: split on tiny E and scale each unreduced block
+// (mdstedc.f90:305-345), DC on every block, then order the eigenpairs
+// (mdstedc.f90:392-420).
+static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   memset(&c.stats, 0, sizeof c.stats);
   c.launches = 0;
   cudaEvent_t ev0, ev1;
@@ -454,89 +473,123 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
   CK(cudaEventCreate(&ev1));
   CK(cudaEventRecord(ev0, st));
   const double EPS = 1.1102230246251565e-16;
-  he.resize(std::max(n, 1), 0.0);
-  double *Q = buf<double>(c, "Q", (size_t)n * n);
-  double *Dp = buf<double>(c, "Dp", n);
-  int *perm = buf<int>(c, "perm", n);
-  double *d = buf<double>(c, "d_in", n), *e = buf<double>(c, "e_in", std::max(n, 1));
+  const int np = (int)pr.size();
+  std::vector<long long> P(np + 1, 0);
+  long long L = 1;
+  for (int p = 0; p < np; ++p) {
+    P[p + 1] = P[p] + pr[p].n;
+    L = std::max<long long>(L, pr[p].n);
+  }
+  const int N = (int)P[np];
+  if (N == 0) return 0;
+  const size_t qsize = (size_t)(N - 1) * (size_t)(L + 1) + 1;
+  double *Q = buf<double>(c, "Q", qsize);
+  double *Dp = buf<double>(c, "Dp", N);
+  int *perm = buf<int>(c, "perm", N);
+  double *d = buf<double>(c, "d_in", N), *e = buf<double>(c, "e_in", N);
+  long long *dP = nullptr;
   // status[0]: error code, status[2..3]: 64-bit sum of secular iterations,
   // status[4..5]: 64-bit count of learned starts that fell back
   int *status = buf<int>(c, "status", 6);
   CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
-  CK(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)n * n, st));
-  // split into unreduced blocks and scale each (mdstedc.f90:305-345)
-  std::vector<int> bstart, bend;
+  if (np == 1) {
+    CK(cudaMemsetAsync(Q, 0, sizeof(double) * qsize, st));
+  } else {
+    dP = buf<long long>(c, "prob_P", np + 1);
+    h2d(dP, P, st);
+    launch_zero_blocks(np, N, dP, Q, L, st);
+    c.launches++;
+  }
+  // global d, e with e = 0 at every block end; split and scale per problem
+  std::vector<double> hd(N), he(N, 0.0);
+  std::vector<int> bstart, bsize, bprob;
   std::vector<double> bscale;
+  std::vector<int> nblocks(np, 0);
   const int smlsiz = std::max(1, std::min(c.cfg.smlsiz, 32));
-  int start = 0;
-  while (start < n) {
-    int finish = start;
-    while (finish < n - 1) {
-      const double tiny = EPS * std::sqrt(std::fabs(hd[finish])) * std::sqrt(std::fabs(hd[finish + 1]));
-      if (std::fabs(he[finish]) > tiny) ++finish; else break;
-    }
-    double nrm = 0.0;
-    for (int i = start; i <= finish; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
-    for (int i = start; i < finish; ++i) nrm = std::max(nrm, std::fabs(he[i]));
-    const int m = finish - start + 1;
-    double scl = 1.0;
-    if (m > smlsiz && nrm > 0.0) {
-      scl = nrm;
-      const double mul = 1.0 / nrm;
-      for (int i = start; i <= finish; ++i) hd[i] *= mul;
-      for (int i = start; i < finish; ++i) he[i] *= mul;
-    }
-    bstart.push_back(start); bend.push_back(finish); bscale.push_back(scl);
-    start = finish + 1;
-  }
-  CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e, he.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
-  for (size_t b = 0; b < bstart.size(); ++b) {
-    const int s0 = bstart[b], m = bend[b] - s0 + 1;
-    double *Qb = Q + (long long)s0 * n + s0;
-    if (m == 1) {
-      k_put1<<<1, 1, 0, st>>>(Q, n, s0, Dp, hd[s0], perm);
-      continue;
-    }
-    if (m <= smlsiz) {
-      std::vector<int> ls(1, 0), lz(1, m);
-      int *dls = buf<int>(c, "leaf_s", 1), *dlz = buf<int>(c, "leaf_z", 1);
-      h2d(dls, ls, st); h2d(dlz, lz, st);
-      launch_leaf(1, dls, dlz, m, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
-      c.launches++;
-    } else {
-      dc_block(c, m, d + s0, e + s0, Qb, n, Dp + s0, perm + s0, status, st);
-    }
-    if (bscale[b] != 1.0) k_scale<<<(m + 255) / 256, 256, 0, st>>>(m, Dp + s0, bscale[b]);
-  }
-  // block-relative slots/perm -> absolute order
-  int *fperm = perm;
-  if (bstart.size() > 1) {
-    std::vector<int> hp(n);
-    std::vector<double> hv(n);
-    CK(cudaMemcpyAsync(hp.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hv.data(), Dp, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    std::vector<std::pair<double, int>> all;
-    all.reserve(n);
-    // perm entries are block-relative slots; Dp is indexed block-relative too
-    for (size_t b = 0; b < bstart.size(); ++b)
-      for (int i = bstart[b]; i <= bend[b]; ++i) {
-        const int slot = bstart[b] + hp[i];
-        all.push_back({hv[slot], slot});
+  for (int p = 0; p < np; ++p) {
+    const int n = pr[p].n, o = (int)P[p];
+    for (int i = 0; i < n; ++i) hd[o + i] = pr[p].hd[i];
+    for (int i = 0; i + 1 < n; ++i) he[o + i] = pr[p].he[i];
+    int start = o;
+    while (start < o + n) {
+      int finish = start;
+      while (finish < o + n - 1) {
+        const double tiny = EPS * std::sqrt(std::fabs(hd[finish])) * std::sqrt(std::fabs(hd[finish + 1]));
+        if (std::fabs(he[finish]) > tiny) ++finish; else break;
       }
-    std::stable_sort(all.begin(), all.end(),
-                     [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
-                       return a.first < b.first;
-                     });
-    std::vector<int> fp(n);
-    for (int i = 0; i < n; ++i) fp[i] = all[i].second;
-    fperm = buf<int>(c, "fperm", n);
-    h2d(fperm, fp, st);
+      he[finish] = 0.0;
+      double nrm = 0.0;
+      for (int i = start; i <= finish; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
+      for (int i = start; i < finish; ++i) nrm = std::max(nrm, std::fabs(he[i]));
+      const int m = finish - start + 1;
+      double scl = 1.0;
+      if (m > smlsiz && nrm > 0.0) {
+        scl = nrm;
+        const double mul = 1.0 / nrm;
+        for (int i = start; i <= finish; ++i) hd[i] *= mul;
+        for (int i = start; i < finish; ++i) he[i] *= mul;
+      }
+      bstart.push_back(start); bsize.push_back(m); bscale.push_back(scl); bprob.push_back(p);
+      nblocks[p]++;
+      start = finish + 1;
+    }
+  }
+  CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e, he.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
+  dc_blocks(c, bstart, bsize, N, d, e, Q, L, Dp, perm, status, st);
+  {
+    std::vector<int> ss, sm;
+    std::vector<double> sc;
+    for (size_t b = 0; b < bstart.size(); ++b)
+      if (bscale[b] != 1.0) { ss.push_back(bstart[b]); sm.push_back(bsize[b]); sc.push_back(bscale[b]); }
+    if (!ss.empty()) {
+      int *x1 = buf<int>(c, "scl_s", ss.size()), *x2 = buf<int>(c, "scl_m", ss.size());
+      double *x3 = buf<double>(c, "scl_v", sc.size());
+      h2d(x1, ss, st); h2d(x2, sm, st); h2d(x3, sc, st);
+      launch_scale_blocks((int)ss.size(), x1, x2, x3, Dp, st);
+      c.launches++;
+    }
+  }
+  // problems split into several blocks: merge the blocks' ascending lists
+  int *fperm = perm;
+  if (*std::max_element(nblocks.begin(), nblocks.end()) > 1) {
+    std::vector<int> hp(N);
+    std::vector<double> hv(N);
+    CK(cudaMemcpyAsync(hp.data(), perm, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hv.data(), Dp, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int p = 0; p < np; ++p) {
+      if (nblocks[p] < 2) continue;
+      std::vector<std::pair<double, int>> all;
+      all.reserve(pr[p].n);
+      // perm holds global slots; Dp is indexed by slot
+      for (long long i = P[p]; i < P[p + 1]; ++i) all.push_back({hv[hp[i]], hp[i]});
+      std::stable_sort(all.begin(), all.end(),
+                       [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+                         return a.first < b.first;
+                       });
+      for (size_t i = 0; i < all.size(); ++i) hp[P[p] + i] = all[i].second;
+    }
+    fperm = buf<int>(c, "fperm", N);
+    h2d(fperm, hp, st);
   }
   stage_begin(HSS_ST_FINAL, st);
-  launch_final_gather(n, fperm, Dp, Q, n, dz, ldz, dw, st);
-  stage_end(HSS_ST_FINAL, st, 16LL * n * n + 20LL * n, 0.0);
+  if (np == 1) {
+    launch_final_gather(N, fperm, Dp, Q, L, pr[0].z, pr[0].ldz, pr[0].w, st);
+  } else {
+    std::vector<double *> hz(np), hw(np);
+    std::vector<long long> hl(np);
+    for (int p = 0; p < np; ++p) { hz[p] = pr[p].z; hw[p] = pr[p].w; hl[p] = pr[p].ldz; }
+    double **dz = buf<double *>(c, "prob_z", np), **dw = buf<double *>(c, "prob_w", np);
+    long long *dl = buf<long long>(c, "prob_ldz", np);
+    h2d(dz, hz, st); h2d(dw, hw, st); h2d(dl, hl, st);
+    launch_final_gather_batch(np, N, dP, fperm, Dp, Q, L, dz, dl, dw, st);
+  }
+  {
+    long long nn = 0;
+    for (auto &q : pr) nn += (long long)q.n * q.n;
+    stage_end(HSS_ST_FINAL, st, 16LL * nn + 20LL * N, 0.0);
+  }
   c.launches++;
   CK(cudaEventRecord(ev1, st));
   int hst[6] = {0, 0, 0, 0, 0, 0};
@@ -562,6 +615,12 @@ static int mdstedc_core(Ctx &c, int n, std::vector<double> hd, std::vector<doubl
     return 1;
   }
   return 0;
+}
+
+// MDSTEDC('I') of one matrix.  hd/he: host copies of d/e (n, n-1).
+static int mdstedc_core(Ctx &c, int n, const std::vector<double> &hd, const std::vector<double> &he,
+                        double *dz, long long ldz, double *dw, cudaStream_t st) {
+  return solve_core(c, {Problem{n, hd.data(), he.data(), dz, ldz, dw}}, st);
 }
 
 // Message for hss_last_error() from entry points that live outside this file.
@@ -634,6 +693,51 @@ int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *strea
     double *dw = buf<double>(c, "w_out", n);
     int info = mdstedc_core(c, n, hd, he, z, ldz, dw, st);
     CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return info;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+int hss_mdstedc_batch_dev(int nprob, const int *n, double *d, double *e, double *z, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (nprob < 0) return -1;
+  if (nprob == 0) return 0;
+  if (!n) return -2;
+  long long N = 0, zz = 0;
+  for (int p = 0; p < nprob; ++p) {
+    if (n[p] < 0) {
+      c.err = "hss_mdstedc_batch_dev: n[" + std::to_string(p) + "] < 0";
+      return -2;
+    }
+    N += n[p];
+    zz += (long long)n[p] * n[p];
+  }
+  if (N > 2147483647LL) {
+    c.err = "hss_mdstedc_batch_dev: total order exceeds 2^31 - 1";
+    return -2;
+  }
+  if (N == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    std::vector<double> hd(N), he(N, 0.0);
+    CK(cudaMemcpyAsync(hd.data(), d, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(he.data(), e, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double *dw = buf<double>(c, "w_out", N);
+    std::vector<Problem> pr;
+    long long o = 0, oz = 0;
+    for (int p = 0; p < nprob; ++p) {
+      if (n[p] > 0)
+        pr.push_back(Problem{n[p], hd.data() + o, he.data() + o, z + oz, n[p], dw + o});
+      o += n[p];
+      oz += (long long)n[p] * n[p];
+    }
+    int info = solve_core(c, pr, st);
+    CK(cudaMemcpyAsync(d, dw, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
     CK(cudaStreamSynchronize(st));
     return info;
   } catch (CudaError &ex) {

@@ -76,11 +76,7 @@ __device__ __forceinline__ int exp_of(double amax) {
 
 // A: M x K (lda) -> planes [tile_m][tile_k][s] of TM x TK, row exponents.
 // One CTA per 128-row panel; pass 1 row max, pass 2 digits.
-__global__ void __launch_bounds__(256)
-k_split_a(const SplitProb *__restrict__ probs, int nprob) {
-  const SplitProb P = probs[blockIdx.y];
-  const int tm = blockIdx.x;
-  if (tm * TM >= P.rows) return;
+__device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
   __shared__ double smax[8][TM];
   __shared__ double sscale[TM];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -131,11 +127,7 @@ k_split_a(const SplitProb *__restrict__ probs, int nprob) {
 
 // B: K x N (ldb) -> planes [tile_n][tile_k][s] of TN x TK (K-major), column
 // exponents.  One CTA per 64-column panel.
-__global__ void __launch_bounds__(256)
-k_split_b(const SplitProb *__restrict__ probs, int nprob) {
-  const SplitProb P = probs[blockIdx.y];
-  const int tn = blockIdx.x;
-  if (tn * TN >= P.rows) return;
+__device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
   __shared__ double sscale[TN];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   for (int c = w; c < TN; c += 8) {  // warp per column: max over k
@@ -172,6 +164,24 @@ k_split_b(const SplitProb *__restrict__ probs, int nprob) {
         *reinterpret_cast<uint4 *>(tile + s * BTILE + tile_off(c, k8 * 8, TN)) =
             *reinterpret_cast<uint4 *>(dg[s]);
     }
+  }
+}
+
+// One CTA per (panel, problem), problems strided over gridDim.y (<= 65535).
+__global__ void __launch_bounds__(256)
+k_split_a(const SplitProb *__restrict__ probs, int nprob) {
+  for (int pi = blockIdx.y; pi < nprob; pi += gridDim.y) {
+    const SplitProb P = probs[pi];
+    if ((int)blockIdx.x * TM < P.rows) split_a_panel(P, blockIdx.x);
+    __syncthreads();
+  }
+}
+__global__ void __launch_bounds__(256)
+k_split_b(const SplitProb *__restrict__ probs, int nprob) {
+  for (int pi = blockIdx.y; pi < nprob; pi += gridDim.y) {
+    const SplitProb P = probs[pi];
+    if ((int)blockIdx.x * TN < P.rows) split_b_panel(P, blockIdx.x);
+    __syncthreads();
   }
 }
 
@@ -452,8 +462,9 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   cudaMemcpyAsync(dsa, sa.data(), sa.size() * sizeof(SplitProb), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(dsb, sb.data(), sb.size() * sizeof(SplitProb), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(dtc, tc.data(), tc.size() * sizeof(TcProb), cudaMemcpyHostToDevice, st);
-  k_split_a<<<dim3(maxtm, (unsigned)sa.size()), 256, 0, st>>>(dsa, (int)sa.size());
-  k_split_b<<<dim3(maxtn, (unsigned)sb.size()), 256, 0, st>>>(dsb, (int)sb.size());
+  const unsigned gy = (unsigned)std::min<size_t>(sa.size(), 65535);
+  k_split_a<<<dim3(maxtm, gy), 256, 0, st>>>(dsa, (int)sa.size());
+  k_split_b<<<dim3(maxtn, gy), 256, 0, st>>>(dsb, (int)sb.size());
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);

@@ -550,16 +550,16 @@ __global__ void k_hss_B(HssDev h, const int *__restrict__ pairs, int nn) {
 __global__ void k_hss_leafD(HssDev h, const int *__restrict__ leaves, const int *__restrict__ lstart,
                             const int *__restrict__ lsize, int nl, const double *__restrict__ u,
                             const double *__restrict__ v) {
-  const int a = blockIdx.y;
-  if (a >= nl) return;
-  const int node = leaves[a], s = lstart[a], m = lsize[a];
-  PoleDiff P{h.FF, h.DIFL, h.DIFR};
-  double *D = h.Dg + h.doff[a];
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m * m; idx += gridDim.x * blockDim.x) {
-    const int i = idx % m, j = idx / m;
-    D[idx] = u[s + i] * v[s + j] / P.fd(s + i, s + j);
+  for (int a = blockIdx.y; a < nl; a += gridDim.y) {
+    const int node = leaves[a], s = lstart[a], m = lsize[a];
+    PoleDiff P{h.FF, h.DIFL, h.DIFR};
+    double *D = h.Dg + h.doff[a];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m * m; idx += gridDim.x * blockDim.x) {
+      const int i = idx % m, j = idx / m;
+      D[idx] = u[s + i] * v[s + j] / P.fd(s + i, s + j);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) h.Dm[node] = m;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) h.Dm[node] = m;
 }
 
 __global__ void k_init_gens(int K, const double *__restrict__ u, const double *__restrict__ v,
@@ -642,7 +642,7 @@ static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F
   int *dleaves = up("hs_leaves", leaves, st), *dls = up("hs_ls", lstart, st),
       *dlz = up("hs_lz", lsize, st);
   {
-    dim3 g((t.mmax * t.mmax + 255) / 256, (unsigned)leaves.size());
+    dim3 g((t.mmax * t.mmax + 255) / 256, (unsigned)std::min<size_t>(leaves.size(), 65535));
     k_hss_leafD<<<g, 256, 0, st>>>(h, dleaves, dls, dlz, (int)leaves.size(), u, v);
   }
   launches += 2;

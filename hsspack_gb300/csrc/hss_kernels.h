@@ -71,6 +71,15 @@ void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const in
                          const LevelScratch &w, int *perm, double *Dp, cudaStream_t st);
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st);
+// many problems per call: P = global start of each problem (np + 1 entries),
+// total = P[np]; problem p's block is Q + P[p] * (ldq + 1), leading dim ldq
+void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
+                        cudaStream_t st);
+void launch_scale_blocks(int nb, const int *bs, const int *bm, const double *bscl, double *Dp,
+                         cudaStream_t st);
+void launch_final_gather_batch(int np, long long total, const long long *P, const int *perm,
+                               const double *Dp, const double *Q, long long ldq, double *const *Z,
+                               const long long *ldz, double *const *W, cudaStream_t st);
 
 // predictor.cu
 int mlp_nparam();

@@ -326,17 +326,18 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
 __global__ void k_givens(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                          const int *__restrict__ ng, const LevelScratch w, double *Q,
                          long long ldq) {
-  const int m = blockIdx.y;
-  const int s = ms[m], n = mn[m], g = ng[m];
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n || g == 0) return;
-  const long long row = s + r;
-  for (int t = 0; t < g; ++t) {
-    const long long p = w.gvp[s + t], q = w.gvq[s + t];
-    const double c = w.gvc[s + t], sn = w.gvs[s + t];
-    const double x = Q[p * ldq + row], y = Q[q * ldq + row];
-    Q[p * ldq + row] = c * x + sn * y;
-    Q[q * ldq + row] = c * y - sn * x;
+  for (int m = blockIdx.y; m < P; m += gridDim.y) {
+    const int s = ms[m], n = mn[m], g = ng[m];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n || g == 0) continue;
+    const long long row = s + r;
+    for (int t = 0; t < g; ++t) {
+      const long long p = w.gvp[s + t], q = w.gvq[s + t];
+      const double c = w.gvc[s + t], sn = w.gvs[s + t];
+      const double x = Q[p * ldq + row], y = Q[q * ldq + row];
+      Q[p * ldq + row] = c * x + sn * y;
+      Q[q * ldq + row] = c * y - sn * x;
+    }
   }
 }
 
@@ -413,7 +414,8 @@ __global__ void k_final_gather(int n, const int *__restrict__ perm, const double
   const long long p = perm[c];
   const double2 *src = reinterpret_cast<const double2 *>(Q + p * ldq);
   double *dst = Z + (long long)c * ldz;
-  if ((ldq % 2 == 0) && (ldz % 2 == 0) && (n % 2 == 0)) {
+  // 16-byte vector copies only when both column starts are 16-byte aligned
+  if ((((uintptr_t)(Q + p * ldq) | (uintptr_t)dst) & 15) == 0 && (n % 2 == 0)) {
     double2 *d2 = reinterpret_cast<double2 *>(dst);
     for (int i = threadIdx.x; i < n / 2; i += blockDim.x) d2[i] = src[i];
   } else {
@@ -421,6 +423,60 @@ __global__ void k_final_gather(int n, const int *__restrict__ perm, const double
     for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = s1[i];
   }
   if (threadIdx.x == 0) wout[c] = Dp[p];
+}
+
+// ------------------------------------------------ many problems per call --
+// Problems of one call sit at global positions P[p] .. P[p+1]-1 and share one
+// Q with leading dimension ldq >= max n_p: problem p's eigenvector block is the
+// column-major n_p x n_p matrix at Q + P[p] * (ldq + 1) with leading dim ldq,
+// so every level kernel addresses it with global positions unchanged.
+
+__device__ __forceinline__ int problem_of(const long long *__restrict__ P, int np, long long c) {
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(P + mid) <= c) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Zero the diagonal blocks of all problems (one CTA per global column).
+__global__ void k_zero_blocks(int np, const long long *__restrict__ P, double *__restrict__ Q,
+                              long long ldq) {
+  const long long c = blockIdx.x;
+  const int p = problem_of(P, np, c);
+  const long long r0 = __ldg(P + p), n = __ldg(P + p + 1) - r0;
+  double *col = Q + c * ldq + r0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) col[i] = 0.0;
+}
+
+// Undo the per-block scaling of the eigenvalues: block b covers positions
+// bs[b] .. bs[b] + bm[b] - 1 (slots of Dp).
+__global__ void k_scale_blocks(int nb, const int *__restrict__ bs, const int *__restrict__ bm,
+                               const double *__restrict__ bscl, double *__restrict__ Dp) {
+  const int b = blockIdx.x;
+  if (b >= nb) return;
+  const int s = bs[b], m = bm[b];
+  const double a = bscl[b];
+  for (int i = threadIdx.x; i < m; i += blockDim.x) Dp[s + i] *= a;
+}
+
+// Final ordering of every problem: column j of problem p's output is the
+// global slot perm[P[p] + j]; its eigenvalue is Dp[slot].  Z[p], W[p] are the
+// per-problem output pointers, ldz[p] their leading dimensions.
+__global__ void k_final_gather_batch(int np, const long long *__restrict__ P,
+                                     const int *__restrict__ perm, const double *__restrict__ Dp,
+                                     const double *__restrict__ Q, long long ldq,
+                                     double *const *__restrict__ Z, const long long *__restrict__ ldz,
+                                     double *const *__restrict__ W) {
+  const long long c = blockIdx.x;
+  const int p = problem_of(P, np, c);
+  const long long r0 = __ldg(P + p), n = __ldg(P + p + 1) - r0, j = c - r0;
+  const long long slot = perm[c];
+  const double *src = Q + slot * ldq + r0;
+  double *dst = Z[p] + j * ldz[p];
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  if (threadIdx.x == 0) W[p][j] = Dp[slot];
 }
 
 // ---------------------------------------------------------------- launch --
@@ -442,7 +498,7 @@ void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const i
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
                    const LevelScratch &w, double *Q, long long ldq, cudaStream_t st) {
   if (P <= 0) return;
-  dim3 grid((maxn + 255) / 256, P);
+  dim3 grid((maxn + 255) / 256, std::min(P, 65535));
   k_givens<<<grid, 256, 0, st>>>(P, ms, mn, ng, w, Q, ldq);
 }
 void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
@@ -473,6 +529,20 @@ void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const in
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st) {
   if (n > 0) k_final_gather<<<n, 256, 0, st>>>(n, perm, Dp, Q, ldq, Z, ldz, wout);
+}
+void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
+                        cudaStream_t st) {
+  if (np > 0 && total > 0) k_zero_blocks<<<(unsigned)total, 256, 0, st>>>(np, P, Q, ldq);
+}
+void launch_scale_blocks(int nb, const int *bs, const int *bm, const double *bscl, double *Dp,
+                         cudaStream_t st) {
+  if (nb > 0) k_scale_blocks<<<nb, 256, 0, st>>>(nb, bs, bm, bscl, Dp);
+}
+void launch_final_gather_batch(int np, long long total, const long long *P, const int *perm,
+                               const double *Dp, const double *Q, long long ldq, double *const *Z,
+                               const long long *ldz, double *const *W, cudaStream_t st) {
+  if (np > 0 && total > 0)
+    k_final_gather_batch<<<(unsigned)total, 256, 0, st>>>(np, P, perm, Dp, Q, ldq, Z, ldz, W);
 }
 
 }  // namespace hss

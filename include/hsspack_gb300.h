@@ -86,6 +86,17 @@ void cauchylike_(double *A, const double *D, const double *F, const double *u,
  * (destroyed); z(ldz, n) out: eigenvectors.  stream may be NULL. */
 int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *stream);
 
+/* Many independent tridiagonal eigensolves in one call, each with COMPZ='I'
+ * semantics of MDSTEDC (SRC/mdstedc.f90:139); no batched counterpart in the
+ * reference, whose drivers take one matrix per call.  n(nprob) on the host;
+ * d, e, z in HBM, packed: problem p starts at o_p = n_0 + ... + n_{p-1} in d
+ * (eigenvalues out, ascending) and e (its n_p - 1 off-diagonals; entry
+ * o_p + n_p - 1 is ignored), and at n_0^2 + ... + n_{p-1}^2 in z (eigenvectors,
+ * leading dim n_p).  All problems' DC levels run together.  Returns 0, -1 / -2
+ * for a bad nprob / n, or > 0 as hss_mdstedc_dev. */
+int hss_mdstedc_batch_dev(int nprob, const int *n, double *d, double *e, double *z,
+                          void *stream);
+
 /* K secular roots of 1 + rho * sum_i z_i^2 / (dlamda_i - x) (the DLAED4 loop of
  * SRC/mdlaed3.f90:207-225).  Outputs lam(K), difl(K) = lam_j - dlamda_j,
  * difr(K) = lam_j - dlamda_{j+1} (difr(K-1) = 0), iters(K) (may be NULL).
