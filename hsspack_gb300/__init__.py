@@ -66,7 +66,7 @@ class Stats(ctypes.Structure):
 
 
 STAGES = ["leaf", "prepare", "givens", "secular", "lowner", "build_S", "gather", "gemm",
-          "scatter", "finish", "final_gather", "hss_build", "hss_multiply", "other"]
+          "scatter", "finish", "final_gather", "hss_build", "hss_multiply", "other", "predict"]
 
 
 _lib = None
@@ -84,6 +84,12 @@ SIGNATURES = {
     "hss_finalize": (ctypes.c_int, []),
     "mdstedc_": (None, [ctypes.c_char_p, _I, _D, _D, _D, _I, _D, _I, _I, _I, _I, ctypes.c_size_t]),
     "cauchylike_": (None, [_D, _D, _D, _D, _D, _I, _I]),
+    "mdsbevd_": (None, [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _D, _I, _D, _D, _I, _D, _I, _I,
+                        _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
+    "mdsbedc_": (None, [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _D, _I, _D, _D, _I, _D, _I, _I,
+                        _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
+    "hss_mdsbevd_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, ctypes.c_int, _V, _V,
+                                       ctypes.c_int, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
@@ -209,6 +215,68 @@ def eigh_tridiagonal(d, e):
     if info != 0:
         raise HssError("MDSTEDC INFO=%d: %s" % (info, _err()))
     return dd, Z
+
+
+def _band_call(name, c1, uplo, n, kd, ab, ldab, w, z, ldz, work, lwork, iwork, liwork):
+    for a, dt in ((ab, np.float64), (w, np.float64), (z, np.float64), (work, np.float64),
+                  (iwork, np.int32)):
+        if a.dtype != dt:
+            raise TypeError("array dtype must be %s" % dt)
+    for a in (ab, z):
+        if a.ndim == 2 and not a.flags.f_contiguous:
+            raise ValueError("band and eigenvector arrays must be Fortran ordered")
+    info = ctypes.c_int(0)
+    ints = [ctypes.c_int(int(x)) for x in (n, kd, ldab, ldz, lwork, liwork)]
+    getattr(load(), name)(c1.encode(), uplo.encode(), ctypes.byref(ints[0]), ctypes.byref(ints[1]),
+                          _pd(ab), ctypes.byref(ints[2]), _pd(w), _pd(z), ctypes.byref(ints[3]),
+                          _pd(work), ctypes.byref(ints[4]), iwork.ctypes.data_as(_I),
+                          ctypes.byref(ints[5]), ctypes.byref(info), 1, 1)
+    return info.value
+
+
+def mdsbevd(compz, uplo, n, kd, ab, ldab, d, q, ldq, work, lwork, iwork, liwork):
+    """MDSBEVD with the Fortran argument list (SRC/mdsbevd.f90:183); numpy
+    arrays, ab and q Fortran ordered.  Returns INFO."""
+    return _band_call("mdsbevd_", compz, uplo, n, kd, ab, ldab, d, q, ldq, work, lwork, iwork,
+                      liwork)
+
+
+def mdsbedc(jobz, uplo, n, kd, ab, ldab, w, z, ldz, work, lwork, iwork, liwork):
+    """MDSBEDC with the Fortran argument list (SRC/mdsbedc.f90:166).  Returns INFO."""
+    return _band_call("mdsbedc_", jobz, uplo, n, kd, ab, ldab, w, z, ldz, work, lwork, iwork,
+                      liwork)
+
+
+def eigh_banded(ab, lower=False):
+    """Eigenvalues (ascending) and eigenvectors of the symmetric band matrix in
+    LAPACK band storage ab (kd + 1, n) through MDSBEDC('V').  Returns (w, Z)."""
+    ab = np.asfortranarray(ab, dtype=np.float64)
+    kd, n = ab.shape[0] - 1, ab.shape[1]
+    w = np.zeros(n)
+    Z = np.zeros((n, n), order="F")
+    work = np.zeros(1)
+    iwork = np.zeros(1, dtype=np.int32)
+    uplo = "L" if lower else "U"
+    info = mdsbedc("V", uplo, n, kd, ab, kd + 1, w, Z, max(1, n), work, -1, iwork, -1)
+    if info != 0:
+        raise HssError("MDSBEDC workspace query: INFO=%d" % info)
+    # the GPU path keeps its workspace in HBM; only WORK(1), IWORK(1) are touched
+    info = mdsbedc("V", uplo, n, kd, ab, kd + 1, w, Z, max(1, n), work, int(work[0]), iwork,
+                   int(iwork[0]))
+    if info != 0:
+        raise HssError("MDSBEDC INFO=%d: %s" % (info, _err()))
+    return w, Z
+
+
+def mdsbevd_dev(kd, ab, w, z, stream=None):
+    """Device band eigensolve: ab (n, kd + 1) tensor whose memory is the
+    column-major (kd + 1) x n upper band storage; w (n,), z (n, n) column-major."""
+    n = w.numel()
+    info = load().hss_mdsbevd_dev(n, kd, _ptr(ab), kd + 1, _ptr(w), _ptr(z), max(1, n),
+                                  _stream(stream))
+    if info != 0:
+        raise HssError("hss_mdsbevd_dev INFO=%d: %s" % (info, _err()))
+    return info
 
 
 def cauchylike(D, F, u, v):

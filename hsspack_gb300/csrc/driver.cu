@@ -201,11 +201,26 @@ static LevelArrays level_arrays(Ctx &c, int n) {
   return a;
 }
 
+// One of the kd rank-one updates of a banded merge (the loop of MDSBED1,
+// SRC/mdsbed1.f90): z per slot (a column of Z = Q^T W), the coupling rho_in
+// per merge of the group, prepare flags, and the columns of Z still to come,
+// which follow the update's Givens rotations and eigenvector matrix.
+struct BandUpdate {
+  const double *z = nullptr;
+  const double *rho = nullptr;
+  int flags = 0;
+  double *zrest = nullptr;
+  int nrest = 0;
+  long long zld = 0;
+};
+
 // Process a group of merges of one level (all of them when batched, one when
-// not).  Arrays ms/mn/mn1 describe the group.
+// not).  Arrays ms/mn/mn1 describe the group.  bu: a banded rank-one update
+// (null for the tridiagonal merge).
 static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int> &mn,
                        const std::vector<int> &mn1, const double *e, double *Q, long long ldq,
-                       double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st) {
+                       double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st,
+                       const BandUpdate *bu = nullptr) {
   const int P = (int)ms.size();
   if (P == 0) return;
   // ---- upload the group and prepare (deflation)
@@ -215,7 +230,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   double *drho = buf<double>(c, "g_rho", P);
   stage_begin(HSS_ST_PREPARE, st);
   launch_merge_prepare(P, *std::max_element(mn.begin(), mn.end()), dms, dmn, dmn1, e, Q, ldq, Dp,
-                       perm, L.w, dout, drho, st);
+                       perm, L.w, dout, drho, st, bu ? bu->z : nullptr, bu ? bu->rho : nullptr,
+                       bu ? bu->flags : 0);
   {
     long long nn = 0;
     for (int x : mn) nn += x;
@@ -269,7 +285,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
         *g3 = buf<int>(c, "gv_g", gs.size());
     h2d(g1, gs, st); h2d(g2, gn, st); h2d(g3, gng, st);
     stage_begin(HSS_ST_GIVENS, st);
-    launch_givens((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, st);
+    launch_givens((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, st, bu ? bu->zrest : nullptr,
+                  bu ? bu->nrest : 0, bu ? bu->zld : 0);
     long long gb = 0;
     for (size_t i = 0; i < gs.size(); ++i) gb += 32LL * gn[i] * gng[i];
     stage_end(HSS_ST_GIVENS, st, gb, 0.0);
@@ -293,8 +310,10 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     guess = buf<float>(c, "guess", L.n);
     stage_begin(HSS_ST_SECULAR, st);
     launch_secular_mid(lv, total, *std::max_element(aK.begin(), aK.end()), L.w.dl, L.w.zw, feat, st);
-    launch_predict(L.n, feat, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
     stage_end(HSS_ST_SECULAR, st, 0, 0.0);
+    stage_begin(HSS_ST_PREDICT, st);
+    launch_predict(L.n, feat, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
+    stage_end(HSS_ST_PREDICT, st, 0, 0.0);
     c.launches += 2;
   }
   stage_begin(HSS_ST_SECULAR, st);
@@ -307,6 +326,16 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st);
   stage_end(HSS_ST_LOWNER, st, 40LL * total, 5.0 * k2);
   c.launches += 2;
+  if (bu && bu->nrest > 0) {
+    // the remaining Z columns follow the new eigenvectors (mdsbed4.f90:266-268)
+    double *zt = buf<double>(c, "band_zt", (size_t)bu->nrest * bu->zld);
+    stage_begin(HSS_ST_OTHER, st);
+    launch_alpha(lv, total, L.w.dl, L.difl, L.difr, L.zhat, L.alpha, st);
+    launch_band_zupdate(lv, total, L.w.dl, L.difl, L.difr, L.zhat, L.alpha, L.w.ndslot, bu->zrest,
+                        bu->nrest, bu->zld, zt, st);
+    stage_end(HSS_ST_OTHER, st, 0, (2.0 + 4.0 * bu->nrest) * k2);
+    c.launches += 3;
+  }
   // ---- dense merges: S, gather, GEMM (block structured), scatter
   const int PD = (int)ds_.size();
   if (PD > 0) {
@@ -617,6 +646,168 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   return 0;
 }
 
+static int mdstedc_core(Ctx &c, int n, const std::vector<double> &hd, const std::vector<double> &he,
+                        double *dz, long long ldz, double *dw, cudaStream_t st);
+
+// ------------------------------------------------------------ band DC ----
+// MDSBEVD('I', 'U') (SRC/mdsbevd.f90:183) of one symmetric band matrix in HBM:
+// ab in upper band storage (ldab >= kd + 1), 2 <= kd <= 32.  Halving tree to
+// leaves of at most max(smlsiz, 2 kd) rows; every cut split by the SVD of its
+// coupling block; dense leaf eigensolves; then per level kd rank-one updates
+// of all merges of the level (MDSBED1, SRC/mdsbed1.f90:2).  z (ldz) and w
+// (ascending) are the outputs.
+static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, double *z,
+                     long long ldz, double *w, cudaStream_t st) {
+  memset(&c.stats, 0, sizeof c.stats);
+  c.launches = 0;
+  cudaEvent_t ev0, ev1;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  CK(cudaEventRecord(ev0, st));
+  const int bound = std::min(64, std::max(std::max(1, std::min(c.cfg.smlsiz, 64)), 2 * kd));
+  std::vector<int> sz(1, n);
+  while (*std::max_element(sz.begin(), sz.end()) > bound) {
+    std::vector<int> nx;
+    for (int x : sz) { nx.push_back(x / 2); nx.push_back((x + 1) / 2); }
+    sz.swap(nx);
+  }
+  const int nl = (int)sz.size(), ncut = nl - 1;
+  std::vector<int> ls(nl), ends(nl), cabove(nl), cbelow(nl), crow(std::max(ncut, 1));
+  int mmax = 1;
+  for (int i = 0, acc = 0; i < nl; ++i) {
+    ls[i] = acc;
+    acc += sz[i];
+    ends[i] = acc;
+    mmax = std::max(mmax, sz[i]);
+    cabove[i] = i > 0 ? i - 1 : -1;
+    cbelow[i] = i < nl - 1 ? i : -1;
+    if (i < nl - 1) crow[i] = acc - 1;
+  }
+  double *Q = buf<double>(c, "Q", (size_t)n * n);
+  double *Dp = buf<double>(c, "Dp", n);
+  int *perm = buf<int>(c, "perm", n);
+  int *status = buf<int>(c, "status", 6);
+  CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  CK(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)n * n, st));
+  const size_t kk = (size_t)kd * kd;
+  double *Uc = buf<double>(c, "band_U", std::max<size_t>(ncut, 1) * kk);
+  double *Vc = buf<double>(c, "band_V", std::max<size_t>(ncut, 1) * kk);
+  double *Sc = buf<double>(c, "band_S", std::max<size_t>(ncut, 1) * kd);
+  int *dcrow = buf<int>(c, "band_crow", crow.size());
+  int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl);
+  int *dca = buf<int>(c, "band_ca", nl), *dcb = buf<int>(c, "band_cb", nl);
+  h2d(dcrow, crow, st); h2d(dls, ls, st); h2d(dlz, sz, st); h2d(dca, cabove, st);
+  h2d(dcb, cbelow, st);
+  stage_begin(HSS_ST_LEAF, st);
+  launch_band_cut_svd(ncut, dcrow, kd, ab, ldab, Uc, Vc, Sc, status, st);
+  launch_band_leaf(nl, dls, dlz, dca, dcb, mmax, kd, ab, ldab, Uc, Vc, Sc, Q, n, Dp, perm, status,
+                   st);
+  {
+    double fl = 0.0;
+    for (int x : sz) fl += 8.0 * x * x * x * 10.0;  // ~10 Jacobi sweeps
+    stage_end(HSS_ST_LEAF, st, 8LL * n * (kd + 1), fl);
+  }
+  c.launches += 2;
+  if (nl > 1) {
+    std::vector<double> hS((size_t)ncut * kd);
+    CK(cudaMemcpyAsync(hS.data(), Sc, sizeof(double) * hS.size(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    LevelArrays L = level_arrays(c, n);
+    double *Z = buf<double>(c, "band_Z", (size_t)kd * n);
+    std::vector<int> lastleaf(nl);
+    for (int i = 0; i < nl; ++i) lastleaf[i] = i;
+    while (ends.size() > 1) {
+      std::vector<int> ms, mn, mn1, mcut, nxe, nxl;
+      for (size_t i = 0; i + 1 < ends.size(); i += 2) {
+        const int s = i == 0 ? 0 : ends[i - 1];
+        ms.push_back(s); mn.push_back(ends[i + 1] - s); mn1.push_back(ends[i] - s);
+        mcut.push_back(lastleaf[i]);
+        nxe.push_back(ends[i + 1]);
+        nxl.push_back(lastleaf[i + 1]);
+      }
+      const int P = (int)ms.size();
+      c.stats.n_levels++;
+      int *zs = buf<int>(c, "bz_s", P), *zn = buf<int>(c, "bz_n", P), *zn1 = buf<int>(c, "bz_n1", P),
+          *zc = buf<int>(c, "bz_c", P);
+      h2d(zs, ms, st); h2d(zn, mn, st); h2d(zn1, mn1, st); h2d(zc, mcut, st);
+      stage_begin(HSS_ST_PREPARE, st);
+      launch_band_z(P, *std::max_element(mn.begin(), mn.end()), zs, zn, zn1, zc, kd, Q, n, Uc, Vc, Z,
+                    n, st);
+      stage_end(HSS_ST_PREPARE, st, 8LL * n * kd * 2, 2.0 * n * kd * kd);
+      c.launches++;
+      double *drho = buf<double>(c, "band_rho", (size_t)P * kd);
+      std::vector<double> hr((size_t)P * kd);
+      for (int k = 0; k < kd; ++k)
+        for (int m = 0; m < P; ++m) hr[(size_t)k * P + m] = hS[(size_t)mcut[m] * kd + k];
+      h2d(drho, hr, st);
+      for (int k = 0; k < kd; ++k) {
+        BandUpdate bu;
+        bu.flags = k == 0 ? 0 : (PREP_SORTED | PREP_DENSE);
+        bu.z = Z + (size_t)k * n;
+        bu.zrest = Z + (size_t)(k + 1) * n;
+        bu.nrest = kd - k - 1;
+        bu.zld = n;
+        if (c.cfg.batched) {
+          bu.rho = drho + (size_t)k * P;
+          run_merges(c, ms, mn, mn1, nullptr, Q, n, Dp, perm, L, status, st, &bu);
+        } else {
+          for (int m = 0; m < P; ++m) {
+            bu.rho = drho + (size_t)k * P + m;
+            run_merges(c, {ms[m]}, {mn[m]}, {mn1[m]}, nullptr, Q, n, Dp, perm, L, status, st, &bu);
+          }
+        }
+      }
+      ends.swap(nxe);
+      lastleaf.swap(nxl);
+    }
+  }
+  stage_begin(HSS_ST_FINAL, st);
+  launch_final_gather(n, perm, Dp, Q, n, z, ldz, w, st);
+  stage_end(HSS_ST_FINAL, st, 16LL * n * n + 20LL * n, 0.0);
+  c.launches++;
+  CK(cudaEventRecord(ev1, st));
+  int hst[6] = {0, 0, 0, 0, 0, 0};
+  CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  unsigned long long its, fb;
+  memcpy(&its, hst + 2, sizeof its);
+  memcpy(&fb, hst + 4, sizeof fb);
+  c.stats.secular_iters = (long long)its;
+  c.stats.predictor_fallbacks = (long long)fb;
+  float ms_ = 0.f;
+  CK(cudaEventElapsedTime(&ms_, ev0, ev1));
+  c.stats.ms_total = ms_;
+  c.stats.kernel_launches = c.launches;
+  collect_stage_times(c);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  CK(cudaGetLastError());
+  if (hst[0] != 0) {
+    c.err = hst[0] == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
+                                          : "leaf Jacobi iteration did not converge";
+    return 1;
+  }
+  return 0;
+}
+
+// Symmetric band eigensolve from device arrays: ab upper band storage
+// (ldab >= kd + 1).  kd <= 1 is a tridiagonal and goes through the
+// tridiagonal solver; 2 <= kd <= 32 through band_core.
+static int band_solve(Ctx &c, int n, int kd, const double *ab, long long ldab, double *z,
+                      long long ldz, double *w, cudaStream_t st) {
+  if (kd <= 1 || n <= 2) {
+    std::vector<double> hab((size_t)ldab * n);
+    CK(cudaMemcpyAsync(hab.data(), ab, sizeof(double) * hab.size(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<double> hd(n), he(std::max(n, 1), 0.0);
+    for (int j = 0; j < n; ++j) hd[j] = hab[(size_t)j * ldab + kd];
+    if (kd >= 1)
+      for (int j = 1; j < n; ++j) he[j - 1] = hab[(size_t)j * ldab + kd - 1];
+    return mdstedc_core(c, n, hd, he, z, ldz, w, st);
+  }
+  return band_core(c, n, kd, ab, ldab, z, ldz, w, st);
+}
+
 // MDSTEDC('I') of one matrix.  hd/he: host copies of d/e (n, n-1).
 static int mdstedc_core(Ctx &c, int n, const std::vector<double> &hd, const std::vector<double> &he,
                         double *dz, long long ldz, double *dw, cudaStream_t st) {
@@ -743,6 +934,143 @@ int hss_mdstedc_batch_dev(int nprob, const int *n, double *d, double *e, double 
   } catch (CudaError &ex) {
     c.err = ex.msg;
     return 1000000;
+  }
+}
+
+int hss_mdsbevd_dev(int n, int kd, const double *ab, int ldab, double *w, double *z, int ldz,
+                    void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  if (kd < 0 || kd > HSS_BAND_KD_MAX) {
+    c.err = "hss_mdsbevd_dev: kd must be in 0.." + std::to_string(HSS_BAND_KD_MAX);
+    return -2;
+  }
+  if (ldab < kd + 1) return -4;
+  if (ldz < std::max(1, n)) return -7;
+  if (n == 0) return 0;
+  try {
+    return band_solve(c, n, kd, ab, ldab, z, ldz, w, (cudaStream_t)stream);
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+// Host band arrays -> device upper storage (lower storage converted), then the
+// device solve; results copied back.  Shared by MDSBEVD and MDSBEDC.
+static int band_host(Ctx &c, bool lower, int n, int kd, const double *ab, int ldab, double *w,
+                     double *z, int ldz, bool wantz) {
+  cudaStream_t st = nullptr;
+  const long long ldu = kd + 1;
+  std::vector<double> hu((size_t)ldu * n, 0.0);
+  for (int j = 0; j < n; ++j)
+    for (int i = std::max(0, j - kd); i <= j; ++i)
+      hu[(size_t)j * ldu + kd + i - j] =
+          lower ? ab[(size_t)i * ldab + (j - i)] : ab[(size_t)j * ldab + kd + i - j];
+  double *dab = buf<double>(c, "band_ab", hu.size());
+  double *dz = buf<double>(c, "z_out", (size_t)n * n);
+  double *dw = buf<double>(c, "w_out", n);
+  CK(cudaMemcpyAsync(dab, hu.data(), sizeof(double) * hu.size(), cudaMemcpyHostToDevice, st));
+  const int info = band_solve(c, n, kd, dab, ldu, dz, n, dw, st);
+  if (wantz)
+    CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n, n,
+                         cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(w, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return info;
+}
+
+void mdsbevd_(const char *compz, const char *uplo, const int *n_, const int *kd_, double *ab,
+              const int *ldab_, double *d, double *q, const int *ldq_, double *work,
+              const int *lwork_, int *iwork, const int *liwork_, int *info, size_t, size_t) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  const int n = *n_, kd = *kd_, ldab = *ldab_, ldq = *ldq_, lwork = *lwork_, liwork = *liwork_;
+  const char cz = compz[0];
+  const int icompz = (cz == 'N' || cz == 'n') ? 0 : (cz == 'I' || cz == 'i') ? 2 : -1;
+  const bool lquery = (lwork == -1 || liwork == -1);
+  *info = 0;
+  // argument numbering as SRC/mdsbevd.f90:228-263
+  if (icompz < 0) *info = -1;
+  else if (n < 0) *info = -2;
+  else if (ldq < 1 || (icompz > 0 && ldq < std::max(1, n))) *info = -6;
+  long long lwmin = 1, liwmin = 1;
+  if (*info == 0) {
+    const int smlsiz = c.cfg.smlsiz;
+    if (n <= 1 || icompz == 0) { lwmin = 1; liwmin = 1; }
+    else if (n <= smlsiz) { lwmin = 2LL * (n - 1); liwmin = 1; }
+    else { lwmin = 1 + 4LL * n + (long long)n * n; liwmin = 3 + 5LL * n; }
+    if (work) work[0] = (double)lwmin;
+    if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
+    if (lwork < lwmin && !lquery) *info = -8;
+    else if (liwork < liwmin && !lquery) *info = -10;
+  }
+  if (*info == 0 && (kd < 0 || kd > HSS_BAND_KD_MAX || ldab < kd + 1)) *info = -4;
+  if (*info != 0) {
+    c.err = "MDSBEVD: illegal argument " + std::to_string(-*info);
+    return;
+  }
+  if (lquery || n == 0) return;
+  if (n == 1) {
+    d[0] = ab[kd];
+    if (icompz != 0) q[0] = 1.0;
+    return;
+  }
+  (void)uplo;  // the reference reads the upper band whatever UPLO says
+  try {
+    *info = band_host(c, false, n, kd, ab, ldab, d, q, ldq, icompz != 0);
+    if (work) work[0] = (double)lwmin;
+    if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
+  }
+}
+
+void mdsbedc_(const char *jobz, const char *uplo, const int *n_, const int *kd_, double *ab,
+              const int *ldab_, double *w, double *z, const int *ldz_, double *work,
+              const int *lwork_, int *iwork, const int *liwork_, int *info, size_t, size_t) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  const int n = *n_, kd = *kd_, ldab = *ldab_, ldz = *ldz_, lwork = *lwork_, liwork = *liwork_;
+  const bool wantz = jobz[0] == 'V' || jobz[0] == 'v';
+  const bool lower = uplo[0] == 'L' || uplo[0] == 'l';
+  const bool lquery = (lwork == -1 || liwork == -1);
+  long long lwmin = 1, liwmin = 1;
+  if (n > 1) {  // SRC/mdsbedc.f90:190-201
+    if (wantz) { liwmin = 3 + 5LL * n; lwmin = 1 + 5LL * n + 2LL * n * n; }
+    else { liwmin = 1; lwmin = 2LL * n; }
+  }
+  *info = 0;
+  if (!(wantz || jobz[0] == 'N' || jobz[0] == 'n')) *info = -1;
+  else if (!(lower || uplo[0] == 'U' || uplo[0] == 'u')) *info = -2;
+  else if (n < 0) *info = -3;
+  else if (kd < 0) *info = -4;
+  else if (ldab < kd + 1) *info = -6;
+  else if (ldz < 1 || (wantz && ldz < n)) *info = -9;
+  if (*info == 0) {
+    if (work) work[0] = (double)lwmin;
+    if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
+    if (lwork < lwmin && !lquery) *info = -11;
+    else if (liwork < liwmin && !lquery) *info = -13;
+  }
+  if (*info == 0 && kd > HSS_BAND_KD_MAX) *info = -4;
+  if (*info != 0) {
+    c.err = "MDSBEDC: illegal argument " + std::to_string(-*info);
+    return;
+  }
+  if (lquery || n == 0) return;
+  if (n == 1) {
+    w[0] = lower ? ab[0] : ab[kd];
+    if (wantz) z[0] = 1.0;
+    return;
+  }
+  try {
+    *info = band_host(c, lower, n, kd, ab, ldab, w, z, ldz, wantz);
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
   }
 }
 

@@ -62,6 +62,17 @@ struct PoleDiff {
   }
 };
 
+// Merge of root r in a level batch: merge m owns positions [s[m], s[m] + K[m])
+// of the level arrays; off is the prefix sum of K (P + 1 entries).
+__device__ __forceinline__ int find_merge(const int *__restrict__ off, int P, int r) {
+  int lo = 0, hi = P;  // off[lo] <= r < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= r) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // Device status words written by kernels; the host maps them to INFO > 0.
 enum HssStatus : int {
   HSS_OK = 0,

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 namespace hss {
@@ -56,11 +57,20 @@ void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int n
                  int *status, cudaStream_t st);
 
 // merge.cu
+// prepare flags: the block is already in ascending order (no merge of two
+// halves); every column is dense (no top / bottom block structure)
+enum { PREP_SORTED = 1, PREP_DENSE = 2 };
+// zsrc: z per slot instead of the rows of Q around the cut; rsrc: the coupling
+// rho_in per merge instead of e[s + n1 - 1]
 void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1, const double *e,
                           const double *Q, long long ldq, double *Dp, int *perm,
-                          const LevelScratch &w, int *out, double *orho, cudaStream_t st);
+                          const LevelScratch &w, int *out, double *orho, cudaStream_t st,
+                          const double *zsrc = nullptr, const double *rsrc = nullptr,
+                          int flags = 0);
+// Zr (nz columns, leading dim zld): rows rotated with the Q columns
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
-                   const LevelScratch &w, double *Q, long long ldq, cudaStream_t st);
+                   const LevelScratch &w, double *Q, long long ldq, cudaStream_t st,
+                   double *Zr = nullptr, int nz = 0, long long zld = 0);
 void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                    const int *ndslot, const int *grp, const long long *boff, const double *Q,
                    long long ldq, double *B, cudaStream_t st);
@@ -96,6 +106,21 @@ void launch_mlp_grad(int n, const float *X, const float *T, const float *norm, c
                      float *G, float *L, cudaStream_t st);
 void launch_adam(int np, float *W, const float *G, float *M, float *V, float lr, int step,
                  void *Wb, cudaStream_t st);
+
+// band.cu: banded divide and conquer (cuts, leaves, Z = Q^T W, Z updates)
+void launch_band_cut_svd(int ncut, const int *cut_row, int kd, const double *AB, long long ldab,
+                         double *Uc, double *Vc, double *Sc, int *status, cudaStream_t st);
+void launch_band_leaf(int nleaf, const int *lstart, const int *lsize, const int *cut_above,
+                      const int *cut_below, int mmax, int kd, const double *AB, long long ldab,
+                      const double *Uc, const double *Vc, const double *Sc, double *Q,
+                      long long ldq, double *Dp, int *perm, int *status, cudaStream_t st);
+void launch_band_z(int P, int maxn, const int *ms, const int *mn, const int *mn1, const int *mcut,
+                   int kd, const double *Q, long long ldq, const double *Uc, const double *Vc,
+                   double *Z, long long zld, cudaStream_t st);
+void launch_band_zupdate(const LevelView &lv, int total, const double *dl, const double *difl,
+                         const double *difr, const double *zhat, const double *alpha,
+                         const int *ndslot, double *Z, int nrest, long long zld, double *Zt,
+                         cudaStream_t st);
 
 // driver.cu: set the message hss_last_error() returns
 void set_last_error(const std::string &msg);

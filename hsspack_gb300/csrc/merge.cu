@@ -101,51 +101,63 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                 const int *__restrict__ mn1, const double *__restrict__ e,
                 const double *__restrict__ Q, long long ldq, double *__restrict__ Dp,
                 int *__restrict__ perm, LevelScratch w, int *__restrict__ out,
-                double *__restrict__ orho) {
+                double *__restrict__ orho, const double *__restrict__ zsrc,
+                const double *__restrict__ rsrc, int flags) {
   const int m = blockIdx.x;
   if (m >= P) return;
   const int s = ms[m], n = mn[m], n1 = mn1[m], n2 = n - n1;
   const int tid = threadIdx.x;
-  const double rho_in = e[s + n1 - 1];
-  // ---- merge the two ascending halves (DLAMRG, ties to the first list) by
-  //      merge path on contiguous copies of their eigenvalues (zs as scratch)
-  for (int i = tid; i < n; i += MT) w.zs[s + i] = Dp[perm[s + i]];
-  __syncthreads();
-  const double *hv = w.zs + s;
-  for (int i = tid; i < n1; i += MT) {
-    const double a = hv[i];
-    int lo = 0, hi = n2;  // count right values < a
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      if (hv[n1 + mid] < a) lo = mid + 1; else hi = mid;
+  const double rho_in = rsrc ? rsrc[m] : e[s + n1 - 1];
+  if (flags & PREP_SORTED) {
+    // ---- the whole block is already ascending (a later rank-one update of a
+    //      banded merge: mdsbed22.f90 takes INDXQ as it is)
+    for (int i = tid; i < n; i += MT) {
+      const int slot = perm[s + i];
+      w.srt[s + i] = slot;
+      w.ds[s + i] = Dp[slot];
     }
-    w.srt[s + i + lo] = perm[s + i];
-    w.ds[s + i + lo] = a;
-  }
-  for (int j = tid; j < n2; j += MT) {
-    const double b = hv[n1 + j];
-    int lo = 0, hi = n1;  // count left values <= b
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      if (hv[mid] <= b) lo = mid + 1; else hi = mid;
+  } else {
+    // ---- merge the two ascending halves (DLAMRG, ties to the first list) by
+    //      merge path on contiguous copies of their eigenvalues (zs as scratch)
+    for (int i = tid; i < n; i += MT) w.zs[s + i] = Dp[perm[s + i]];
+    __syncthreads();
+    const double *hv = w.zs + s;
+    for (int i = tid; i < n1; i += MT) {
+      const double a = hv[i];
+      int lo = 0, hi = n2;  // count right values < a
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (hv[n1 + mid] < a) lo = mid + 1; else hi = mid;
+      }
+      w.srt[s + i + lo] = perm[s + i];
+      w.ds[s + i + lo] = a;
     }
-    w.srt[s + j + lo] = perm[s + n1 + j];
-    w.ds[s + j + lo] = b;
+    for (int j = tid; j < n2; j += MT) {
+      const double b = hv[n1 + j];
+      int lo = 0, hi = n1;  // count left values <= b
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (hv[mid] <= b) lo = mid + 1; else hi = mid;
+      }
+      w.srt[s + j + lo] = perm[s + n1 + j];
+      w.ds[s + j + lo] = b;
+    }
   }
   __syncthreads();
   // ---- z = [last row of Q1, first row of Q2] / sqrt(2) (mdlaed1.f90:178-180,
-  //      mdlaed2.f90:203-211) in merged order
+  //      mdlaed2.f90:203-211) in merged order, or a given z per slot (Q^T w
+  //      of a banded cut, scaled the same way at mdsbed22.f90)
   const double sc = 1.0 / sqrt(2.0);
   double dmax = 0.0, zmax = 0.0;
   for (int i = tid; i < n; i += MT) {
     const int slot = w.srt[s + i];
     const bool top = slot < s + n1;
-    double z = Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
+    double z = zsrc ? zsrc[slot] : Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
     if (!top && rho_in < 0.0) z = -z;
     z *= sc;
     const double dv = w.ds[s + i];
     w.zs[s + i] = z;
-    w.typ[s + i] = top ? 1 : 3;
+    w.typ[s + i] = (flags & PREP_DENSE) ? 2 : top ? 1 : 3;
     dmax = fmax(dmax, fabs(dv));
     zmax = fmax(zmax, fabs(z));
   }
@@ -323,20 +335,26 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
 
 // Apply each merge's Givens rotations, in order, to its slot pairs: one thread
 // per row (rows of a block are independent; columns are read coalesced).
+// Threads r >= n rotate rows p, q of column r - n of Zr (nz columns, leading
+// dim zld) the same way: the remaining columns of a banded merge's
+// Z = Q^T W follow the rotated eigenvectors (mdsbed22.f90 rotates Z(:, 2:)).
 __global__ void k_givens(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                          const int *__restrict__ ng, const LevelScratch w, double *Q,
-                         long long ldq) {
+                         long long ldq, double *Zr, int nz, long long zld) {
   for (int m = blockIdx.y; m < P; m += gridDim.y) {
     const int s = ms[m], n = mn[m], g = ng[m];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n || g == 0) continue;
-    const long long row = s + r;
+    if (r >= n + nz || g == 0) continue;
+    double *base;
+    long long ld, row;
+    if (r < n) { base = Q; ld = ldq; row = s + r; }
+    else { base = Zr + (r - n) * zld; ld = 1; row = 0; }
     for (int t = 0; t < g; ++t) {
       const long long p = w.gvp[s + t], q = w.gvq[s + t];
       const double c = w.gvc[s + t], sn = w.gvs[s + t];
-      const double x = Q[p * ldq + row], y = Q[q * ldq + row];
-      Q[p * ldq + row] = c * x + sn * y;
-      Q[q * ldq + row] = c * y - sn * x;
+      const double x = base[p * ld + row], y = base[q * ld + row];
+      base[p * ld + row] = c * x + sn * y;
+      base[q * ld + row] = c * y - sn * x;
     }
   }
 }
@@ -486,20 +504,30 @@ static int merge_threads(int maxn) {
 
 void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1,
                           const double *e, const double *Q, long long ldq, double *Dp, int *perm,
-                          const LevelScratch &w, int *out, double *orho, cudaStream_t st) {
+                          const LevelScratch &w, int *out, double *orho, cudaStream_t st,
+                          const double *zsrc, const double *rsrc, int flags) {
   if (P <= 0) return;
+#define PREP_CASE(T)                                                                        \
+  case T:                                                                                  \
+    k_merge_prepare<T><<<P, T, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho, \
+                                        zsrc, rsrc, flags);                                \
+    break;
   switch (merge_threads(maxn)) {
-    case 64: k_merge_prepare<64><<<P, 64, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
-    case 128: k_merge_prepare<128><<<P, 128, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
-    case 256: k_merge_prepare<256><<<P, 256, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
-    default: k_merge_prepare<512><<<P, 512, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho); break;
+    PREP_CASE(64)
+    PREP_CASE(128)
+    PREP_CASE(256)
+    default:
+    PREP_CASE(512)
   }
+#undef PREP_CASE
 }
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
-                   const LevelScratch &w, double *Q, long long ldq, cudaStream_t st) {
+                   const LevelScratch &w, double *Q, long long ldq, cudaStream_t st, double *Zr,
+                   int nz, long long zld) {
   if (P <= 0) return;
-  dim3 grid((maxn + 255) / 256, std::min(P, 65535));
-  k_givens<<<grid, 256, 0, st>>>(P, ms, mn, ng, w, Q, ldq);
+  if (!Zr) nz = 0;
+  dim3 grid((maxn + nz + 255) / 256, std::min(P, 65535));
+  k_givens<<<grid, 256, 0, st>>>(P, ms, mn, ng, w, Q, ldq, Zr, nz, zld);
 }
 void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                    const int *ndslot, const int *grp, const long long *boff, const double *Q,

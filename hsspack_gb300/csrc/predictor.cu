@@ -73,22 +73,60 @@ struct bf16w {
 
 // Inference: feat[(s+j)*(NF+1) + i] from the midpoint pass (slot NF holds the
 // side: 0 root in (d_j, midpoint], 1 in (midpoint, d_{j+1}), -1 no prediction).
-__global__ void __launch_bounds__(128)
+// One thread per position.  The weights (converted to FP32) sit in shared
+// memory and are read as broadcasts; each thread keeps its activation row in
+// a padded shared-memory row (stride NH + 1: conflict-free) and computes 16
+// outputs at a time in registers, so every activation load feeds 16 FMAs.
+// The sums run in the same order as mlp_forward (bias, then inputs ascending).
+constexpr int PT = 128;          // positions per CTA
+constexpr int AST = NH + 1;      // activation row stride (floats)
+constexpr int OB = 16;           // outputs per register block
+constexpr size_t PREDICT_SMEM = sizeof(float) * ((size_t)((NPARAM + 3) / 4 * 4) + 2 * PT * AST);
+
+template <int NIN>
+__device__ __forceinline__ void dense_relu_rows(const float *__restrict__ in, int in_stride,
+                                                const float *__restrict__ W, const float *__restrict__ b,
+                                                float *__restrict__ out) {
+#pragma unroll 1
+  for (int o0 = 0; o0 < NH; o0 += OB) {
+    float acc[OB];
+#pragma unroll
+    for (int j = 0; j < OB; ++j) acc[j] = b[o0 + j];
+#pragma unroll 4
+    for (int i = 0; i < NIN; ++i) {
+      const float x = in[i * in_stride];
+      const float *w = W + i * NH + o0;
+#pragma unroll
+      for (int j = 0; j < OB; ++j) acc[j] = fmaf(x, w[j], acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < OB; ++j) out[o0 + j] = fmaxf(acc[j], 0.f);
+  }
+}
+
+__global__ void __launch_bounds__(PT)
 k_predict(int n, const float *__restrict__ feat, const __nv_bfloat16 *__restrict__ Wb,
           const float *__restrict__ norm, float *__restrict__ guess) {
-  __shared__ __nv_bfloat16 sW[NPARAM];
-  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) sW[i] = Wb[i];
+  extern __shared__ float psm[];
+  float *sW = psm;
+  float *A = psm + (NPARAM + 3) / 4 * 4;
+  float *B = A + PT * AST;
+  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) sW[i] = __bfloat162float(Wb[i]);
   __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.x * PT + threadIdx.x;
   if (r >= n) return;
   const float *f = feat + (long long)r * (NF + 1);
   const float side = f[NF];
   if (side < 0.f) { guess[r] = 2.0f; return; }  // no prediction
-  float fn[NF];
+  float *a = A + threadIdx.x * AST, *bb = B + threadIdx.x * AST;
+  // normalised features in this thread's row of B (stride 1)
 #pragma unroll
-  for (int i = 0; i < NF; ++i) fn[i] = (f[i] - norm[i]) / norm[NF + i];
-  float h1[NH], h2[NH], h3[NH];
-  const float y = mlp_forward(fn, reinterpret_cast<const bf16w *>(sW), h1, h2, h3);
+  for (int i = 0; i < NF; ++i) bb[i] = (f[i] - norm[i]) / norm[NF + i];
+  dense_relu_rows<NF>(bb, 1, sW + P_W1, sW + P_B1, a);
+  dense_relu_rows<NH>(a, 1, sW + P_W2, sW + P_B2, bb);
+  dense_relu_rows<NH>(bb, 1, sW + P_W3, sW + P_B3, a);
+  float y = sW[P_B4];
+  for (int i = 0; i < NH; ++i) y = fmaf(a[i], sW[P_W4 + i], y);
   const float l = f[NF - 1] + clampf(y, -1.f, 1.f);
   // signed distance to the nearer pole: +u (left pole), -u (right pole)
   float u;
@@ -204,7 +242,13 @@ int mlp_nfeat() { return NF; }
 void launch_predict(int n, const float *feat, const void *Wb, const float *norm, float *guess,
                     cudaStream_t st) {
   if (n <= 0) return;
-  k_predict<<<(n + 127) / 128, 128, 0, st>>>(n, feat, (const __nv_bfloat16 *)Wb, norm, guess);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PREDICT_SMEM);
+    attr = true;
+  }
+  k_predict<<<(n + PT - 1) / PT, PT, PREDICT_SMEM, st>>>(n, feat, (const __nv_bfloat16 *)Wb, norm,
+                                                         guess);
 }
 
 void launch_train_targets(int K, const double *d, const double *difl, const double *difr,

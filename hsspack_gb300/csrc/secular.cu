@@ -221,16 +221,7 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
 }
 
 // ------------------------------------------------------------- kernels -----
-// Batched over the merges of one DC level.  Merge m owns positions
-// [s[m], s[m] + K[m]) of the level arrays; rootoff is the prefix sum of K.
-__device__ __forceinline__ int find_merge(const int *__restrict__ off, int P, int r) {
-  int lo = 0, hi = P;  // off[lo] <= r < off[hi]
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (__ldg(off + mid) <= r) lo = mid; else hi = mid;
-  }
-  return lo;
-}
+// Batched over the merges of one DC level (find_merge: hss_common.cuh).
 
 // One root per group of L lanes (L = 1..32 chosen from the level's largest
 // K so that each lane sums ~8 pole terms and the group reductions stay cheap).

@@ -38,7 +38,8 @@ typedef struct hss_config {
 enum hss_stage {
   HSS_ST_LEAF = 0, HSS_ST_PREPARE, HSS_ST_GIVENS, HSS_ST_SECULAR, HSS_ST_LOWNER,
   HSS_ST_BUILD_S, HSS_ST_GATHER, HSS_ST_GEMM, HSS_ST_SCATTER, HSS_ST_FINISH,
-  HSS_ST_FINAL, HSS_ST_HSS_BUILD, HSS_ST_HSS_MM, HSS_ST_OTHER, HSS_NSTAGE = 16
+  HSS_ST_FINAL, HSS_ST_HSS_BUILD, HSS_ST_HSS_MM, HSS_ST_OTHER, HSS_ST_PREDICT,
+  HSS_NSTAGE = 16
 };
 
 typedef struct hss_stats {
@@ -75,6 +76,31 @@ void mdstedc_(const char *compz, const int *n, double *d, double *e, double *z,
               const int *ldz, double *work, const int *lwork, int *iwork,
               const int *liwork, int *info, size_t compz_len);
 
+/* Largest band half-width of the banded divide and conquer (leaves of up to
+ * 2 kd rows are solved by one warp each). */
+#define HSS_BAND_KD_MAX 32
+
+/* MDSBEVD(COMPZ,UPLO,N,KD,AB,LDAB,D,Q,LDQ,WORK,LWORK,IWORK,LIWORK,INFO)
+ * replaces SRC/mdsbevd.f90:183: eigenpairs of the symmetric band matrix in
+ * upper band storage AB (the reference reads the upper band whatever UPLO
+ * says); COMPZ = 'I' computes Q, 'N' eigenvalues only.  Argument errors and
+ * workspace queries as the reference (INFO = -1, -2, -6, -8, -10); KD outside
+ * 0..HSS_BAND_KD_MAX or LDAB < KD+1 gives INFO = -4. */
+void mdsbevd_(const char *compz, const char *uplo, const int *n, const int *kd,
+              double *ab, const int *ldab, double *d, double *q, const int *ldq,
+              double *work, const int *lwork, int *iwork, const int *liwork,
+              int *info, size_t compz_len, size_t uplo_len);
+
+/* MDSBEDC(JOBZ,UPLO,N,KD,AB,LDAB,W,Z,LDZ,WORK,LWORK,IWORK,LIWORK,INFO)
+ * replaces SRC/mdsbedc.f90:166: JOBZ = 'V' / 'N', UPLO = 'U' / 'L' (lower
+ * storage is converted; the reference passes it on as upper).  Workspace
+ * LWMIN = 1+5N+2N^2, LIWMIN = 3+5N (JOBZ = 'V') as mdsbedc.f90:190-201;
+ * KD > HSS_BAND_KD_MAX gives INFO = -4. */
+void mdsbedc_(const char *jobz, const char *uplo, const int *n, const int *kd,
+              double *ab, const int *ldab, double *w, double *z, const int *ldz,
+              double *work, const int *lwork, int *iwork, const int *liwork,
+              int *info, size_t jobz_len, size_t uplo_len);
+
 /* Cauchylike(A,D,F,u,v,M,N): A(i,j) = u(i) v(j) / (D(i) - F(j)),
  * replaces SRC/Cauchylike.f90:1 (computed on the GPU). */
 void cauchylike_(double *A, const double *D, const double *F, const double *u,
@@ -85,6 +111,12 @@ void cauchylike_(double *A, const double *D, const double *F, const double *u,
  * d(n) in: diagonal, out: eigenvalues ascending; e(n-1) off-diagonal
  * (destroyed); z(ldz, n) out: eigenvectors.  stream may be NULL. */
 int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *stream);
+
+/* Symmetric band eigensolve in HBM (the MDSBEVD path): ab(ldab, n) upper band
+ * storage, 0 <= kd <= HSS_BAND_KD_MAX; w(n) eigenvalues ascending, z(ldz, n)
+ * eigenvectors.  Returns 0, -i for a bad i-th argument, > 0 on failure. */
+int hss_mdsbevd_dev(int n, int kd, const double *ab, int ldab, double *w, double *z,
+                    int ldz, void *stream);
 
 /* Many independent tridiagonal eigensolves in one call, each with COMPZ='I'
  * semantics of MDSTEDC (SRC/mdstedc.f90:139); no batched counterpart in the

@@ -68,3 +68,40 @@ def test_mdstedc_quick_returns_without_gpu():
     d = np.array([3.0]); e = np.zeros(1); z = np.zeros((1, 1), order="F")
     info = hp.mdstedc("I", 1, d, e, z, 1, np.zeros(1), 1, np.zeros(1, dtype=np.int32), 1)
     assert info == 0 and z[0, 0] == 1.0 and d[0] == 3.0
+
+
+def _band_call(fn, c1, uplo, n, kd, ldab, ldz, lwork, liwork):
+    ab = np.zeros((max(ldab, 1), max(n, 1)), order="F")
+    w = np.zeros(max(n, 1))
+    z = np.zeros((max(ldz, 1), max(n, 1)), order="F")
+    work, iwork = np.zeros(1), np.zeros(1, dtype=np.int32)
+    info = fn(c1, uplo, n, kd, ab, ldab, w, z, ldz, work, lwork, iwork, liwork)
+    return info, work[0], iwork[0]
+
+
+def test_mdsbedc_arguments_and_workspace():
+    # argument numbering and workspace sizes of SRC/mdsbedc.f90:190-228
+    n = 300
+    assert _band_call(hp.mdsbedc, "X", "U", n, 4, 5, n, -1, -1)[0] == -1
+    assert _band_call(hp.mdsbedc, "V", "X", n, 4, 5, n, -1, -1)[0] == -2
+    assert _band_call(hp.mdsbedc, "V", "U", -1, 4, 5, n, -1, -1)[0] == -3
+    assert _band_call(hp.mdsbedc, "V", "U", n, -1, 5, n, -1, -1)[0] == -4
+    assert _band_call(hp.mdsbedc, "V", "U", n, 4, 4, n, -1, -1)[0] == -6
+    assert _band_call(hp.mdsbedc, "V", "U", n, 4, 5, n - 1, -1, -1)[0] == -9
+    info, lw, liw = _band_call(hp.mdsbedc, "V", "U", n, 4, 5, n, -1, -1)
+    assert info == 0 and lw == 1 + 5 * n + 2 * n * n and liw == 3 + 5 * n
+    info, lw, liw = _band_call(hp.mdsbedc, "N", "L", n, 4, 5, 1, -1, -1)
+    assert info == 0 and lw == 2 * n and liw == 1
+    assert _band_call(hp.mdsbedc, "V", "U", n, 4, 5, n, 10, 10)[0] == -11
+    assert _band_call(hp.mdsbedc, "V", "U", n, 40, 41, n, -1, -1)[0] == -4  # beyond 32
+
+
+def test_mdsbevd_arguments_and_workspace():
+    # SRC/mdsbevd.f90:228-263 (its own numbering: -1, -2, -6, -8, -10)
+    n = 300
+    assert _band_call(hp.mdsbevd, "X", "U", n, 4, 5, n, -1, -1)[0] == -1
+    assert _band_call(hp.mdsbevd, "I", "U", -1, 4, 5, n, -1, -1)[0] == -2
+    assert _band_call(hp.mdsbevd, "I", "U", n, 4, 5, n - 1, -1, -1)[0] == -6
+    info, lw, liw = _band_call(hp.mdsbevd, "I", "U", n, 4, 5, n, -1, -1)
+    assert info == 0 and lw == 1 + 4 * n + n * n and liw == 3 + 5 * n
+    assert _band_call(hp.mdsbevd, "I", "U", n, 4, 5, n, 10, 10)[0] == -8
