@@ -90,6 +90,10 @@ SIGNATURES = {
                         _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
     "hss_mdsbevd_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, ctypes.c_int, _V, _V,
                                        ctypes.c_int, _V]),
+    "mdbdsdc_": (None, [ctypes.c_char_p, ctypes.c_char_p, _I, _D, _D, _D, _I, _D, _I, _D, _I, _D,
+                        _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
+    "hss_mdbdsdc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V, ctypes.c_int,
+                                       _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
@@ -276,6 +280,53 @@ def mdsbevd_dev(kd, ab, w, z, stream=None):
                                   _stream(stream))
     if info != 0:
         raise HssError("hss_mdsbevd_dev INFO=%d: %s" % (info, _err()))
+    return info
+
+
+def mdbdsdc(uplo, compq, n, d, e, u, ldu, vt, ldvt, q, iq, work, iwork):
+    """MDBDSDC with the Fortran argument list (SRC/mdbdsdc.f90:1); numpy arrays,
+    u and vt Fortran ordered.  Returns INFO."""
+    for a, dt in ((d, np.float64), (e, np.float64), (u, np.float64), (vt, np.float64),
+                  (q, np.float64), (work, np.float64), (iq, np.int32), (iwork, np.int32)):
+        if a.dtype != dt:
+            raise TypeError("array dtype must be %s" % dt)
+    for a in (u, vt):
+        if a.ndim == 2 and not a.flags.f_contiguous:
+            raise ValueError("u and vt must be Fortran ordered")
+    info = ctypes.c_int(0)
+    n_, ldu_, ldvt_ = (ctypes.c_int(int(x)) for x in (n, ldu, ldvt))
+    load().mdbdsdc_(uplo.encode(), compq.encode(), ctypes.byref(n_), _pd(d), _pd(e), _pd(u),
+                    ctypes.byref(ldu_), _pd(vt), ctypes.byref(ldvt_), _pd(q),
+                    iq.ctypes.data_as(_I), _pd(work), iwork.ctypes.data_as(_I),
+                    ctypes.byref(info), 1, 1)
+    return info.value
+
+
+def svd_bidiagonal(d, e, lower=False):
+    """(s descending, U, VT) of the square bidiagonal (d, e) through MDBDSDC('I')."""
+    n = len(d)
+    dd = np.array(d, dtype=np.float64, copy=True)
+    ee = np.zeros(max(n, 1))
+    ee[:max(n - 1, 0)] = np.asarray(e, dtype=np.float64)[:max(n - 1, 0)]
+    U = np.zeros((n, n), order="F")
+    VT = np.zeros((n, n), order="F")
+    one = np.zeros(1)
+    ione = np.zeros(1, dtype=np.int32)
+    info = mdbdsdc("L" if lower else "U", "I", n, dd, ee, U, max(1, n), VT, max(1, n), one, ione,
+                   one, ione)
+    if info != 0:
+        raise HssError("MDBDSDC INFO=%d: %s" % (info, _err()))
+    return dd, U, VT
+
+
+def mdbdsdc_dev(d, e, u, vt, stream=None):
+    """Device bidiagonal SVD: d (n,) -> singular values (descending), u and vt
+    (n, n) column-major storage."""
+    n = d.numel()
+    info = load().hss_mdbdsdc_dev(n, _ptr(d), _ptr(e), _ptr(u), max(1, n), _ptr(vt), max(1, n),
+                                  _stream(stream))
+    if info != 0:
+        raise HssError("hss_mdbdsdc_dev INFO=%d: %s" % (info, _err()))
     return info
 
 

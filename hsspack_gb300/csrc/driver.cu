@@ -790,6 +790,274 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   return 0;
 }
 
+__global__ void k_scale(int n, double *x, double a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] *= a;
+}
+
+// ------------------------------------------------------------- SVD DC ----
+// One level of bidiagonal SVD merges (MDLASD1, SRC/mdlasd1.f90): deflation
+// (MDLASD2), the secular equation and the z rebuild in squared mode, the K x K
+// U and V blocks, the products U2 Ub and V2 Vb (DLASD3's products), the new
+// ascending order.  Merge m covers rows ms[m] .. ms[m] + N - 1, N = nl+1+nr.
+static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int> &mnl,
+                           const std::vector<int> &mnr, const std::vector<int> &msq,
+                           const double *d, const double *e, double *U, double *V, long long ld,
+                           double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st) {
+  const int P = (int)ms.size();
+  if (P == 0) return;
+  std::vector<int> mN(P), mM(P);
+  for (int m = 0; m < P; ++m) { mN[m] = mnl[m] + 1 + mnr[m]; mM[m] = mN[m] + msq[m]; }
+  const int maxN = *std::max_element(mN.begin(), mN.end());
+  const int maxM = *std::max_element(mM.begin(), mM.end());
+  int *dms = buf<int>(c, "sv_s", P), *dnl = buf<int>(c, "sv_nl", P), *dnr = buf<int>(c, "sv_nr", P),
+      *dsq = buf<int>(c, "sv_sq", P), *dN = buf<int>(c, "sv_N", P), *dM = buf<int>(c, "sv_M", P);
+  h2d(dms, ms, st); h2d(dnl, mnl, st); h2d(dnr, mnr, st); h2d(dsq, msq, st); h2d(dN, mN, st);
+  h2d(dM, mM, st);
+  int *dout = buf<int>(c, "g_out", 5 * P);
+  double *dnrm = buf<double>(c, "sv_nrm", P);
+  stage_begin(HSS_ST_PREPARE, st);
+  launch_svd_prepare(P, maxN, dms, dnl, dnr, dsq, d, e, U, ld, V, ld, Dp, perm, L.w, dout, dnrm,
+                     st);
+  {
+    long long nn = 0;
+    for (int x : mN) nn += x;
+    stage_end(HSS_ST_PREPARE, st, 64 * nn, 0.0);
+  }
+  c.launches++;
+  int *hout = (int *)pinned(c, (size_t)P * 5 * sizeof(int));
+  CK(cudaMemcpyAsync(hout, dout, (size_t)P * 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<int> aK(P), aoff(P + 1, 0), gs, gN, gM, gng;
+  std::vector<double> ones(P, 1.0);
+  std::vector<long long> qU(P), qV(P), bo(P);
+  long long totU = 0, totV = 0, totB = 0;
+  int maxK = 1, maxNg = 0, maxMg = 0;
+  for (int m = 0; m < P; ++m) {
+    const int K = hout[5 * m], ng = hout[5 * m + 1];
+    aK[m] = K;
+    aoff[m + 1] = aoff[m] + K;
+    maxK = std::max(maxK, K);
+    c.stats.n_merges++;
+    c.stats.n_dense_merges++;
+    c.stats.total_k += K;
+    c.stats.max_k = std::max(c.stats.max_k, K);
+    qU[m] = totU; totU += (long long)mN[m] * K;
+    qV[m] = totV; totV += (long long)mM[m] * K;
+    bo[m] = totB; totB += (long long)K * K;
+    if (ng > 0) {
+      gs.push_back(ms[m]); gN.push_back(mN[m]); gM.push_back(mM[m]); gng.push_back(ng);
+      maxNg = std::max(maxNg, mN[m]); maxMg = std::max(maxMg, mM[m]);
+    }
+  }
+  if (!gs.empty()) {  // deflating rotations of U columns and V columns (mdlasd2.f90)
+    const int G = (int)gs.size();
+    int *g1 = buf<int>(c, "sg_s", G), *g2 = buf<int>(c, "sg_N", G), *g3 = buf<int>(c, "sg_M", G),
+        *g4 = buf<int>(c, "sg_g", G);
+    h2d(g1, gs, st); h2d(g2, gN, st); h2d(g3, gM, st); h2d(g4, gng, st);
+    stage_begin(HSS_ST_GIVENS, st);
+    launch_givens(G, maxNg, g1, g2, g4, L.w, U, ld, st);
+    launch_givens(G, maxMg, g1, g3, g4, L.w, V, ld, st);
+    stage_end(HSS_ST_GIVENS, st, 0, 0.0);
+    c.launches += 2;
+  }
+  int *vK = buf<int>(c, "sv_K", P), *voff = buf<int>(c, "sv_off", P + 1);
+  double *vr = buf<double>(c, "sv_rho", P);
+  long long *dqU = buf<long long>(c, "sv_qU", P), *dqV = buf<long long>(c, "sv_qV", P),
+            *dbo = buf<long long>(c, "sv_bo", P);
+  h2d(vK, aK, st); h2d(voff, aoff, st); h2d(vr, ones, st); h2d(dqU, qU, st); h2d(dqV, qV, st);
+  h2d(dbo, bo, st);
+  LevelView lv{dms, vK, vr, voff, P};
+  const int total = aoff.back();
+  c.stats.secular_roots += total;
+  double k2 = 0.0;
+  for (int K : aK) k2 += (double)K * K;
+  stage_begin(HSS_ST_SECULAR, st);
+  launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
+                 (unsigned long long *)(status + 2), nullptr, st, true);
+  stage_end(HSS_ST_SECULAR, st, 40LL * total, 12.0 * 4.0 * k2);
+  stage_begin(HSS_ST_LOWNER, st);
+  launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true);
+  stage_end(HSS_ST_LOWNER, st, 40LL * total, 8.0 * k2);
+  double *Ub = buf<double>(c, "sv_Ub", totB), *Vb = buf<double>(c, "sv_Vb", totB);
+  stage_begin(HSS_ST_BUILD_S, st);
+  launch_svd_vectors(lv, total, L.w.dl, L.difl, L.difr, L.zhat, dbo, Ub, Vb, dnrm, L.lam, st);
+  stage_end(HSS_ST_BUILD_S, st, 16LL * totB, 20.0 * k2);
+  c.launches += 4;
+  double *U2 = buf<double>(c, "sv_U2", totU), *TU = buf<double>(c, "sv_TU", totU);
+  double *V2 = buf<double>(c, "sv_V2", totV), *TV = buf<double>(c, "sv_TV", totV);
+  stage_begin(HSS_ST_GATHER, st);
+  launch_gather(P, total, maxN, dms, dN, voff, L.w.ndslot, nullptr, dqU, U, ld, U2, st);
+  launch_gather(P, total, maxM, dms, dM, voff, L.w.ndslot, nullptr, dqV, V, ld, V2, st);
+  stage_end(HSS_ST_GATHER, st, 16LL * (totU + totV), 0.0);
+  std::vector<GemmDesc> probs;
+  int tiles = 0;
+  double fl = 0.0;
+  long long gb = 0;
+  for (int m = 0; m < P; ++m) {
+    const int K = aK[m], N = mN[m], M = mM[m];
+    probs.push_back(GemmDesc{U2 + qU[m], Ub + bo[m], TU + qU[m], N, K, N, N, K, K, 0, tiles});
+    tiles += gemm_tiles(N, K);
+    probs.push_back(GemmDesc{V2 + qV[m], Vb + bo[m], TV + qV[m], M, K, M, M, K, K, 0, tiles});
+    tiles += gemm_tiles(M, K);
+    fl += 2.0 * (double)(N + M) * K * K;
+    gb += 8LL * ((long long)(N + M) * K * 2 + 2LL * K * K);
+  }
+  stage_begin(HSS_ST_GEMM, st);
+  launch_gemm(probs, c.cfg.precision, st);
+  stage_end(HSS_ST_GEMM, st, gb, fl);
+  stage_begin(HSS_ST_SCATTER, st);
+  launch_scatter(P, total, maxN, dms, dN, voff, L.w.ndslot, dqU, TU, U, ld, st);
+  launch_scatter(P, total, maxM, dms, dM, voff, L.w.ndslot, dqV, TV, V, ld, st);
+  stage_end(HSS_ST_SCATTER, st, 16LL * (totU + totV), 0.0);
+  stage_begin(HSS_ST_FINISH, st);
+  launch_merge_finish(P, maxN, dms, dN, vK, L.lam, L.w, perm, Dp, st);
+  stage_end(HSS_ST_FINISH, st, 0, 0.0);
+  c.launches += 6;
+}
+
+// MDBDSDC('U', COMPQ) (SRC/mdbdsdc.f90:1) of the upper bidiagonal (d, e) in
+// HBM: singular values into w (descending), U (ldu) and VT (ldvt) when
+// vectors.  Tree as DLASDT: a node of N rows splits into nl = N/2 rows, the
+// center row, and nr = N - nl - 1 rows, down to leaves of at most smlsiz
+// rows; left children carry the center's column (sqre = 1).
+static int svd_core(Ctx &c, int n, const double *d, const double *e, double *Uo, long long ldu,
+                    double *VT, long long ldvt, double *w, bool vectors, cudaStream_t st) {
+  memset(&c.stats, 0, sizeof c.stats);
+  c.launches = 0;
+  cudaEvent_t ev0, ev1;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  CK(cudaEventRecord(ev0, st));
+  const int smlsiz = std::max(4, std::min(c.cfg.smlsiz, 32));
+  // levels of nodes, root first: (start, rows, sqre)
+  struct Node { int a, N, sq; };
+  std::vector<std::vector<Node>> lv(1, std::vector<Node>{Node{0, n, 0}});
+  while (true) {
+    int mx = 0;
+    for (auto &x : lv.back()) mx = std::max(mx, x.N);
+    if (mx <= smlsiz) break;
+    std::vector<Node> nx;
+    for (auto &x : lv.back()) {
+      const int nl = x.N / 2, nr = x.N - nl - 1;
+      nx.push_back(Node{x.a, nl, 1});
+      nx.push_back(Node{x.a + nl + 1, nr, x.sq});
+    }
+    lv.push_back(nx);
+  }
+  double *U = buf<double>(c, "sv_U", (size_t)n * n);
+  double *V = buf<double>(c, "sv_V", (size_t)n * n);
+  double *Dp = buf<double>(c, "Dp", n);
+  int *perm = buf<int>(c, "perm", n);
+  int *status = buf<int>(c, "status", 6);
+  CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  CK(cudaMemsetAsync(U, 0, sizeof(double) * (size_t)n * n, st));
+  CK(cudaMemsetAsync(V, 0, sizeof(double) * (size_t)n * n, st));
+  {
+    const std::vector<Node> &leaves = lv.back();
+    std::vector<int> ls, lz, lq;
+    int rmax = 1;
+    double flops = 0.0;
+    for (auto &x : leaves) {
+      ls.push_back(x.a); lz.push_back(x.N); lq.push_back(x.sq);
+      rmax = std::max(rmax, x.N);
+      flops += 40.0 * x.N * x.N * x.N;
+    }
+    const int nl = (int)ls.size();
+    int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl), *dlq = buf<int>(c, "leaf_q", nl);
+    h2d(dls, ls, st); h2d(dlz, lz, st); h2d(dlq, lq, st);
+    stage_begin(HSS_ST_LEAF, st);
+    launch_svd_leaf(nl, dls, dlz, dlq, rmax, d, e, U, n, V, n, Dp, perm, status, st);
+    stage_end(HSS_ST_LEAF, st, 16LL * n * smlsiz, flops);
+    c.launches++;
+  }
+  if (lv.size() > 1) {
+    LevelArrays L = level_arrays(c, n);
+    for (int k = (int)lv.size() - 2; k >= 0; --k) {  // merges bottom-up
+      std::vector<int> ms, mnl, mnr, msq;
+      for (auto &x : lv[k]) {
+        const int nl = x.N / 2;
+        ms.push_back(x.a); mnl.push_back(nl); mnr.push_back(x.N - nl - 1); msq.push_back(x.sq);
+      }
+      c.stats.n_levels++;
+      if (c.cfg.batched) {
+        run_svd_merges(c, ms, mnl, mnr, msq, d, e, U, V, n, Dp, perm, L, status, st);
+      } else {
+        for (size_t m = 0; m < ms.size(); ++m)
+          run_svd_merges(c, {ms[m]}, {mnl[m]}, {mnr[m]}, {msq[m]}, d, e, U, V, n, Dp, perm, L,
+                         status, st);
+      }
+    }
+  }
+  stage_begin(HSS_ST_FINAL, st);
+  launch_svd_outputs(n, perm, Dp, U, n, V, n, Uo, ldu, VT, ldvt, w, vectors, st);
+  stage_end(HSS_ST_FINAL, st, vectors ? 32LL * n * n : 16LL * n, 0.0);
+  c.launches += 2;
+  CK(cudaEventRecord(ev1, st));
+  int hst[6] = {0, 0, 0, 0, 0, 0};
+  CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  unsigned long long its;
+  memcpy(&its, hst + 2, sizeof its);
+  c.stats.secular_iters = (long long)its;
+  float ms_ = 0.f;
+  CK(cudaEventElapsedTime(&ms_, ev0, ev1));
+  c.stats.ms_total = ms_;
+  c.stats.kernel_launches = c.launches;
+  collect_stage_times(c);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  CK(cudaGetLastError());
+  if (hst[0] != 0) {
+    c.err = hst[0] == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
+                                          : "leaf SVD iteration did not converge";
+    return 1;
+  }
+  return 0;
+}
+
+// Host front end of MDBDSDC (SRC/mdbdsdc.f90): lower bidiagonal rotated to upper
+// (the DLARTG loop), scaling by max |d|, |e|, the device solve, the rotations
+// applied back to U (DLASR), the scale undone.  hd/he: host copies.
+static int svd_solve(Ctx &c, bool lower, int n, std::vector<double> hd, std::vector<double> he,
+                     double *dU, long long ldu, double *dVT, long long ldvt, double *dw,
+                     bool vectors, cudaStream_t st) {
+  he.resize(std::max(n, 1), 0.0);
+  std::vector<double> cs, sn;
+  if (lower) {
+    cs.resize(std::max(n - 1, 1)); sn.resize(std::max(n - 1, 1));
+    for (int i = 0; i + 1 < n; ++i) {
+      const double f = hd[i], g = he[i];
+      const double r = std::hypot(f, g);
+      const double cc = r == 0.0 ? 1.0 : f / r, ss = r == 0.0 ? 0.0 : g / r;
+      hd[i] = r;
+      he[i] = ss * hd[i + 1];
+      hd[i + 1] = cc * hd[i + 1];
+      cs[i] = cc;
+      sn[i] = -ss;
+    }
+  }
+  double nrm = 0.0;
+  for (int i = 0; i < n; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
+  for (int i = 0; i + 1 < n; ++i) nrm = std::max(nrm, std::fabs(he[i]));
+  const double scl = nrm > 0.0 ? nrm : 1.0;
+  for (int i = 0; i < n; ++i) hd[i] /= scl;
+  for (int i = 0; i + 1 < n; ++i) he[i] /= scl;
+  double *d = buf<double>(c, "svd_d", n), *e = buf<double>(c, "svd_e", std::max(n, 1));
+  CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e, he.data(), sizeof(double) * he.size(), cudaMemcpyHostToDevice, st));
+  const int info = svd_core(c, n, d, e, dU, ldu, dVT, ldvt, dw, vectors, st);
+  k_scale<<<(n + 255) / 256, 256, 0, st>>>(n, dw, scl);
+  if (lower && vectors) {
+    double *dcs = buf<double>(c, "svd_cs", cs.size()), *dsn = buf<double>(c, "svd_sn", sn.size());
+    h2d(dcs, cs, st); h2d(dsn, sn, st);
+    launch_rows_rotate_back(n, n, dcs, dsn, dU, ldu, st);
+  }
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  return info;
+}
+
 // Symmetric band eigensolve from device arrays: ab upper band storage
 // (ldab >= kd + 1).  kd <= 1 is a tridiagonal and goes through the
 // tridiagonal solver; 2 <= kd <= 32 through band_core.
@@ -954,6 +1222,85 @@ int hss_mdsbevd_dev(int n, int kd, const double *ab, int ldab, double *w, double
   } catch (CudaError &ex) {
     c.err = ex.msg;
     return 1000000;
+  }
+}
+
+int hss_mdbdsdc_dev(int n, double *d, double *e, double *u, int ldu, double *vt, int ldvt,
+                    void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  if (ldu < std::max(1, n)) return -5;
+  if (ldvt < std::max(1, n)) return -7;
+  if (n == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    std::vector<double> hd(n), he(std::max(n, 1), 0.0);
+    CK(cudaMemcpyAsync(hd.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (n > 1) CK(cudaMemcpyAsync(he.data(), e, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double *dw = buf<double>(c, "w_out", n);
+    const int info = svd_solve(c, false, n, hd, he, u, ldu, vt, ldvt, dw, true, st);
+    CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return info;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
+void mdbdsdc_(const char *uplo, const char *compq, const int *n_, double *d, double *e, double *u,
+              const int *ldu_, double *vt, const int *ldvt_, double *q, int *iq, double *work,
+              int *iwork, int *info, size_t, size_t) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  (void)q; (void)iq; (void)work; (void)iwork;
+  const int n = *n_, ldu = *ldu_, ldvt = *ldvt_;
+  const char cu = uplo[0], cq = compq[0];
+  const int iuplo = (cu == 'U' || cu == 'u') ? 1 : (cu == 'L' || cu == 'l') ? 2 : 0;
+  const int icompq = (cq == 'N' || cq == 'n') ? 0 : (cq == 'P' || cq == 'p') ? 1 : (cq == 'I' || cq == 'i') ? 2 : -1;
+  *info = 0;  // argument numbering as SRC/mdbdsdc.f90 (DBDSDC)
+  if (iuplo == 0) *info = -1;
+  else if (icompq < 0) *info = -2;
+  else if (n < 0) *info = -3;
+  else if (ldu < 1 || (icompq == 2 && ldu < n)) *info = -7;
+  else if (ldvt < 1 || (icompq == 2 && ldvt < n)) *info = -9;
+  if (*info == 0 && icompq == 1) {  // the compact form (DLASDA) is not built
+    *info = -2;
+    c.err = "MDBDSDC: COMPQ = 'P' (compact singular vectors) is not supported";
+    return;
+  }
+  if (*info != 0) {
+    c.err = "MDBDSDC: illegal argument " + std::to_string(-*info);
+    return;
+  }
+  if (n == 0) return;
+  if (n == 1) {  // mdbdsdc.f90: U = sign(d), VT = 1, d = |d|
+    if (icompq == 2) { u[0] = d[0] < 0.0 ? -1.0 : 1.0; vt[0] = 1.0; }
+    d[0] = std::fabs(d[0]);
+    return;
+  }
+  try {
+    cudaStream_t st = nullptr;
+    std::vector<double> hd(d, d + n), he(e, e + (n - 1));
+    const bool vec = icompq == 2;
+    double *dU = buf<double>(c, "z_out", vec ? (size_t)n * n : 1);
+    double *dVT = buf<double>(c, "vt_out", vec ? (size_t)n * n : 1);
+    double *dw = buf<double>(c, "w_out", n);
+    *info = svd_solve(c, iuplo == 2, n, hd, he, dU, n, dVT, n, dw, vec, st);
+    if (vec) {
+      CK(cudaMemcpy2DAsync(u, sizeof(double) * ldu, dU, sizeof(double) * n, sizeof(double) * n, n,
+                           cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpy2DAsync(vt, sizeof(double) * ldvt, dVT, sizeof(double) * n, sizeof(double) * n,
+                           n, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int i = 0; i + 1 < n; ++i) e[i] = 0.0;  // E is destroyed, as in the reference
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
   }
 }
 

@@ -48,17 +48,24 @@ __device__ __forceinline__ ArgMax warp_argmax(ArgMax a) {
 // DIFL/DIFR so that no cancellation occurs near the poles
 // (SRC/CauchyHssEig.f90:470-568, computfd / computdd).
 //   fd(p, q) = F_p - lam_q ;  dd(p, q) = lam_p - lam_q
+// Singular-value mode (sq = true, the SVD merge of MDLASD3/MDLASD8): F holds
+// the poles d, lam = sigma with DIFL/DIFR = sigma - d, and the differences are
+// of squares, d_p^2 - sigma_q^2 = (d_p - sigma_q)(d_p + sigma_q), each factor
+// formed without cancellation (as DLASD8 does).
 struct PoleDiff {
   const double *__restrict__ F;
   const double *__restrict__ difl;
   const double *__restrict__ difr;
+  bool sq = false;
   __device__ __forceinline__ double fd(int p, int q) const {
-    return p <= q ? (__ldg(F + p) - __ldg(F + q)) - __ldg(difl + q)
-                  : (__ldg(F + p) - __ldg(F + q + 1)) - __ldg(difr + q);
+    const double lin = p <= q ? (__ldg(F + p) - __ldg(F + q)) - __ldg(difl + q)
+                              : (__ldg(F + p) - __ldg(F + q + 1)) - __ldg(difr + q);
+    return sq ? lin * (__ldg(F + p) + (__ldg(F + q) + __ldg(difl + q))) : lin;
   }
   __device__ __forceinline__ double dd(int p, int q) const {
-    return p < q ? (__ldg(F + p + 1) - __ldg(F + q)) + __ldg(difr + p) - __ldg(difl + q)
-                 : (__ldg(F + p) - __ldg(F + q + 1)) + __ldg(difl + p) - __ldg(difr + q);
+    const double lin = p < q ? (__ldg(F + p + 1) - __ldg(F + q)) + __ldg(difr + p) - __ldg(difl + q)
+                             : (__ldg(F + p) - __ldg(F + q + 1)) + __ldg(difl + p) - __ldg(difr + q);
+    return sq ? lin * ((__ldg(F + p) + __ldg(difl + p)) + (__ldg(F + q) + __ldg(difl + q))) : lin;
   }
 };
 

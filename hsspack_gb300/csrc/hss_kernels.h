@@ -36,13 +36,17 @@ struct LevelScratch {
 };
 
 // secular.cu
+// sq: singular-value mode (poles d_i^2, outputs sigma and DIFL/DIFR = sigma - d)
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
-                    unsigned long long *itsum, const float *guess, cudaStream_t st);
+                    unsigned long long *itsum, const float *guess, cudaStream_t st,
+                    bool sq = false);
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
-                   const double *difr, const double *zw, double *zhat, cudaStream_t st);
+                   const double *difr, const double *zw, double *zhat, cudaStream_t st,
+                   bool sq = false);
 void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
-                  const double *difr, const double *zhat, double *alpha, cudaStream_t st);
+                  const double *difr, const double *zhat, double *alpha, cudaStream_t st,
+                  bool sq = false);
 void launch_build_S(const LevelView &lv, int total, const double *dl, const double *difl,
                     const double *difr, const double *zhat, const int *grp,
                     const long long *soff, double *Sws, cudaStream_t st);
@@ -121,6 +125,25 @@ void launch_band_zupdate(const LevelView &lv, int total, const double *dl, const
                          const double *difr, const double *zhat, const double *alpha,
                          const int *ndslot, double *Z, int nrest, long long zld, double *Zt,
                          cudaStream_t st);
+
+// svd.cu: bidiagonal SVD divide and conquer
+void launch_svd_leaf(int nleaf, const int *lstart, const int *lsize, const int *lsqre, int rmax,
+                     const double *d, const double *e, double *U, long long ldu, double *V,
+                     long long ldv, double *Dp, int *perm, int *status, cudaStream_t st);
+void launch_svd_prepare(int P, int maxn, const int *ms, const int *mnl, const int *mnr,
+                        const int *msq, const double *d, const double *e, double *U,
+                        long long ldu, double *V, long long ldv, const double *Dp, const int *perm,
+                        const LevelScratch &w, int *out, double *onrm, cudaStream_t st);
+// U / V blocks (K x K per merge at boff) and sigma rescaled by onrm
+void launch_svd_vectors(const LevelView &lv, int total, const double *dl, const double *difl,
+                        const double *difr, const double *zhat, const long long *boff, double *Ub,
+                        double *Vb, const double *onrm, double *lam, cudaStream_t st);
+// outputs in descending order: Uo (ldu), VT (ldvt), w; only w if !vectors
+void launch_svd_outputs(int n, const int *perm, const double *Dp, const double *Uq,
+                        long long ldq, const double *V, long long ldv, double *Uo, long long ldu,
+                        double *VT, long long ldvt, double *w, bool vectors, cudaStream_t st);
+void launch_rows_rotate_back(int n, int ncols, const double *cs, const double *sn, double *A,
+                             long long lda, cudaStream_t st);
 
 // driver.cu: set the message hss_last_error() returns
 void set_last_error(const std::string &msg);

@@ -33,18 +33,22 @@ __device__ __forceinline__ double group_sum(double v) {
   return v;
 }
 
-// Sums over i of z_i^2/(d_i - x) split at jl (psi: i <= jl, phi: i > jl),
-// their derivatives, and sum |z_i^2/(d_i - x)| for the rounding-error bound.
-// x = o + tau; every gap is formed as (d_i - o) - tau.  Lane gl of the group
-// takes terms gl, gl + L, ...
-template <int L>
+// Sums over i of z_i^2/(p_i - x) split at jl (psi: i <= jl, phi: i > jl),
+// their derivatives, and sum |z_i^2/(p_i - x)| for the rounding-error bound.
+// x = p_oi + tau; every gap is formed as (p_i - p_oi) - tau.  Poles p_i = d_i,
+// or p_i = d_i^2 in singular-value mode (SQ, DLASD4's equation
+// 1 + sum z_i^2 / (d_i^2 - sigma^2) = 0) with p_i - p_oi = (d_i - d_oi)(d_i + d_oi).
+// Lane gl of the group takes terms gl, gl + L, ...
+template <int L, bool SQ>
 __device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
-                                            const double *__restrict__ z, int K, double o,
+                                            const double *__restrict__ z, int K, int oi,
                                             double tau, int jl, int gl) {
   double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0, e = 0.0;
+  const double o = K > 0 ? __ldg(d + oi) : 0.0;
   for (int i = gl; i < K; i += L) {
     const double zi = __ldg(z + i);
-    const double del = (__ldg(d + i) - o) - tau;
+    const double di = __ldg(d + i);
+    const double del = (SQ ? (di - o) * (di + o) : (di - o)) - tau;
     const double t = zi / del;
     const double v = zi * t;
     const double dv = t * t;
@@ -93,8 +97,9 @@ __device__ __forceinline__ bool two_pole_root(double c, double A, double B, doub
 // finished groups keep taking part in the (harmless) shuffles.
 struct RootState {
   const double *d, *z;
-  int K, j, jl, jr;
-  double rho, rhoinv, o, tau, lo, hi, delta, top;
+  int K, j, jl, jr, oi;  // oi: index of the origin pole
+  bool sq;               // singular-value mode: poles d_i^2
+  double rho, rhoinv, tau, lo, hi, delta, top;
   int phase;  // 0: first evaluation (midpoint), 1: iterating, 2: done
   int iters, status;
   bool last;
@@ -103,6 +108,13 @@ struct RootState {
 };
 
 __device__ __forceinline__ double pole(const RootState &r, int i) { return __ldg(r.d + i); }
+// p_i - p_k, exactly as the pole sums form it
+__device__ __forceinline__ double pdiff(const RootState &r, int i, int k) {
+  const double a = pole(r, i), b = pole(r, k);
+  return r.sq ? (a - b) * (a + b) : a - b;
+}
+// p_i - origin
+__device__ __forceinline__ double gap(const RootState &r, int i) { return pdiff(r, i, r.oi); }
 
 // First evaluation point: the midpoint of the pole interval (standard guess),
 // or the learned position (phase 1 directly).
@@ -113,24 +125,24 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq)
   r.last = (r.j == r.K - 1);
   r.jl = r.last ? r.K - 2 : r.j;
   r.jr = r.jl + 1;
-  r.delta = r.last ? 0.0 : pole(r, r.j + 1) - pole(r, r.j);
+  r.delta = r.last ? 0.0 : pdiff(r, r.j + 1, r.j);
   r.top = r.rho * zsq;
   r.phase = 0;
   r.learned = false;
   r.fell_back = false;
   if (!r.last) {
-    r.o = pole(r, r.j);
+    r.oi = r.j;
     r.tau = 0.5 * r.delta;
     if (guess != 0.0f && fabsf(guess) <= 0.5f) {  // learned signed distance to the nearer pole
       // the midpoint pass already fixed the half interval (one evaluation)
-      if (guess > 0.0f) { r.o = pole(r, r.j); r.tau = (double)guess * r.delta; r.lo = 0.0; r.hi = 0.5 * r.delta; }
-      else { r.o = pole(r, r.j + 1); r.tau = (double)guess * r.delta; r.lo = -0.5 * r.delta; r.hi = 0.0; }
+      if (guess > 0.0f) { r.oi = r.j; r.tau = (double)guess * r.delta; r.lo = 0.0; r.hi = 0.5 * r.delta; }
+      else { r.oi = r.j + 1; r.tau = (double)guess * r.delta; r.lo = -0.5 * r.delta; r.hi = 0.0; }
       r.phase = 1;
       r.learned = true;
       r.iters = 1;
     }
   } else {
-    r.o = pole(r, r.K - 1);
+    r.oi = r.K - 1;
     r.tau = 0.5 * r.top;
   }
 }
@@ -143,7 +155,7 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   const double w = r.rhoinv + s.psi + s.phi;
   if (r.phase == 0) {
     // two-pole model with the far poles frozen at the midpoint value
-    const double gl = (pole(r, r.jl) - r.o) - r.tau, gr = (pole(r, r.jr) - r.o) - r.tau;
+    const double gl = gap(r, r.jl) - r.tau, gr = gap(r, r.jr) - r.tau;
     const double c = w - zl * (zl / gl) - zr * (zr / gr);
     double t;
     if (!r.last) {
@@ -152,13 +164,13 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
         r.lo = 0.0; r.hi = tm;
         if (!two_pole_root(c, zl * zl, zr * zr, 0.0, r.delta, r.lo, r.hi, t)) t = 0.5 * tm;
       } else {         // root in (midpoint, d_{j+1}): measure from d_{j+1}
-        r.o = pole(r, r.j + 1);
+        r.oi = r.j + 1;
         r.lo = tm - r.delta; r.hi = 0.0;
         if (!two_pole_root(c, zl * zl, zr * zr, -r.delta, 0.0, r.lo, r.hi, t)) t = 0.5 * r.lo;
       }
     } else {
       const double tm = r.tau;
-      const double da = pole(r, r.jl) - r.o;
+      const double da = gap(r, r.jl);
       if (w >= 0.0) { r.lo = 0.0; r.hi = tm; }
       else { r.lo = tm; r.hi = r.top * (1.0 + 4.0 * HSS_EPS); }
       if (!two_pole_root(c, zl * zl, zr * zr, da, 0.0, r.lo, r.hi, t)) t = 0.5 * (r.lo + r.hi);
@@ -185,14 +197,14 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
     if (!(fabs(w / dw) <= 0.45 * r.delta)) {
       r.fell_back = true;
       r.phase = 0;
-      r.o = pole(r, r.j);
+      r.oi = r.j;
       r.tau = 0.5 * r.delta;
       return;
     }
   }
   if (w < 0.0) r.lo = fmax(r.lo, r.tau); else r.hi = fmin(r.hi, r.tau);
-  const double gl = (pole(r, r.jl) - r.o) - r.tau;
-  const double gr = (pole(r, r.jr) - r.o) - r.tau;
+  const double gl = gap(r, r.jl) - r.tau;
+  const double gr = gap(r, r.jr) - r.tau;
   const double a = (gl + gr) * w - gl * gr * dw;
   const double b = gl * gr * w;
   const double c = w - gl * s.dpsi - gr * s.dphi;
@@ -210,10 +222,10 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   const double step = tn - r.tau;
   r.tau = tn;
   if (!r.last) {  // keep the origin at the pole nearer the iterate
-    if (r.o == pole(r, r.j) && r.tau > 0.5 * r.delta) {
-      r.o = pole(r, r.j + 1); r.tau -= r.delta; r.lo -= r.delta; r.hi -= r.delta;
-    } else if (r.o == pole(r, r.j + 1) && r.tau < -0.5 * r.delta) {
-      r.o = pole(r, r.j); r.tau += r.delta; r.lo += r.delta; r.hi += r.delta;
+    if (r.oi == r.j && r.tau > 0.5 * r.delta) {
+      r.oi = r.j + 1; r.tau -= r.delta; r.lo -= r.delta; r.hi -= r.delta;
+    } else if (r.oi == r.j + 1 && r.tau < -0.5 * r.delta) {
+      r.oi = r.j; r.tau += r.delta; r.lo += r.delta; r.hi += r.delta;
     }
   }
   if (fabs(step) <= 2.0 * HSS_EPS * fabs(r.tau) || r.hi - r.lo <= 2.0 * HSS_EPS * fabs(r.tau))
@@ -225,7 +237,7 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
 
 // One root per group of L lanes (L = 1..32 chosen from the level's largest
 // K so that each lane sums ~8 pole terms and the group reductions stay cheap).
-template <int L>
+template <int L, bool SQ>
 __global__ void __launch_bounds__(256)
 k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
           double *__restrict__ lam, double *__restrict__ difl, double *__restrict__ difr,
@@ -248,6 +260,8 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
   }
   st.d = dl + s;
   st.z = zw + s;
+  st.sq = SQ;
+  st.oi = 0;
   double zsq = 0.0;
   for (int i = gl; i < st.K; i += L) zsq += __ldg(st.z + i) * __ldg(st.z + i);
   zsq = group_sum<L>(zsq);
@@ -255,19 +269,34 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
   if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq);
   else st.phase = 2;
   while (__any_sync(HSS_FULL, st.phase != 2)) {
-    const SecSums sm = sec_eval<L>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.o, st.tau, st.jl, gl);
+    const SecSums sm = sec_eval<L, SQ>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.oi, st.tau, st.jl,
+                                       gl);
     root_step(st, sm);
   }
   if (valid && gl == 0) {
     double lm, dfl, dfr;
     if (st.K == 1) {
       const double zz = __ldg(st.z) * __ldg(st.z);
-      lm = __ldg(st.d) + st.rho * zz; dfl = st.rho * zz; dfr = 0.0;
+      const double d0 = __ldg(st.d);
+      if (SQ) {  // sigma^2 = d_0^2 + rho z^2
+        lm = d0 + st.rho * zz / (d0 + sqrt(d0 * d0 + st.rho * zz));
+        dfl = lm - d0;
+      } else {
+        lm = d0 + st.rho * zz; dfl = st.rho * zz;
+      }
+      dfr = 0.0;
       st.iters = 0; st.status = HSS_OK;
+    } else if (SQ) {
+      // sigma = sqrt(d_o^2 + tau) = d_o + tau / (d_o + sigma); DIFL / DIFR as
+      // sigma - d from (sigma^2 - d^2) / (sigma + d)
+      const double o = pole(st, st.oi);
+      lm = o + st.tau / (o + sqrt(o * o + st.tau));
+      dfl = (st.tau - gap(st, st.j)) / (lm + pole(st, st.j));
+      dfr = st.last ? 0.0 : (st.tau - gap(st, st.j + 1)) / (lm + pole(st, st.j + 1));
     } else {
-      lm = st.o + st.tau;
-      dfl = -((pole(st, st.j) - st.o) - st.tau);
-      dfr = st.last ? 0.0 : -((pole(st, st.j + 1) - st.o) - st.tau);
+      lm = pole(st, st.oi) + st.tau;
+      dfl = -(gap(st, st.j) - st.tau);
+      dfr = st.last ? 0.0 : -(gap(st, st.j + 1) - st.tau);
     }
     lam[s + st.j] = lm;
     difl[s + st.j] = dfl;
@@ -285,9 +314,12 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
 // (SRC/mdlaed3.f90:217-230).  Numerators and denominators are multiplied
 // separately and renormalised by their binary exponents every 8 factors, so
 // there is one multiply per factor and no division in the O(K^2) loop.
+//   Singular-value mode (sq): z_hat_i^2 = prod_j (sigma_j^2 - d_i^2) /
+// prod_{j != i} (d_j^2 - d_i^2) (the z recomputation of DLASD3 / MDLASD8), every
+// factor formed as a product of a difference and a sum.
 __global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
                          const double *__restrict__ difl, const double *__restrict__ difr,
-                         const double *__restrict__ zw, double *__restrict__ zhat) {
+                         const double *__restrict__ zw, double *__restrict__ zhat, bool sq) {
   const int lane = threadIdx.x & 31;
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= __ldg(lv.rootoff + lv.P)) return;
@@ -295,13 +327,16 @@ __global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
   const int i = r - __ldg(lv.rootoff + m);
   const int s = __ldg(lv.s + m);
   const int K = __ldg(lv.K + m);
-  PoleDiff P{dl + s, difl + s, difr + s};
+  PoleDiff P{dl + s, difl + s, difr + s, sq};
   const double di = __ldg(dl + s + i);
   double num = 1.0, den = 1.0;
   int en = 0, ed = 0, cnt = 0;
   for (int j = lane; j < K; j += HSS_WARP) {
     num *= P.fd(i, j);
-    if (j != i) den *= (di - __ldg(dl + s + j));
+    if (j != i) {
+      const double dj = __ldg(dl + s + j);
+      den *= sq ? (di - dj) * (di + dj) : (di - dj);
+    }
     if (++cnt == 8) {
       int e;
       num = frexp(num, &e); en += e;
@@ -333,7 +368,7 @@ __global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
 // alpha_j = 1 / || (z_hat_i / (d_i - lam_j))_i ||_2  (SRC/mdlaed3.f90:233-249).
 __global__ void k_alpha(LevelView lv, const double *__restrict__ dl,
                         const double *__restrict__ difl, const double *__restrict__ difr,
-                        const double *__restrict__ zhat, double *__restrict__ alpha) {
+                        const double *__restrict__ zhat, double *__restrict__ alpha, bool sq) {
   const int lane = threadIdx.x & 31;
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= __ldg(lv.rootoff + lv.P)) return;
@@ -341,7 +376,7 @@ __global__ void k_alpha(LevelView lv, const double *__restrict__ dl,
   const int j = r - __ldg(lv.rootoff + m);
   const int s = __ldg(lv.s + m);
   const int K = __ldg(lv.K + m);
-  PoleDiff P{dl + s, difl + s, difr + s};
+  PoleDiff P{dl + s, difl + s, difr + s, sq};
   double acc = 0.0;
   for (int i = lane; i < K; i += HSS_WARP) {
     const double w = __ldg(zhat + s + i) / P.fd(i, j);
@@ -462,7 +497,7 @@ k_secular_mid(LevelView lv, const double *__restrict__ dl, const double *__restr
     delta = __ldg(d + j + 1) - o;
     tm = 0.5 * delta;
   }
-  const SecSums sm = sec_eval<L>(d, z, active ? K : 0, o, tm, j, gl);
+  const SecSums sm = sec_eval<L, false>(d, z, active ? K : 0, j, tm, j, gl);
   if (r >= total || gl != 0) return;
   float *f = feat + (long long)(s + j) * NFP;
   if (!active) { f[NFP - 1] = -1.f; return; }
@@ -497,18 +532,19 @@ static inline int warp_grid(int total, int threads) {
 }
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
-                    unsigned long long *itsum, const float *guess, cudaStream_t st) {
+                    unsigned long long *itsum, const float *guess, cudaStream_t st, bool sq) {
   if (total <= 0) return;
   int L = 1;
   while (L < 32 && L * 8 < maxk) L *= 2;  // ~8 pole terms per lane
   const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
-  switch (L) {
-#define SEC_CASE(LL)                                                                         \
-  case LL:                                                                                   \
-    k_secular<LL><<<grid, 256, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status, itsum, \
-                                        guess);                                              \
+  switch (L * 2 + (sq ? 1 : 0)) {
+#define SEC_CASE(LL, SQ)                                                                     \
+  case LL * 2 + SQ:                                                                          \
+    k_secular<LL, SQ><<<grid, 256, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,    \
+                                            itsum, guess);                                   \
     break;
-    SEC_CASE(1) SEC_CASE(2) SEC_CASE(4) SEC_CASE(8) SEC_CASE(16) SEC_CASE(32)
+    SEC_CASE(1, 0) SEC_CASE(2, 0) SEC_CASE(4, 0) SEC_CASE(8, 0) SEC_CASE(16, 0) SEC_CASE(32, 0)
+    SEC_CASE(1, 1) SEC_CASE(2, 1) SEC_CASE(4, 1) SEC_CASE(8, 1) SEC_CASE(16, 1) SEC_CASE(32, 1)
 #undef SEC_CASE
   }
 }
@@ -527,14 +563,15 @@ void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *
 }
 
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
-                   const double *difr, const double *zw, double *zhat, cudaStream_t st) {
+                   const double *difr, const double *zw, double *zhat, cudaStream_t st, bool sq) {
   if (total <= 0) return;
-  k_lowner<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zw, zhat);
+  k_lowner<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zw, zhat, sq);
 }
 void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
-                  const double *difr, const double *zhat, double *alpha, cudaStream_t st) {
+                  const double *difr, const double *zhat, double *alpha, cudaStream_t st,
+                  bool sq) {
   if (total <= 0) return;
-  k_alpha<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, alpha);
+  k_alpha<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, alpha, sq);
 }
 void launch_build_S(const LevelView &lv, int total, const double *dl, const double *difl,
                     const double *difr, const double *zhat, const int *grp,

@@ -76,6 +76,17 @@ void mdstedc_(const char *compz, const int *n, double *d, double *e, double *z,
               const int *ldz, double *work, const int *lwork, int *iwork,
               const int *liwork, int *info, size_t compz_len);
 
+/* MDBDSDC(UPLO,COMPQ,N,D,E,U,LDU,VT,LDVT,Q,IQ,WORK,IWORK,INFO) replaces
+ * SRC/mdbdsdc.f90:1: SVD of the N x N upper (UPLO = 'U') or lower ('L')
+ * bidiagonal (D, E); D returns the singular values in decreasing order, U and
+ * VT the singular vectors (COMPQ = 'I') or nothing (COMPQ = 'N').  COMPQ = 'P'
+ * (compact form) returns INFO = -2.  Argument numbering as the reference
+ * (-1, -2, -3, -7, -9); WORK, IWORK, Q, IQ are not touched (the workspace is
+ * in device memory); E is destroyed. */
+void mdbdsdc_(const char *uplo, const char *compq, const int *n, double *d, double *e,
+              double *u, const int *ldu, double *vt, const int *ldvt, double *q, int *iq,
+              double *work, int *iwork, int *info, size_t uplo_len, size_t compq_len);
+
 /* Largest band half-width of the banded divide and conquer (leaves of up to
  * 2 kd rows are solved by one warp each). */
 #define HSS_BAND_KD_MAX 32
@@ -111,6 +122,13 @@ void cauchylike_(double *A, const double *D, const double *F, const double *u,
  * d(n) in: diagonal, out: eigenvalues ascending; e(n-1) off-diagonal
  * (destroyed); z(ldz, n) out: eigenvectors.  stream may be NULL. */
 int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *stream);
+
+/* SVD of the upper bidiagonal (d, e) in HBM (the MDBDSDC path, COMPQ = 'I'):
+ * d(n) in: diagonal, out: singular values descending; e(n-1) superdiagonal;
+ * u(ldu, n), vt(ldvt, n) out.  Returns 0, -i for a bad i-th argument, > 0 on
+ * failure. */
+int hss_mdbdsdc_dev(int n, double *d, double *e, double *u, int ldu, double *vt, int ldvt,
+                    void *stream);
 
 /* Symmetric band eigensolve in HBM (the MDSBEVD path): ab(ldab, n) upper band
  * storage, 0 <= kd <= HSS_BAND_KD_MAX; w(n) eigenvalues ascending, z(ldz, n)
