@@ -830,8 +830,6 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
   CK(cudaStreamSynchronize(st));
   std::vector<int> aK(P), aoff(P + 1, 0), gs, gN, gM, gng;
   std::vector<double> ones(P, 1.0);
-  std::vector<long long> qU(P), qV(P), bo(P);
-  long long totU = 0, totV = 0, totB = 0;
   int maxK = 1, maxNg = 0, maxMg = 0;
   for (int m = 0; m < P; ++m) {
     const int K = hout[5 * m], ng = hout[5 * m + 1];
@@ -842,9 +840,6 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
     c.stats.n_dense_merges++;
     c.stats.total_k += K;
     c.stats.max_k = std::max(c.stats.max_k, K);
-    qU[m] = totU; totU += (long long)mN[m] * K;
-    qV[m] = totV; totV += (long long)mM[m] * K;
-    bo[m] = totB; totB += (long long)K * K;
     if (ng > 0) {
       gs.push_back(ms[m]); gN.push_back(mN[m]); gM.push_back(mM[m]); gng.push_back(ng);
       maxNg = std::max(maxNg, mN[m]); maxMg = std::max(maxMg, mM[m]);
@@ -863,10 +858,7 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
   }
   int *vK = buf<int>(c, "sv_K", P), *voff = buf<int>(c, "sv_off", P + 1);
   double *vr = buf<double>(c, "sv_rho", P);
-  long long *dqU = buf<long long>(c, "sv_qU", P), *dqV = buf<long long>(c, "sv_qV", P),
-            *dbo = buf<long long>(c, "sv_bo", P);
-  h2d(vK, aK, st); h2d(voff, aoff, st); h2d(vr, ones, st); h2d(dqU, qU, st); h2d(dqV, qV, st);
-  h2d(dbo, bo, st);
+  h2d(vK, aK, st); h2d(voff, aoff, st); h2d(vr, ones, st);
   LevelView lv{dms, vK, vr, voff, P};
   const int total = aoff.back();
   c.stats.secular_roots += total;
@@ -879,41 +871,85 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
   stage_begin(HSS_ST_LOWNER, st);
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true);
   stage_end(HSS_ST_LOWNER, st, 40LL * total, 8.0 * k2);
-  double *Ub = buf<double>(c, "sv_Ub", totB), *Vb = buf<double>(c, "sv_Vb", totB);
-  stage_begin(HSS_ST_BUILD_S, st);
-  launch_svd_vectors(lv, total, L.w.dl, L.difl, L.difr, L.zhat, dbo, Ub, Vb, dnrm, L.lam, st);
-  stage_end(HSS_ST_BUILD_S, st, 16LL * totB, 20.0 * k2);
-  c.launches += 4;
-  double *U2 = buf<double>(c, "sv_U2", totU), *TU = buf<double>(c, "sv_TU", totU);
-  double *V2 = buf<double>(c, "sv_V2", totV), *TV = buf<double>(c, "sv_TV", totV);
-  stage_begin(HSS_ST_GATHER, st);
-  launch_gather(P, total, maxN, dms, dN, voff, L.w.ndslot, nullptr, dqU, U, ld, U2, st);
-  launch_gather(P, total, maxM, dms, dM, voff, L.w.ndslot, nullptr, dqV, V, ld, V2, st);
-  stage_end(HSS_ST_GATHER, st, 16LL * (totU + totV), 0.0);
-  std::vector<GemmDesc> probs;
-  int tiles = 0;
-  double fl = 0.0;
-  long long gb = 0;
+  c.launches += 2;
+  // ---- dense merges (K < bsmlz): K x K U / V blocks, batched GEMMs
+  std::vector<int> ds_, dN_, dM_, dK_, doff_(1, 0);
+  std::vector<long long> qU, qV, bo;
+  long long totU = 0, totV = 0, totB = 0;
+  int maxNd = 1, maxMd = 1;
+  std::vector<int> hsel;
   for (int m = 0; m < P; ++m) {
-    const int K = aK[m], N = mN[m], M = mM[m];
-    probs.push_back(GemmDesc{U2 + qU[m], Ub + bo[m], TU + qU[m], N, K, N, N, K, K, 0, tiles});
-    tiles += gemm_tiles(N, K);
-    probs.push_back(GemmDesc{V2 + qV[m], Vb + bo[m], TV + qV[m], M, K, M, M, K, K, 0, tiles});
-    tiles += gemm_tiles(M, K);
-    fl += 2.0 * (double)(N + M) * K * K;
-    gb += 8LL * ((long long)(N + M) * K * 2 + 2LL * K * K);
+    const int K = aK[m];
+    if (K >= c.cfg.bsmlz) { hsel.push_back(m); continue; }
+    ds_.push_back(ms[m]); dN_.push_back(mN[m]); dM_.push_back(mM[m]); dK_.push_back(K);
+    doff_.push_back(doff_.back() + K);
+    qU.push_back(totU); totU += (long long)mN[m] * K;
+    qV.push_back(totV); totV += (long long)mM[m] * K;
+    bo.push_back(totB); totB += (long long)K * K;
+    maxNd = std::max(maxNd, mN[m]); maxMd = std::max(maxMd, mM[m]);
   }
-  stage_begin(HSS_ST_GEMM, st);
-  launch_gemm(probs, c.cfg.precision, st);
-  stage_end(HSS_ST_GEMM, st, gb, fl);
-  stage_begin(HSS_ST_SCATTER, st);
-  launch_scatter(P, total, maxN, dms, dN, voff, L.w.ndslot, dqU, TU, U, ld, st);
-  launch_scatter(P, total, maxM, dms, dM, voff, L.w.ndslot, dqV, TV, V, ld, st);
-  stage_end(HSS_ST_SCATTER, st, 16LL * (totU + totV), 0.0);
+  const int PD = (int)ds_.size();
+  if (PD > 0) {
+    int *xs = buf<int>(c, "svd_s", PD), *xN = buf<int>(c, "svd_N", PD), *xM = buf<int>(c, "svd_M", PD),
+        *xK = buf<int>(c, "svd_K", PD), *xoff = buf<int>(c, "svd_off", PD + 1);
+    long long *dqU = buf<long long>(c, "sv_qU", PD), *dqV = buf<long long>(c, "sv_qV", PD),
+              *dbo = buf<long long>(c, "sv_bo", PD);
+    h2d(xs, ds_, st); h2d(xN, dN_, st); h2d(xM, dM_, st); h2d(xK, dK_, st); h2d(xoff, doff_, st);
+    h2d(dqU, qU, st); h2d(dqV, qV, st); h2d(dbo, bo, st);
+    LevelView dv{xs, xK, vr, xoff, PD};
+    const int dtot = doff_.back();
+    double *Ub = buf<double>(c, "sv_Ub", totB), *Vb = buf<double>(c, "sv_Vb", totB);
+    stage_begin(HSS_ST_BUILD_S, st);
+    launch_svd_vectors(dv, dtot, L.w.dl, L.difl, L.difr, L.zhat, dbo, Ub, Vb, st);
+    stage_end(HSS_ST_BUILD_S, st, 16LL * totB, 20.0 * k2);
+    double *U2 = buf<double>(c, "sv_U2", totU), *TU = buf<double>(c, "sv_TU", totU);
+    double *V2 = buf<double>(c, "sv_V2", totV), *TV = buf<double>(c, "sv_TV", totV);
+    stage_begin(HSS_ST_GATHER, st);
+    launch_gather(PD, dtot, maxNd, xs, xN, xoff, L.w.ndslot, nullptr, dqU, U, ld, U2, st);
+    launch_gather(PD, dtot, maxMd, xs, xM, xoff, L.w.ndslot, nullptr, dqV, V, ld, V2, st);
+    stage_end(HSS_ST_GATHER, st, 16LL * (totU + totV), 0.0);
+    std::vector<GemmDesc> probs;
+    int tiles = 0;
+    double fl = 0.0;
+    long long gb = 0;
+    for (int m = 0; m < PD; ++m) {
+      const int K = dK_[m], N = dN_[m], M = dM_[m];
+      probs.push_back(GemmDesc{U2 + qU[m], Ub + bo[m], TU + qU[m], N, K, N, N, K, K, 0, tiles});
+      tiles += gemm_tiles(N, K);
+      probs.push_back(GemmDesc{V2 + qV[m], Vb + bo[m], TV + qV[m], M, K, M, M, K, K, 0, tiles});
+      tiles += gemm_tiles(M, K);
+      fl += 2.0 * (double)(N + M) * K * K;
+      gb += 8LL * ((long long)(N + M) * K * 2 + 2LL * K * K);
+    }
+    stage_begin(HSS_ST_GEMM, st);
+    launch_gemm(probs, c.cfg.precision, st);
+    stage_end(HSS_ST_GEMM, st, gb, fl);
+    stage_begin(HSS_ST_SCATTER, st);
+    launch_scatter(PD, dtot, maxNd, xs, xN, xoff, L.w.ndslot, dqU, TU, U, ld, st);
+    launch_scatter(PD, dtot, maxMd, xs, xM, xoff, L.w.ndslot, dqV, TV, V, ld, st);
+    stage_end(HSS_ST_SCATTER, st, 16LL * (totU + totV), 0.0);
+    c.launches += 6;
+  }
+  // ---- HSS merges (K >= bsmlz): two HSS products each (DHSSVCS)
+  for (int m : hsel) {
+    SvdHssArgs h;
+    h.s = ms[m]; h.N = mN[m]; h.M = mM[m]; h.K = aK[m];
+    h.leaf = c.cfg.hss_leaf; h.tol = c.cfg.tol; h.precision = c.cfg.precision;
+    h.dl = L.w.dl + h.s; h.difl = L.difl + h.s; h.difr = L.difr + h.s; h.zhat = L.zhat + h.s;
+    h.ndslot = L.w.ndslot + h.s;
+    h.U = U; h.V = V; h.ld = ld;
+    int rank = 0;
+    c.launches += svd_hss_merge(h, &rank, st);
+    c.stats.n_hss_merges++;
+    c.stats.n_dense_merges--;
+    c.stats.max_rank = std::max(c.stats.max_rank, rank);
+  }
+  // ---- sigma back to scale, new ascending order
   stage_begin(HSS_ST_FINISH, st);
+  launch_svd_unscale(lv, total, dnrm, L.lam, st);
   launch_merge_finish(P, maxN, dms, dN, vK, L.lam, L.w, perm, Dp, st);
   stage_end(HSS_ST_FINISH, st, 0, 0.0);
-  c.launches += 6;
+  c.launches += 2;
 }
 
 // MDBDSDC('U', COMPQ) (SRC/mdbdsdc.f90:1) of the upper bidiagonal (d, e) in

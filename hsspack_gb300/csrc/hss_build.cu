@@ -121,6 +121,7 @@ __device__ __forceinline__ double warp_prod(double v) {
 // Node state shared by the row and column kernels.
 struct HssDev {
   const double *FF, *DIFL, *DIFR;  // poles and root gaps (length K)
+  bool sq;                         // singular-value mode (differences of squares)
   int K, ltr, rmax;
   // current compressed generators (row side: U, PL; column side: V, PU)
   double *U, *V;
@@ -156,7 +157,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
     return ROW ? P.fd(pl, pu) : -P.fd(pu, pl);
   };
   auto rowdiff = [&](int i, int j) -> double {  // row pole i minus row pole j
-    return ROW ? (F[i] - F[j]) : P.dd(PL[i], PL[j]);
+    return ROW ? P.fv(F[i], F[j]) : P.dd(PL[i], PL[j]);
   };
   for (int i = tid; i < M; i += HT) { Z[i] = A[i]; PQ[i] = i; }
   if (tid == 0) s_rk = -1;
@@ -279,13 +280,13 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
       Z[j] *= rowdiff(j, k) / den(PL[j], PU[k]);
     for (int j = k + 1 + tid; j < N; j += HT)
       V[j] *= ROW ? P.dd(PU[j], PU[k]) / (-P.fd(PL[k], PU[j]))
-                  : (__ldg(P.F + PU[j]) - __ldg(P.F + PU[k])) / P.fd(PU[j], PL[k]);
+                  : P.fv(__ldg(P.F + PU[j]), __ldg(P.F + PU[k])) / P.fd(PU[j], PL[k]);
     for (int j = tid; j < k; j += HT)
-      W[j] *= ROW ? (-P.fd(PL[j], PU[k])) / (Fk - F[j]) : P.fd(PU[k], PL[j]) / P.dd(PL[k], PL[j]);
+      W[j] *= ROW ? (-P.fd(PL[j], PU[k])) / P.fv(Fk, F[j]) : P.fd(PU[k], PL[j]) / P.dd(PL[k], PL[j]);
     if (tid < 32) {  // W[k] = den(k,k)/A[k] * prod_{j<k} ...
       double pr = 1.0;
       for (int j = tid; j < k; j += 32)
-        pr *= ROW ? (-P.fd(PL[k], PU[j])) / (F[j] - Fk) : P.fd(PU[j], PL[k]) / P.dd(PL[j], PL[k]);
+        pr *= ROW ? (-P.fd(PL[k], PU[j])) / P.fv(F[j], Fk) : P.fd(PU[j], PL[k]) / P.dd(PL[j], PL[k]);
       pr = warp_prod(pr);
       if (tid == 0) W[k] = (den(PL[k], PU[k]) / A[k]) * pr;
     }
@@ -323,8 +324,8 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
           for (int j = tid; j <= k; j += 32) {
             if (j == ii) continue;
             if (ROW) {
-              pu *= (F[ii] - F[j]) / P.fd(PL[ii], PU[j]);
-              pw *= (-P.fd(PL[jj], PU[j])) / (F[j] - F[jj]);
+              pu *= P.fv(F[ii], F[j]) / P.fd(PL[ii], PU[j]);
+              pw *= (-P.fd(PL[jj], PU[j])) / P.fv(F[j], F[jj]);
             } else {
               pu *= P.dd(PL[ii], PL[j]) / (-P.fd(PU[j], PL[ii]));
               pw *= P.fd(PU[j], PL[jj]) / P.dd(PL[j], PL[jj]);
@@ -397,7 +398,7 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
     W[i] = 0.0;
   }
   __syncthreads();
-  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
   int Rk = rrlu_node<true>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1);
   __syncthreads();
   for (int i = tid; i < M; i += HT) { h.U[r0 + i] = A[i]; h.PL[r0 + i] = PL[i]; INV[PQ[i]] = i; }
@@ -407,7 +408,7 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   if (Rk < mn) {
     for (int idx = tid; idx < M * Rk; idx += HT) {
       const int r = idx % M, j = idx / M, p = INV[r];
-      G[idx] = (p < Rk) ? (p == j ? 1.0 : 0.0) : Z[p] * W[j] / (F[p] - F[j]);
+      G[idx] = (p < Rk) ? (p == j ? 1.0 : 0.0) : Z[p] * W[j] / P.fv(F[p], F[j]);
     }
   } else {
     Rk = M;
@@ -449,7 +450,7 @@ k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
     W[i] = 0.0;
   }
   __syncthreads();
-  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
   int Rk = rrlu_node<false>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1);
   __syncthreads();
   for (int i = tid; i < M; i += HT) { h.V[c0 + i] = A[i]; h.PU[c0 + i] = PL[i]; INV[PQ[i]] = i; }
@@ -536,7 +537,7 @@ __global__ void k_hss_B(HssDev h, const int *__restrict__ pairs, int nn) {
   const int node = pairs[2 * a], sib = pairs[2 * a + 1];
   const int r0 = h.lr0[node], m = h.lr1[node] - r0 + 1;
   const int c0 = h.lc0[sib], n = h.lc1[sib] - c0 + 1;
-  PoleDiff P{h.FF, h.DIFL, h.DIFR};
+  PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
   double *B = h.Bg + (long long)node * h.bcap;
   if ((long long)m * n > h.bcap) { if (threadIdx.x == 0) atomicOr(h.flag, 1); return; }
   for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
@@ -552,7 +553,7 @@ __global__ void k_hss_leafD(HssDev h, const int *__restrict__ leaves, const int 
                             const double *__restrict__ v) {
   for (int a = blockIdx.y; a < nl; a += gridDim.y) {
     const int node = leaves[a], s = lstart[a], m = lsize[a];
-    PoleDiff P{h.FF, h.DIFL, h.DIFR};
+    PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
     double *D = h.Dg + h.doff[a];
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m * m; idx += gridDim.x * blockDim.x) {
       const int i = idx % m, j = idx / m;
@@ -587,14 +588,15 @@ struct HssPlan {
 
 // Build the HSS generators on the device; on return the ranks are on the host.
 static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F, const double *u,
-                         const double *v, const double *difl, const double *difr, cudaStream_t st) {
+                         const double *v, const double *difl, const double *difr, cudaStream_t st,
+                         bool sq = false) {
   int launches = 0;
   pl.t = make_tree(K, ni);
   const HostTree &t = pl.t;
   const int ltr = t.ltr;
   const int rmax = std::max(HSS_RMIN, t.mmax);
   HssDev &h = pl.h;
-  h.FF = F; h.DIFL = difl; h.DIFR = difr;
+  h.FF = F; h.DIFL = difl; h.DIFR = difr; h.sq = sq;
   h.K = K; h.ltr = ltr; h.rmax = rmax;
   h.U = pool<double>("hs_U", K); h.V = pool<double>("hs_V", K);
   h.PL = pool<int>("hs_PL", K); h.PU = pool<int>("hs_PU", K);
@@ -772,9 +774,9 @@ static int hss_multiply(const HssPlan &pl, const double *X, long long ldx, int n
 
 static void dense_product(int K, const double *F, const double *u, const double *v,
                           const double *difl, const double *difr, const double *X, long long ldx,
-                          int nrows, double *Y, long long ldy, cudaStream_t st) {
+                          int nrows, double *Y, long long ldy, cudaStream_t st, bool sq = false) {
   double *C = pool<double>("hss_denseC", (size_t)K * K);
-  launch_cauchy_eig(K, F, u, v, difl, difr, C, st);
+  launch_cauchy_eig(K, F, u, v, difl, difr, C, st, sq);
   std::vector<GemmDesc> g{{X, C, Y, (int)ldx, K, (int)ldy, nrows, K, K, 0, 0}};
   launch_gemm(g, 0, st);
 }
@@ -816,6 +818,54 @@ int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st) {
     *rank = a.K;
   }
   launch_scatter(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, boff, T, a.Q, a.ldq, st);
+  return launches + 1;
+}
+
+// HSS path of one bidiagonal SVD merge (DHSSVCS, SRC/CauchyHssvd_VPS.f90:3587-3803):
+// V2 <- V2 C_V with C_V(i,j) = zhat_i alpha_j / (d_i^2 - sigma_j^2), and
+// U2 <- U2 C_U - U2(:, 0) beta^T with C_U(i,j) = d_i zhat_i beta_j /
+// (d_i^2 - sigma_j^2): row 0 of C_U vanishes (d_0 = 0), and the -beta_j entries
+// of DLASD3's first row are the rank-one term (the reference's DGER,
+// SRC/mdlasd1.f90).  Both Cauchy-like matrices are compressed by the same
+// structured RRLU in singular-value mode (differences of squares).
+int svd_hss_merge(const SvdHssArgs &a, int *rank, cudaStream_t st) {
+  int launches = 0;
+  double *alpha = pool<double>("svh_alpha", a.K), *beta = pool<double>("svh_beta", a.K),
+         *ud = pool<double>("svh_ud", a.K);
+  launch_svd_norms(a.K, a.dl, a.difl, a.difr, a.zhat, alpha, beta, ud, st);
+  const int rows = std::max(a.N, a.M);
+  double *X = pool<double>("hss_X", (size_t)rows * a.K);
+  double *T = pool<double>("hss_T", (size_t)rows * a.K);
+  std::vector<long long> z0{0};
+  long long *boff = up("hss_boff", z0, st);
+  *rank = 0;
+  for (int side = 0; side < 2; ++side) {  // 0: right vectors V, 1: left vectors U
+    const int nr = side == 0 ? a.M : a.N;
+    double *Q = side == 0 ? a.V : a.U;
+    std::vector<int> hv{a.s, nr, 0, a.K};
+    int *dv = up(side == 0 ? "svh_gv0" : "svh_gv1", hv, st);
+    launch_gather(1, a.K, nr, dv, dv + 1, dv + 2, a.ndslot - a.s, nullptr, boff, Q, a.ld, X, st);
+    const double *u = side == 0 ? a.zhat : ud;
+    const double *v = side == 0 ? alpha : beta;
+    HssPlan pl;
+    stage_begin(HSS_ST_HSS_BUILD, st);
+    launches += hss_construct(pl, a.K, a.leaf, a.tol, a.dl, u, v, a.difl, a.difr, st, true);
+    stage_end(HSS_ST_HSS_BUILD, st, 0, 0.0);
+    if (pl.ok) {
+      stage_begin(HSS_ST_HSS_MM, st);
+      double fl = 0.0;
+      long long by = 0;
+      launches += hss_multiply(pl, X, nr, nr, T, nr, a.precision, st, &fl, &by);
+      stage_end(HSS_ST_HSS_MM, st, by, fl);
+      *rank = std::max(*rank, pl.max_rank);
+    } else {
+      dense_product(a.K, a.dl, u, v, a.difl, a.difr, X, nr, nr, T, nr, st, true);
+      *rank = a.K;
+    }
+    if (side == 1) launch_svd_rank1(nr, a.K, X, nr, beta, T, nr, st);
+    launch_scatter(1, a.K, nr, dv, dv + 1, dv + 2, a.ndslot - a.s, boff, T, Q, a.ld, st);
+    launches += 4;
+  }
   return launches + 1;
 }
 

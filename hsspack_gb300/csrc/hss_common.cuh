@@ -62,6 +62,10 @@ struct PoleDiff {
                               : (__ldg(F + p) - __ldg(F + q + 1)) - __ldg(difr + q);
     return sq ? lin * (__ldg(F + p) + (__ldg(F + q) + __ldg(difl + q))) : lin;
   }
+  // a - b for two pole values (a^2 - b^2 in singular-value mode)
+  __device__ __forceinline__ double fv(double a, double b) const {
+    return sq ? (a - b) * (a + b) : a - b;
+  }
   __device__ __forceinline__ double dd(int p, int q) const {
     const double lin = p < q ? (__ldg(F + p + 1) - __ldg(F + q)) + __ldg(difr + p) - __ldg(difl + q)
                              : (__ldg(F + p) - __ldg(F + q + 1)) + __ldg(difl + p) - __ldg(difr + q);

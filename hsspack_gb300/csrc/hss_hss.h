@@ -30,6 +30,20 @@ struct HssMergeArgs {
 // Returns the number of kernels launched; *rank receives the largest HSS rank.
 int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st);
 
+// One bidiagonal SVD merge with K >= bsmlz: U and V updated through two HSS
+// products (the merge's rows s .. s+N-1 of U, s .. s+M-1 of V; leading dim ld).
+struct SvdHssArgs {
+  int s, N, M, K;
+  int leaf;
+  double tol;
+  int precision;
+  const double *dl, *difl, *difr, *zhat;  // the merge's slices (sigma mode)
+  const int *ndslot;
+  double *U, *V;
+  long long ld;
+};
+int svd_hss_merge(const SvdHssArgs &a, int *rank, cudaStream_t st);
+
 // DHSSEVC on caller arrays: Q(0:nrows, 0:K) <- Q * C.
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,

@@ -51,7 +51,8 @@ void launch_build_S(const LevelView &lv, int total, const double *dl, const doub
                     const double *difr, const double *zhat, const int *grp,
                     const long long *soff, double *Sws, cudaStream_t st);
 void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
-                       const double *difl, const double *difr, double *C, cudaStream_t st);
+                       const double *difl, const double *difr, double *C, cudaStream_t st,
+                       bool sq = false);
 void launch_cauchylike(int M, int N, const double *D, const double *F, const double *u,
                        const double *v, double *A, cudaStream_t st);
 
@@ -134,10 +135,18 @@ void launch_svd_prepare(int P, int maxn, const int *ms, const int *mnl, const in
                         const int *msq, const double *d, const double *e, double *U,
                         long long ldu, double *V, long long ldv, const double *Dp, const int *perm,
                         const LevelScratch &w, int *out, double *onrm, cudaStream_t st);
-// U / V blocks (K x K per merge at boff) and sigma rescaled by onrm
+// U / V blocks (K x K per merge at boff); sigma rescaled by onrm
 void launch_svd_vectors(const LevelView &lv, int total, const double *dl, const double *difl,
                         const double *difr, const double *zhat, const long long *boff, double *Ub,
-                        double *Vb, const double *onrm, double *lam, cudaStream_t st);
+                        double *Vb, cudaStream_t st);
+void launch_svd_unscale(const LevelView &lv, int total, const double *onrm, double *lam,
+                        cudaStream_t st);
+// HSS path of one SVD merge: norms and U generator; the row-0 rank-one term
+void launch_svd_norms(int K, const double *dl, const double *difl, const double *difr,
+                      const double *zhat, double *alpha, double *beta, double *ud,
+                      cudaStream_t st);
+void launch_svd_rank1(int nrows, int K, const double *X, long long ldx, const double *beta,
+                      double *T, long long ldt, cudaStream_t st);
 // outputs in descending order: Uo (ldu), VT (ldvt), w; only w if !vectors
 void launch_svd_outputs(int n, const int *perm, const double *Dp, const double *Uq,
                         long long ldq, const double *V, long long ldv, double *Uo, long long ldu,

@@ -426,8 +426,8 @@ __global__ void k_build_S(LevelView lv, const double *__restrict__ dl,
 // Dense Cauchy-like block for the standalone API.
 __global__ void k_cauchy_eig(int K, const double *__restrict__ F, const double *__restrict__ u,
                              const double *__restrict__ v, const double *__restrict__ difl,
-                             const double *__restrict__ difr, double *__restrict__ C) {
-  PoleDiff P{F, difl, difr};
+                             const double *__restrict__ difr, double *__restrict__ C, bool sq) {
+  PoleDiff P{F, difl, difr, sq};
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)K * K) return;
   const int i = (int)(idx % K), j = (int)(idx / K);
@@ -580,10 +580,10 @@ void launch_build_S(const LevelView &lv, int total, const double *dl, const doub
   k_build_S<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, grp, soff, Sws);
 }
 void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
-                       const double *difl, const double *difr, double *C, cudaStream_t st) {
+                       const double *difl, const double *difr, double *C, cudaStream_t st, bool sq) {
   const long long tot = (long long)K * K;
   if (tot <= 0) return;
-  k_cauchy_eig<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(K, F, u, v, difl, difr, C);
+  k_cauchy_eig<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(K, F, u, v, difl, difr, C, sq);
 }
 void launch_cauchylike(int M, int N, const double *D, const double *F, const double *u,
                        const double *v, double *A, cudaStream_t st) {

@@ -435,6 +435,56 @@ __global__ void k_svd_vectors(LevelView lv, const double *__restrict__ dl,
   }
 }
 
+// One merge's column norms for the HSS path: alpha_j (V block), beta_j (U
+// block, including the -1 of row 0) and the U generator ud_i = d_i zhat_i
+// (arrays already offset to the merge; warp per column).
+__global__ void k_svd_norms(int K, const double *__restrict__ dl, const double *__restrict__ difl,
+                            const double *__restrict__ difr, const double *__restrict__ zhat,
+                            double *__restrict__ alpha, double *__restrict__ beta,
+                            double *__restrict__ ud) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= K) return;
+  PoleDiff P{dl, difl, difr, true};
+  double sv = 0.0, su = 0.0;
+  for (int i = lane; i < K; i += HSS_WARP) {
+    const double v = __ldg(zhat + i) / P.fd(i, j);
+    sv += v * v;
+    if (i > 0) { const double u = __ldg(dl + i) * v; su += u * u; }
+  }
+  sv = warp_sum(sv);
+  su = warp_sum(su);
+  if (lane == 0) {
+    alpha[j] = 1.0 / sqrt(sv);
+    beta[j] = 1.0 / sqrt(1.0 + su);
+    ud[j] = __ldg(dl + j) * __ldg(zhat + j);
+  }
+}
+
+// T(:, j) -= beta_j X(:, 0): the row-0 entries -beta_j of the U block.
+__global__ void k_svd_rank1(int nrows, int K, const double *__restrict__ X, long long ldx,
+                            const double *__restrict__ beta, double *__restrict__ T,
+                            long long ldt) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nrows * K) return;
+  const int i = (int)(idx % nrows), j = (int)(idx / nrows);
+  T[(long long)j * ldt + i] -= beta[j] * X[i];
+}
+
+void launch_svd_norms(int K, const double *dl, const double *difl, const double *difr,
+                      const double *zhat, double *alpha, double *beta, double *ud,
+                      cudaStream_t st) {
+  if (K > 0)
+    k_svd_norms<<<(unsigned)(((long long)K * 32 + 255) / 256), 256, 0, st>>>(K, dl, difl, difr,
+                                                                             zhat, alpha, beta, ud);
+}
+void launch_svd_rank1(int nrows, int K, const double *X, long long ldx, const double *beta,
+                      double *T, long long ldt, cudaStream_t st) {
+  const long long tot = (long long)nrows * K;
+  if (tot > 0)
+    k_svd_rank1<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(nrows, K, X, ldx, beta, T, ldt);
+}
+
 // sigma of every root back to the merge's scale (lam *= onrm[m]).
 __global__ void k_svd_unscale(LevelView lv, const double *__restrict__ onrm,
                               double *__restrict__ lam) {
@@ -547,11 +597,14 @@ void launch_svd_prepare(int P, int maxn, const int *ms, const int *mnl, const in
 
 void launch_svd_vectors(const LevelView &lv, int total, const double *dl, const double *difl,
                         const double *difr, const double *zhat, const long long *boff, double *Ub,
-                        double *Vb, const double *onrm, double *lam, cudaStream_t st) {
+                        double *Vb, cudaStream_t st) {
   if (total <= 0) return;
   k_svd_vectors<<<(unsigned)(((long long)total * 32 + 255) / 256), 256, 0, st>>>(
       lv, dl, difl, difr, zhat, boff, Ub, Vb);
-  k_svd_unscale<<<(total + 255) / 256, 256, 0, st>>>(lv, onrm, lam);
+}
+void launch_svd_unscale(const LevelView &lv, int total, const double *onrm, double *lam,
+                        cudaStream_t st) {
+  if (total > 0) k_svd_unscale<<<(total + 255) / 256, 256, 0, st>>>(lv, onrm, lam);
 }
 
 void launch_svd_outputs(int n, const int *perm, const double *Dp, const double *Uq,

@@ -129,3 +129,23 @@ def test_svd_16384_full_size():
     lam = eigvalsh_tridiagonal(np.zeros(2 * n), gk)
     sref = np.sort(lam[n:])[::-1]
     assert float(np.max(np.abs(sc - sref))) / nb <= SV_TOL
+
+
+@pytest.mark.parametrize("kind", ["ones", "random"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_svd_hss_merges(kind, precision):
+    # merges with K >= bsmlz go through two HSS products (DHSSVCS); HSS leaf 64,
+    # tolerance 1e-14 as the acceptance bar states
+    n = 2048
+    if kind == "ones":
+        d, e = np.ones(n), np.ones(n - 1)
+    else:
+        d, e = _bidiag(n, seed=21)
+    old = hp.set_config(bsmlz=48, hss_leaf=64, tol=1e-14, precision=precision)
+    try:
+        s, U, VT = hp.svd_bidiagonal(d, e)
+        st = hp.get_stats()
+    finally:
+        hp.restore_config(old)
+    assert st["n_hss_merges"] > 0
+    _check(d, e, s, U, VT)
