@@ -94,6 +94,10 @@ SIGNATURES = {
                         _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
     "hss_mdbdsdc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V, ctypes.c_int,
                                        _V]),
+    "cauchyhssmm_": (None, [_D, _D, _D, _D, _I, _I, _D, _I, _D, _I, _D]),
+    "hss_cauchyhssmm_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, ctypes.c_int,
+                                           ctypes.c_double, _V, ctypes.c_int, ctypes.c_int, _V,
+                                           _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
@@ -328,6 +332,35 @@ def mdbdsdc_dev(d, e, u, vt, stream=None):
     if info != 0:
         raise HssError("hss_mdbdsdc_dev INFO=%d: %s" % (info, _err()))
     return info
+
+
+def cauchyhssmm(D, F, U, V, B, ni, tol, ncol=None):
+    """CauchyHssMM (SRC/cauchyhssmm.f90:1): B <- C B in place (B Fortran-ordered
+    n x n), C(i,j) = U_i V_j / (D_i - F_j) in HSS form.  Returns time(1:2)."""
+    D, F, U, V = (np.ascontiguousarray(x, dtype=np.float64) for x in (D, F, U, V))
+    n = len(D)
+    if B.dtype != np.float64 or not B.flags.f_contiguous:
+        raise ValueError("B must be a Fortran-ordered float64 array")
+    t = np.zeros(2)
+    ints = [ctypes.c_int(int(x)) for x in (n, ni, ncol or n, B.shape[0])]
+    load().cauchyhssmm_(_pd(D), _pd(F), _pd(U), _pd(V), ctypes.byref(ints[0]),
+                        ctypes.byref(ints[1]), ctypes.byref(ctypes.c_double(tol)),
+                        ctypes.byref(ints[2]), _pd(B), ctypes.byref(ints[3]), _pd(t))
+    return t
+
+
+def cauchyhssmm_dev(D, F, u, v, B, ni, tol, stream=None):
+    """B (tensor whose memory is column-major n x ncb) <- C B on the device;
+    returns (construction ms, multiply ms)."""
+    n = D.numel()
+    ncb = B.numel() // max(n, 1)
+    t = (ctypes.c_float * 2)()
+    rc = load().hss_cauchyhssmm_dev(n, _ptr(D), _ptr(F), _ptr(u), _ptr(v), int(ni), float(tol),
+                                    _ptr(B), max(1, n), ncb, ctypes.cast(t, ctypes.c_void_p),
+                                    _stream(stream))
+    if rc != 0:
+        raise HssError("hss_cauchyhssmm_dev rc=%d: %s" % (rc, _err()))
+    return t[0], t[1]
 
 
 def cauchylike(D, F, u, v):

@@ -1623,6 +1623,71 @@ int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u,
   }
 }
 
+int hss_cauchyhssmm_dev(int n, const double *D, const double *F, const double *u, const double *v,
+                        int ni, double tol, double *B, int ldb, int ncb, float *times,
+                        void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  if (ni < 1) return -6;
+  if (ldb < std::max(1, n)) return -9;
+  if (ncb < 0) return -10;
+  if (n == 0 || ncb == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    int rank = 0;
+    hss_cauchyhssmm_core(n, D, F, u, v, ni, tol, c.cfg.precision, B, ldb, ncb, &rank, times, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    c.stats.max_rank = rank;
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+void cauchyhssmm_(const double *D, const double *F, const double *U, const double *V, const int *n_,
+                  const int *ni_, const double *tol_, const int *ncol_, double *B, const int *ldb_,
+                  double *time) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  const int n = *n_, ni = *ni_, ldb = *ldb_;
+  (void)ncol_;  // the GPU multiply takes all columns of B in one pass
+  if (n <= 0 || ni < 1 || ldb < n) {
+    c.err = "CauchyHssMM: bad N, ni or LDB";
+    if (time) { time[0] = 0.0; time[1] = 0.0; }
+    return;
+  }
+  try {
+    cudaStream_t st = nullptr;
+    double *dv = buf<double>(c, "chm_in", 4 * (size_t)n);
+    double *dB = buf<double>(c, "chm_B", (size_t)n * n);
+    CK(cudaMemcpyAsync(dv, D, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv + n, F, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv + 2 * n, U, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv + 3 * n, V, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpy2DAsync(dB, sizeof(double) * n, B, sizeof(double) * ldb, sizeof(double) * n, n,
+                         cudaMemcpyHostToDevice, st));
+    int rank = 0;
+    float t[2] = {0.f, 0.f};
+    hss_cauchyhssmm_core(n, dv, dv + n, dv + 2 * n, dv + 3 * n, ni, *tol_, c.cfg.precision, dB, n,
+                         n, &rank, t, st);
+    CK(cudaMemcpy2DAsync(B, sizeof(double) * ldb, dB, sizeof(double) * n, sizeof(double) * n, n,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c.stats.max_rank = rank;
+    if (time) { time[0] = 1e-3 * t[0]; time[1] = 1e-3 * t[1]; }
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+  }
+}
+
 int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B, int ldb,
                  double *C, int ldc, int beta, int precision, void *stream) {
   Ctx &c = ctx();

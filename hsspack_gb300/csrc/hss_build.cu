@@ -869,6 +869,78 @@ int svd_hss_merge(const SvdHssArgs &a, int *rank, cudaStream_t st) {
   return launches + 1;
 }
 
+// Generic Cauchy matrix in the merge representation: row poles F (the "old
+// poles"), column poles D (the "roots"): DIFL_j = D_j - F_j, DIFR_j = D_j - F_{j+1},
+// and the column generator -u.
+__global__ void k_cauchy_repr(int n, const double *__restrict__ D, const double *__restrict__ F,
+                              const double *__restrict__ u, double *__restrict__ difl,
+                              double *__restrict__ difr, double *__restrict__ mu) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  difl[j] = D[j] - F[j];
+  difr[j] = j + 1 < n ? D[j] - F[j + 1] : 0.0;
+  mu[j] = -u[j];
+}
+
+// Out (cols x rows, ldo) = In^T for In (rows x cols, ldi): 32 x 32 tiles.
+__global__ void k_transpose(int rows, int cols, const double *__restrict__ In, long long ldi,
+                            double *__restrict__ Out, long long ldo) {
+  __shared__ double t[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + threadIdx.x, cc = c0 + k;
+    if (r < rows && cc < cols) t[k][threadIdx.x] = In[(long long)cc * ldi + r];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int cc = c0 + threadIdx.x, r = r0 + k;
+    if (r < rows && cc < cols) Out[(long long)r * ldo + cc] = t[threadIdx.x][k];
+  }
+}
+
+static void transpose(int rows, int cols, const double *In, long long ldi, double *Out,
+                      long long ldo, cudaStream_t st) {
+  dim3 g((rows + 31) / 32, (cols + 31) / 32);
+  k_transpose<<<g, dim3(32, 8), 0, st>>>(rows, cols, In, ldi, Out, ldo);
+}
+
+// CauchyHssMM (SRC/cauchyhssmm.f90:1): B (n x ncb, ldb) <- C B with
+// C_ij = u_i v_j / (D_i - F_j) compressed to HSS (leaf ni, tolerance tol).
+// Computed as (B^T C^T)^T: C^T is Cauchy-like with row poles F, column poles D
+// and generators (v, -u), so the structured RRLU and the multiply of the merge
+// apply unchanged.  times[0] / times[1]: construction / multiplication (ms).
+int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *u,
+                         const double *v, int ni, double tol, int precision, double *B,
+                         long long ldb, int ncb, int *rank, float *times, cudaStream_t st) {
+  double *difl = pool<double>("chm_difl", n), *difr = pool<double>("chm_difr", n),
+         *mu = pool<double>("chm_mu", n);
+  double *X = pool<double>("chm_X", (size_t)ncb * n), *Y = pool<double>("chm_Y", (size_t)ncb * n);
+  cudaEvent_t e0, e1, e2;
+  HCK(cudaEventCreate(&e0)); HCK(cudaEventCreate(&e1)); HCK(cudaEventCreate(&e2));
+  HCK(cudaEventRecord(e0, st));
+  k_cauchy_repr<<<(n + 255) / 256, 256, 0, st>>>(n, D, F, u, difl, difr, mu);
+  HssPlan pl;
+  int launches = 1 + hss_construct(pl, n, ni, tol, F, v, mu, difl, difr, st);
+  HCK(cudaEventRecord(e1, st));
+  transpose(n, ncb, B, ldb, X, ncb, st);
+  if (pl.ok) {
+    launches += hss_multiply(pl, X, ncb, ncb, Y, ncb, precision, st);
+    *rank = pl.max_rank;
+  } else {
+    dense_product(n, F, v, mu, difl, difr, X, ncb, ncb, Y, ncb, st);
+    *rank = n;
+  }
+  transpose(ncb, n, Y, ncb, B, ldb, st);
+  HCK(cudaEventRecord(e2, st));
+  HCK(cudaEventSynchronize(e2));
+  if (times) {
+    HCK(cudaEventElapsedTime(&times[0], e0, e1));
+    HCK(cudaEventElapsedTime(&times[1], e1, e2));
+  }
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  return launches + 2;
+}
+
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
                      long long ldq, int nrows, int *rank, cudaStream_t st) {

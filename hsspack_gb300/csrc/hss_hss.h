@@ -44,6 +44,11 @@ struct SvdHssArgs {
 };
 int svd_hss_merge(const SvdHssArgs &a, int *rank, cudaStream_t st);
 
+// CauchyHssMM on device arrays: B (n x ncb, ldb) <- C B, C_ij = u_i v_j / (D_i - F_j).
+int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *u,
+                         const double *v, int ni, double tol, int precision, double *B,
+                         long long ldb, int ncb, int *rank, float *times, cudaStream_t st);
+
 // DHSSEVC on caller arrays: Q(0:nrows, 0:K) <- Q * C.
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,

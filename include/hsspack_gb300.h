@@ -87,6 +87,15 @@ void mdbdsdc_(const char *uplo, const char *compq, const int *n, double *d, doub
               double *u, const int *ldu, double *vt, const int *ldvt, double *q, int *iq,
               double *work, int *iwork, int *info, size_t uplo_len, size_t compq_len);
 
+/* CauchyHssMM(D,F,U,V,N,ni,tol,ncol,B,LDB,time) replaces SRC/cauchyhssmm.f90:1:
+ * B(1:N, 1:N) <- C * B for the Cauchy-like C(i,j) = U(i) V(j) / (D(i) - F(j)),
+ * compressed to HSS with leaf ni and tolerance tol; time(1) / time(2) return
+ * the construction / multiplication seconds.  ncol (the reference's panel
+ * width) is accepted and ignored: all columns are multiplied in one pass. */
+void cauchyhssmm_(const double *D, const double *F, const double *U, const double *V,
+                  const int *n, const int *ni, const double *tol, const int *ncol, double *B,
+                  const int *ldb, double *time);
+
 /* Largest band half-width of the banded divide and conquer (leaves of up to
  * 2 kd rows are solved by one warp each). */
 #define HSS_BAND_KD_MAX 32
@@ -178,6 +187,13 @@ int hss_lowner_noalloc_dev(int k, const double *dlamda, const double *difl,
 int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u,
                     const double *v, const double *difl, const double *difr,
                     double *Q, int ldq, int nrows, void *stream);
+
+/* CauchyHssMM on device arrays: B(n, ncb; ldb) <- C B with
+ * C(i,j) = u_i v_j / (D_i - F_j) in HSS form (leaf ni, tolerance tol);
+ * times[0..1] (may be NULL) receive construction / multiply milliseconds. */
+int hss_cauchyhssmm_dev(int n, const double *D, const double *F, const double *u,
+                        const double *v, int ni, double tol, double *B, int ldb, int ncb,
+                        float *times, void *stream);
 
 /* Dense Cauchy-like eigenvector block C(i,j) = u_i v_j / (F_i - lam_j) through
  * DIFL/DIFR (SRC/CauchyHssEig.f90:1688, CauchylikeEig), k-by-k column-major. */
