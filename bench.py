@@ -329,11 +329,12 @@ def run_ours(args):
     # "plain": per-merge launches, FP64 products, standard secular guess
     full_cfg = {"batched": 1, "precision": 1}
     from hsspack_gb300 import predictor as _pred
-    if _pred.install():  # committed weights trained by hsspack_gb300/predictor.py
-        full_cfg["predictor"] = 1
-    # DC leaf size from the project's autotuner (timed outside the measured region)
+    have_pred = _pred.install()  # committed weights trained by hsspack_gb300/predictor.py
+    # DC leaf size and learned start from the project's autotuner (timed
+    # outside the measured region)
     from hsspack_gb300 import autotune
-    tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg)
+    tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
+                                   predictor=(0, 1) if have_pred else (0,))
     full_cfg.update(tuned)
     plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()

@@ -41,7 +41,8 @@ class Config(ctypes.Structure):
     _fields_ = [("hss_leaf", ctypes.c_int), ("bsmlz", ctypes.c_int), ("tol", ctypes.c_double),
                 ("smlsiz", ctypes.c_int), ("precision", ctypes.c_int),
                 ("predictor", ctypes.c_int), ("batched", ctypes.c_int),
-                ("profile", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+                ("profile", ctypes.c_int), ("sec_terms", ctypes.c_int),
+                ("split_min_log2", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

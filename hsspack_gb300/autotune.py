@@ -1,8 +1,8 @@
 """Autotuner for the divide-and-conquer configuration.
 
 Chooses, per problem-size bucket (powers of two), the DC leaf size SMLSIZ and
-the K threshold between dense and HSS merges by timing candidate settings on a
-seeded random tridiagonal of that size (device time from the library's CUDA
+whether the learned secular start is used, by timing the candidate settings on
+a seeded random tridiagonal of that size (device time from the library's CUDA
 events).  Results are cached in ``_lib/autotune.json`` next to the library and
 applied with :func:`apply`.
 """
@@ -30,9 +30,10 @@ def load_cache():
     return {}
 
 
-def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None):
-    """Time MDSTEDC('I') at size n for each DC leaf size; return the best
-    config dict and cache it under the size bucket."""
+def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None, predictor=(0,)):
+    """Time MDSTEDC('I') at size n for each DC leaf size and learned-start
+    setting; return the best config dict (and all timings, keyed
+    "smlsiz" or "smlsiz+learned") and cache it under the size bucket."""
     import torch
     import hsspack_gb300 as hp
     rng = np.random.default_rng(seed)
@@ -41,33 +42,40 @@ def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None):
     e0 = torch.tensor(e, dtype=torch.float64, device="cuda")
     dw, ew = d0.clone(), e0.clone()
     z = torch.empty(n * n, dtype=torch.float64, device="cuda")
-    results = {}
-    for sml in candidates:
-        old = hp.set_config(smlsiz=int(sml), **(base or {}))
-        try:
-            best = float("inf")
-            for _ in range(reps + 1):
-                dw.copy_(d0)
-                ew.copy_(e0)
-                hp.mdstedc_dev(dw, ew, z)
-                best = min(best, hp.get_stats()["ms_total"])
-            results[int(sml)] = best
-        finally:
-            hp.restore_config(old)
-    sml = min(results, key=results.get)
+    results, cfgs = {}, {}
+    for pred in predictor:
+        for sml in candidates:
+            key = "%d%s" % (sml, "+learned" if pred else "")
+            cfg = dict(base or {}, smlsiz=int(sml), predictor=int(pred))
+            old = hp.set_config(**cfg)
+            try:
+                best = float("inf")
+                for _ in range(reps + 1):
+                    dw.copy_(d0)
+                    ew.copy_(e0)
+                    hp.mdstedc_dev(dw, ew, z)
+                    best = min(best, hp.get_stats()["ms_total"])
+                results[key] = best
+                cfgs[key] = {"smlsiz": int(sml), "predictor": int(pred)}
+            finally:
+                hp.restore_config(old)
+    key = min(results, key=results.get)
+    sml = cfgs[key]["smlsiz"]
     cache = load_cache()
-    cache[_bucket(n)] = {"smlsiz": sml, "ms": results}
+    cache[_bucket(n)] = dict(cfgs[key], ms=results)
     try:
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
         json.dump(cache, open(CACHE, "w"), indent=1)
     except OSError:
         pass
-    return {"smlsiz": sml}, results
+    return dict(cfgs[key]), results
 
 
 def lookup(n):
     ent = load_cache().get(_bucket(n))
-    return {"smlsiz": ent["smlsiz"]} if ent else None
+    if not ent:
+        return None
+    return {k: ent[k] for k in ("smlsiz", "predictor") if k in ent}
 
 
 def apply(n):

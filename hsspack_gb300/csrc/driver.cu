@@ -229,9 +229,21 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   int *dout = buf<int>(c, "g_out", 5 * P);
   double *drho = buf<double>(c, "g_rho", P);
   stage_begin(HSS_ST_PREPARE, st);
+  int pflags = bu ? bu->flags : 0;
+  if (!(pflags & PREP_SORTED)) {
+    // merged order and z for every position of the level in one wide launch
+    std::vector<int> poff(P + 1, 0);
+    for (int m = 0; m < P; ++m) poff[m + 1] = poff[m] + mn[m];
+    int *dpo = buf<int>(c, "g_poff", P + 1);
+    h2d(dpo, poff, st);
+    launch_merge_front(P, poff[P], dpo, dms, dmn, dmn1, e, Q, ldq, Dp, perm, L.w,
+                       bu ? bu->z : nullptr, bu ? bu->rho : nullptr, pflags, st);
+    pflags |= PREP_FRONT;
+    c.launches++;
+  }
   launch_merge_prepare(P, *std::max_element(mn.begin(), mn.end()), dms, dmn, dmn1, e, Q, ldq, Dp,
                        perm, L.w, dout, drho, st, bu ? bu->z : nullptr, bu ? bu->rho : nullptr,
-                       bu ? bu->flags : 0);
+                       pflags);
   {
     long long nn = 0;
     for (int x : mn) nn += x;
@@ -1147,6 +1159,8 @@ void hss_set_config(const hss_config *cfg) {
   Ctx &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
   c.cfg = *cfg;
+  set_secular_terms(cfg->sec_terms);
+  set_split_min_log2(cfg->split_min_log2);
 }
 void hss_get_config(hss_config *cfg) {
   Ctx &c = ctx();

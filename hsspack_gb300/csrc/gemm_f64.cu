@@ -91,6 +91,29 @@ k_gemm_f64(int nprob, const GemmDesc *__restrict__ probs) {
 
 int gemm_tiles(int M, int N) { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN); }
 
+// Small products (N, K <= 32: the lowest DC levels): one thread per output
+// element, the K-term dot product from L1 (a 64 x 64 tile would be mostly
+// empty).  Problem p owns outputs [eoff[p], eoff[p+1]).
+__global__ void __launch_bounds__(256)
+k_gemm_small(int nprob, const GemmDesc *__restrict__ probs, const long long *__restrict__ eoff) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= eoff[nprob]) return;
+  int lo = 0, hi = nprob;
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (eoff[mid] <= idx) lo = mid; else hi = mid; }
+  const GemmDesc P = probs[lo];
+  const long long e = idx - eoff[lo];
+  const int i = (int)(e % P.M), j = (int)(e / P.M);
+  const double *a = P.A + i, *b = P.B + (long long)j * P.ldb;
+  double acc = 0.0;
+  for (int k = 0; k < P.K; ++k) acc = fma(__ldg(a + (long long)k * P.lda), __ldg(b + k), acc);
+  double *c = P.C + (long long)j * P.ldc + i;
+  *c = P.beta ? *c + acc : acc;
+}
+
+// split-BF16 threshold (hss_config.split_min_log2): M*N*K >= 2^g_split_log2
+static int g_split_log2 = 17;
+void set_split_min_log2(int v) { g_split_log2 = v > 0 ? v : 17; }
+
 void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaStream_t st) {
   if (nprob <= 0 || total_tiles <= 0) return;
   k_gemm_f64<<<total_tiles, GT, 0, st>>>(nprob, d_probs);
@@ -104,7 +127,7 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
     // operand byte; small products stay on the FP64 pipe
     std::vector<GemmDesc> big;
     for (const auto &p : probs_in) {
-      if ((double)p.M * p.N * p.K >= (double)(1 << 20) && p.M >= 256) big.push_back(p);
+      if ((double)p.M * p.N * p.K >= ldexp(1.0, g_split_log2) && p.M >= 256) big.push_back(p);
       else probs.push_back(p);
     }
     int *err = pool<int>("gemm_err", 1);
@@ -113,11 +136,25 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
   } else {
     probs = probs_in;
   }
+  // tiny products (N, K <= 32) by the element kernel, the rest by 64 x 64 tiles
+  std::vector<GemmDesc> tiny, tiled;
+  for (const auto &p : probs) (p.N <= 32 && p.K <= 32 ? tiny : tiled).push_back(p);
+  if (!tiny.empty()) {
+    std::vector<long long> eoff(1, 0);
+    for (const auto &p : tiny) eoff.push_back(eoff.back() + (long long)p.M * p.N);
+    GemmDesc *d = pool<GemmDesc>("gemm_small_probs", tiny.size());
+    long long *de = pool<long long>("gemm_small_eoff", eoff.size());
+    cudaMemcpyAsync(d, tiny.data(), tiny.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(de, eoff.data(), eoff.size() * sizeof(long long), cudaMemcpyHostToDevice, st);
+    if (eoff.back() > 0)
+      k_gemm_small<<<(unsigned)((eoff.back() + 255) / 256), 256, 0, st>>>((int)tiny.size(), d, de);
+  }
+  if (tiled.empty()) return;
   int tiles = 0;
-  for (auto &p : probs) { p.tile0 = tiles; tiles += gemm_tiles(p.M, p.N); }
-  GemmDesc *d = pool<GemmDesc>("gemm_f64_probs", probs.size());
-  cudaMemcpyAsync(d, probs.data(), probs.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice, st);
-  launch_gemm_f64((int)probs.size(), tiles, d, st);
+  for (auto &p : tiled) { p.tile0 = tiles; tiles += gemm_tiles(p.M, p.N); }
+  GemmDesc *d = pool<GemmDesc>("gemm_f64_probs", tiled.size());
+  cudaMemcpyAsync(d, tiled.data(), tiled.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice, st);
+  launch_gemm_f64((int)tiled.size(), tiles, d, st);
 }
 
 }  // namespace hss

@@ -36,6 +36,8 @@ struct LevelScratch {
 };
 
 // secular.cu
+// lane-group width target of the secular kernels (pole terms per lane; 0: 8)
+void set_secular_terms(int t);
 // sq: singular-value mode (poles d_i^2, outputs sigma and DIFL/DIFR = sigma - d)
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
@@ -64,7 +66,7 @@ void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int n
 // merge.cu
 // prepare flags: the block is already in ascending order (no merge of two
 // halves); every column is dense (no top / bottom block structure)
-enum { PREP_SORTED = 1, PREP_DENSE = 2 };
+enum { PREP_SORTED = 1, PREP_DENSE = 2, PREP_FRONT = 4 /* order and z from k_merge_front */ };
 // zsrc: z per slot instead of the rows of Q around the cut; rsrc: the coupling
 // rho_in per merge instead of e[s + n1 - 1]
 void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1, const double *e,
@@ -72,6 +74,11 @@ void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const i
                           const LevelScratch &w, int *out, double *orho, cudaStream_t st,
                           const double *zsrc = nullptr, const double *rsrc = nullptr,
                           int flags = 0);
+// merged order and z of every position of a level (poff: prefix of mn, P + 1)
+void launch_merge_front(int P, int total, const int *poff, const int *ms, const int *mn,
+                        const int *mn1, const double *e, const double *Q, long long ldq,
+                        const double *Dp, const int *perm, const LevelScratch &w,
+                        const double *zsrc, const double *rsrc, int flags, cudaStream_t st);
 // Zr (nz columns, leading dim zld): rows rotated with the Q columns
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
                    const LevelScratch &w, double *Q, long long ldq, cudaStream_t st,

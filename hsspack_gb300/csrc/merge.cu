@@ -29,7 +29,9 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   const int s = ms[m], n = mn[m], n1 = mn1[m], n2 = n - n1;
   const int tid = threadIdx.x;
   const double rho_in = rsrc ? rsrc[m] : e[s + n1 - 1];
-  if (flags & PREP_SORTED) {
+  if (flags & PREP_FRONT) {
+    // merged order and z already written by k_merge_front
+  } else if (flags & PREP_SORTED) {
     // ---- the whole block is already ascending (a later rank-one update of a
     //      banded merge: mdsbed22.f90 takes INDXQ as it is)
     for (int i = tid; i < n; i += MT) {
@@ -71,15 +73,19 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   const double sc = 1.0 / sqrt(2.0);
   double dmax = 0.0, zmax = 0.0;
   for (int i = tid; i < n; i += MT) {
-    const int slot = w.srt[s + i];
-    const bool top = slot < s + n1;
-    double z = zsrc ? zsrc[slot] : Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
-    if (!top && rho_in < 0.0) z = -z;
-    z *= sc;
-    const double dv = w.ds[s + i];
-    w.zs[s + i] = z;
-    w.typ[s + i] = (flags & PREP_DENSE) ? 2 : top ? 1 : 3;
-    dmax = fmax(dmax, fabs(dv));
+    double z;
+    if (flags & PREP_FRONT) {
+      z = w.zs[s + i];
+    } else {
+      const int slot = w.srt[s + i];
+      const bool top = slot < s + n1;
+      z = zsrc ? zsrc[slot] : Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
+      if (!top && rho_in < 0.0) z = -z;
+      z *= sc;
+      w.zs[s + i] = z;
+      w.typ[s + i] = (flags & PREP_DENSE) ? 2 : top ? 1 : 3;
+    }
+    dmax = fmax(dmax, fabs(w.ds[s + i]));
     zmax = fmax(zmax, fabs(z));
   }
   dmax = block_max<MT>(dmax);
@@ -235,10 +241,17 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   // (mdlaed2.f90:340-356 inserts them in order), so sort those and merge.
   if (nrot > 1) block_sort_pairs(w.l2val + s, w.l2slot + s, w.ds + s, w.cand + s, nrot);
   const int n1l = (n - K) - nrot;
+  // the (short) rotated list in shared memory for the searches of the long one
+  const bool l2s = nrot <= NCS;
+  const double *l2 = l2s ? c_z : w.l2val + s;
+  if (l2s) {
+    for (int i = tid; i < nrot; i += MT) c_z[i] = w.l2val[s + i];
+    __syncthreads();
+  }
   for (int i = tid; i < n1l; i += MT) {  // L1 element: count L2 < v
     const double v = w.l1val[s + i];
     int lo = 0, hi = nrot;
-    while (lo < hi) { int md = (lo + hi) >> 1; if (w.l2val[s + md] < v) lo = md + 1; else hi = md; }
+    while (lo < hi) { int md = (lo + hi) >> 1; if (l2[md] < v) lo = md + 1; else hi = md; }
     w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = w.l1slot[s + i];
   }
   for (int i = tid; i < nrot; i += MT) {  // L2 element: count L1 <= v
@@ -256,6 +269,44 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
 
 // Apply each merge's Givens rotations, in order, to its slot pairs: one thread
 // per row (rows of a block are independent; columns are read coalesced).
+// Front half of the prepare for all merges of a level, one thread per
+// position (positions of merge m: poff[m] .. poff[m+1]-1): the merged order of
+// the two ascending halves (DLAMRG by merge path: each element counts the
+// partner half's values below it) and z in merged order, as k_merge_prepare
+// would compute them with one CTA per merge.
+__global__ void k_merge_front(int P, const int *__restrict__ poff, const int *__restrict__ ms,
+                              const int *__restrict__ mn, const int *__restrict__ mn1,
+                              const double *__restrict__ e, const double *__restrict__ Q,
+                              long long ldq, const double *__restrict__ Dp,
+                              const int *__restrict__ perm, LevelScratch w,
+                              const double *__restrict__ zsrc, const double *__restrict__ rsrc,
+                              int flags) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= poff[P]) return;
+  int lo = 0, hi = P;
+  while (hi - lo > 1) { const int md = (lo + hi) >> 1; if (poff[md] <= t) lo = md; else hi = md; }
+  const int m = lo, i = t - poff[m];
+  const int s = ms[m], n1 = mn1[m], n2 = mn[m] - n1;
+  const bool top = i < n1;
+  const int slot = perm[s + i];  // left: perm[s+i]; right: perm[s+n1+(i-n1)]
+  const double v = Dp[slot];
+  int a = 0, b = top ? n2 : n1;
+  const int base = top ? s + n1 : s;
+  while (a < b) {  // top: count right values < v;  bottom: count left values <= v
+    const int md = (a + b) >> 1;
+    const double u = Dp[perm[base + md]];
+    if (top ? (u < v) : (u <= v)) a = md + 1; else b = md;
+  }
+  const int pos = (top ? i : i - n1) + a;
+  const double rho_in = rsrc ? rsrc[m] : e[s + n1 - 1];
+  double z = zsrc ? zsrc[slot] : Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
+  if (!top && rho_in < 0.0) z = -z;
+  w.srt[s + pos] = slot;
+  w.ds[s + pos] = v;
+  w.zs[s + pos] = z * (1.0 / sqrt(2.0));
+  w.typ[s + pos] = (flags & PREP_DENSE) ? 2 : top ? 1 : 3;
+}
+
 // Threads r >= n rotate rows p, q of column r - n of Zr (nz columns, leading
 // dim zld) the same way: the remaining columns of a banded merge's
 // Z = Q^T W follow the rotated eigenvectors (mdsbed22.f90 rotates Z(:, 2:)).
@@ -324,11 +375,21 @@ __global__ void __launch_bounds__(MT)
 k_merge_finish(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                const int *__restrict__ mK, const double *__restrict__ lam,
                const LevelScratch w, int *__restrict__ perm, double *__restrict__ Dp) {
+  constexpr int LS = 2048;
+  __shared__ double sl[LS];
   const int m = blockIdx.x;
   const int s = ms[m], n = mn[m], K = mK[m];
   const int nd = n - K;
+  // the (short) list of new eigenvalues in shared memory for the searches of
+  // the long deflated list
+  const bool in_s = K <= LS;
+  if (in_s) {
+    for (int j = threadIdx.x; j < K; j += MT) sl[j] = lam[s + j];
+    __syncthreads();
+  }
+  const double *lm = in_s ? sl : lam + s;
   for (int j = threadIdx.x; j < K; j += MT) {
-    const double a = lam[s + j];
+    const double a = lm[j];
     int lo = 0, hi = nd;
     while (lo < hi) { int mid = (lo + hi) >> 1; if (w.dfval[s + mid] < a) lo = mid + 1; else hi = mid; }
     const int slot = w.ndslot[s + j];
@@ -338,7 +399,7 @@ k_merge_finish(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   for (int a_ = threadIdx.x; a_ < nd; a_ += MT) {
     const double b = w.dfval[s + a_];
     int lo = 0, hi = K;
-    while (lo < hi) { int mid = (lo + hi) >> 1; if (lam[s + mid] <= b) lo = mid + 1; else hi = mid; }
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (lm[mid] <= b) lo = mid + 1; else hi = mid; }
     perm[s + a_ + lo] = w.dfslot[s + a_];
   }
 }
@@ -393,11 +454,12 @@ __global__ void k_zero_blocks(int np, const long long *__restrict__ P, double *_
 // bs[b] .. bs[b] + bm[b] - 1 (slots of Dp).
 __global__ void k_scale_blocks(int nb, const int *__restrict__ bs, const int *__restrict__ bm,
                                const double *__restrict__ bscl, double *__restrict__ Dp) {
-  const int b = blockIdx.x;
-  if (b >= nb) return;
-  const int s = bs[b], m = bm[b];
-  const double a = bscl[b];
-  for (int i = threadIdx.x; i < m; i += blockDim.x) Dp[s + i] *= a;
+  for (int b = blockIdx.y; b < nb; b += gridDim.y) {
+    const int s = bs[b], m = bm[b];
+    const double a = bscl[b];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+      Dp[s + i] *= a;
+  }
 }
 
 // Final ordering of every problem: column j of problem p's output is the
@@ -421,6 +483,15 @@ __global__ void k_final_gather_batch(int np, const long long *__restrict__ P,
 // ---------------------------------------------------------------- launch --
 static int merge_threads(int maxn) {
   return maxn <= 64 ? 64 : maxn <= 256 ? 128 : maxn <= 2048 ? 256 : 512;
+}
+
+void launch_merge_front(int P, int total, const int *poff, const int *ms, const int *mn,
+                        const int *mn1, const double *e, const double *Q, long long ldq,
+                        const double *Dp, const int *perm, const LevelScratch &w,
+                        const double *zsrc, const double *rsrc, int flags, cudaStream_t st) {
+  if (P <= 0 || total <= 0) return;
+  k_merge_front<<<(total + 255) / 256, 256, 0, st>>>(P, poff, ms, mn, mn1, e, Q, ldq, Dp, perm,
+                                                     w, zsrc, rsrc, flags);
 }
 
 void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1,
@@ -485,7 +556,7 @@ void launch_zero_blocks(int np, long long total, const long long *P, double *Q, 
 }
 void launch_scale_blocks(int nb, const int *bs, const int *bm, const double *bscl, double *Dp,
                          cudaStream_t st) {
-  if (nb > 0) k_scale_blocks<<<nb, 256, 0, st>>>(nb, bs, bm, bscl, Dp);
+  if (nb > 0) k_scale_blocks<<<dim3(64, std::min(nb, 65535)), 256, 0, st>>>(nb, bs, bm, bscl, Dp);
 }
 void launch_final_gather_batch(int np, long long total, const long long *P, const int *perm,
                                const double *Dp, const double *Q, long long ldq, double *const *Z,

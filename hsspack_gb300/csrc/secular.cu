@@ -530,12 +530,16 @@ k_secular_mid(LevelView lv, const double *__restrict__ dl, const double *__restr
 static inline int warp_grid(int total, int threads) {
   return (int)(((long long)total * 32 + threads - 1) / threads);
 }
+// Pole terms per lane the lane-group width aims at (hss_config.sec_terms).
+static int g_sec_terms = 8;
+void set_secular_terms(int t) { g_sec_terms = t > 0 ? t : 8; }
+
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st, bool sq) {
   if (total <= 0) return;
   int L = 1;
-  while (L < 32 && L * 8 < maxk) L *= 2;  // ~8 pole terms per lane
+  while (L < 32 && L * g_sec_terms < maxk) L *= 2;  // ~sec_terms pole terms per lane
   const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
   switch (L * 2 + (sq ? 1 : 0)) {
 #define SEC_CASE(LL, SQ)                                                                     \
@@ -552,7 +556,7 @@ void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *
                         const double *zw, float *feat, cudaStream_t st) {
   if (total <= 0) return;
   int L = 1;
-  while (L < 32 && L * 8 < maxk) L *= 2;
+  while (L < 32 && L * g_sec_terms < maxk) L *= 2;
   const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
   switch (L) {
 #define MID_CASE(LL) \

@@ -31,7 +31,11 @@ typedef struct hss_config {
   int predictor;  /* 0: standard secular initial guess; 1: learned initial guess    */
   int batched;    /* 1: one launch per stage per DC level; 0: launches per merge    */
   int profile;    /* 1: time every stage with CUDA events (hss_stats.stage_ms)      */
-  int reserved[8];
+  int sec_terms;  /* secular solver: pole terms per lane (lanes per root = the    */
+                  /* smallest power of two covering K / sec_terms); 0: 8        */
+  int split_min_log2; /* split-BF16 products for M*N*K >= 2^this (and M >= 256); */
+                      /* 0: 17                                                   */
+  int reserved[6];
 } hss_config;
 
 /* stages timed when hss_config.profile = 1 */
