@@ -240,6 +240,99 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
     return out
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (CUDA cores) rate
+# per stage: the unit that bounds it on GB300
+STAGE_BOUND = {"secular": "fp64", "lowner": "fp64", "build_S": "fp64", "leaf": "fp64",
+               "gemm": "fp64-equivalent", "final_gather": "hbm", "prepare": "hbm",
+               "gather": "hbm", "scatter": "hbm", "givens": "hbm", "finish": "hbm"}
+
+
+def stage_rooflines(acc, pk):
+    """Achieved rate of every timed stage from its algorithmic bytes / flops:
+    HBM stages against the measured copy bandwidth, FP64 stages against the
+    nominal FP64 rate, the products as FP64-equivalent TFLOP/s (the split-BF16
+    path is meant to exceed the FP64 rate)."""
+    out = {}
+    for st, ms in acc["ms"].items():
+        if ms <= 0 or st not in STAGE_BOUND:
+            continue
+        b = STAGE_BOUND[st]
+        if b == "hbm":
+            a = acc["bytes"][st] / (ms * 1e-3) / 1e9
+            out[st] = {"bound": "hbm", "achieved": a, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                       "frac": a / pk["hbm_gbs"], "peak_source": pk["source"]}
+        else:
+            a = acc["flops"][st] / (ms * 1e-3) / 1e12
+            out[st] = {"bound": b, "achieved": a, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                       "frac": a / FP64_NOMINAL_TFLOPS, "peak_source": "nominal FP64 rate"}
+    return out
+
+
+def _timed_ms(torch, fn, reps=3):
+    fn()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(reps):
+        fn()
+    t1.record()
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1) / reps
+
+
+def run_extra(torch, hp, full_cfg):
+    """Secondary figures (not the metric): the other configurations' device
+    times through the library's device entry points."""
+    out = {}
+    old = hp.set_config(**{k: v for k, v in full_cfg.items() if k != "predictor"})
+    try:
+        # bidiagonal SVD n = 16384, d, e iid U(0, 1] (seed 0)
+        n = 16384
+        rng = np.random.default_rng(0)
+        d = torch.tensor(1.0 - rng.uniform(0.0, 1.0, n), device="cuda")
+        e = torch.tensor(1.0 - rng.uniform(0.0, 1.0, n - 1), device="cuda")
+        dw, ew = d.clone(), e.clone()
+        u = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        vt = torch.empty_like(u)
+
+        def svd():
+            dw.copy_(d)
+            ew.copy_(e)
+            hp.mdbdsdc_dev(dw, ew, u, vt)
+
+        out["bidiagonal_svd_n16384_ms"] = _timed_ms(torch, svd)
+        del u, vt
+        # banded n = 16384, kd = 4, entries iid U[-1, 1] (seed 0)
+        kd = 4
+        ab = rng.uniform(-1.0, 1.0, (kd + 1, n))
+        abd = torch.tensor(np.ascontiguousarray(ab.T), device="cuda")
+        w = torch.empty(n, dtype=torch.float64, device="cuda")
+        z = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        out["banded_n16384_kd4_ms"] = _timed_ms(torch, lambda: hp.mdsbevd_dev(kd, abd, w, z))
+        del z
+        # Cauchy merge n = 8192: secular, Loewner, HSS compression (leaf 128,
+        # tol 1e-14) and the product with a dense 8192 x 8192 matrix
+        n = 8192
+        rng = np.random.default_rng(0)
+        dd = torch.tensor(np.sort(rng.uniform(0.0, 1.0, n)), device="cuda")
+        zz = torch.tensor(rng.standard_normal(n) / np.sqrt(n), device="cuda")
+        lam, difl, difr = (torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3))
+        out["cauchy_secular_n8192_ms"] = _timed_ms(
+            torch, lambda: hp.secular_dev(dd, zz, 1.0, lam, difl, difr))
+        zh, al = zz.clone(), torch.zeros(n, dtype=torch.float64, device="cuda")
+        hp.lowner_dev(dd, difl, difr, zh, al)
+        Q = torch.randn(n * n, dtype=torch.float64, device="cuda")
+        for prec in (0, 1):
+            hp.set_config(precision=prec)
+            out["cauchy_hss_multiply_n8192_%s_ms" % ("fp64" if prec == 0 else "split_bf16")] = \
+                _timed_ms(torch, lambda: hp.dhssevc_dev(dd, zh, al, difl, difr, Q, n, n, ni=128,
+                                                        tol=1e-14))
+        out["cauchy_hss_max_rank"] = hp.get_stats()["max_rank"]
+    finally:
+        hp.restore_config(old)
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -333,8 +426,11 @@ def run_ours(args):
     # DC leaf size and learned start from the project's autotuner (timed
     # outside the measured region)
     from hsspack_gb300 import autotune
-    tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
-                                   predictor=(0, 1) if have_pred else (0,))
+    if args.smlsiz > 0:
+        tuned, tune_ms = {"smlsiz": args.smlsiz, "predictor": 0}, None
+    else:
+        tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
+                                       predictor=(0, 1) if have_pred else (0,))
     full_cfg.update(tuned)
     plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()
@@ -384,7 +480,12 @@ def run_ours(args):
     if not args.no_batch:
         batch = run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist)
 
-    # dominant stage -> roofline
+    extra = None
+    if not args.no_extra and rank == 0:
+        extra = run_extra(torch, hp, full_cfg)
+
+    # dominant stage -> roofline (contract object), plus every stage against
+    # the bound that applies to it
     pk = peaks()
     top = max(acc["ms"], key=lambda s: acc["ms"][s])
     calls = max(1, acc["calls"][top])
@@ -395,10 +496,13 @@ def run_ours(args):
     tpath = os.path.join(ROOT, "profiles", "traffic_%s.json" % top)
     if os.path.exists(tpath):
         traffic = json.load(open(tpath)).get("bytes_per_launch")
+    stage_roof = stage_rooflines(acc, pk)
     roof = {"bound": "hbm", "kernel_stage": top, "achieved": achieved, "peak": pk["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
             "peak_source": pk["source"], "per_launch_ms": per_launch_ms,
-            "algorithmic_bytes_per_launch": per_launch_bytes}
+            "algorithmic_bytes_per_launch": per_launch_bytes,
+            "pipe_bound": stage_roof.get(top, {}).get("bound"),
+            "pipe_roofline": stage_roof.get(top)}
     if rank != 0:
         return
     cpu = None
@@ -430,6 +534,8 @@ def run_ours(args):
         "full_vs_plain": ms_plain / ms,
         "accuracy": acc_chk,
         "batch": batch,
+        "stage_rooflines": stage_roof,
+        "other_workloads": extra,
         "stages_ms_per_step": {k: v / args.steps for k, v in acc["ms"].items() if v > 0},
         "profiled_stage_share": {k: v / total_ms for k, v in acc["ms"].items() if v > 0},
         "stats": {k: st[k] for k in ("n_levels", "n_merges", "n_hss_merges", "n_dense_merges",
@@ -451,6 +557,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batch figures")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
+    ap.add_argument("--smlsiz", type=int, default=0,
+                    help="fixed DC leaf size instead of the autotuner (profiling runs)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warmup + timed solves (for ncu launch lists)")
     args = ap.parse_args()

@@ -527,6 +527,11 @@ k_secular_mid(LevelView lv, const double *__restrict__ dl, const double *__restr
 }
 
 // ---------------------------------------------------------------- launch --
+// Threads per CTA for the root kernels: 256 when the level fills the GPU
+// several times over, else 64 so that a small level still spreads over all
+// 152 SMs (the kernels use no shared memory and no block barriers).
+static inline int root_block(long long threads) { return threads >= 152LL * 256 * 2 ? 256 : 64; }
+
 static inline int warp_grid(int total, int threads) {
   return (int)(((long long)total * 32 + threads - 1) / threads);
 }
@@ -540,11 +545,12 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
   if (total <= 0) return;
   int L = 1;
   while (L < 32 && L * g_sec_terms < maxk) L *= 2;  // ~sec_terms pole terms per lane
-  const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
+  const int tb = root_block((long long)total * L);
+  const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
   switch (L * 2 + (sq ? 1 : 0)) {
 #define SEC_CASE(LL, SQ)                                                                     \
   case LL * 2 + SQ:                                                                          \
-    k_secular<LL, SQ><<<grid, 256, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,    \
+    k_secular<LL, SQ><<<grid, tb, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,     \
                                             itsum, guess);                                   \
     break;
     SEC_CASE(1, 0) SEC_CASE(2, 0) SEC_CASE(4, 0) SEC_CASE(8, 0) SEC_CASE(16, 0) SEC_CASE(32, 0)
@@ -557,10 +563,11 @@ void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *
   if (total <= 0) return;
   int L = 1;
   while (L < 32 && L * g_sec_terms < maxk) L *= 2;
-  const unsigned grid = (unsigned)(((long long)total * L + 255) / 256);
+  const int tb = root_block((long long)total * L);
+  const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
   switch (L) {
 #define MID_CASE(LL) \
-  case LL: k_secular_mid<LL><<<grid, 256, 0, st>>>(lv, dl, zw, feat); break;
+  case LL: k_secular_mid<LL><<<grid, tb, 0, st>>>(lv, dl, zw, feat); break;
     MID_CASE(1) MID_CASE(2) MID_CASE(4) MID_CASE(8) MID_CASE(16) MID_CASE(32)
 #undef MID_CASE
   }
@@ -569,19 +576,22 @@ void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
                    const double *difr, const double *zw, double *zhat, cudaStream_t st, bool sq) {
   if (total <= 0) return;
-  k_lowner<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zw, zhat, sq);
+  const int tb = root_block((long long)total * 32);
+  k_lowner<<<warp_grid(total, tb), tb, 0, st>>>(lv, dl, difl, difr, zw, zhat, sq);
 }
 void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
                   const double *difr, const double *zhat, double *alpha, cudaStream_t st,
                   bool sq) {
   if (total <= 0) return;
-  k_alpha<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, alpha, sq);
+  const int tb = root_block((long long)total * 32);
+  k_alpha<<<warp_grid(total, tb), tb, 0, st>>>(lv, dl, difl, difr, zhat, alpha, sq);
 }
 void launch_build_S(const LevelView &lv, int total, const double *dl, const double *difl,
                     const double *difr, const double *zhat, const int *grp,
                     const long long *soff, double *Sws, cudaStream_t st) {
   if (total <= 0) return;
-  k_build_S<<<warp_grid(total, 256), 256, 0, st>>>(lv, dl, difl, difr, zhat, grp, soff, Sws);
+  const int tb = root_block((long long)total * 32);
+  k_build_S<<<warp_grid(total, tb), tb, 0, st>>>(lv, dl, difl, difr, zhat, grp, soff, Sws);
 }
 void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
                        const double *difl, const double *difr, double *C, cudaStream_t st, bool sq) {
