@@ -168,6 +168,7 @@ struct LevelArrays {
   LevelScratch w;
   double *lam, *difl, *difr, *zhat, *alpha;
   int *iters;
+  int2 *sup = nullptr;  // per slot rows holding data (tridiagonal path; Q not zero-filled)
 };
 
 static LevelArrays level_arrays(Ctx &c, int n) {
@@ -237,13 +238,13 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     int *dpo = buf<int>(c, "g_poff", P + 1);
     h2d(dpo, poff, st);
     launch_merge_front(P, poff[P], dpo, dms, dmn, dmn1, e, Q, ldq, Dp, perm, L.w,
-                       bu ? bu->z : nullptr, bu ? bu->rho : nullptr, pflags, st);
+                       bu ? bu->z : nullptr, bu ? bu->rho : nullptr, pflags, st, L.sup);
     pflags |= PREP_FRONT;
     c.launches++;
   }
   launch_merge_prepare(P, *std::max_element(mn.begin(), mn.end()), dms, dmn, dmn1, e, Q, ldq, Dp,
                        perm, L.w, dout, drho, st, bu ? bu->z : nullptr, bu ? bu->rho : nullptr,
-                       pflags);
+                       pflags, L.sup);
   {
     long long nn = 0;
     for (int x : mn) nn += x;
@@ -297,6 +298,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
         *g3 = buf<int>(c, "gv_g", gs.size());
     h2d(g1, gs, st); h2d(g2, gn, st); h2d(g3, gng, st);
     stage_begin(HSS_ST_GIVENS, st);
+    launch_widen((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, L.sup, st);
     launch_givens((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, st, bu ? bu->zrest : nullptr,
                   bu ? bu->nrest : 0, bu ? bu->zld : 0);
     long long gb = 0;
@@ -366,7 +368,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     stage_end(HSS_ST_BUILD_S, st, 8LL * stot * 2, 0.0);
     int maxnd = *std::max_element(dn_.begin(), dn_.end());
     stage_begin(HSS_ST_GATHER, st);
-    launch_gather(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, L.w.grp, xq2, Q, ldq, Q2, st);
+    launch_gather(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, L.w.grp, xq2, Q, ldq, Q2, st, L.sup);
     stage_end(HSS_ST_GATHER, st, 16LL * q2tot, 0.0);
     // GEMM problems: top rows use type 1,2 columns, bottom rows type 2,3
     std::vector<GemmDesc> probs;
@@ -396,7 +398,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     launch_gemm(probs, c.cfg.precision, st);
     stage_end(HSS_ST_GEMM, st, gbytes, fl);
     stage_begin(HSS_ST_SCATTER, st);
-    launch_scatter(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, xq2, T, Q, ldq, st);
+    launch_scatter(PD, dtot, maxnd, xs, xn, xoff, L.w.ndslot, xq2, T, Q, ldq, st, L.sup);
     stage_end(HSS_ST_SCATTER, st, 16LL * q2tot, 0.0);
     c.launches += 4;
   }
@@ -407,7 +409,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     h.leaf = c.cfg.hss_leaf; h.tol = c.cfg.tol; h.precision = c.cfg.precision;
     h.dl = L.w.dl + h.s; h.difl = L.difl + h.s; h.difr = L.difr + h.s; h.zhat = L.zhat + h.s;
     h.alpha = L.alpha + h.s; h.ndslot = L.w.ndslot + h.s;
-    h.Q = Q; h.ldq = ldq;
+    h.Q = Q; h.ldq = ldq; h.sup = L.sup;
     int rank = 0;
     c.launches += hss_merge(h, &rank, st);  // times its own stages
     c.stats.max_rank = std::max(c.stats.max_rank, rank);
@@ -431,7 +433,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
 // one tree level of all blocks are processed together.
 static void dc_blocks(Ctx &c, const std::vector<int> &bs, const std::vector<int> &bm, int N,
                       const double *d, const double *e, double *Q, long long ldq, double *Dp,
-                      int *perm, int *status, cudaStream_t st) {
+                      int *perm, int *status, cudaStream_t st, int2 *sup) {
   const int smlsiz = std::max(1, std::min(c.cfg.smlsiz, 32));
   const int nb = (int)bs.size();
   std::vector<std::vector<int>> ends(nb);
@@ -458,13 +460,14 @@ static void dc_blocks(Ctx &c, const std::vector<int> &bs, const std::vector<int>
   int *dls = buf<int>(c, "leaf_s", nl), *dlz = buf<int>(c, "leaf_z", nl);
   h2d(dls, ls, st); h2d(dlz, lz, st);
   stage_begin(HSS_ST_LEAF, st);
-  launch_leaf(nl, dls, dlz, mmax, N, d, e, Q, ldq, Dp, perm, status, st);
+  launch_leaf(nl, dls, dlz, mmax, N, d, e, Q, ldq, Dp, perm, status, st, sup);
   stage_end(HSS_ST_LEAF, st, 8LL * N * smlsiz, fl);
   c.launches++;
   bool more = false;
   for (auto &v : ends) more |= v.size() > 1;
   if (!more) return;
   LevelArrays L = level_arrays(c, N);
+  L.sup = sup;
   while (more) {
     MergeLevel lvl;
     more = false;
@@ -533,13 +536,12 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   // status[4..5]: 64-bit count of learned starts that fell back
   int *status = buf<int>(c, "status", 6);
   CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
-  if (np == 1) {
-    CK(cudaMemsetAsync(Q, 0, sizeof(double) * qsize, st));
-  } else {
+  // no zero fill of Q: every column is tracked with the rows it holds data on
+  // (set by the leaves, widened by merges) and read as zero elsewhere
+  int2 *sup = buf<int2>(c, "sup", N);
+  if (np > 1) {
     dP = buf<long long>(c, "prob_P", np + 1);
     h2d(dP, P, st);
-    launch_zero_blocks(np, N, dP, Q, L, st);
-    c.launches++;
   }
   // global d, e with e = 0 at every block end; split and scale per problem
   std::vector<double> hd(N), he(N, 0.0);
@@ -577,7 +579,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   }
   CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e, he.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
-  dc_blocks(c, bstart, bsize, N, d, e, Q, L, Dp, perm, status, st);
+  dc_blocks(c, bstart, bsize, N, d, e, Q, L, Dp, perm, status, st, sup);
   {
     std::vector<int> ss, sm;
     std::vector<double> sc;
@@ -616,7 +618,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   }
   stage_begin(HSS_ST_FINAL, st);
   if (np == 1) {
-    launch_final_gather(N, fperm, Dp, Q, L, pr[0].z, pr[0].ldz, pr[0].w, st);
+    launch_final_gather(N, fperm, Dp, Q, L, pr[0].z, pr[0].ldz, pr[0].w, st, sup);
   } else {
     std::vector<double *> hz(np), hw(np);
     std::vector<long long> hl(np);
@@ -624,7 +626,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
     double **dz = buf<double *>(c, "prob_z", np), **dw = buf<double *>(c, "prob_w", np);
     long long *dl = buf<long long>(c, "prob_ldz", np);
     h2d(dz, hz, st); h2d(dw, hw, st); h2d(dl, hl, st);
-    launch_final_gather_batch(np, N, dP, fperm, Dp, Q, L, dz, dl, dw, st);
+    launch_final_gather_batch(np, N, dP, fperm, Dp, Q, L, dz, dl, dw, st, sup);
   }
   {
     long long nn = 0;

@@ -799,7 +799,8 @@ int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st) {
   int *dv = up("hss_gview", hv, st);
   std::vector<long long> z0{0};
   long long *boff = up("hss_boff", z0, st);
-  launch_gather(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, nullptr, boff, a.Q, a.ldq, X, st);
+  launch_gather(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, nullptr, boff, a.Q, a.ldq, X, st,
+                a.sup);
   launches += 2;
   HssPlan pl;
   stage_begin(HSS_ST_HSS_BUILD, st);
@@ -817,7 +818,7 @@ int hss_merge(const HssMergeArgs &a, int *rank, cudaStream_t st) {
     launches += 2;
     *rank = a.K;
   }
-  launch_scatter(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, boff, T, a.Q, a.ldq, st);
+  launch_scatter(1, a.K, a.n, dv, dv + 1, dv + 2, a.ndslot - a.s, boff, T, a.Q, a.ldq, st, a.sup);
   return launches + 1;
 }
 

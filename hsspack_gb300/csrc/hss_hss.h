@@ -25,6 +25,7 @@ struct HssMergeArgs {
   const int *ndslot;
   double *Q;
   long long ldq;
+  int2 *sup = nullptr;  // rows each Q column holds data on (nullptr: all)
 };
 
 // Returns the number of kernels launched; *rank receives the largest HSS rank.

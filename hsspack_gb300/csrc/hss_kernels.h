@@ -61,7 +61,7 @@ void launch_cauchylike(int M, int N, const double *D, const double *F, const dou
 // leaf.cu
 void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int nblk,
                  const double *d, const double *e, double *Q, long long ldq, double *Dp, int *perm,
-                 int *status, cudaStream_t st);
+                 int *status, cudaStream_t st, int2 *sup = nullptr);
 
 // merge.cu
 // prepare flags: the block is already in ascending order (no merge of two
@@ -73,26 +73,34 @@ void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const i
                           const double *Q, long long ldq, double *Dp, int *perm,
                           const LevelScratch &w, int *out, double *orho, cudaStream_t st,
                           const double *zsrc = nullptr, const double *rsrc = nullptr,
-                          int flags = 0);
+                          int flags = 0, const int2 *sup = nullptr);
 // merged order and z of every position of a level (poff: prefix of mn, P + 1)
 void launch_merge_front(int P, int total, const int *poff, const int *ms, const int *mn,
                         const int *mn1, const double *e, const double *Q, long long ldq,
                         const double *Dp, const int *perm, const LevelScratch &w,
-                        const double *zsrc, const double *rsrc, int flags, cudaStream_t st);
+                        const double *zsrc, const double *rsrc, int flags, cudaStream_t st,
+                        const int2 *sup = nullptr);
 // Zr (nz columns, leading dim zld): rows rotated with the Q columns
 void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
                    const LevelScratch &w, double *Q, long long ldq, cudaStream_t st,
                    double *Zr = nullptr, int nz = 0, long long zld = 0);
+// sup (optional): per slot the rows [x, y) a column holds data on (zero
+// elsewhere); gathers read within it, scatters set it to the merge's rows
 void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                    const int *ndslot, const int *grp, const long long *boff, const double *Q,
-                   long long ldq, double *B, cudaStream_t st);
+                   long long ldq, double *B, cudaStream_t st, const int2 *sup = nullptr);
 void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                     const int *ndslot, const long long *toff, const double *T, double *Q,
-                    long long ldq, cudaStream_t st);
+                    long long ldq, cudaStream_t st, int2 *sup = nullptr);
+// columns about to be rotated: zeros written outside their support, support
+// widened to the merge's rows
+void launch_widen(int P, int maxn, const int *ms, const int *mn, const int *ng,
+                  const LevelScratch &w, double *Q, long long ldq, int2 *sup, cudaStream_t st);
 void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const int *mK, const double *lam,
                          const LevelScratch &w, int *perm, double *Dp, cudaStream_t st);
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
-                         double *Z, long long ldz, double *wout, cudaStream_t st);
+                         double *Z, long long ldz, double *wout, cudaStream_t st,
+                         const int2 *sup = nullptr);
 // many problems per call: P = global start of each problem (np + 1 entries),
 // total = P[np]; problem p's block is Q + P[p] * (ldq + 1), leading dim ldq
 void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
@@ -101,7 +109,8 @@ void launch_scale_blocks(int nb, const int *bs, const int *bm, const double *bsc
                          cudaStream_t st);
 void launch_final_gather_batch(int np, long long total, const long long *P, const int *perm,
                                const double *Dp, const double *Q, long long ldq, double *const *Z,
-                               const long long *ldz, double *const *W, cudaStream_t st);
+                               const long long *ldz, double *const *W, cudaStream_t st,
+                               const int2 *sup = nullptr);
 
 // predictor.cu
 int mlp_nparam();

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(32)
 k_leaf_ql(int nleaf, const int *__restrict__ lstart, const int *__restrict__ lsize, int mmax,
           int nblk, const double *__restrict__ d, const double *__restrict__ e,
           double *__restrict__ Q, long long ldq, double *__restrict__ Dp,
-          int *__restrict__ perm, int *__restrict__ status) {
+          int *__restrict__ perm, int *__restrict__ status, int2 *__restrict__ sup) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x, LW = blockDim.x;
   const int leaf = blockIdx.x * LW + lane;
@@ -113,6 +113,7 @@ k_leaf_ql(int nleaf, const int *__restrict__ lstart, const int *__restrict__ lsi
     for (int i = 0; i < m; ++i) {
       Dp[s + i] = DD(i);
       perm[s + i] = s + i;
+      if (sup) sup[s + i] = make_int2(s, s + m);  // rows the column is written on
     }
     if (bad) atomicMax(status, HSS_LEAF_NOCONV);
   }
@@ -132,7 +133,7 @@ k_leaf_ql(int nleaf, const int *__restrict__ lstart, const int *__restrict__ lsi
 
 void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int nblk,
                  const double *d, const double *e, double *Q, long long ldq, double *Dp, int *perm,
-                 int *status, cudaStream_t st) {
+                 int *status, cudaStream_t st, int2 *sup) {
   if (nleaf <= 0) return;
   mmax = std::max(1, std::min(mmax, LEAF_MAX));
   // leaves per CTA: enough CTAs to cover the SMs, and the block within smem
@@ -146,7 +147,7 @@ void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int n
     attr = smem;
   }
   k_leaf_ql<<<(nleaf + lw - 1) / lw, lw, smem, st>>>(nleaf, lstart, lsize, mmax, nblk, d, e, Q, ldq,
-                                                      Dp, perm, status);
+                                                      Dp, perm, status, sup);
 }
 
 }  // namespace hss

@@ -15,6 +15,17 @@
 
 namespace hss {
 
+// Q(row, slot) where the column is known to be zero outside the rows
+// sup[slot] = [lo, hi) it has been written on (sup == nullptr: all rows valid).
+__device__ __forceinline__ double qat(const double *__restrict__ Q, long long ldq,
+                                      const int2 *__restrict__ sup, int slot, long long row) {
+  if (sup) {
+    const int2 r = sup[slot];
+    if (row < r.x || row >= r.y) return 0.0;
+  }
+  return Q[(long long)slot * ldq + row];
+}
+
 // out[5*m + {0..4}] = K, #rotations, #type1, #type2, #type3 ; orho[m] = |2 rho|
 template <int MT>
 __global__ void __launch_bounds__(MT)
@@ -23,7 +34,7 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                 const double *__restrict__ Q, long long ldq, double *__restrict__ Dp,
                 int *__restrict__ perm, LevelScratch w, int *__restrict__ out,
                 double *__restrict__ orho, const double *__restrict__ zsrc,
-                const double *__restrict__ rsrc, int flags) {
+                const double *__restrict__ rsrc, int flags, const int2 *__restrict__ sup) {
   const int m = blockIdx.x;
   if (m >= P) return;
   const int s = ms[m], n = mn[m], n1 = mn1[m], n2 = n - n1;
@@ -79,7 +90,7 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     } else {
       const int slot = w.srt[s + i];
       const bool top = slot < s + n1;
-      z = zsrc ? zsrc[slot] : Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
+      z = zsrc ? zsrc[slot] : qat(Q, ldq, sup, slot, top ? s + n1 - 1 : s + n1);
       if (!top && rho_in < 0.0) z = -z;
       z *= sc;
       w.zs[s + i] = z;
@@ -280,7 +291,7 @@ __global__ void k_merge_front(int P, const int *__restrict__ poff, const int *__
                               long long ldq, const double *__restrict__ Dp,
                               const int *__restrict__ perm, LevelScratch w,
                               const double *__restrict__ zsrc, const double *__restrict__ rsrc,
-                              int flags) {
+                              int flags, const int2 *__restrict__ sup) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= poff[P]) return;
   int lo = 0, hi = P;
@@ -299,12 +310,37 @@ __global__ void k_merge_front(int P, const int *__restrict__ poff, const int *__
   }
   const int pos = (top ? i : i - n1) + a;
   const double rho_in = rsrc ? rsrc[m] : e[s + n1 - 1];
-  double z = zsrc ? zsrc[slot] : Q[(long long)slot * ldq + (top ? s + n1 - 1 : s + n1)];
+  double z = zsrc ? zsrc[slot] : qat(Q, ldq, sup, slot, top ? s + n1 - 1 : s + n1);
   if (!top && rho_in < 0.0) z = -z;
   w.srt[s + pos] = slot;
   w.ds[s + pos] = v;
   w.zs[s + pos] = z * (1.0 / sqrt(2.0));
   w.typ[s + pos] = (flags & PREP_DENSE) ? 2 : top ? 1 : 3;
+}
+
+// Before the deflating rotations of merge m: every column they touch is made
+// valid on all rows s .. s+n-1 of the merge (zeros written outside the rows it
+// held data on) and its support widened, so the rotations read true values.
+// One CTA per merge, rotations in order (a slot may take part in several).
+__global__ void k_widen(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+                        const int *__restrict__ ng, const LevelScratch w, double *Q, long long ldq,
+                        int2 *__restrict__ sup) {
+  for (int m = blockIdx.x; m < P; m += gridDim.x) {
+    const int s = ms[m], n = mn[m], g = ng[m];
+    for (int t = 0; t < g; ++t)
+      for (int side = 0; side < 2; ++side) {
+        const int slot = side == 0 ? w.gvp[s + t] : w.gvq[s + t];
+        __syncthreads();  // the previous update of sup is visible to all threads
+        const int2 r = sup[slot];
+        if (r.x == s && r.y == s + n) continue;  // uniform across the CTA
+        double *col = Q + (long long)slot * ldq;
+        for (int i = s + threadIdx.x; i < s + n; i += blockDim.x)
+          if (i < r.x || i >= r.y) col[i] = 0.0;
+        __syncthreads();
+        if (threadIdx.x == 0) sup[slot] = make_int2(s, s + n);
+      }
+    __syncthreads();
+  }
 }
 
 // Threads r >= n rotate rows p, q of column r - n of Zr (nz columns, leading
@@ -336,7 +372,8 @@ __global__ void k_givens(int P, const int *__restrict__ ms, const int *__restric
 __global__ void k_gather(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                          const int *__restrict__ rootoff, const int *__restrict__ ndslot,
                          const int *__restrict__ grp, const long long *__restrict__ boff,
-                         const double *__restrict__ Q, long long ldq, double *__restrict__ B) {
+                         const double *__restrict__ Q, long long ldq, double *__restrict__ B,
+                         const int2 *__restrict__ sup) {
   const int r = blockIdx.x;
   if (r >= rootoff[P]) return;
   int lo = 0, hi = P;
@@ -344,17 +381,20 @@ __global__ void k_gather(int P, const int *__restrict__ ms, const int *__restric
   const int m = lo, j = r - rootoff[m];
   const int s = ms[m], n = mn[m];
   const int col = grp ? grp[s + j] : j;
-  const double *src = Q + (long long)ndslot[s + j] * ldq + s;
+  const int slot = ndslot[s + j];
+  const double *src = Q + (long long)slot * ldq + s;
   double *dst = B + boff[m] + (long long)col * n;
+  int vlo = 0, vhi = n;  // rows of the column that hold data (zero elsewhere)
+  if (sup) { const int2 sr = sup[slot]; vlo = max(0, sr.x - s); vhi = min(n, sr.y - s); }
   for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x)
-    dst[i] = src[i];
+    dst[i] = (i >= vlo && i < vhi) ? src[i] : 0.0;
 }
 
 // Write the new eigenvectors (columns of T, n_m x K) into the non-deflated slots.
 __global__ void k_scatter(int P, const int *__restrict__ ms, const int *__restrict__ mn,
                           const int *__restrict__ rootoff, const int *__restrict__ ndslot,
                           const long long *__restrict__ toff, const double *__restrict__ T,
-                          double *__restrict__ Q, long long ldq) {
+                          double *__restrict__ Q, long long ldq, int2 *__restrict__ sup) {
   const int r = blockIdx.x;
   if (r >= rootoff[P]) return;
   int lo = 0, hi = P;
@@ -363,6 +403,7 @@ __global__ void k_scatter(int P, const int *__restrict__ ms, const int *__restri
   const int s = ms[m], n = mn[m];
   const double *src = T + toff[m] + (long long)j * n;
   double *dst = Q + (long long)ndslot[s + j] * ldq + s;
+  if (sup && blockIdx.y == 0 && threadIdx.x == 0) sup[ndslot[s + j]] = make_int2(s, s + n);
   for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x)
     dst[i] = src[i];
 }
@@ -408,10 +449,19 @@ k_merge_finish(int P, const int *__restrict__ ms, const int *__restrict__ mn,
 // w(i) = Dp(perm(i)).  One CTA per column.
 __global__ void k_final_gather(int n, const int *__restrict__ perm, const double *__restrict__ Dp,
                                const double *__restrict__ Q, long long ldq, double *__restrict__ Z,
-                               long long ldz, double *__restrict__ wout) {
+                               long long ldz, double *__restrict__ wout,
+                               const int2 *__restrict__ sup) {
   const int c = blockIdx.x;
   if (c >= n) return;
   const long long p = perm[c];
+  if (sup) {  // read only the rows the column holds data on; zeros elsewhere
+    const int2 r = sup[p];
+    const double *s1 = Q + p * ldq;
+    double *dst = Z + (long long)c * ldz;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = (i >= r.x && i < r.y) ? s1[i] : 0.0;
+    if (threadIdx.x == 0) wout[c] = Dp[p];
+    return;
+  }
   const double2 *src = reinterpret_cast<const double2 *>(Q + p * ldq);
   double *dst = Z + (long long)c * ldz;
   // 16-byte vector copies only when both column starts are 16-byte aligned
@@ -469,14 +519,16 @@ __global__ void k_final_gather_batch(int np, const long long *__restrict__ P,
                                      const int *__restrict__ perm, const double *__restrict__ Dp,
                                      const double *__restrict__ Q, long long ldq,
                                      double *const *__restrict__ Z, const long long *__restrict__ ldz,
-                                     double *const *__restrict__ W) {
+                                     double *const *__restrict__ W, const int2 *__restrict__ sup) {
   const long long c = blockIdx.x;
   const int p = problem_of(P, np, c);
   const long long r0 = __ldg(P + p), n = __ldg(P + p + 1) - r0, j = c - r0;
   const long long slot = perm[c];
   const double *src = Q + slot * ldq + r0;
   double *dst = Z[p] + j * ldz[p];
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  long long lo = 0, hi = n;  // rows holding data (global rows sup[slot]) relative to r0
+  if (sup) { const int2 r = sup[slot]; lo = r.x - r0; hi = r.y - r0; }
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) dst[i] = (i >= lo && i < hi) ? src[i] : 0.0;
   if (threadIdx.x == 0) W[p][j] = Dp[slot];
 }
 
@@ -488,21 +540,22 @@ static int merge_threads(int maxn) {
 void launch_merge_front(int P, int total, const int *poff, const int *ms, const int *mn,
                         const int *mn1, const double *e, const double *Q, long long ldq,
                         const double *Dp, const int *perm, const LevelScratch &w,
-                        const double *zsrc, const double *rsrc, int flags, cudaStream_t st) {
+                        const double *zsrc, const double *rsrc, int flags, cudaStream_t st,
+                        const int2 *sup) {
   if (P <= 0 || total <= 0) return;
   k_merge_front<<<(total + 255) / 256, 256, 0, st>>>(P, poff, ms, mn, mn1, e, Q, ldq, Dp, perm,
-                                                     w, zsrc, rsrc, flags);
+                                                     w, zsrc, rsrc, flags, sup);
 }
 
 void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const int *mn1,
                           const double *e, const double *Q, long long ldq, double *Dp, int *perm,
                           const LevelScratch &w, int *out, double *orho, cudaStream_t st,
-                          const double *zsrc, const double *rsrc, int flags) {
+                          const double *zsrc, const double *rsrc, int flags, const int2 *sup) {
   if (P <= 0) return;
 #define PREP_CASE(T)                                                                        \
   case T:                                                                                  \
     k_merge_prepare<T><<<P, T, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho, \
-                                        zsrc, rsrc, flags);                                \
+                                        zsrc, rsrc, flags, sup);                           \
     break;
   switch (merge_threads(maxn)) {
     PREP_CASE(64)
@@ -523,17 +576,22 @@ void launch_givens(int P, int maxn, const int *ms, const int *mn, const int *ng,
 }
 void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                    const int *ndslot, const int *grp, const long long *boff, const double *Q,
-                   long long ldq, double *B, cudaStream_t st) {
+                   long long ldq, double *B, cudaStream_t st, const int2 *sup) {
   if (total <= 0) return;
   dim3 grid(total, (maxn + 1023) / 1024);
-  k_gather<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, grp, boff, Q, ldq, B);
+  k_gather<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, grp, boff, Q, ldq, B, sup);
 }
 void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                     const int *ndslot, const long long *toff, const double *T, double *Q,
-                    long long ldq, cudaStream_t st) {
+                    long long ldq, cudaStream_t st, int2 *sup) {
   if (total <= 0) return;
   dim3 grid(total, (maxn + 1023) / 1024);
-  k_scatter<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, toff, T, Q, ldq);
+  k_scatter<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, toff, T, Q, ldq, sup);
+}
+void launch_widen(int P, int maxn, const int *ms, const int *mn, const int *ng,
+                  const LevelScratch &w, double *Q, long long ldq, int2 *sup, cudaStream_t st) {
+  if (P <= 0 || !sup) return;
+  k_widen<<<std::min(P, 65535), maxn <= 256 ? 128 : 512, 0, st>>>(P, ms, mn, ng, w, Q, ldq, sup);
 }
 void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const int *mK,
                          const double *lam, const LevelScratch &w, int *perm, double *Dp,
@@ -547,8 +605,9 @@ void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const in
   }
 }
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
-                         double *Z, long long ldz, double *wout, cudaStream_t st) {
-  if (n > 0) k_final_gather<<<n, 256, 0, st>>>(n, perm, Dp, Q, ldq, Z, ldz, wout);
+                         double *Z, long long ldz, double *wout, cudaStream_t st,
+                         const int2 *sup) {
+  if (n > 0) k_final_gather<<<n, 256, 0, st>>>(n, perm, Dp, Q, ldq, Z, ldz, wout, sup);
 }
 void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
                         cudaStream_t st) {
@@ -560,9 +619,11 @@ void launch_scale_blocks(int nb, const int *bs, const int *bm, const double *bsc
 }
 void launch_final_gather_batch(int np, long long total, const long long *P, const int *perm,
                                const double *Dp, const double *Q, long long ldq, double *const *Z,
-                               const long long *ldz, double *const *W, cudaStream_t st) {
+                               const long long *ldz, double *const *W, cudaStream_t st,
+                               const int2 *sup) {
   if (np > 0 && total > 0)
-    k_final_gather_batch<<<(unsigned)total, 256, 0, st>>>(np, P, perm, Dp, Q, ldq, Z, ldz, W);
+    k_final_gather_batch<<<(unsigned)total, 256, 0, st>>>(np, P, perm, Dp, Q, ldq, Z, ldz, W,
+                                                          sup);
 }
 
 }  // namespace hss
