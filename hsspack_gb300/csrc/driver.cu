@@ -337,7 +337,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 8.0 * 4.0 * k2);
   stage_begin(HSS_ST_LOWNER, st);
-  launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st);
+  launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, false,
+                *std::max_element(aK.begin(), aK.end()));
   stage_end(HSS_ST_LOWNER, st, 40LL * total, 5.0 * k2);
   c.launches += 2;
   if (bu && bu->nrest > 0) {
@@ -883,7 +884,7 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
                  (unsigned long long *)(status + 2), nullptr, st, true);
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 12.0 * 4.0 * k2);
   stage_begin(HSS_ST_LOWNER, st);
-  launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true);
+  launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true, maxK);
   stage_end(HSS_ST_LOWNER, st, 40LL * total, 8.0 * k2);
   c.launches += 2;
   // ---- dense merges (K < bsmlz): K x K U / V blocks, batched GEMMs
@@ -1163,6 +1164,7 @@ void hss_set_config(const hss_config *cfg) {
   c.cfg = *cfg;
   set_secular_terms(cfg->sec_terms);
   set_split_min_log2(cfg->split_min_log2);
+  set_small_nk(cfg->reserved[0]);
 }
 void hss_get_config(hss_config *cfg) {
   Ctx &c = ctx();

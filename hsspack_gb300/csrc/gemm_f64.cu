@@ -110,6 +110,11 @@ k_gemm_small(int nprob, const GemmDesc *__restrict__ probs, const long long *__r
   *c = P.beta ? *c + acc : acc;
 }
 
+// largest N and K taken by the element kernel (hss_config.reserved[0]; 0: 128,
+// measured faster than 64 x 64 FP64 tiles for the DC merges' K <= 128)
+static int g_small_nk = 128;
+void set_small_nk(int v) { g_small_nk = v > 0 ? v : 128; }
+
 // split-BF16 threshold (hss_config.split_min_log2): M*N*K >= 2^g_split_log2
 static int g_split_log2 = 17;
 void set_split_min_log2(int v) { g_split_log2 = v > 0 ? v : 17; }
@@ -136,9 +141,9 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
   } else {
     probs = probs_in;
   }
-  // tiny products (N, K <= 32) by the element kernel, the rest by 64 x 64 tiles
+  // small products (N, K <= g_small_nk) by the element kernel, the rest by 64 x 64 tiles
   std::vector<GemmDesc> tiny, tiled;
-  for (const auto &p : probs) (p.N <= 32 && p.K <= 32 ? tiny : tiled).push_back(p);
+  for (const auto &p : probs) (p.N <= g_small_nk && p.K <= g_small_nk ? tiny : tiled).push_back(p);
   if (!tiny.empty()) {
     std::vector<long long> eoff(1, 0);
     for (const auto &p : tiny) eoff.push_back(eoff.back() + (long long)p.M * p.N);

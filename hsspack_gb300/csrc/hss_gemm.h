@@ -31,6 +31,8 @@ void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaSt
 // FP64-accurate products on the BF16 tensor cores (digit-plane splitting);
 // d_err receives 1/2 if a bounded wait timed out.
 void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStream_t st);
+// largest N and K of the element kernel for small products (0: 128)
+void set_small_nk(int v);
 // products with M*N*K >= 2^v (and M >= 256) take the split path (0: 17)
 void set_split_min_log2(int v);
 // precision 0: FP64 CUDA cores, 1: split BF16 tensor cores

@@ -43,9 +43,11 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st,
                     bool sq = false);
+// maxk: the largest K of the launch (lanes per root as the secular kernel;
+// the default keeps a full warp per root)
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
                    const double *difr, const double *zw, double *zhat, cudaStream_t st,
-                   bool sq = false);
+                   bool sq = false, int maxk = 1 << 30);
 void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
                   const double *difr, const double *zhat, double *alpha, cudaStream_t st,
                   bool sq = false);

@@ -317,21 +317,27 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
 //   Singular-value mode (sq): z_hat_i^2 = prod_j (sigma_j^2 - d_i^2) /
 // prod_{j != i} (d_j^2 - d_i^2) (the z recomputation of DLASD3 / MDLASD8), every
 // factor formed as a product of a difference and a sum.
+template <int L>
 __global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
                          const double *__restrict__ difl, const double *__restrict__ difr,
                          const double *__restrict__ zw, double *__restrict__ zhat, bool sq) {
-  const int lane = threadIdx.x & 31;
-  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= __ldg(lv.rootoff + lv.P)) return;
-  const int m = find_merge(lv.rootoff, lv.P, r);
-  const int i = r - __ldg(lv.rootoff + m);
-  const int s = __ldg(lv.s + m);
-  const int K = __ldg(lv.K + m);
+  // one root per group of L lanes (as the secular kernel); every lane of the
+  // warp takes part in the group shuffles
+  const int lane = threadIdx.x & 31, gl = lane & (L - 1);
+  const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
+  const bool valid = r < __ldg(lv.rootoff + lv.P);
+  int i = 0, s = 0, K = 0;
+  if (valid) {
+    const int m = find_merge(lv.rootoff, lv.P, r);
+    i = r - __ldg(lv.rootoff + m);
+    s = __ldg(lv.s + m);
+    K = __ldg(lv.K + m);
+  }
   PoleDiff P{dl + s, difl + s, difr + s, sq};
-  const double di = __ldg(dl + s + i);
+  const double di = valid ? __ldg(dl + s + i) : 0.0;
   double num = 1.0, den = 1.0;
   int en = 0, ed = 0, cnt = 0;
-  for (int j = lane; j < K; j += HSS_WARP) {
+  for (int j = gl; j < K; j += L) {
     num *= P.fd(i, j);
     if (j != i) {
       const double dj = __ldg(dl + s + j);
@@ -350,7 +356,7 @@ __global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
     den = frexp(den, &e); ed += e;
   }
 #pragma unroll
-  for (int ofs = 16; ofs > 0; ofs >>= 1) {
+  for (int ofs = L / 2; ofs > 0; ofs >>= 1) {
     double on = __shfl_xor_sync(HSS_FULL, num, ofs);
     double od = __shfl_xor_sync(HSS_FULL, den, ofs);
     int oen = __shfl_xor_sync(HSS_FULL, en, ofs);
@@ -359,7 +365,7 @@ __global__ void k_lowner(LevelView lv, const double *__restrict__ dl,
     num = frexp(num * on, &e); en += oen + e;
     den = frexp(den * od, &e); ed += oed + e;
   }
-  if (lane == 0) {
+  if (valid && gl == 0) {
     const double q = ldexp(fabs(num / den), en - ed);
     zhat[s + i] = copysign(sqrt(q), __ldg(zw + s + i));
   }
@@ -574,10 +580,19 @@ void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *
 }
 
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,
-                   const double *difr, const double *zw, double *zhat, cudaStream_t st, bool sq) {
+                   const double *difr, const double *zw, double *zhat, cudaStream_t st, bool sq,
+                   int maxk) {
   if (total <= 0) return;
-  const int tb = root_block((long long)total * 32);
-  k_lowner<<<warp_grid(total, tb), tb, 0, st>>>(lv, dl, difl, difr, zw, zhat, sq);
+  int L = 1;
+  while (L < 32 && L * g_sec_terms < maxk) L *= 2;
+  const int tb = root_block((long long)total * L);
+  const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
+  switch (L) {
+#define LOW_CASE(LL) \
+  case LL: k_lowner<LL><<<grid, tb, 0, st>>>(lv, dl, difl, difr, zw, zhat, sq); break;
+    LOW_CASE(1) LOW_CASE(2) LOW_CASE(4) LOW_CASE(8) LOW_CASE(16) LOW_CASE(32)
+#undef LOW_CASE
+  }
 }
 void launch_alpha(const LevelView &lv, int total, const double *dl, const double *difl,
                   const double *difr, const double *zhat, double *alpha, cudaStream_t st,
