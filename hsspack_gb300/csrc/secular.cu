@@ -271,7 +271,15 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
   while (__any_sync(HSS_FULL, st.phase != 2)) {
     const SecSums sm = sec_eval<L, SQ>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.oi, st.tau, st.jl,
                                        gl);
-    root_step(st, sm);
+    // the scalar step runs on the group's first lane only (FP64 issue slots
+    // are scarce on this part); the others receive what the next pole sums need
+    if (L == 1 || gl == 0) root_step(st, sm);
+    if (L > 1) {
+      const int lead = lane & ~(L - 1);
+      st.tau = __shfl_sync(HSS_FULL, st.tau, lead);
+      st.oi = __shfl_sync(HSS_FULL, st.oi, lead);
+      st.phase = __shfl_sync(HSS_FULL, st.phase, lead);
+    }
   }
   if (valid && gl == 0) {
     double lm, dfl, dfr;
