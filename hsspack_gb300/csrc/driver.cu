@@ -417,7 +417,13 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   }
   // ---- new ascending order and eigenvalues of the rewritten slots
   stage_begin(HSS_ST_FINISH, st);
-  launch_merge_finish(PA, maxn, vs, vn, vK, L.lam, L.w, perm, Dp, st);
+  {
+    std::vector<int> apoff(PA + 1, 0);
+    for (int a = 0; a < PA; ++a) apoff[a + 1] = apoff[a] + an[a];
+    int *dapo = buf<int>(c, "a_poff", PA + 1);
+    h2d(dapo, apoff, st);
+    launch_merge_finish_grid(PA, apoff[PA], dapo, vs, vK, L.lam, L.w, perm, Dp, st);
+  }
   {
     long long nn = 0;
     for (int x : an) nn += x;

@@ -100,6 +100,11 @@ void launch_widen(int P, int maxn, const int *ms, const int *mn, const int *ng,
                   const LevelScratch &w, double *Q, long long ldq, int2 *sup, cudaStream_t st);
 void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const int *mK, const double *lam,
                          const LevelScratch &w, int *perm, double *Dp, cudaStream_t st);
+// the finish of all merges with one thread per position (poff: prefix of the
+// merges' sizes, P + 1 entries)
+void launch_merge_finish_grid(int P, int total, const int *poff, const int *ms, const int *mK,
+                              const double *lam, const LevelScratch &w, int *perm, double *Dp,
+                              cudaStream_t st);
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st,
                          const int2 *sup = nullptr);

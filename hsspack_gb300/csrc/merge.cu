@@ -151,8 +151,11 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
       for (int t = 1; t < nc; ++t) {
         const int nj = t;
         const double zp = c_z[pj], zn = c_z[nj];
-        const double tau = hypot(zn, zp);
         const double tt = c_d[nj] - c_d[pj];
+        // |tt c s| = |tt zn zp| / (zn^2 + zp^2): pairs clearly above tol skip the
+        // hypot and divides of the exact test (decisions unchanged)
+        if (fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp)) { pj = nj; continue; }
+        const double tau = hypot(zn, zp);
         const double c = zn / tau, sn = -zp / tau;
         if (fabs(tt * c * sn) <= tol) {
           c_z[nj] = tau;
@@ -175,8 +178,9 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
       for (int t = 1; t < nc; ++t) {
         const int nj = w.cand[s + t];
         const double zp = w.zs[s + pj], zn = w.zs[s + nj];
-        const double tau = hypot(zn, zp);
         const double tt = w.ds[s + nj] - w.ds[s + pj];
+        if (fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp)) { pj = nj; continue; }
+        const double tau = hypot(zn, zp);
         const double c = zn / tau, sn = -zp / tau;
         if (fabs(tt * c * sn) <= tol) {
           w.zs[s + nj] = tau;
@@ -445,6 +449,36 @@ k_merge_finish(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   }
 }
 
+// The finish of all merges of a level with one thread per position
+// (positions of merge m: poff[m] .. poff[m+1]-1, its first K[m] the new roots):
+// the same ascending order as k_merge_finish, without one CTA per merge
+// serialising the top levels.
+__global__ void k_merge_finish_grid(int P, const int *__restrict__ poff, const int *__restrict__ ms,
+                                    const int *__restrict__ mK, const double *__restrict__ lam,
+                                    const LevelScratch w, int *__restrict__ perm,
+                                    double *__restrict__ Dp) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= poff[P]) return;
+  int lo = 0, hi = P;
+  while (hi - lo > 1) { const int md = (lo + hi) >> 1; if (poff[md] <= t) lo = md; else hi = md; }
+  const int m = lo, i = t - poff[m];
+  const int s = ms[m], K = mK[m], nd = poff[m + 1] - poff[m] - K;
+  if (i < K) {  // new root: count deflated values below it
+    const double a = lam[s + i];
+    int a0 = 0, b0 = nd;
+    while (a0 < b0) { const int md = (a0 + b0) >> 1; if (w.dfval[s + md] < a) a0 = md + 1; else b0 = md; }
+    const int slot = w.ndslot[s + i];
+    perm[s + i + a0] = slot;
+    Dp[slot] = a;
+  } else {      // deflated: count roots at or below it
+    const int j = i - K;
+    const double b = w.dfval[s + j];
+    int a0 = 0, b0 = K;
+    while (a0 < b0) { const int md = (a0 + b0) >> 1; if (lam[s + md] <= b) a0 = md + 1; else b0 = md; }
+    perm[s + j + a0] = w.dfslot[s + j];
+  }
+}
+
 // Final column permutation (mdlaed0.f90:355-362): Z(:, i) = Q(:, perm(i)),
 // w(i) = Dp(perm(i)).  One CTA per column.
 __global__ void k_final_gather(int n, const int *__restrict__ perm, const double *__restrict__ Dp,
@@ -603,6 +637,12 @@ void launch_merge_finish(int P, int maxn, const int *ms, const int *mn, const in
     case 256: k_merge_finish<256><<<P, 256, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp); break;
     default: k_merge_finish<512><<<P, 512, 0, st>>>(P, ms, mn, mK, lam, w, perm, Dp); break;
   }
+}
+void launch_merge_finish_grid(int P, int total, const int *poff, const int *ms, const int *mK,
+                              const double *lam, const LevelScratch &w, int *perm, double *Dp,
+                              cudaStream_t st) {
+  if (P > 0 && total > 0)
+    k_merge_finish_grid<<<(total + 255) / 256, 256, 0, st>>>(P, poff, ms, mK, lam, w, perm, Dp);
 }
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st,
