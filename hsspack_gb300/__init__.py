@@ -99,6 +99,11 @@ SIGNATURES = {
     "hss_cauchyhssmm_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, ctypes.c_int,
                                            ctypes.c_double, _V, ctypes.c_int, ctypes.c_int, _V,
                                            _V]),
+    "dhssmm_": (None, [_D, _I, _I, _I, _D, _I, _I, _D, _I, _I, _I, _D, _I]),
+    "dhssmml_": (None, [_D, _I, _I, _I, _D, _I, _I, _D, _I, _I, _I, _D, _I]),
+    "hss_dhssmm_dev": (ctypes.c_int, [ctypes.c_int, _V, ctypes.c_int, _V, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      _V, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
@@ -361,6 +366,55 @@ def cauchyhssmm_dev(D, F, u, v, B, ni, tol, stream=None):
                                     _stream(stream))
     if rc != 0:
         raise HssError("hss_cauchyhssmm_dev rc=%d: %s" % (rc, _err()))
+    return t[0], t[1]
+
+
+def _dhssmm_call(fn, A, B, ni, tol, prank, ncol, m=None):
+    if A.dtype != np.float64 or not A.flags.f_contiguous:
+        raise ValueError("A must be a Fortran-ordered float64 array")
+    if B.dtype != np.float64 or not B.flags.f_contiguous:
+        raise ValueError("B must be a Fortran-ordered float64 array")
+    n = A.shape[1]
+    k = B.shape[1] if fn == "dhssmm_" else B.shape[0]
+    if fn == "dhssmml_" and B.shape[1] < n:
+        raise ValueError("DHSSMML: B must have N columns")
+    t = np.zeros(2)
+    info = ctypes.c_int(0)
+    ints = [ctypes.c_int(int(x)) for x in (A.shape[0], n if m is None else m, n, B.shape[0], k,
+                                           prank, ni, ncol)]
+    getattr(load(), fn)(_pd(A), ctypes.byref(ints[0]), ctypes.byref(ints[1]),
+                        ctypes.byref(ints[2]), _pd(B), ctypes.byref(ints[3]),
+                        ctypes.byref(ints[4]), ctypes.byref(ctypes.c_double(tol)),
+                        ctypes.byref(ints[5]), ctypes.byref(ints[6]), ctypes.byref(ints[7]),
+                        _pd(t), ctypes.byref(info))
+    return info.value, t
+
+
+def dhssmm(A, B, ni, tol, prank=0, ncol=100, m=None):
+    """DHSSMM (SRC/DHSSMM.f90:1): B(n x k) <- A_hss B in place (A, B
+    Fortran-ordered float64; A is not modified).  Returns (INFO, time(1:2))."""
+    return _dhssmm_call("dhssmm_", A, B, ni, tol, prank, ncol, m)
+
+
+def dhssmml(A, B, ni, tol, prank=0, ncol=100, m=None):
+    """DHSSMML (SRC/DHSSMML.f90:2): B(k x n) <- B A_hss in place.  Returns
+    (INFO, time(1:2))."""
+    return _dhssmm_call("dhssmml_", A, B, ni, tol, prank, ncol, m)
+
+
+def dhssmm_dev(A, B, ni, tol, side=0, stream=None):
+    """Device DHSSMM (side 0: B (n x k) <- A_hss B) or DHSSMML (side 1: B (k x n)
+    <- B A_hss).  A: tensor whose memory is column-major n x n; B: column-major
+    with leading dimension n (side 0) or k (side 1).  Returns (construction ms,
+    multiply ms)."""
+    n = int(round(A.numel() ** 0.5))
+    k = B.numel() // max(n, 1)
+    t = (ctypes.c_float * 2)()
+    rc = load().hss_dhssmm_dev(n, _ptr(A), max(1, n), _ptr(B), max(1, n if side == 0 else k), k,
+                               float(tol), int(ni), int(side), ctypes.cast(t, ctypes.c_void_p),
+                               _stream(stream))
+    if rc != 0:
+        raise HssError("hss_dhssmm_dev rc=%d: %s" % (rc, _err()))
     return t[0], t[1]
 
 

@@ -1712,6 +1712,94 @@ void cauchyhssmm_(const double *D, const double *F, const double *U, const doubl
   }
 }
 
+int hss_dhssmm_dev(int n, const double *A, int lda, double *B, int ldb, int k, double tol, int ni,
+                   int side, float *times, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  if (lda < std::max(1, n)) return -3;
+  if (ldb < std::max(1, side == 0 ? n : k)) return -5;
+  if (k < 0) return -6;
+  if (ni < 1) return -8;
+  if (side != 0 && side != 1) return -9;
+  if (n == 0 || k == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    int rank = 0;
+    hss_dhssmm_core(n, A, lda, B, ldb, k, tol, ni, side, c.cfg.precision, &rank, times, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    c.stats.max_rank = rank;
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+// DHSSMM (side 0) and DHSSMML (side 1) with host arrays.  INFO numbering
+// follows the argument list A,LDA,M,N,B,LDB,K,tol,prank,ni,ncol,time,info.
+static void dhssmm_host(int side, const double *A, int lda, int m, int n, double *B, int ldb,
+                        int k, double tol, int ni, int ncol, double *time, int *info) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  *info = 0;
+  if (n < 0) *info = -4;
+  else if (m != n) *info = -3;
+  else if (lda < std::max(1, n)) *info = -2;
+  else if (ldb < std::max(1, side == 0 ? n : k)) *info = -6;
+  else if (k < 0) *info = -7;
+  else if (ni < 1) *info = -10;
+  else if (ncol < 1) *info = -11;
+  if (time) { time[0] = 0.0; time[1] = 0.0; }
+  if (*info != 0) {
+    c.err = side == 0 ? "DHSSMM: bad argument" : "DHSSMML: bad argument";
+    return;
+  }
+  if (n == 0 || k == 0) return;
+  try {
+    cudaStream_t st = nullptr;
+    const int br = side == 0 ? n : k, bc = side == 0 ? k : n;
+    double *dA = buf<double>(c, "hm_A", (size_t)n * n);
+    double *dB = buf<double>(c, "hm_B", (size_t)br * bc);
+    CK(cudaMemcpy2DAsync(dA, sizeof(double) * n, A, sizeof(double) * lda, sizeof(double) * n, n,
+                         cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpy2DAsync(dB, sizeof(double) * br, B, sizeof(double) * ldb, sizeof(double) * br, bc,
+                         cudaMemcpyHostToDevice, st));
+    int rank = 0;
+    float t[2] = {0.f, 0.f};
+    hss_dhssmm_core(n, dA, n, dB, br, k, tol, ni, side, c.cfg.precision, &rank, t, st);
+    CK(cudaMemcpy2DAsync(B, sizeof(double) * ldb, dB, sizeof(double) * br, sizeof(double) * br, bc,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c.stats.max_rank = rank;
+    if (time) { time[0] = 1e-3 * t[0]; time[1] = 1e-3 * t[1]; }
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    *info = 1000001;
+  }
+}
+
+void dhssmm_(const double *A, const int *lda, const int *m, const int *n, double *B, const int *ldb,
+             const int *k, const double *tol, const int *prank, const int *ni, const int *ncol,
+             double *time, int *info) {
+  (void)prank;  // declared but not read by the reference's construction
+  dhssmm_host(0, A, *lda, *m, *n, B, *ldb, *k, *tol, *ni, *ncol, time, info);
+}
+
+void dhssmml_(const double *A, const int *lda, const int *m, const int *n, double *B, const int *ldb,
+              const int *k, const double *tol, const int *prank, const int *ni, const int *ncol,
+              double *time, int *info) {
+  (void)prank;
+  dhssmm_host(1, A, *lda, *m, *n, B, *ldb, *k, *tol, *ni, *ncol, time, info);
+}
+
 int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B, int ldb,
                  double *C, int ldc, int beta, int precision, void *stream) {
   Ctx &c = ctx();

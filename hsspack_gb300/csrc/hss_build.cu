@@ -26,6 +26,7 @@
 #include "hss_common.cuh"
 #include "hss_gemm.h"
 #include "hss_hss.h"
+#include "hss_plan.h"
 #include "hss_kernels.h"
 #include "hss_pool.h"
 #include "../../include/hsspack_gb300.h"
@@ -42,16 +43,6 @@ constexpr int HT = 256;        // threads per node CTA
 constexpr int HSS_RMIN = 256;  // rank capacity floor
 
 // ------------------------------------------------------------- host tree --
-// npart / n2tree / GetTreeInfo (SRC/aux_hss.f90:238-307, :737-827): nodes
-// 1..ltr in post order, parent[root] = 0, depth[root] = 0.
-struct HostTree {
-  int lm = 0, ltr = 0, lvl = 0, mmax = 0;
-  std::vector<int> m, parent, c1, c2, depth, leafstart;
-  std::vector<std::vector<int>> ttr;
-  bool leaf(int i) const { return c1[i] == 0 && c2[i] == 0; }
-  int sibling(int i) const { int p = parent[i]; return c1[p] == i ? c2[p] : c1[p]; }
-};
-
 static void perfect_tree(int n, int off, std::vector<int> &par) {
   if (n == 1) { par[off + 1] = 0; return; }
   int h = (n - 1) / 2;
@@ -69,7 +60,7 @@ static void n2tree(int n, int off, std::vector<int> &par) {
   par[off + n1] = off + n; par[off + n - 1] = off + n; par[off + n] = 0;
 }
 
-static HostTree make_tree(int K, int ni) {
+HostTree make_tree(int K, int ni) {
   HostTree t;
   int lm = K / ni, mr = K % ni;
   if (lm == 0) { lm = 1; t.m.assign(1, K); }
@@ -117,27 +108,6 @@ __device__ __forceinline__ double warp_prod(double v) {
   for (int o = 16; o > 0; o >>= 1) v *= __shfl_xor_sync(HSS_FULL, v, o);
   return v;
 }
-
-// Node state shared by the row and column kernels.
-struct HssDev {
-  const double *FF, *DIFL, *DIFR;  // poles and root gaps (length K)
-  bool sq;                         // singular-value mode (differences of squares)
-  int K, ltr, rmax;
-  // current compressed generators (row side: U, PL; column side: V, PU)
-  double *U, *V;
-  int *PL, *PU;
-  double *Ut, *Vt;  // compaction temporaries
-  int *PLt, *PUt;
-  int *lr0, *lr1, *lc0, *lc1;    // per node ranges in the current arrays
-  int *Ur, *Uc, *Vr, *Vc, *Br, *Bc, *Dm;
-  double *Ug, *Vg, *Bg, *Dg;     // generator storage
-  long long ucap, vcap, bcap;    // per node capacity (doubles)
-  const long long *doff;         // leaf diagonal block offsets
-  double *oval;                  // per node "other side" scratch (values)
-  int *oidx;                     //                              (pole indices)
-  int *lda, *lca;                // current row / column counts
-  int *flag;                     // [0]: rank overflow, [1]: swap count
-};
 
 // Structured strong RRLU of one node (row or column case).  Node side (length
 // M) in shared memory, other side (length N) in global scratch.
@@ -577,15 +547,6 @@ static T *up(const char *name, const std::vector<T> &v, cudaStream_t st) {
   return d;
 }
 
-struct HssPlan {
-  HostTree t;
-  HssDev h;
-  std::vector<int> Uc, Ur, Vr, Vc, Br, Bc, Dm;
-  std::vector<long long> doff;
-  bool ok = true;
-  int max_rank = 0;
-};
-
 // Build the HSS generators on the device; on return the ranks are on the host.
 static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F, const double *u,
                          const double *v, const double *difl, const double *difr, cudaStream_t st,
@@ -690,9 +651,8 @@ static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F
 }
 
 // Y (nrows x K, ldy) = X (nrows x K, ldx) * H, FP64 grouped GEMMs per level.
-static int hss_multiply(const HssPlan &pl, const double *X, long long ldx, int nrows, double *Y,
-                        long long ldy, int precision, cudaStream_t st, double *flops = nullptr,
-                        long long *bytes = nullptr) {
+int hss_multiply(const HssPlan &pl, const double *X, long long ldx, int nrows, double *Y,
+                 long long ldy, int precision, cudaStream_t st, double *flops, long long *bytes) {
   const HostTree &t = pl.t;
   const HssDev &h = pl.h;
   const int ltr = t.ltr;
@@ -899,8 +859,8 @@ __global__ void k_transpose(int rows, int cols, const double *__restrict__ In, l
   }
 }
 
-static void transpose(int rows, int cols, const double *In, long long ldi, double *Out,
-                      long long ldo, cudaStream_t st) {
+void transpose(int rows, int cols, const double *In, long long ldi, double *Out, long long ldo,
+               cudaStream_t st) {
   dim3 g((rows + 31) / 32, (cols + 31) / 32);
   k_transpose<<<g, dim3(32, 8), 0, st>>>(rows, cols, In, ldi, Out, ldo);
 }

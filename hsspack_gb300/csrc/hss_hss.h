@@ -55,4 +55,13 @@ int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, 
                      const double *v, const double *difl, const double *difr, double *Q,
                      long long ldq, int nrows, int *rank, cudaStream_t st);
 
+// DHSSMM / DHSSMML on device arrays (mat2hss.cu): A (n x n, lda) compressed to
+// HSS by truncated SVD (leaf ni, absolute tolerance tol); side 0: B (n x k,
+// ldb) <- A_hss B; side 1: B (k x n, ldb) <- B A_hss.  times[0..1]:
+// construction / multiplication (ms); *rank: largest HSS rank (n if a node
+// outgrew the compression kernels and A was applied densely).
+int hss_dhssmm_core(int n, const double *A, long long lda, double *B, long long ldb, int k,
+                    double tol, int ni, int side, int precision, int *rank, float *times,
+                    cudaStream_t st);
+
 }  // namespace hss

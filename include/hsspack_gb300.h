@@ -100,6 +100,27 @@ void cauchyhssmm_(const double *D, const double *F, const double *U, const doubl
                   const int *n, const int *ni, const double *tol, const int *ncol, double *B,
                   const int *ldb, double *time);
 
+/* DHSSMM(A,LDA,M,N,B,LDB,K,tol,prank,ni,ncol,time,info) replaces
+ * SRC/DHSSMM.f90:1-125: B(1:N, 1:K) <- A_hss * B, where A_hss is the HSS
+ * approximation of the dense N x N matrix A built by truncated SVDs of its
+ * block rows and columns (mat2hssvd, SRC/ConstructHssd.f90:371: leaf size ni,
+ * singular values above the absolute tolerance tol kept).  M must equal N (the
+ * reference assumes LDA = M = N).  A is not modified (the reference uses it as
+ * workspace).  prank is accepted and ignored, as by the reference's
+ * construction; ncol (the reference's panel width) must be >= 1 and is
+ * otherwise ignored (all K columns in one pass).  time(1) / time(2): seconds of
+ * construction / multiplication.  INFO = -i for a bad i-th argument,
+ * 1000000 / 1000001 for a CUDA / construction failure (hss_last_error()). */
+void dhssmm_(const double *A, const int *lda, const int *m, const int *n, double *B,
+             const int *ldb, const int *k, const double *tol, const int *prank,
+             const int *ni, const int *ncol, double *time, int *info);
+
+/* DHSSMML(...) replaces SRC/DHSSMML.f90:2-122: B(1:K, 1:N) <- B * A_hss
+ * (B is K x N, LDB >= K); otherwise as DHSSMM. */
+void dhssmml_(const double *A, const int *lda, const int *m, const int *n, double *B,
+              const int *ldb, const int *k, const double *tol, const int *prank,
+              const int *ni, const int *ncol, double *time, int *info);
+
 /* Largest band half-width of the banded divide and conquer (leaves of up to
  * 2 kd rows are solved by one warp each). */
 #define HSS_BAND_KD_MAX 32
@@ -198,6 +219,15 @@ int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u,
 int hss_cauchyhssmm_dev(int n, const double *D, const double *F, const double *u,
                         const double *v, int ni, double tol, double *B, int ldb, int ncb,
                         float *times, void *stream);
+
+/* DHSSMM / DHSSMML on device arrays: A (n x n, lda) compressed to HSS (leaf
+ * ni, tolerance tol; A is read only); side 0: B (n x k, ldb) <- A_hss B,
+ * side 1: B (k x n, ldb) <- B A_hss.  times[0..1] (may be NULL): construction
+ * / multiply milliseconds; hss_get_stats()->max_rank: the largest HSS rank (n
+ * when a node dimension exceeded 128 and A was applied as a dense product).
+ * Returns 0, -i for a bad i-th argument, or 1000000 / 1000001. */
+int hss_dhssmm_dev(int n, const double *A, int lda, double *B, int ldb, int k, double tol,
+                   int ni, int side, float *times, void *stream);
 
 /* Dense Cauchy-like eigenvector block C(i,j) = u_i v_j / (F_i - lam_j) through
  * DIFL/DIFR (SRC/CauchyHssEig.f90:1688, CauchylikeEig), k-by-k column-major. */

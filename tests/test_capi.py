@@ -105,3 +105,17 @@ def test_mdsbevd_arguments_and_workspace():
     info, lw, liw = _band_call(hp.mdsbevd, "I", "U", n, 4, 5, n, -1, -1)
     assert info == 0 and lw == 1 + 4 * n + n * n and liw == 3 + 5 * n
     assert _band_call(hp.mdsbevd, "I", "U", n, 4, 5, n, 10, 10)[0] == -8
+
+
+def test_dhssmm_arguments_without_gpu():
+    # argument checks and the N = 0 quick return happen on the host
+    A = np.zeros((4, 4), order="F")
+    B = np.zeros((4, 3), order="F")
+    assert hp.dhssmm(A, B, 2, 1e-11, m=3)[0] == -3                      # M != N
+    assert hp.dhssmm(A, np.zeros((3, 2), order="F"), 2, 1e-11)[0] == -6  # LDB < N
+    assert hp.dhssmm(A, B, 0, 1e-11)[0] == -10                          # ni < 1
+    assert hp.dhssmm(A, B, 2, 1e-11, ncol=0)[0] == -11                  # ncol < 1
+    assert hp.dhssmml(A, np.zeros((3, 4), order="F"), 2, 1e-11, ncol=0)[0] == -11
+    A0 = np.zeros((1, 0), order="F")
+    B0 = np.zeros((1, 0), order="F")
+    assert hp.dhssmm(A0, B0, 2, 1e-11)[0] == 0

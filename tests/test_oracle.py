@@ -96,3 +96,23 @@ def test_band_restatement_matches_lapack(n, kd):
     assert np.max(np.abs(w - wl)) <= 1e-13 * na
     assert np.linalg.norm(A @ Q - Q * w) / (n * na) <= 1e-14
     assert np.linalg.norm(Q.T @ Q - np.eye(n)) / n <= 1e-14
+
+
+def test_hssmm_oracle_tree_and_accuracy():
+    # npart leaf sizes (SRC/aux_hss.f90:807-818) and the reference test's error
+    # level: DHSSMM / DHSSMML products within 2e-11 of the dense ones at
+    # tol = 1e-11, ni = 64 (TEST/testfmm.f90 prints this absolute error)
+    from oracle import hssmm_ref
+    assert hssmm_ref.leaf_sizes(2000, 64) == [64] * 30 + [80]
+    assert hssmm_ref.leaf_sizes(1100, 64) == [64] * 16 + [76]
+    assert hssmm_ref.leaf_sizes(100, 64) == [64, 36]
+    assert hssmm_ref.leaf_sizes(40, 64) == [40]
+    ltr, par, ch = hssmm_ref.post_order_tree(3)
+    assert ltr == 5 and par[1:] == [3, 3, 5, 5, 0]
+    n = 700
+    A = hssmm_ref.fmm_test_matrix(n)
+    B = np.random.default_rng(2).uniform(size=(n, 60))
+    Y, rank = hssmm_ref.dhssmm(A, B, 64, 1e-11)
+    assert np.abs(Y - A @ B).max() <= 2e-11 and 20 <= rank <= 45
+    Y2, _ = hssmm_ref.dhssmml(A, B.T, 64, 1e-11)
+    assert np.abs(Y2 - B.T @ A).max() <= 2e-11
