@@ -104,6 +104,7 @@ SIGNATURES = {
     "hss_dhssmm_dev": (ctypes.c_int, [ctypes.c_int, _V, ctypes.c_int, _V, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                       _V, _V]),
+    "hss_rcp_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),

@@ -1712,6 +1712,21 @@ void cauchyhssmm_(const double *D, const double *F, const double *U, const doubl
   }
 }
 
+int hss_rcp_dev(int n, const double *x, double *y, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  try {
+    launch_rcp(n, x, y, (cudaStream_t)stream);
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
 int hss_dhssmm_dev(int n, const double *A, int lda, double *B, int ldb, int k, double tol, int ni,
                    int side, float *times, void *stream) {
   Ctx &c = ctx();

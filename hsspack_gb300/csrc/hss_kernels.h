@@ -60,6 +60,9 @@ void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
 void launch_cauchylike(int M, int N, const double *D, const double *F, const double *u,
                        const double *v, double *A, cudaStream_t st);
 
+// the reciprocal of the pole sums (rcp_nr), for its accuracy test
+void launch_rcp(int n, const double *x, double *y, cudaStream_t st);
+
 // leaf.cu
 void launch_leaf(int nleaf, const int *lstart, const int *lsize, int mmax, int nblk,
                  const double *d, const double *e, double *Q, long long ldq, double *Dp, int *perm,

@@ -49,7 +49,7 @@ __device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
     const double zi = __ldg(z + i);
     const double di = __ldg(d + i);
     const double del = (SQ ? (di - o) * (di + o) : (di - o)) - tau;
-    const double t = zi / del;
+    const double t = zi * rcp_nr(del);
     const double v = zi * t;
     const double dv = t * t;
     if (i <= jl) { a0 += v; a1 += dv; } else { b0 += v; b1 += dv; }
@@ -393,7 +393,7 @@ __global__ void k_alpha(LevelView lv, const double *__restrict__ dl,
   PoleDiff P{dl + s, difl + s, difr + s, sq};
   double acc = 0.0;
   for (int i = lane; i < K; i += HSS_WARP) {
-    const double w = __ldg(zhat + s + i) / P.fd(i, j);
+    const double w = __ldg(zhat + s + i) * rcp_nr(P.fd(i, j));
     acc += w * w;
   }
   acc = warp_sum(acc);
@@ -424,7 +424,7 @@ __global__ void k_build_S(LevelView lv, const double *__restrict__ dl,
   PoleDiff P{dl + s, difl + s, difr + s};
   double acc = 0.0;
   for (int i = lane; i < K; i += HSS_WARP) {
-    const double w = __ldg(zhat + s + i) / P.fd(i, j);
+    const double w = __ldg(zhat + s + i) * rcp_nr(P.fd(i, j));
     S[__ldg(grp + s + i)] = w;
     acc += w * w;
   }
@@ -621,6 +621,13 @@ void launch_cauchy_eig(int K, const double *F, const double *u, const double *v,
   const long long tot = (long long)K * K;
   if (tot <= 0) return;
   k_cauchy_eig<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(K, F, u, v, difl, difr, C, sq);
+}
+__global__ void k_rcp(int n, const double *__restrict__ x, double *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = rcp_nr(x[i]);
+}
+void launch_rcp(int n, const double *x, double *y, cudaStream_t st) {
+  if (n > 0) k_rcp<<<(n + 255) / 256, 256, 0, st>>>(n, x, y);
 }
 void launch_cauchylike(int M, int N, const double *D, const double *F, const double *u,
                        const double *v, double *A, cudaStream_t st) {

@@ -235,6 +235,12 @@ int hss_cauchy_eig_dev(int k, const double *F, const double *u, const double *v,
                        const double *difl, const double *difr, double *C,
                        void *stream);
 
+/* Diagnostic (no counterpart in the reference): y[i] = 1 / x[i] by the
+ * reciprocal the secular pole sums and the eigenvector blocks use instead of
+ * a correctly rounded divide (two Newton-Raphson steps from the hardware
+ * estimate; within a few ulp for normal x), so its accuracy can be checked. */
+int hss_rcp_dev(int n, const double *x, double *y, void *stream);
+
 /* C(m x n, ldc) = A(m x k, lda) * B(k x n, ldb) [+ C if beta != 0], FP64
  * column-major device arrays; precision 0 = FP64 CUDA cores, 1 = split-BF16
  * tensor cores (6 digit planes, FP64-accurate to ~3.5e-15 relative).  The
