@@ -1170,7 +1170,8 @@ void hss_set_config(const hss_config *cfg) {
   c.cfg = *cfg;
   set_secular_terms(cfg->sec_terms);
   set_split_min_log2(cfg->split_min_log2);
-  set_small_nk(cfg->reserved[0]);
+  set_small_nk(cfg->small_nk);
+  set_split_min_m(cfg->split_min_m);
 }
 void hss_get_config(hss_config *cfg) {
   Ctx &c = ctx();

@@ -110,14 +110,17 @@ k_gemm_small(int nprob, const GemmDesc *__restrict__ probs, const long long *__r
   *c = P.beta ? *c + acc : acc;
 }
 
-// largest N and K taken by the element kernel (hss_config.reserved[0]; 0: 128,
+// largest N and K taken by the element kernel (hss_config.small_nk; 0: 128,
 // measured faster than 64 x 64 FP64 tiles for the DC merges' K <= 128)
 static int g_small_nk = 128;
 void set_small_nk(int v) { g_small_nk = v > 0 ? v : 128; }
 
-// split-BF16 threshold (hss_config.split_min_log2): M*N*K >= 2^g_split_log2
+// split-BF16 thresholds (hss_config.split_min_log2, split_min_m):
+// M*N*K >= 2^g_split_log2 and M >= g_split_m
 static int g_split_log2 = 17;
 void set_split_min_log2(int v) { g_split_log2 = v > 0 ? v : 17; }
+static int g_split_m = 256;
+void set_split_min_m(int v) { g_split_m = v > 0 ? v : 256; }
 
 void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaStream_t st) {
   if (nprob <= 0 || total_tiles <= 0) return;
@@ -132,7 +135,7 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
     // operand byte; small products stay on the FP64 pipe
     std::vector<GemmDesc> big;
     for (const auto &p : probs_in) {
-      if ((double)p.M * p.N * p.K >= ldexp(1.0, g_split_log2) && p.M >= 256) big.push_back(p);
+      if ((double)p.M * p.N * p.K >= ldexp(1.0, g_split_log2) && p.M >= g_split_m) big.push_back(p);
       else probs.push_back(p);
     }
     int *err = pool<int>("gemm_err", 1);

@@ -5,20 +5,22 @@
 // matrix multiplication by using fast routines of matrix multiplication and
 // its applications", Numer. Algorithms 59, 2012):
 //
-//   A_ik = 2^{e_i} sum_{s<S} a^s_ik 2^{-8(s+1)},  B_kj = 2^{f_j} sum_{t<S} b^t_kj 2^{-8(t+1)}
+//   A_ik = 2^{e_i - 60} sum_{s<S} a^s_ik 2^{53 - 8s},  B_kj likewise with f_j,
 //
-// with integer digits |a^s|, |b^t| <= 256 (exact in BF16), e_i / f_j the row /
-// column exponents.  Digit products are integers; for a group g = s + t the
-// partial sums over a K window of 128 stay below 2^24 for g <= 2, so the FP32
-// tensor-core accumulation is exact there; groups g >= 3 weigh <= 2^-24
-// relative and their FP32 rounding is below FP64 resolution.  The S(S+1)/2
-// digit-plane products with s + t < S are accumulated per group in TMEM and
-// folded into FP64 registers after each window:
+// e_i / f_j the row / column exponents (|A_ik| <= 2^{e_i}), so the scaled
+// value is below 2^60 and every rounded digit satisfies |a^s|, |b^t| <= 128
+// (exact in BF16).  Digit products are integers below 2^14; group g = s + t
+// has g + 1 of them per k, so its partial sums over a K window of 128 stay
+// below (g + 1) 2^21 < 2^24 for every g < S = 7: the FP32 tensor-core
+// accumulation in TMEM is exact for all groups.  After each window the group
+// sums are folded into two exact int64 accumulators per output,
 //
-//   C_ij = 2^{e_i + f_j} sum_g acc_g 2^{-8(g+2)}
+//   H = acc_0 2^16 + acc_1 2^8 + acc_2,   L = acc_3 2^24 + acc_4 2^16 + acc_5 2^8 + acc_6,
 //
-// S = 6 digit planes give 48 significant bits (relative error ~2^-48 of
-// sum_k |A_ik||B_kj| bounds, i.e. ~3.5e-15).
+// and the epilogue forms C_ij = 2^{e_i + f_j - 30} (H + 2^-32 L) with one FP64
+// fma: the main loop issues no FP64 instruction (the FP64 pipe is the scarce
+// unit on this part).  S = 7 planes carry 56 bits; the products dropped
+// (s + t >= 7) weigh below 2^-56 of sum_k |A_ik||B_kj|.
 //
 // Kernels: k_split_a / k_split_b write the digit planes pre-tiled in the
 // tcgen05 shared-memory image (K-major, no swizzle, 8x16-byte core matrices),
@@ -38,7 +40,7 @@
 
 namespace hss {
 
-constexpr int SP = 6;        // digit planes
+constexpr int SP = 7;        // digit planes
 constexpr int TM = 128;      // output tile rows (tcgen05 M)
 constexpr int TN = 64;       // output tile cols (tcgen05 N)
 constexpr int TK = 64;       // K per staged chunk
@@ -56,10 +58,10 @@ __device__ __forceinline__ int tile_off(int r, int k, int R) {
 }
 
 __device__ __forceinline__ void split_digits(double x, double scale, __nv_bfloat16 *dig) {
-  long long q = __double2ll_rn(x * scale);  // |q| < 2^62
+  long long q = __double2ll_rn(x * scale);  // |q| <= 2^60
 #pragma unroll
   for (int s = 0; s < SP; ++s) {
-    const int sh = 54 - 8 * s;
+    const int sh = 53 - 8 * s;
     const long long d = (q + (1ll << (sh - 1))) >> sh;
     q -= d << sh;
     dig[s] = __float2bfloat16_rn((float)d);
@@ -97,7 +99,7 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
     const int e = exp_of(m);
     const int r = tm * TM + tid;
     if (r < P.rows) P.expo[r] = e;
-    sscale[tid] = ldexp(1.0, 62 - e);
+    sscale[tid] = ldexp(1.0, 60 - e);
   }
   __syncthreads();
   // pass 2: thread handles (row, 8 consecutive k) -> 16-byte rows of core matrices
@@ -139,7 +141,7 @@ __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
     if (lane == 0) {
       const int e = exp_of(m);
       if (gc < P.rows) P.expo[gc] = e;
-      sscale[c] = ldexp(1.0, 62 - e);
+      sscale[c] = ldexp(1.0, 60 - e);
     }
   }
   __syncthreads();
@@ -289,7 +291,9 @@ struct TcProb {
   int tile0;             // first flattened tile index
 };
 
-constexpr int GTH = 128;  // 4 warps: TMEM lanes 0..127
+// 8 warps: warp w drains TMEM lanes 32 (w % 4) .. + 31 (its row quarter) and
+// columns 32 (w / 4) .. + 31 of each group
+constexpr int GTH = 256;
 // 16 KB of slack keeps every descriptor-addressed byte inside the allocation
 constexpr int SMEM_TC = SP * ATILE + SP * BTILE + 16384;
 
@@ -328,9 +332,10 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tbase = tmem_base;
   const uint32_t idesc = make_idesc(TM, TN);
-  double acc[TN];
+  constexpr int TH = TN / 2;  // output columns per thread
+  long long hacc[TH], lacc[TH];
 #pragma unroll
-  for (int j = 0; j < TN; ++j) acc[j] = 0.0;
+  for (int j = 0; j < TH; ++j) { hacc[j] = 0; lacc[j] = 0; }
   uint32_t ph_tma = 0, ph_mma = 0;
   bool ok = true;
   const int kwin = KWIN / TK;  // chunks per exactness window
@@ -376,43 +381,37 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
     if (!ok) break;
-    // drain the group accumulators of this window.  Groups 0..2 hold exact
-    // integers (< 2^24): combine them exactly in int64; groups 3..5 weigh
-    // <= 2^-24 and are combined in FP32; one FP64 add per element:
-    //   window sum * 2^32 = (a0 2^16 + a1 2^8 + a2) + (a3 + a4 2^-8 + a5 2^-16) 2^-8
-    const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
+    // drain the group sums of this window (exact integers below 2^24) into
+    // the int64 accumulators; integer and conversion pipes only
+    const uint32_t lane_addr =
+        tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TH);
 #pragma unroll
-    for (int c = 0; c < TN; c += 16) {
-      long long hi[16];
-      float lo[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) { hi[i] = 0; lo[i] = 0.0f; }
+    for (int c = 0; c < TH; c += 16) {
 #pragma unroll
       for (int g = 0; g < SP; ++g) {
         float v[16];
         tmem_ld16(lane_addr + g * TN + c, v);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          if (g < 3) hi[i] += (long long)__float2int_rn(v[i]) << (8 * (2 - g));
-          else lo[i] = fmaf(v[i], g == 3 ? 1.0f : g == 4 ? 0x1p-8f : 0x1p-16f, lo[i]);
+          const long long x = (long long)__float2int_rn(v[i]);
+          if (g < 3) hacc[c + i] += x * (1ll << (8 * (2 - g)));
+          else lacc[c + i] += x * (1ll << (8 * (6 - g)));
         }
       }
-#pragma unroll
-      for (int i = 0; i < 16; ++i) acc[c + i] += fma((double)lo[i], 0x1p-8, (double)hi[i]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  // epilogue: C = 2^{e_i + f_j} acc (+ C)
-  const int r = tm * TM + tid;
+  // epilogue: C = 2^{e_i + f_j - 30} (H + 2^-32 L) (+ C)
+  const int r = tm * TM + (warp & 3) * 32 + (tid & 31);
   if (ok && r < P.M) {
     const int ei = P.ea[r];
 #pragma unroll
-    for (int j = 0; j < TN; ++j) {
-      const int c = tn * TN + j;
+    for (int j = 0; j < TH; ++j) {
+      const int c = tn * TN + (warp >> 2) * TH + j;
       if (c < P.N) {
-        const double v = ldexp(acc[j], ei + P.eb[c] - 32);
+        const double v = ldexp(fma((double)lacc[j], 0x1p-32, (double)hacc[j]), ei + P.eb[c] - 30);
         double *dst = P.C + (long long)c * P.ldc + r;
         *dst = P.beta ? *dst + v : v;
       }

@@ -33,8 +33,10 @@ void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaSt
 void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStream_t st);
 // largest N and K of the element kernel for small products (0: 128)
 void set_small_nk(int v);
-// products with M*N*K >= 2^v (and M >= 256) take the split path (0: 17)
+// products with M*N*K >= 2^v and M >= set_split_min_m take the split path (0: 17)
 void set_split_min_log2(int v);
+// smallest M of a split product (0: 256)
+void set_split_min_m(int v);
 // precision 0: FP64 CUDA cores, 1: split BF16 tensor cores
 void launch_gemm(const std::vector<GemmDesc> &probs, int precision, cudaStream_t st);
 

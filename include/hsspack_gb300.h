@@ -33,9 +33,12 @@ typedef struct hss_config {
   int profile;    /* 1: time every stage with CUDA events (hss_stats.stage_ms)      */
   int sec_terms;  /* secular solver: pole terms per lane (lanes per root = the    */
                   /* smallest power of two covering K / sec_terms); 0: 8        */
-  int split_min_log2; /* split-BF16 products for M*N*K >= 2^this (and M >= 256); */
-                      /* 0: 17                                                   */
-  int reserved[6];
+  int split_min_log2; /* split-BF16 products for M*N*K >= 2^this and M >=     */
+                      /* split_min_m; 0: 17                                    */
+  int small_nk;       /* FP64 products with N, K <= this on the element      */
+                      /* kernel (thread per output); 0: 128                    */
+  int split_min_m;    /* smallest M of a split-BF16 product; 0: 256            */
+  int reserved[4];
 } hss_config;
 
 /* stages timed when hss_config.profile = 1 */
@@ -243,7 +246,8 @@ int hss_rcp_dev(int n, const double *x, double *y, void *stream);
 
 /* C(m x n, ldc) = A(m x k, lda) * B(k x n, ldb) [+ C if beta != 0], FP64
  * column-major device arrays; precision 0 = FP64 CUDA cores, 1 = split-BF16
- * tensor cores (6 digit planes, FP64-accurate to ~3.5e-15 relative).  The
+ * tensor cores (7 digit planes, exact integer accumulation; error below
+ * 2^-56 of sum |A||B|).  The
  * grouped GEMM behind the dense merge update of LAPACK DLAED3 (called at
  * SRC/mdlaed1.f90:199) and the HSS multiply (SRC/ConstructHssd.f90:1394). */
 int hss_gemm_dev(int m, int n, int k, const double *A, int lda, const double *B, int ldb,

@@ -1,7 +1,11 @@
 """Grouped GEMM: FP64 CUDA-core path and the split-BF16 tensor-core path
-(6 digit planes) against numpy FP64 products.  Tolerance for the split path:
-|C - AB| <= 2^-44 * (|A| |B|)_ij elementwise bound scale (S = 6 planes give
-48 bits; 16x slack for the FP32 group accumulation and FP64 recombination)."""
+(7 digit planes, exact integer accumulation) against numpy FP64 products and,
+on a small case, against the exact rational product.  Tolerances for the
+split path: |C - AB| <= 2^-44 (|A| |B|)_ij against numpy (whose own rounding
+dominates at large k), <= 2^-50 (|A| |B|)_ij against the exact product (the
+digits keep 56 bits relative to each row's / column's largest entry)."""
+from fractions import Fraction
+
 import numpy as np
 import pytest
 import torch
@@ -60,3 +64,20 @@ def test_split_orthogonal_update_accuracy():
     S, _ = np.linalg.qr(rng.standard_normal((512, 512)))
     C = _run(Q, S, precision=1)
     assert np.linalg.norm(C.T @ C - np.eye(512)) / 512 <= 1e-14
+
+
+def test_split_gemm_against_exact_product():
+    rng = np.random.default_rng(17)
+    m, n, k = 24, 12, 300  # three K windows of 128
+    A = rng.standard_normal((m, k)) * np.exp(rng.uniform(-3, 3, (m, 1)))
+    B = rng.standard_normal((k, n))
+    C = _run(A, B, precision=1)
+    Af = [[Fraction(float(x)) for x in row] for row in A]
+    Bf = [[Fraction(float(B[p, j])) for p in range(k)] for j in range(n)]
+    bound = np.abs(A) @ np.abs(B)
+    worst = 0.0
+    for i in range(m):
+        for j in range(n):
+            exact = sum(a * b for a, b in zip(Af[i], Bf[j]))
+            worst = max(worst, abs(float(Fraction(float(C[i, j])) - exact)) / bound[i, j])
+    assert worst <= 2.0 ** -50, worst
