@@ -15,9 +15,9 @@
 //   row phase     node i: the block row Ah(I_i, ~J_i) (r_i x N) is factored
 //                 through its transpose, R = qr(Ah(I_i, ~J_i)^T) (k_tall_qr:
 //                 Householder on row tiles in shared memory; R factors of row
-//                 ranges stacked and factored again), then one-sided Jacobi on
-//                 R^T (k_jacobi_basis): its normalised columns are the block
-//                 row's left singular vectors, those of norm > tol form U_i.
+//                 ranges stacked and factored again), then a pivoted QR of R
+//                 and one-sided Jacobi on its leading rows (k_node_basis): the
+//                 block row's left singular vectors, those above tol form U_i.
 //                 Ah(I_i, :) <- U_i^T Ah(I_i, :) by the grouped GEMM.
 //   column phase  the same on the block column Ah(~I_j, J_j) (R = qr of the
 //                 block column; the Jacobi columns are its right singular
@@ -211,62 +211,140 @@ k_tall_qr(const TallDesc *__restrict__ descs, const QrJob *__restrict__ jobs) {
   }
 }
 
-// One-sided Jacobi (Hestenes) on X = R^T, round-robin pair order, one group of
-// lanes per pair: X V = W Sigma.  The columns of W with sigma > tol, ordered by
-// decreasing sigma, are the left singular vectors of R^T -- the left singular
-// vectors of a block row whose transpose has R as QR factor, or the right
-// singular vectors of a block column with R as QR factor.  The columns enter
-// in decreasing norm; squared norms are cached (refreshed each sweep, updated
-// exactly by each rotation: a' = a - t c, b' = b + t c), so a pair costs one
-// dot product; one lane per group forms the rotation.  A column below tol/100
-// stays below tol under the rotations and moves the kept subspace by less than
-// that, so it leaves the sweeps.  status |= 1 if the sweep limit is reached.
+// Basis of one node from its R factor: the left singular vectors of R^T with
+// singular value > tol, in decreasing order (the left singular vectors of a
+// block row whose transpose has R as QR factor, or the right singular vectors
+// of a block column with R as QR factor).
+//   A. Householder QR with column pivoting of R, R Pi = Q2 R2, in shared memory
+//      (squared trailing column norms downdated, recomputed when they lose
+//      three digits); it stops at the first step k0 where the trailing block's
+//      Frobenius norm is below tol / 100, so R2's rows from k0 on are dropped:
+//      they move the kept subspace by less than that.
+//   B. One-sided Jacobi (Hestenes) on the k0 leading rows of R2 as vectors of
+//      length r (R^T = Pi R2^T Q2^T, so the left singular vectors of R^T are Pi
+//      times those of R2^T, i.e. of the rows): round-robin pairs, one group of
+//      lanes per pair, squared norms cached (refreshed each sweep, a' = a - t c,
+//      b' = b + t c), one lane forms each rotation, rows below tol / 100 left
+//      out.  Pivoting makes the rows graded (Drmac & Veselic, "New fast and
+//      accurate Jacobi SVD algorithm", SIAM J. Matrix Anal. Appl. 29, 2008),
+//      so few sweeps are needed, on k0 ~ rank rows instead of r.
+//   C. Normalised rows with norm > tol, un-permuted, sorted by decreasing norm.
+// status |= 1 if the sweep limit is reached.
 __global__ void __launch_bounds__(QT)
-k_jacobi_basis(const BasisJob *__restrict__ jobs, double tol, int *status) {
-  extern __shared__ double X[];
-  __shared__ double nrm[QR_MAXC];
-  __shared__ int pos[QR_MAXC];
-  __shared__ int s_k;
+k_node_basis(const BasisJob *__restrict__ jobs, double tol, int *status) {
+  extern __shared__ double M[];  // column j at M + j * LDM
+  __shared__ double cn[QR_MAXC], cref[QR_MAXC], nrm[QR_MAXC];
+  __shared__ int prm[QR_MAXC], pos[QR_MAXC];
+  __shared__ HousePar s_h;
+  __shared__ int s_piv, s_k;
   const BasisJob jb = jobs[blockIdx.x];
-  const int r = jb.r, LDX = r + 1, tid = threadIdx.x;
-  const int rp = r + (r & 1), np = rp / 2;
-  const int gs = group_size(np);
+  const int r = jb.r, LDM = r + 1, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int e = tid; e < r * r; e += QT) {
+    const int c = e / r, i = e - c * r;
+    M[c * LDM + i] = i <= c ? jb.R[i + (long long)c * r] : 0.0;
+  }
+  __syncthreads();
+  {
+    const int gs = group_size(r), grp = tid / gs, ln = tid - grp * gs;
+    const unsigned mask = group_mask(gs);
+    for (int c = grp; c < r; c += QT / gs) {
+      double a = 0.0;
+      for (int i = ln; i <= c; i += gs) { const double u = M[c * LDM + i]; a = fma(u, u, a); }
+      a = group_sum(a, gs, mask);
+      if (ln == 0) { cn[c] = a; cref[c] = a; prm[c] = c; }
+    }
+  }
+  __syncthreads();
+  // ---- A: pivoted QR, stopped when the trailing block is negligible
+  const double stop2 = tol > 0.0 ? 1e-4 * tol * tol : 0.0;
+  int k0 = r;
+  for (int k = 0; k < r; ++k) {
+    if (wid == 0) {
+      ArgMax am{-1.0, r};
+      for (int j = k + lane; j < r; j += 32) am = argmax_merge(am, ArgMax{cn[j], j});
+      am = warp_argmax(am);
+      if (lane == 0) s_piv = ((double)(r - k) * am.v <= stop2) ? -1 : am.i;
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p < 0) { k0 = k; break; }
+    if (p != k) {
+      for (int i = tid; i < r; i += QT) {
+        const double t = M[k * LDM + i];
+        M[k * LDM + i] = M[p * LDM + i];
+        M[p * LDM + i] = t;
+      }
+      if (tid == 0) {
+        double t = cn[k]; cn[k] = cn[p]; cn[p] = t;
+        t = cref[k]; cref[k] = cref[p]; cref[p] = t;
+        const int q = prm[k]; prm[k] = prm[p]; prm[p] = q;
+      }
+      __syncthreads();
+    }
+    if (wid == 0) {
+      double q = 0.0;
+      for (int i = k + 1 + lane; i < r; i += 32) { const double u = M[k * LDM + i]; q = fma(u, u, q); }
+      q = warp_sum(q);
+      if (lane == 0) s_h = house_par(M[k * LDM + k], q);
+    }
+    __syncthreads();
+    const HousePar h = s_h;
+    const int left = r - k - 1;
+    if (left > 0) {
+      const int gs = group_size(left), grp = tid / gs, ln = tid - grp * gs;
+      if (grp < left) {
+        const unsigned mask = group_mask(gs);
+        const int j = k + 1 + grp;
+        double *Mj = M + j * LDM;
+        const double *Mk = M + k * LDM;
+        double rk = Mj[k];
+        if (h.tau != 0.0) {
+          double dd = 0.0;
+          for (int i = k + 1 + ln; i < r; i += gs) dd = fma(Mk[i], Mj[i], dd);
+          dd = group_sum(dd, gs, mask);
+          const double tw = h.tau * fma(h.scale, dd, rk), tws = tw * h.scale;
+          for (int i = k + 1 + ln; i < r; i += gs) Mj[i] = fma(-tws, Mk[i], Mj[i]);
+          rk -= tw;
+        }
+        // trailing norm of column j without row k
+        double c2 = fma(-rk, rk, cn[j]);
+        double cr = cref[j];
+        if (c2 < 1e-3 * cr) {  // cancellation: recompute
+          double a = 0.0;
+          for (int i = k + 1 + ln; i < r; i += gs) { const double u = Mj[i]; a = fma(u, u, a); }
+          c2 = group_sum(a, gs, mask);
+          cr = c2;
+        }
+        __syncwarp(mask);
+        if (ln == 0) { Mj[k] = rk; cn[j] = c2; cref[j] = cr; }
+      }
+    }
+    if (tid == 0) M[k * LDM + k] = h.beta;
+    __syncthreads();
+  }
+  // rows 0..k0-1 of R2 (upper trapezoidal): clear the reflectors stored below
+  // the diagonal inside them
+  for (int e = tid; e < k0 * k0; e += QT) {
+    const int j = e / k0, i = e - j * k0;
+    if (i > j) M[j * LDM + i] = 0.0;
+  }
+  __syncthreads();
+  // ---- B: one-sided Jacobi on the k0 rows
+  const int rp = k0 + (k0 & 1), np = rp / 2;
+  const int gs = group_size(np > 0 ? np : 1);
   const int grp = tid / gs, ln = tid - grp * gs;
   const unsigned mask = group_mask(gs);
   const int ng = QT / gs;
-  const int lead = (tid & 31) & ~(gs - 1);  // the group leader's lane
-  // sorted load: X(:, pos(c)) = row c of R
-  for (int c = grp; c < r; c += ng) {
-    double a = 0.0;
-    for (int i = c + ln; i < r; i += gs) { const double u = jb.R[c + (long long)i * r]; a = fma(u, u, a); }
-    a = group_sum(a, gs, mask);
-    if (ln == 0) nrm[c] = a;
-  }
-  __syncthreads();
-  for (int c = tid; c < r; c += QT) {
-    const double v = nrm[c];
-    int p = 0;
-    for (int c2 = 0; c2 < r; ++c2) {
-      const double w = nrm[c2];
-      p += (w > v) || (w == v && c2 < c);
-    }
-    pos[c] = p;
-  }
-  __syncthreads();
-  for (int e = tid; e < r * r; e += QT) {
-    const int c = e / r, i = e - c * r;
-    X[pos[c] * LDX + i] = c <= i ? jb.R[c + (long long)i * r] : 0.0;
-  }
+  const int lead = (tid & 31) & ~(gs - 1);
   const double jtol = HSS_EPS * (r > 16 ? r : 16);
-  const double frz2 = tol > 0.0 ? 1e-4 * tol * tol : 0.0;
-  int conv = 0;
-  for (int sweep = 0; sweep < JAC_SWEEPS; ++sweep) {
-    __syncthreads();
-    for (int c = grp; c < r; c += ng) {
+  const double frz2 = stop2;
+  int conv = k0 < 2;
+  for (int sweep = 0; sweep < JAC_SWEEPS && !conv; ++sweep) {
+    for (int t = grp; t < k0; t += ng) {
       double a = 0.0;
-      for (int i = ln; i < r; i += gs) { const double u = X[c * LDX + i]; a = fma(u, u, a); }
+      for (int j = ln; j < r; j += gs) { const double u = M[j * LDM + t]; a = fma(u, u, a); }
       a = group_sum(a, gs, mask);
-      if (ln == 0) nrm[c] = a;
+      if (ln == 0) nrm[t] = a;
     }
     __syncthreads();
     int rot = 0;
@@ -275,12 +353,11 @@ k_jacobi_basis(const BasisJob *__restrict__ jobs, double tol, int *status) {
         int p, q;
         if (grp == 0) { p = 0; q = 1 + s % (rp - 1); }
         else { p = 1 + (s + grp) % (rp - 1); q = 1 + (s - grp + rp - 1) % (rp - 1); }
-        if (p < r && q < r) {
+        if (p < k0 && q < k0) {
           const double a = nrm[p], b = nrm[q];
           if (a > 0.0 && b > 0.0 && a >= frz2 && b >= frz2) {
-            double *xp = X + p * LDX, *xq = X + q * LDX;
             double c = 0.0;
-            for (int i = ln; i < r; i += gs) c = fma(xp[i], xq[i], c);
+            for (int j = ln; j < r; j += gs) c = fma(M[j * LDM + p], M[j * LDM + q], c);
             c = group_sum(c, gs, mask);
             double cs = 1.0, sn = 0.0;
             int go = 0;
@@ -299,10 +376,10 @@ k_jacobi_basis(const BasisJob *__restrict__ jobs, double tol, int *status) {
             if (go) {
               cs = __shfl_sync(mask, cs, lead);
               sn = __shfl_sync(mask, sn, lead);
-              for (int i = ln; i < r; i += gs) {
-                const double u = xp[i], v = xq[i];
-                xp[i] = fma(cs, u, -sn * v);
-                xq[i] = fma(sn, u, cs * v);
+              for (int j = ln; j < r; j += gs) {
+                const double u = M[j * LDM + p], v = M[j * LDM + q];
+                M[j * LDM + p] = fma(cs, u, -sn * v);
+                M[j * LDM + q] = fma(sn, u, cs * v);
               }
               rot = 1;
             }
@@ -311,41 +388,43 @@ k_jacobi_basis(const BasisJob *__restrict__ jobs, double tol, int *status) {
       }
       __syncthreads();
     }
-    if (!__syncthreads_or(rot)) { conv = 1; break; }
+    conv = !__syncthreads_or(rot);
   }
   if (!conv && tid == 0) atomicOr(status, 1);
   __syncthreads();
-  for (int c = grp; c < r; c += ng) {
+  // ---- C: norms, order, rank, outputs
+  for (int t = grp; t < k0; t += ng) {
     double a = 0.0;
-    for (int i = ln; i < r; i += gs) { const double u = X[c * LDX + i]; a = fma(u, u, a); }
+    for (int j = ln; j < r; j += gs) { const double u = M[j * LDM + t]; a = fma(u, u, a); }
     a = group_sum(a, gs, mask);
-    if (ln == 0) nrm[c] = sqrt(a);
+    if (ln == 0) nrm[t] = sqrt(a);
   }
   __syncthreads();
-  for (int c = tid; c < r; c += QT) {
-    const double v = nrm[c];
+  for (int t = tid; t < k0; t += QT) {
+    const double v = nrm[t];
     int p = 0;
-    for (int c2 = 0; c2 < r; ++c2) {
-      const double w = nrm[c2];
-      p += (w > v) || (w == v && c2 < c);
+    for (int t2 = 0; t2 < k0; ++t2) {
+      const double w = nrm[t2];
+      p += (w > v) || (w == v && t2 < t);
     }
-    pos[c] = p;
+    pos[t] = p;
   }
   if (tid == 0) {
     int k = 0;
-    for (int c = 0; c < r; ++c) k += nrm[c] > tol;
+    for (int t = 0; t < k0; ++t) k += nrm[t] > tol;
     s_k = k;
     *jb.rank = k;
   }
   __syncthreads();
   const int k = s_k;
-  for (int e = tid; e < r * r; e += QT) {
-    const int c = e / r, i = e - c * r;
-    const int pc = pos[c];
-    if (pc < k) {
-      const double val = X[c * LDX + i] / nrm[c];
-      jb.P[i + (long long)pc * r] = val;
-      jb.PT[pc + (long long)i * k] = val;
+  for (int e = tid; e < k0 * r; e += QT) {
+    const int t = e / r, j = e - t * r;
+    const int pt = pos[t];
+    if (pt < k) {
+      const double val = M[j * LDM + t] / nrm[t];
+      const int row = prm[j];
+      jb.P[row + (long long)pt * r] = val;
+      jb.PT[pt + (long long)row * k] = val;
     }
   }
 }
@@ -405,7 +484,7 @@ static std::vector<int> tall_bases(const std::vector<TallDesc> &ds, const std::v
   if (!attr) {
     MCK(cudaFuncSetAttribute(k_tall_qr, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              QR_TILE * (int)sizeof(double)));
-    MCK(cudaFuncSetAttribute(k_jacobi_basis, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    MCK(cudaFuncSetAttribute(k_node_basis, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              QR_MAXC * (QR_MAXC + 1) * (int)sizeof(double)));
     attr = true;
   }
@@ -462,7 +541,7 @@ static std::vector<int> tall_bases(const std::vector<TallDesc> &ds, const std::v
     rmax = std::max(rmax, ds[i].ncol);
   }
   BasisJob *db = upload("m2h_bjob", bj, st);
-  k_jacobi_basis<<<nd, QT, (size_t)rmax * (rmax + 1) * sizeof(double), st>>>(db, tol, drk + nd);
+  k_node_basis<<<nd, QT, (size_t)rmax * (rmax + 1) * sizeof(double), st>>>(db, tol, drk + nd);
   ++launches;
   std::vector<int> h(nd + 1);
   MCK(cudaMemcpyAsync(h.data(), drk, sizeof(int) * (nd + 1), cudaMemcpyDeviceToHost, st));
