@@ -135,6 +135,19 @@ def cpu_reference_sample(n_sample, n_target, threads):
     return t, t * scale, scale
 
 
+def cpu_lapack_sample(n_sample, n_target, threads):
+    """LAPACK DSTEDC (OpenBLAS, the oracle's accuracy reference) on one solve of
+    size n_sample, scaled like cpu_reference_sample."""
+    import oracle
+    oracle.set_threads(threads)
+    d, e = inputs(n_sample, seed=0)
+    t = time.perf_counter()
+    oracle.dstedc_lapack(d, e)
+    t = time.perf_counter() - t
+    scale = (n_target / n_sample) ** 2 * (np.log2(n_target) / np.log2(n_sample))
+    return t, t * scale, scale
+
+
 BATCH_COUNT, BATCH_LO, BATCH_HI = 512, 256, 4096
 
 
@@ -328,6 +341,32 @@ def run_extra(torch, hp, full_cfg):
                 _timed_ms(torch, lambda: hp.dhssevc_dev(dd, zh, al, difl, difr, Q, n, n, ni=128,
                                                         tol=1e-14))
         out["cauchy_hss_max_rank"] = hp.get_stats()["max_rank"]
+        del Q
+        # DHSSMM: the Cauchy-like matrix of TEST/testfmm.f90 (interlaced points,
+        # z, v iid U(0, 1)), tol 1e-11, leaf 64, times B (n x k, iid U(0, 1))
+        hp.set_config(precision=full_cfg.get("precision", 1))
+        for n, k in ((2000, 2000), (8192, 1024)):
+            gap = 8.9 / (2 * n)
+            x = 0.1 + gap * (2 * np.arange(1, n + 1) - 1)
+            rng = np.random.default_rng(0)
+            zv, vv = rng.uniform(size=n), rng.uniform(size=n)
+            A = torch.tensor(np.ascontiguousarray((zv[:, None] * vv[None, :] / (x[:, None] - x[None, :] - gap)).T),
+                             device="cuda")
+            B0 = torch.rand(k, n, dtype=torch.float64, device="cuda")
+            ref = (A.T @ B0.T).T
+            Bd = B0.clone()
+            hp.dhssmm_dev(A, Bd, 64, 1e-11, side=0)
+            ts = []
+            for _ in range(3):
+                Bd.copy_(B0)
+                ts.append(hp.dhssmm_dev(A, Bd, 64, 1e-11, side=0))
+            tb = min(t[0] for t in ts)
+            tm = min(t[1] for t in ts)
+            out["dhssmm_n%d_k%d" % (n, k)] = {
+                "build_ms": round(tb, 3), "multiply_ms": round(tm, 3),
+                "max_rank": hp.get_stats()["max_rank"],
+                "max_abs_err_vs_dense": float((Bd - ref).abs().max())}
+            del A, B0, Bd, ref
     finally:
         hp.restore_config(old)
     return out
@@ -512,6 +551,14 @@ def run_ours(args):
         cpu = {"value": scaled, "unit": "s", "cores": threads, "kind": "port",
                "sample": "one n=%d solve (%.2f s), x%.2f (n^2 log n) to n=%d"
                          % (args.cpu_sample, t_s, scale, n)}
+        # the same restatement on one thread, and LAPACK's own DSTEDC (the
+        # accuracy oracle) on all threads, both on smaller samples
+        t1, s1, sc1 = cpu_reference_sample(4096, n, 1)
+        cpu["one_thread"] = {"value": s1, "unit": "s", "cores": 1,
+                             "sample": "one n=4096 solve (%.2f s), x%.1f to n=%d" % (t1, sc1, n)}
+        t2, s2, sc2 = cpu_lapack_sample(8192, n, threads)
+        cpu["lapack_dstedc"] = {"value": s2, "unit": "s", "cores": threads,
+                                "sample": "one n=8192 DSTEDC (%.2f s), x%.1f to n=%d" % (t2, sc2, n)}
     total_ms = sum(acc["ms"].values())
     line = {
         "metric": METRIC, "value": ms / 1000.0, "unit": "s", "n_gpus": world, "steps": args.steps,
