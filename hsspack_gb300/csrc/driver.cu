@@ -1174,6 +1174,7 @@ void hss_set_config(const hss_config *cfg) {
   set_split_min_log2(cfg->split_min_log2);
   set_small_nk(cfg->small_nk);
   set_split_min_m(cfg->split_min_m);
+  set_secular_threads(cfg->sec_threads);
 }
 void hss_get_config(hss_config *cfg) {
   Ctx &c = ctx();

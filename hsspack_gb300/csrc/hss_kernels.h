@@ -38,6 +38,8 @@ struct LevelScratch {
 // secular.cu
 // lane-group width target of the secular kernels (pole terms per lane; 0: 8)
 void set_secular_terms(int t);
+// threads a secular level should reach before lanes per root shrink (0: 152 * 256)
+void set_secular_threads(int t);
 // sq: singular-value mode (poles d_i^2, outputs sigma and DIFL/DIFR = sigma - d)
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,

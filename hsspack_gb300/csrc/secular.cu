@@ -552,13 +552,28 @@ static inline int warp_grid(int total, int threads) {
 // Pole terms per lane the lane-group width aims at (hss_config.sec_terms).
 static int g_sec_terms = 8;
 void set_secular_terms(int t) { g_sec_terms = t > 0 ? t : 8; }
+static long long g_sec_threads = 152LL * 256;
+void set_secular_threads(int t) { g_sec_threads = t > 0 ? t : 152LL * 256; }
+
+// Lanes per root of a level with `total` roots and largest merge maxk: the
+// fewest lanes that (a) keep a lane's share at or below 64 pole terms and
+// (b) give at least sec_threads threads (enough warps to keep the FP64 pipes
+// of every SM busy), but never more than needed for sec_terms terms per lane.
+// A level with many roots runs one lane per root (no per-root reduction or
+// replicated step work); a level with few roots spreads each root.
+static int lanes_per_root(int total, int maxk) {
+  int cap = 1;
+  while (cap < 32 && cap * g_sec_terms < maxk) cap *= 2;
+  int L = 1;
+  while (L < cap && (L * 64 < maxk || (long long)total * L < g_sec_threads)) L *= 2;
+  return L;
+}
 
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st, bool sq) {
   if (total <= 0) return;
-  int L = 1;
-  while (L < 32 && L * g_sec_terms < maxk) L *= 2;  // ~sec_terms pole terms per lane
+  const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
   const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
   switch (L * 2 + (sq ? 1 : 0)) {
@@ -575,8 +590,7 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
 void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *dl,
                         const double *zw, float *feat, cudaStream_t st) {
   if (total <= 0) return;
-  int L = 1;
-  while (L < 32 && L * g_sec_terms < maxk) L *= 2;
+  const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
   const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
   switch (L) {
@@ -591,8 +605,7 @@ void launch_lowner(const LevelView &lv, int total, const double *dl, const doubl
                    const double *difr, const double *zw, double *zhat, cudaStream_t st, bool sq,
                    int maxk) {
   if (total <= 0) return;
-  int L = 1;
-  while (L < 32 && L * g_sec_terms < maxk) L *= 2;
+  const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
   const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
   switch (L) {

@@ -31,14 +31,17 @@ typedef struct hss_config {
   int predictor;  /* 0: standard secular initial guess; 1: learned initial guess    */
   int batched;    /* 1: one launch per stage per DC level; 0: launches per merge    */
   int profile;    /* 1: time every stage with CUDA events (hss_stats.stage_ms)      */
-  int sec_terms;  /* secular solver: pole terms per lane (lanes per root = the    */
-                  /* smallest power of two covering K / sec_terms); 0: 8        */
+  int sec_terms;  /* secular solver: at most this many lanes' worth of work per  */
+                  /* root (lanes <= the power of two covering K / sec_terms); 0: 8 */
   int split_min_log2; /* split-BF16 products for M*N*K >= 2^this and M >=     */
                       /* split_min_m; 0: 17                                    */
   int small_nk;       /* FP64 products with N, K <= this on the element      */
                       /* kernel (thread per output); 0: 128                    */
   int split_min_m;    /* smallest M of a split-BF16 product; 0: 256            */
-  int reserved[4];
+  int sec_threads;    /* secular solver: fewest lanes per root that give this  */
+                      /* many threads per level (and <= 64 terms per lane);    */
+                      /* 0: 152 * 256                                          */
+  int reserved[3];
 } hss_config;
 
 /* stages timed when hss_config.profile = 1 */
