@@ -43,22 +43,43 @@ template <int L, bool SQ>
 __device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
                                             const double *__restrict__ z, int K, int oi,
                                             double tau, int jl, int gl) {
-  double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0, e = 0.0;
+  // Every lane of the warp calls this (lanes without a root pass K = 0).
+  // Each side of the split (i <= jl, i > jl) holds terms of one sign, so
+  // sum |v| = |psi| + |phi|; and the stretches that are on the same side for
+  // every lane of the warp (below the warp's smallest jl, above its largest)
+  // are summed without a per-term branch.
+  double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
   const double o = K > 0 ? __ldg(d + oi) : 0.0;
-  for (int i = gl; i < K; i += L) {
+  const int jlo = __reduce_min_sync(HSS_FULL, K > 0 ? jl : (1 << 29));
+  const int jhi = __reduce_max_sync(HSS_FULL, K > 0 ? jl : -1);
+  auto term = [&](int i, double &v, double &dv) {
     const double zi = __ldg(z + i);
     const double di = __ldg(d + i);
     const double del = (SQ ? (di - o) * (di + o) : (di - o)) - tau;
     const double t = zi * rcp_nr(del);
-    const double v = zi * t;
-    const double dv = t * t;
+    v = zi * t;
+    dv = t * t;
+  };
+  int i = gl;
+  for (const int e = min(K, jlo + 1); i < e; i += L) {
+    double v, dv;
+    term(i, v, dv);
+    a0 += v; a1 += dv;
+  }
+  for (const int e = min(K, jhi + 1); i < e; i += L) {
+    double v, dv;
+    term(i, v, dv);
     if (i <= jl) { a0 += v; a1 += dv; } else { b0 += v; b1 += dv; }
-    e += fabs(v);
+  }
+  for (; i < K; i += L) {
+    double v, dv;
+    term(i, v, dv);
+    b0 += v; b1 += dv;
   }
   SecSums s;
   s.psi = group_sum<L>(a0); s.dpsi = group_sum<L>(a1);
   s.phi = group_sum<L>(b0); s.dphi = group_sum<L>(b1);
-  s.eabs = group_sum<L>(e);
+  s.eabs = fabs(s.psi) + fabs(s.phi);
   return s;
 }
 
