@@ -373,43 +373,56 @@ __global__ void k_givens(int P, const int *__restrict__ ms, const int *__restric
 
 // Copy the K non-deflated columns of merge m into a dense n_m x K buffer
 // (column `grp` when grouped, else column j).  One CTA per (column, row chunk).
-__global__ void k_gather(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+// One warp per (column, segment of GS_SEG rows), lanes along the rows: the
+// bottom levels have many short columns (a CTA per column would schedule
+// hundreds of thousands of blocks that copy a few dozen values each).
+constexpr int GS_SEG = 256;
+
+__device__ __forceinline__ int gs_merge(const int *__restrict__ rootoff, int P, int r) {
+  int lo = 0, hi = P;
+  while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (rootoff[mid] <= r) lo = mid; else hi = mid; }
+  return lo;
+}
+
+__global__ void k_gather(int P, int nseg, const int *__restrict__ ms, const int *__restrict__ mn,
                          const int *__restrict__ rootoff, const int *__restrict__ ndslot,
                          const int *__restrict__ grp, const long long *__restrict__ boff,
                          const double *__restrict__ Q, long long ldq, double *__restrict__ B,
                          const int2 *__restrict__ sup) {
-  const int r = blockIdx.x;
+  const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int r = (int)(wg / nseg), q = (int)(wg - (long long)r * nseg);
   if (r >= rootoff[P]) return;
-  int lo = 0, hi = P;
-  while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (rootoff[mid] <= r) lo = mid; else hi = mid; }
-  const int m = lo, j = r - rootoff[m];
+  const int m = gs_merge(rootoff, P, r), j = r - rootoff[m];
   const int s = ms[m], n = mn[m];
+  const int i0 = q * GS_SEG, i1 = min(n, i0 + GS_SEG);
+  if (i0 >= i1) return;
   const int col = grp ? grp[s + j] : j;
   const int slot = ndslot[s + j];
   const double *src = Q + (long long)slot * ldq + s;
   double *dst = B + boff[m] + (long long)col * n;
   int vlo = 0, vhi = n;  // rows of the column that hold data (zero elsewhere)
   if (sup) { const int2 sr = sup[slot]; vlo = max(0, sr.x - s); vhi = min(n, sr.y - s); }
-  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x)
-    dst[i] = (i >= vlo && i < vhi) ? src[i] : 0.0;
+  for (int i = i0 + lane; i < i1; i += 32) dst[i] = (i >= vlo && i < vhi) ? src[i] : 0.0;
 }
 
 // Write the new eigenvectors (columns of T, n_m x K) into the non-deflated slots.
-__global__ void k_scatter(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+__global__ void k_scatter(int P, int nseg, const int *__restrict__ ms, const int *__restrict__ mn,
                           const int *__restrict__ rootoff, const int *__restrict__ ndslot,
                           const long long *__restrict__ toff, const double *__restrict__ T,
                           double *__restrict__ Q, long long ldq, int2 *__restrict__ sup) {
-  const int r = blockIdx.x;
+  const long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int r = (int)(wg / nseg), q = (int)(wg - (long long)r * nseg);
   if (r >= rootoff[P]) return;
-  int lo = 0, hi = P;
-  while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (rootoff[mid] <= r) lo = mid; else hi = mid; }
-  const int m = lo, j = r - rootoff[m];
+  const int m = gs_merge(rootoff, P, r), j = r - rootoff[m];
   const int s = ms[m], n = mn[m];
+  const int i0 = q * GS_SEG, i1 = min(n, i0 + GS_SEG);
+  if (i0 >= i1) return;
   const double *src = T + toff[m] + (long long)j * n;
   double *dst = Q + (long long)ndslot[s + j] * ldq + s;
-  if (sup && blockIdx.y == 0 && threadIdx.x == 0) sup[ndslot[s + j]] = make_int2(s, s + n);
-  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x)
-    dst[i] = src[i];
+  if (sup && q == 0 && lane == 0) sup[ndslot[s + j]] = make_int2(s, s + n);
+  for (int i = i0 + lane; i < i1; i += 32) dst[i] = src[i];
 }
 
 // New ascending order of each merged block: roots (ascending) merged with the
@@ -612,15 +625,19 @@ void launch_gather(int P, int total, int maxn, const int *ms, const int *mn, con
                    const int *ndslot, const int *grp, const long long *boff, const double *Q,
                    long long ldq, double *B, cudaStream_t st, const int2 *sup) {
   if (total <= 0) return;
-  dim3 grid(total, (maxn + 1023) / 1024);
-  k_gather<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, grp, boff, Q, ldq, B, sup);
+  const int nseg = (maxn + GS_SEG - 1) / GS_SEG;
+  const long long warps = (long long)total * nseg;
+  k_gather<<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(P, nseg, ms, mn, rootoff, ndslot, grp, boff,
+                                                        Q, ldq, B, sup);
 }
 void launch_scatter(int P, int total, int maxn, const int *ms, const int *mn, const int *rootoff,
                     const int *ndslot, const long long *toff, const double *T, double *Q,
                     long long ldq, cudaStream_t st, int2 *sup) {
   if (total <= 0) return;
-  dim3 grid(total, (maxn + 1023) / 1024);
-  k_scatter<<<grid, 256, 0, st>>>(P, ms, mn, rootoff, ndslot, toff, T, Q, ldq, sup);
+  const int nseg = (maxn + GS_SEG - 1) / GS_SEG;
+  const long long warps = (long long)total * nseg;
+  k_scatter<<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(P, nseg, ms, mn, rootoff, ndslot, toff, T,
+                                                         Q, ldq, sup);
 }
 void launch_widen(int P, int maxn, const int *ms, const int *mn, const int *ng,
                   const LevelScratch &w, double *Q, long long ldq, int2 *sup, cudaStream_t st) {
