@@ -44,7 +44,7 @@ class Config(ctypes.Structure):
                 ("profile", ctypes.c_int), ("sec_terms", ctypes.c_int),
                 ("split_min_log2", ctypes.c_int), ("small_nk", ctypes.c_int),
                 ("split_min_m", ctypes.c_int), ("sec_threads", ctypes.c_int),
-                ("reserved", ctypes.c_int * 3)]
+                ("gemm_path", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

@@ -1175,6 +1175,7 @@ void hss_set_config(const hss_config *cfg) {
   set_small_nk(cfg->small_nk);
   set_split_min_m(cfg->split_min_m);
   set_secular_threads(cfg->sec_threads);
+  set_gemm_path(cfg->gemm_path);
 }
 void hss_get_config(hss_config *cfg) {
   Ctx &c = ctx();

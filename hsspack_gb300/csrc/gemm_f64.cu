@@ -117,10 +117,15 @@ void set_small_nk(int v) { g_small_nk = v > 0 ? v : 128; }
 
 // split-BF16 thresholds (hss_config.split_min_log2, split_min_m):
 // M*N*K >= 2^g_split_log2 and M >= g_split_m
-static int g_split_log2 = 17;
-void set_split_min_log2(int v) { g_split_log2 = v > 0 ? v : 17; }
-static int g_split_m = 256;
-void set_split_min_m(int v) { g_split_m = v > 0 ? v : 256; }
+static int g_split_log2 = 15;
+void set_split_min_log2(int v) { g_split_log2 = v > 0 ? v : 15; }
+static int g_split_m = 128;
+void set_split_min_m(int v) { g_split_m = v > 0 ? v : 128; }
+// 0: digit planes written to global memory first, then the TMA-fed product
+// kernel; 1: operands split inside each CTA of the product kernel
+// (hss_config.gemm_path; the staged form measures faster on the DC shapes)
+static int g_gemm_path = 0;
+void set_gemm_path(int v) { g_gemm_path = v == 1 ? 1 : 0; }
 
 void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaStream_t st) {
   if (nprob <= 0 || total_tiles <= 0) return;
@@ -139,7 +144,10 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
       else probs.push_back(p);
     }
     int *err = pool<int>("gemm_err", 1);
-    if (!big.empty()) launch_gemm_split(big, err, st);
+    if (!big.empty()) {
+      if (g_gemm_path == 1) launch_gemm_fused(big, err, st);
+      else launch_gemm_split(big, err, st);
+    }
     if (probs.empty()) return;
   } else {
     probs = probs_in;

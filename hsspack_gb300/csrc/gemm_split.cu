@@ -57,14 +57,95 @@ __device__ __forceinline__ int tile_off(int r, int k, int R) {
   return ((k >> 3) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
-__device__ __forceinline__ void split_digits(double x, double scale, __nv_bfloat16 *dig) {
-  long long q = __double2ll_rn(x * scale);  // |q| <= 2^60
+// Conversions between integer and floating types issue on the FP64 pipe of
+// this part, which is its scarcest unit; the digit planes are built and read
+// back with integer operations on the bit patterns instead.
+
+// round(x * 2^(60 - e)) for |x| < 2^e by integer operations on the bits
+__device__ __forceinline__ long long scaled_int(double x, int e) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  long long m = b & 0xFFFFFFFFFFFFFll;
+  if (ex) m |= 1ll << 52;
+  const int sh = (ex ? ex : 1) - 1015 - e;  // x = m 2^{(ex ? ex : 1) - 1075}
+  long long q;
+  if (sh >= 0) q = m << sh;  // sh <= 8 since |x| < 2^e
+  else if (sh > -62) q = (m + (1ll << (-sh - 1))) >> (-sh);
+  else q = 0;
+  return b < 0 ? -q : q;
+}
+
+// BF16 bit pattern of an integer |d| <= 128 (exact)
+__device__ __forceinline__ uint32_t bf16_of_int(int d) {
+  const uint32_t a = (uint32_t)(d < 0 ? -d : d);
+  const int e = 31 - __clz((int)(a | 1u));  // a in [2^e, 2^(e+1)), e <= 7
+  const uint32_t bits = (d < 0 ? 0x8000u : 0u) | ((uint32_t)(e + 127) << 7) | ((a << (7 - e)) & 0x7Fu);
+  return a ? bits : 0u;
+}
+
+// the value of an FP32 that holds an exact integer below 2^31 in magnitude
+__device__ __forceinline__ int int_of_float(float v) {
+  const int f = __float_as_int(v);
+  const int E = ((f >> 23) & 0xFF) - 127;
+  const int M = (f & 0x7FFFFF) | 0x800000;
+  const int a = E < 0 ? 0 : (E >= 23 ? M << (E - 23) : M >> (23 - E));
+  return f < 0 ? -a : a;
+}
+
+// (H + 2^-32 L) 2^e rounded to the nearest double (ties to even), from the
+// exact 128-bit integer H 2^32 + L by integer operations; the FP64 pipe is
+// used only when the result leaves the normal range.
+__device__ __forceinline__ double exact_double(long long H, long long L, int e) {
+  unsigned long long lo = (unsigned long long)H << 32;
+  unsigned long long hi = (unsigned long long)(H >> 32);
+  const unsigned long long l = (unsigned long long)L;
+  const unsigned long long nlo = lo + l;
+  hi += (unsigned long long)(L >> 63) + (nlo < lo ? 1ull : 0ull);
+  lo = nlo;
+  const bool neg = (long long)hi < 0;
+  if (neg) {  // two's complement of the 128-bit value
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+  if ((hi | lo) == 0ull) return 0.0;
+  const int n = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);  // bit length
+  unsigned long long mant;
+  int nn = n;
+  if (n <= 53) {
+    mant = lo << (53 - n);
+  } else {
+    const int sh = n - 53;  // 1 .. 75
+    mant = sh < 64 ? (lo >> sh) | (sh ? hi << (64 - sh) : 0ull) : hi >> (sh - 64);
+    const int hb = sh - 1;  // the rounding bit
+    const unsigned long long half =
+        hb < 64 ? (lo >> hb) & 1ull : (hi >> (hb - 64)) & 1ull;
+    bool sticky;
+    if (hb < 64) sticky = hb ? (lo & ((1ull << hb) - 1ull)) != 0ull : false;
+    else sticky = lo != 0ull || (hb > 64 && (hi & ((1ull << (hb - 64)) - 1ull)) != 0ull);
+    if (half && (sticky || (mant & 1ull))) {
+      ++mant;
+      if (mant == (1ull << 53)) { mant >>= 1; ++nn; }
+    }
+  }
+  const int be = (nn - 1) + e - 32 + 1023;  // biased exponent of the leading bit
+  if (be <= 0 || be >= 2047) {  // out of the normal range: scale in FP64
+    const double v = ldexp((double)mant, nn - 53 + e - 32);
+    return neg ? -v : v;
+  }
+  const unsigned long long bits = (neg ? 0x8000000000000000ull : 0ull) |
+                                  ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+// the SP digits of q (|q| <= 2^60): d_s = round(q_s / 2^{53 - 8s}), |d_s| <= 128
+__device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 *dig) {
+  long long q = scaled_int(x, e);
 #pragma unroll
   for (int s = 0; s < SP; ++s) {
     const int sh = 53 - 8 * s;
     const long long d = (q + (1ll << (sh - 1))) >> sh;
-    q -= d << sh;
-    dig[s] = __float2bfloat16_rn((float)d);
+    q -= d * (1ll << sh);
+    dig[s] = __ushort_as_bfloat16((unsigned short)bf16_of_int((int)d));
   }
 }
 
@@ -80,7 +161,7 @@ __device__ __forceinline__ int exp_of(double amax) {
 // One CTA per 128-row panel; pass 1 row max, pass 2 digits.
 __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
   __shared__ double smax[8][TM];
-  __shared__ double sscale[TM];
+  __shared__ int sexp[TM];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   // pass 1: each warp takes columns k = w, w+8, ...; lanes cover 4 x 32 rows
   double mx[4] = {0, 0, 0, 0};
@@ -99,7 +180,7 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
     const int e = exp_of(m);
     const int r = tm * TM + tid;
     if (r < P.rows) P.expo[r] = e;
-    sscale[tid] = ldexp(1.0, 60 - e);
+    sexp[tid] = e;
   }
   __syncthreads();
   // pass 2: thread handles (row, 8 consecutive k) -> 16-byte rows of core matrices
@@ -115,7 +196,7 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
         const int gk = kt * TK + k8 * 8 + c;
         const double x = (gr < P.rows && gk < P.inner) ? P.src[(long long)gk * P.ld + gr] : 0.0;
         __nv_bfloat16 d[SP];
-        split_digits(x, sscale[r], d);
+        split_digits(x, sexp[r], d);
 #pragma unroll
         for (int s = 0; s < SP; ++s) dg[s][c] = d[s];
       }
@@ -130,7 +211,7 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
 // B: K x N (ldb) -> planes [tile_n][tile_k][s] of TN x TK (K-major), column
 // exponents.  One CTA per 64-column panel.
 __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
-  __shared__ double sscale[TN];
+  __shared__ int sexp[TN];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   for (int c = w; c < TN; c += 8) {  // warp per column: max over k
     const int gc = tn * TN + c;
@@ -141,7 +222,7 @@ __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
     if (lane == 0) {
       const int e = exp_of(m);
       if (gc < P.rows) P.expo[gc] = e;
-      sscale[c] = ldexp(1.0, 60 - e);
+      sexp[c] = e;
     }
   }
   __syncthreads();
@@ -157,7 +238,7 @@ __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
         const int gk = kt * TK + k8 * 8 + q;
         const double x = (gc < P.rows && gk < P.inner) ? P.src[(long long)gc * P.ld + gk] : 0.0;
         __nv_bfloat16 d[SP];
-        split_digits(x, sscale[c], d);
+        split_digits(x, sexp[c], d);
 #pragma unroll
         for (int s = 0; s < SP; ++s) dg[s][q] = d[s];
       }
@@ -393,7 +474,7 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
         tmem_ld16(lane_addr + g * TN + c, v);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          const long long x = (long long)__float2int_rn(v[i]);
+          const long long x = (long long)int_of_float(v[i]);
           if (g < 3) hacc[c + i] += x * (1ll << (8 * (2 - g)));
           else lacc[c + i] += x * (1ll << (8 * (6 - g)));
         }
@@ -411,7 +492,7 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
     for (int j = 0; j < TH; ++j) {
       const int c = tn * TN + (warp >> 2) * TH + j;
       if (c < P.N) {
-        const double v = ldexp(fma((double)lacc[j], 0x1p-32, (double)hacc[j]), ei + P.eb[c] - 30);
+        const double v = exact_double(hacc[j], lacc[j], ei + P.eb[c] - 30);
         double *dst = P.C + (long long)c * P.ldc + r;
         *dst = P.beta ? *dst + v : v;
       }
@@ -421,6 +502,241 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512));
+}
+
+// ------------------------------------------------- fused split GEMM -----
+// Many small and medium products (the dense merge updates of the middle DC
+// levels): each CTA splits its own FP64 A and B chunks into the SP digit
+// planes directly in shared memory and issues the plane products on the
+// tensor cores, so no plane buffer goes through global memory and no FP64
+// instruction is spent on the splitting (the digits come from the operands'
+// bit patterns; row / column exponents from a small pre-pass).  Tile 128 x 32,
+// K chunks of 32 (56 MMAs of 128 x 32 x 16 each), 128-deep exactness windows
+// drained into correctly rounded doubles (integer operations) and summed.
+// About 100 KB of shared memory and 256 TMEM columns per CTA: two CTAs share
+// an SM, so one's splitting overlaps the other's MMAs.  (Measured on the DC shapes it is issue bound -- every A
+// element is split once per 32-column tile -- and slower than the staged
+// planes, so it is the alternative, hss_config.gemm_path = 1.)
+constexpr int FM = 128, FN = 32, FK = 32;
+constexpr int FATILE = FM * FK * 2;  // 8 KB per A plane
+constexpr int FBTILE = FN * FK * 2;  // 2 KB per B plane
+constexpr int FSMEM = 100 * 1024;    // >= SP * (FATILE + FBTILE); caps residency at 2 CTAs per SM
+static_assert(SP * (FATILE + FBTILE) + 1024 <= FSMEM, "fused GEMM tiles exceed the shared budget");
+
+struct FusedProb {
+  const double *A, *B;
+  double *C;
+  const int *ea, *eb;  // row / column exponents (frexp convention)
+  int lda, ldb, ldc, M, N, K, beta;
+  int tile0;
+};
+struct ExpJob {  // rows of A (stride = lda between k) or columns of B (contiguous k)
+  const double *X;
+  int ld, count, K;
+  int *out;
+  int off;       // first flattened item of this job
+};
+
+// frexp exponent of the largest |x| from its bit pattern (0 for zero)
+__device__ __forceinline__ int bits_exp(unsigned long long b) {
+  if (b == 0) return 0;
+  const int ex = (int)(b >> 52);
+  return ex ? ex - 1022 : (64 - __clzll((long long)b)) - 1074;
+}
+
+// the SP digits of q (|q| <= 2^60) as BF16 bit patterns, packed into the
+// 16-byte core-matrix rows (element c of the 8 at half-word c)
+__device__ __forceinline__ void digits_into(long long q, int c, uint32_t (*pk)[4]) {
+#pragma unroll
+  for (int s = 0; s < SP; ++s) {
+    const int sh = 53 - 8 * s;
+    const long long d = (q + (1ll << (sh - 1))) >> sh;
+    q -= d * (1ll << sh);
+    pk[s][c >> 1] |= bf16_of_int((int)d) << (16 * (c & 1));
+  }
+}
+
+__global__ void k_row_exps(const ExpJob *__restrict__ jobs, int nj, int total) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int lo = 0, hi = nj;
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (jobs[mid].off <= t) lo = mid; else hi = mid; }
+  const ExpJob J = jobs[lo];
+  const int r = t - J.off;
+  unsigned long long m = 0;
+  for (int k = 0; k < J.K; ++k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(J.X[(long long)k * J.ld + r]) & 0x7FFFFFFFFFFFFFFFull;
+    m = b > m ? b : m;
+  }
+  J.out[r] = bits_exp(m);
+}
+
+__global__ void k_col_exps(const ExpJob *__restrict__ jobs, int nj, int total) {
+  const int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (w >= total) return;
+  int lo = 0, hi = nj;
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (jobs[mid].off <= w) lo = mid; else hi = mid; }
+  const ExpJob J = jobs[lo];
+  const int c = w - J.off;
+  unsigned long long m = 0;
+  for (int k = lane; k < J.K; k += 32) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(J.X[(long long)c * J.ld + k]) & 0x7FFFFFFFFFFFFFFFull;
+    m = b > m ? b : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(HSS_FULL, m, o);
+    m = v > m ? v : m;
+  }
+  if (lane == 0) J.out[c] = bits_exp(m);
+}
+
+__global__ void __launch_bounds__(128, 2)
+k_gemm_fused(const FusedProb *__restrict__ probs, int nprob, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char fsm[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  int lo = 0, hi = nprob;
+  const int b = blockIdx.x;
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (probs[mid].tile0 <= b) lo = mid; else hi = mid; }
+  const FusedProb P = probs[lo];
+  const int t = b - P.tile0, ntm = (P.M + FM - 1) / FM;
+  const int tm = t % ntm, tn = t / ntm;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *sa = fsm, *sb = fsm + SP * FATILE;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tbase = tmem_base;
+  const uint32_t idesc = make_idesc(FM, FN);
+  const int r = tm * FM + tid;
+  const bool rok = r < P.M;
+  const int er = rok ? P.ea[r] : 0;
+  const int cb = tid >> 2, ko = tid & 3;  // this thread's B column and k octet
+  const int gcb = tn * FN + cb;
+  const bool cok = gcb < P.N;
+  const int ecb = cok ? P.eb[gcb] : 0;
+  __shared__ int s_eb[FN];
+  if (tid < FN) s_eb[tid] = (tn * FN + tid < P.N) ? P.eb[tn * FN + tid] : 0;
+  double acc[FN];
+#pragma unroll
+  for (int j = 0; j < FN; ++j) acc[j] = 0.0;
+  uint32_t ph = 0;
+  bool ok = true;
+  for (int w0 = 0; w0 < P.K && ok; w0 += KWIN) {
+    const int w1 = min(P.K, w0 + KWIN);
+    for (int k0 = w0; k0 < w1; k0 += FK) {
+      // split this thread's row of the A chunk (coalesced over the rows)
+#pragma unroll 1
+      for (int k8 = 0; k8 < FK / 8; ++k8) {
+        uint32_t pk[SP][4];
+#pragma unroll
+        for (int s2 = 0; s2 < SP; ++s2) pk[s2][0] = pk[s2][1] = pk[s2][2] = pk[s2][3] = 0u;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int gk = k0 + k8 * 8 + c;
+          const double x = (rok && gk < w1) ? P.A[(long long)gk * P.lda + r] : 0.0;
+          digits_into(scaled_int(x, er), c, pk);
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < SP; ++s2)
+          *reinterpret_cast<uint4 *>(sa + s2 * FATILE + tile_off(tid, k8 * 8, FM)) =
+              make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+      }
+      // split one k octet of one B column
+      {
+        uint32_t pk[SP][4];
+#pragma unroll
+        for (int s2 = 0; s2 < SP; ++s2) pk[s2][0] = pk[s2][1] = pk[s2][2] = pk[s2][3] = 0u;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int gk = k0 + ko * 8 + c;
+          const double x = (cok && gk < w1) ? P.B[(long long)gcb * P.ldb + gk] : 0.0;
+          digits_into(scaled_int(x, ecb), c, pk);
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < SP; ++s2)
+          *reinterpret_cast<uint4 *>(sb + s2 * FBTILE + tile_off(cb, ko * 8, FN)) =
+              make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+      }
+      // generic-proxy stores -> visible to the tensor cores' async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+        for (int kk = 0; kk < FK / 16; ++kk)
+#pragma unroll 1
+          for (int s2 = 0; s2 < SP; ++s2)
+#pragma unroll 1
+            for (int q = 0; q + s2 < SP; ++q) {
+              const uint32_t aaddr = smem_u32(sa + s2 * FATILE) + kk * 2 * (FM * 16);
+              const uint32_t baddr = smem_u32(sb + q * FBTILE) + kk * 2 * (FN * 16);
+              const uint32_t accum = (k0 > w0 || kk > 0 || s2 > 0) ? 1u : 0u;
+              umma(tbase + (s2 + q) * FN, make_desc(aaddr, FM * 16, 128),
+                   make_desc(baddr, FN * 16, 128), idesc, accum);
+            }
+        umma_commit(&bar);
+      }
+      __syncwarp();
+      ok = __syncthreads_and(mbar_wait(&bar, ph));
+      ph ^= 1;
+      if (!ok) { if (tid == 0) atomicOr(err, 2); break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (!ok) break;
+    // drain the window's exact group sums
+    const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int c = 0; c < FN; c += 16) {
+      long long hv[16], lv[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) { hv[i] = 0; lv[i] = 0; }
+#pragma unroll
+      for (int g = 0; g < SP; ++g) {
+        float v[16];
+        tmem_ld16(lane_addr + g * FN + c, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const long long x = (long long)int_of_float(v[i]);
+          if (g < 3) hv[i] += x * (1ll << (8 * (2 - g)));
+          else lv[i] += x * (1ll << (8 * (6 - g)));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const double v = exact_double(hv[i], lv[i], er + s_eb[c + i] - 30);
+        acc[c + i] = w0 == 0 ? v : acc[c + i] + v;
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (ok && rok) {
+#pragma unroll
+    for (int j = 0; j < FN; ++j) {
+      const int c = tn * FN + j;
+      if (c < P.N) {
+        double *dst = P.C + (long long)c * P.ldc + r;
+        *dst = P.beta ? *dst + acc[j] : acc[j];
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(256));
 }
 
 // ----------------------------------------------------------------- host ---
@@ -470,6 +786,41 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
     attr = true;
   }
   k_gemm_tc<<<tiles, GTH, SMEM_TC, st>>>(dtc, (int)tc.size(), d_err);
+}
+
+
+void launch_gemm_fused(const std::vector<GemmDesc> &probs, int *d_err, cudaStream_t st) {
+  if (probs.empty()) return;
+  std::vector<ExpJob> rj, cj;
+  std::vector<FusedProb> fp;
+  int rows = 0, cols = 0, tiles = 0;
+  for (const auto &p : probs) {
+    rj.push_back({p.A, p.lda, p.M, p.K, nullptr, rows});
+    cj.push_back({p.B, p.ldb, p.N, p.K, nullptr, cols});
+    FusedProb f{p.A, p.B, p.C, nullptr, nullptr, p.lda, p.ldb, p.ldc, p.M, p.N, p.K, p.beta, tiles};
+    fp.push_back(f);
+    rows += p.M;
+    cols += p.N;
+    tiles += ((p.M + FM - 1) / FM) * ((p.N + FN - 1) / FN);
+  }
+  int *EA = pool<int>("gf_ea", rows + 1), *EB = pool<int>("gf_eb", cols + 1);
+  for (size_t i = 0; i < probs.size(); ++i) {
+    rj[i].out = EA + rj[i].off; cj[i].out = EB + cj[i].off;
+    fp[i].ea = rj[i].out; fp[i].eb = cj[i].out;
+  }
+  ExpJob *drj = pool<ExpJob>("gf_rj", rj.size()), *dcj = pool<ExpJob>("gf_cj", cj.size());
+  FusedProb *dfp = pool<FusedProb>("gf_fp", fp.size());
+  cudaMemcpyAsync(drj, rj.data(), rj.size() * sizeof(ExpJob), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dcj, cj.data(), cj.size() * sizeof(ExpJob), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dfp, fp.data(), fp.size() * sizeof(FusedProb), cudaMemcpyHostToDevice, st);
+  k_row_exps<<<(rows + 255) / 256, 256, 0, st>>>(drj, (int)rj.size(), rows);
+  k_col_exps<<<(unsigned)(((long long)cols * 32 + 255) / 256), 256, 0, st>>>(dcj, (int)cj.size(), cols);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gemm_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, FSMEM);
+    attr = true;
+  }
+  k_gemm_fused<<<tiles, 128, FSMEM, st>>>(dfp, (int)fp.size(), d_err);
 }
 
 }  // namespace hss

@@ -34,14 +34,17 @@ typedef struct hss_config {
   int sec_terms;  /* secular solver: at most this many lanes' worth of work per  */
                   /* root (lanes <= the power of two covering K / sec_terms); 0: 8 */
   int split_min_log2; /* split-BF16 products for M*N*K >= 2^this and M >=     */
-                      /* split_min_m; 0: 17                                    */
+                      /* split_min_m; 0: 15                                    */
   int small_nk;       /* FP64 products with N, K <= this on the element      */
                       /* kernel (thread per output); 0: 128                    */
-  int split_min_m;    /* smallest M of a split-BF16 product; 0: 256            */
+  int split_min_m;    /* smallest M of a split-BF16 product; 0: 128            */
   int sec_threads;    /* secular solver: fewest lanes per root that give this  */
                       /* many threads per level (and <= 64 terms per lane);    */
                       /* 0: 152 * 256                                          */
-  int reserved[3];
+  int gemm_path;      /* split-BF16 products: 0 digit planes staged in global  */
+                      /* memory, then the TMA-fed kernel (faster on the DC     */
+                      /* shapes); 1 operands split inside each CTA             */
+  int reserved[2];
 } hss_config;
 
 /* stages timed when hss_config.profile = 1 */
