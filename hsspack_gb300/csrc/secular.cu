@@ -52,29 +52,29 @@ __device__ __forceinline__ SecSums sec_eval(const double *__restrict__ d,
   const double o = K > 0 ? __ldg(d + oi) : 0.0;
   const int jlo = __reduce_min_sync(HSS_FULL, K > 0 ? jl : (1 << 29));
   const int jhi = __reduce_max_sync(HSS_FULL, K > 0 ? jl : -1);
-  auto term = [&](int i, double &v, double &dv) {
-    const double zi = __ldg(z + i);
+  // t = z_i / (d_i - x); the sums take z_i t and t^2 by fused multiply-adds
+  auto term = [&](int i, double &zi, double &t) {
+    zi = __ldg(z + i);
     const double di = __ldg(d + i);
     const double del = (SQ ? (di - o) * (di + o) : (di - o)) - tau;
-    const double t = zi * rcp_nr(del);
-    v = zi * t;
-    dv = t * t;
+    t = zi * rcp_nr(del);
   };
   int i = gl;
   for (const int e = min(K, jlo + 1); i < e; i += L) {
-    double v, dv;
-    term(i, v, dv);
-    a0 += v; a1 += dv;
+    double zi, t;
+    term(i, zi, t);
+    a0 = fma(zi, t, a0); a1 = fma(t, t, a1);
   }
   for (const int e = min(K, jhi + 1); i < e; i += L) {
-    double v, dv;
-    term(i, v, dv);
-    if (i <= jl) { a0 += v; a1 += dv; } else { b0 += v; b1 += dv; }
+    double zi, t;
+    term(i, zi, t);
+    if (i <= jl) { a0 = fma(zi, t, a0); a1 = fma(t, t, a1); }
+    else { b0 = fma(zi, t, b0); b1 = fma(t, t, b1); }
   }
   for (; i < K; i += L) {
-    double v, dv;
-    term(i, v, dv);
-    b0 += v; b1 += dv;
+    double zi, t;
+    term(i, zi, t);
+    b0 = fma(zi, t, b0); b1 = fma(t, t, b1);
   }
   SecSums s;
   s.psi = group_sum<L>(a0); s.dpsi = group_sum<L>(a1);
