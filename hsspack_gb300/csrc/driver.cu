@@ -55,6 +55,8 @@ struct Ctx {
   bool pred_ready = false;  // learned secular predictor installed
   void *pinned = nullptr;
   size_t pinned_cap = 0;
+  char *ring = nullptr;  // pinned staging ring for small parameter uploads
+  size_t ring_cap = 0, ring_head = 0;
   long long launches = 0;
   Ctx() {
     hss_default_config(&cfg);
@@ -113,6 +115,36 @@ static void *pinned(Ctx &c, size_t bytes) {
 
 void *pool_get(const char *name, size_t bytes) { return buf<char>(ctx(), name, bytes); }
 
+// Host->device parameter uploads (level views, product descriptors).  Small
+// ones stay pageable copies (measured faster: they travel with the command
+// stream); the larger lists of the batched levels go through a pinned ring --
+// a host memcpy plus an asynchronous copy, instead of a pageable copy staged
+// by the driver on the host while the GPU waits.  A ring region is reused
+// only after a device synchronisation.
+void stage_h2d(void *dst, const void *src, size_t bytes, void *stream) {
+  if (bytes == 0) return;
+  Ctx &c = ctx();
+  cudaStream_t st = (cudaStream_t)stream;
+  constexpr size_t RING = 16u << 20;
+  if (bytes <= (64u << 10) || bytes > RING / 4) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return;
+  }
+  if (!c.ring) {
+    CK(cudaMallocHost((void **)&c.ring, RING));
+    c.ring_cap = RING;
+    c.ring_head = 0;
+  }
+  if (c.ring_head + bytes > c.ring_cap) {
+    CK(cudaDeviceSynchronize());
+    c.ring_head = 0;
+  }
+  char *p = c.ring + c.ring_head;
+  memcpy(p, src, bytes);
+  CK(cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, st));
+  c.ring_head += (bytes + 255) & ~(size_t)255;
+}
+
 static cudaEvent_t next_event(Ctx &c) {
   if (c.evused == c.evpool.size()) {
     cudaEvent_t e;
@@ -154,7 +186,7 @@ static void collect_stage_times(Ctx &c) {
 
 template <class T>
 static void h2d(T *dst, const std::vector<T> &src, cudaStream_t st) {
-  if (!src.empty()) CK(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  if (!src.empty()) stage_h2d(dst, src.data(), src.size() * sizeof(T), st);
 }
 
 // ------------------------------------------------------------- DC block --
@@ -1199,6 +1231,9 @@ int hss_finalize(void) {
   if (c.pinned) cudaFreeHost(c.pinned);
   c.pinned = nullptr;
   c.pinned_cap = 0;
+  if (c.ring) cudaFreeHost(c.ring);
+  c.ring = nullptr;
+  c.ring_cap = c.ring_head = 0;
   return 0;
 }
 

@@ -160,8 +160,8 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
     for (const auto &p : tiny) eoff.push_back(eoff.back() + (long long)p.M * p.N);
     GemmDesc *d = pool<GemmDesc>("gemm_small_probs", tiny.size());
     long long *de = pool<long long>("gemm_small_eoff", eoff.size());
-    cudaMemcpyAsync(d, tiny.data(), tiny.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(de, eoff.data(), eoff.size() * sizeof(long long), cudaMemcpyHostToDevice, st);
+    stage_h2d(d, tiny.data(), tiny.size() * sizeof(GemmDesc), st);
+    stage_h2d(de, eoff.data(), eoff.size() * sizeof(long long), st);
     if (eoff.back() > 0)
       k_gemm_small<<<(unsigned)((eoff.back() + 255) / 256), 256, 0, st>>>((int)tiny.size(), d, de);
   }
@@ -169,7 +169,7 @@ void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStrea
   int tiles = 0;
   for (auto &p : tiled) { p.tile0 = tiles; tiles += gemm_tiles(p.M, p.N); }
   GemmDesc *d = pool<GemmDesc>("gemm_f64_probs", tiled.size());
-  cudaMemcpyAsync(d, tiled.data(), tiled.size() * sizeof(GemmDesc), cudaMemcpyHostToDevice, st);
+  stage_h2d(d, tiled.data(), tiled.size() * sizeof(GemmDesc), st);
   launch_gemm_f64((int)tiled.size(), tiles, d, st);
 }
 

@@ -774,9 +774,9 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   }
   SplitProb *dsa = pool<SplitProb>("gs_sa", sa.size()), *dsb = pool<SplitProb>("gs_sb", sb.size());
   TcProb *dtc = pool<TcProb>("gs_tc", tc.size());
-  cudaMemcpyAsync(dsa, sa.data(), sa.size() * sizeof(SplitProb), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(dsb, sb.data(), sb.size() * sizeof(SplitProb), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(dtc, tc.data(), tc.size() * sizeof(TcProb), cudaMemcpyHostToDevice, st);
+  stage_h2d(dsa, sa.data(), sa.size() * sizeof(SplitProb), st);
+  stage_h2d(dsb, sb.data(), sb.size() * sizeof(SplitProb), st);
+  stage_h2d(dtc, tc.data(), tc.size() * sizeof(TcProb), st);
   const unsigned gy = (unsigned)std::min<size_t>(sa.size(), 65535);
   k_split_a<<<dim3(maxtm, gy), 256, 0, st>>>(dsa, (int)sa.size());
   k_split_b<<<dim3(maxtn, gy), 256, 0, st>>>(dsb, (int)sb.size());
@@ -810,9 +810,9 @@ void launch_gemm_fused(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   }
   ExpJob *drj = pool<ExpJob>("gf_rj", rj.size()), *dcj = pool<ExpJob>("gf_cj", cj.size());
   FusedProb *dfp = pool<FusedProb>("gf_fp", fp.size());
-  cudaMemcpyAsync(drj, rj.data(), rj.size() * sizeof(ExpJob), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(dcj, cj.data(), cj.size() * sizeof(ExpJob), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(dfp, fp.data(), fp.size() * sizeof(FusedProb), cudaMemcpyHostToDevice, st);
+  stage_h2d(drj, rj.data(), rj.size() * sizeof(ExpJob), st);
+  stage_h2d(dcj, cj.data(), cj.size() * sizeof(ExpJob), st);
+  stage_h2d(dfp, fp.data(), fp.size() * sizeof(FusedProb), st);
   k_row_exps<<<(rows + 255) / 256, 256, 0, st>>>(drj, (int)rj.size(), rows);
   k_col_exps<<<(unsigned)(((long long)cols * 32 + 255) / 256), 256, 0, st>>>(dcj, (int)cj.size(), cols);
   static bool attr = false;

@@ -543,7 +543,7 @@ __global__ void k_init_gens(int K, const double *__restrict__ u, const double *_
 template <class T>
 static T *up(const char *name, const std::vector<T> &v, cudaStream_t st) {
   T *d = pool<T>(name, std::max<size_t>(v.size(), 1));
-  if (!v.empty()) HCK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  if (!v.empty()) stage_h2d(d, v.data(), v.size() * sizeof(T), st);
   return d;
 }
 

@@ -444,7 +444,7 @@ __global__ void k_copy_blocks(const CopyDesc *__restrict__ ds, int nd) {
 template <class T>
 static T *upload(const char *name, const std::vector<T> &v, cudaStream_t st) {
   T *d = pool<T>(name, std::max<size_t>(v.size(), 1));
-  if (!v.empty()) MCK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  if (!v.empty()) stage_h2d(d, v.data(), v.size() * sizeof(T), st);
   return d;
 }
 
