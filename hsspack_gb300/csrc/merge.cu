@@ -115,17 +115,34 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   // ---- candidates: z large enough (deflation by small z, mdlaed2.f90:304-313)
   const int chunk = (n + MT - 1) / MT;
   const int b0 = min(n, tid * chunk), b1 = min(n, b0 + chunk);
+  // The chunk loops take PB positions per step, loads first: each thread's
+  // chunk is contiguous (order-preserving compaction from one block scan),
+  // so the loads are not coalesced, and batching them hides the latency.
+  constexpr int PB = 8;
   int cnt = 0;
-  for (int i = b0; i < b1; ++i) {
-    const bool big = rho * fabs(w.zs[s + i]) > tol;  // typ 4: deflated, small z
-    cnt += big;
-    if (!big) w.typ[s + i] = 4;
+  for (int i0 = b0; i0 < b1; i0 += PB) {
+    double zv[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) zv[u] = i0 + u < b1 ? w.zs[s + i0 + u] : 0.0;
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      if (i0 + u >= b1) break;
+      const bool big = rho * fabs(zv[u]) > tol;  // typ 4: deflated, small z
+      cnt += big;
+      if (!big) w.typ[s + i0 + u] = 4;
+    }
   }
   unsigned long long tot;
   int pos = (int)block_scan64<MT>((unsigned long long)cnt, &tot);
   const int nc = (int)tot;
-  for (int i = b0; i < b1; ++i)
-    if (w.typ[s + i] != 4) w.cand[s + pos++] = i;
+  for (int i0 = b0; i0 < b1; i0 += PB) {
+    unsigned char tv[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) tv[u] = i0 + u < b1 ? w.typ[s + i0 + u] : 4;
+#pragma unroll
+    for (int u = 0; u < PB; ++u)
+      if (tv[u] != 4) w.cand[s + pos++] = i0 + u;
+  }
   __syncthreads();
   // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371): a
   //      sequential chain over the candidates, run by one thread on a shared-
@@ -215,10 +232,16 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   //      and deflated (slots, values) lists
   unsigned long long pk = 0;
   int n5 = 0;
-  for (int i = b0; i < b1; ++i) {
-    const int t = w.typ[s + i];
-    if (t <= 3) pk += 1ull << (21 * (t == 1 ? 0 : t == 2 ? 1 : 2));
-    n5 += (t == 5);
+  for (int i0 = b0; i0 < b1; i0 += PB) {
+    unsigned char tv[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) tv[u] = i0 + u < b1 ? w.typ[s + i0 + u] : 4;
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      const int t = tv[u];
+      if (t <= 3) pk += 1ull << (21 * (t == 1 ? 0 : t == 2 ? 1 : 2));
+      n5 += (t == 5);
+    }
   }
   unsigned long long ptot, t5;
   unsigned long long pre = block_scan64<MT>(pk, &ptot);
@@ -229,25 +252,41 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   const int nrot = (int)t5;
   int r1 = (int)(pre & 0x1fffff), r2 = (int)((pre >> 21) & 0x1fffff),
       r3 = (int)((pre >> 42) & 0x1fffff);
-  for (int i = b0; i < b1; ++i) {
-    const int t = w.typ[s + i];
-    const int j = r1 + r2 + r3;  // non-deflated before position i
-    if (t <= 3) {
-      w.dl[s + j] = w.ds[s + i];
-      w.zw[s + j] = w.zs[s + i];
-      w.ndslot[s + j] = w.srt[s + i];
-      w.grp[s + j] = (t == 1) ? r1 : (t == 2) ? c1 + r2 : c1 + c2 + r3;
-      if (t == 1) ++r1; else if (t == 2) ++r2; else ++r3;
-    } else {
-      const int a = i - j;  // deflated before position i
-      const int slot = w.srt[s + i];
-      const double v = w.ds[s + i];
-      Dp[slot] = v;
-      if (t == 5) {
-        w.l2slot[s + r5] = slot; w.l2val[s + r5] = v; ++r5;
+  for (int i0 = b0; i0 < b1; i0 += PB) {
+    unsigned char tv[PB];
+    double dv[PB], zv[PB];
+    int sv[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      const bool in = i0 + u < b1;
+      tv[u] = in ? w.typ[s + i0 + u] : 0;
+      dv[u] = in ? w.ds[s + i0 + u] : 0.0;
+      zv[u] = in ? w.zs[s + i0 + u] : 0.0;
+      sv[u] = in ? w.srt[s + i0 + u] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      const int i = i0 + u;
+      if (i >= b1) break;
+      const int t = tv[u];
+      const int j = r1 + r2 + r3;  // non-deflated before position i
+      if (t <= 3) {
+        w.dl[s + j] = dv[u];
+        w.zw[s + j] = zv[u];
+        w.ndslot[s + j] = sv[u];
+        w.grp[s + j] = (t == 1) ? r1 : (t == 2) ? c1 + r2 : c1 + c2 + r3;
+        if (t == 1) ++r1; else if (t == 2) ++r2; else ++r3;
       } else {
-        const int a1 = a - r5;  // small-z deflated before position i
-        w.l1slot[s + a1] = slot; w.l1val[s + a1] = v;
+        const int a = i - j;  // deflated before position i
+        const int slot = sv[u];
+        const double v = dv[u];
+        Dp[slot] = v;
+        if (t == 5) {
+          w.l2slot[s + r5] = slot; w.l2val[s + r5] = v; ++r5;
+        } else {
+          const int a1 = a - r5;  // small-z deflated before position i
+          w.l1slot[s + a1] = slot; w.l1val[s + a1] = v;
+        }
       }
     }
   }
