@@ -43,10 +43,10 @@ namespace hss {
 constexpr int SP = 7;        // digit planes
 constexpr int TM = 128;      // output tile rows (tcgen05 M)
 constexpr int TN = 64;       // output tile cols (tcgen05 N)
-constexpr int TK = 64;       // K per staged chunk
+constexpr int TK = 32;       // K per staged chunk (two chunks in flight)
 constexpr int KWIN = 128;    // exactness window for groups 0..2
-constexpr int ATILE = TM * TK * 2;  // bytes of one A digit-plane tile (16 KB)
-constexpr int BTILE = TN * TK * 2;  // bytes of one B digit-plane tile (8 KB)
+constexpr int ATILE = TM * TK * 2;  // bytes of one A digit-plane tile (8 KB)
+constexpr int BTILE = TN * TK * 2;  // bytes of one B digit-plane tile (4 KB)
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
 
 // ------------------------------------------------------------ splitting ---
@@ -376,14 +376,15 @@ struct TcProb {
 // columns 32 (w / 4) .. + 31 of each group
 constexpr int GTH = 256;
 // 16 KB of slack keeps every descriptor-addressed byte inside the allocation
-constexpr int SMEM_TC = SP * ATILE + SP * BTILE + 16384;
+constexpr int STAGE_TC = SP * (ATILE + BTILE);      // one K chunk of both operands
+constexpr int SMEM_TC = 2 * STAGE_TC + 16384;
 
 __global__ void __launch_bounds__(GTH, 1)
 k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t bar_tma, bar_mma;
+  __shared__ uint64_t full[2], empty[2];
   __shared__ uint32_t tmem_base;
-  // locate problem and tile
+  __shared__ int s_ok;
   int lo = 0, hi = nprob;
   const int b = blockIdx.x;
   while (hi - lo > 1) {
@@ -395,8 +396,9 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   const int ntm = (P.M + TM - 1) / TM;
   const int tm = t % ntm, tn = t / ntm;
   const int tid = threadIdx.x, warp = tid >> 5;
-  unsigned char *sa = smem;                   // SP A planes
-  unsigned char *sb = smem + SP * ATILE;      // SP B planes
+  // stage q: A planes at smem + q * STAGE_TC, B planes after them
+  auto sa = [&](int q) { return smem + q * STAGE_TC; };
+  auto sb = [&](int q) { return smem + q * STAGE_TC + SP * ATILE; };
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base)),
@@ -404,8 +406,9 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    mbar_init(&bar_tma, 1);
-    mbar_init(&bar_mma, 1);
+    mbar_init(&full[0], 1); mbar_init(&full[1], 1);
+    mbar_init(&empty[0], 1); mbar_init(&empty[1], 1);
+    s_ok = 1;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -417,53 +420,64 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   long long hacc[TH], lacc[TH];
 #pragma unroll
   for (int j = 0; j < TH; ++j) { hacc[j] = 0; lacc[j] = 0; }
-  uint32_t ph_tma = 0, ph_mma = 0;
-  bool ok = true;
+  // thread 0: TMA producer and MMA issuer.  Chunk k lives in stage k & 1;
+  // chunk k + 2 is loaded into it once chunk k's MMAs have completed, so a
+  // chunk's copy overlaps the previous chunk's MMAs.  Every barrier phase is
+  // waited on exactly once, each wait bounded.
+  uint32_t ph_full[2] = {0, 0}, ph_empty[2] = {0, 0};
+  int issued = 0;  // chunks whose copies were started
+  auto load = [&](int kt) {
+    const int q = kt & 1;
+    mbar_expect_tx(&full[q], STAGE_TC);
+    const char *ga = P.a_planes + ((long long)tm * P.ktiles + kt) * SP * ATILE;
+    const char *gb = P.b_planes + ((long long)tn * P.ktiles + kt) * SP * BTILE;
+    tma_load(sa(q), ga, SP * ATILE, &full[q]);
+    tma_load(sb(q), gb, SP * BTILE, &full[q]);
+    ++issued;
+  };
+  if (tid == 0) {
+    if (P.ktiles > 0) load(0);
+    if (P.ktiles > 1) load(1);
+  }
   const int kwin = KWIN / TK;  // chunks per exactness window
-  for (int kt0 = 0; kt0 < P.ktiles && ok; kt0 += kwin) {
+  int waited = 0;              // chunks whose copies were waited for
+  for (int kt0 = 0; kt0 < P.ktiles; kt0 += kwin) {
     const int kt1 = min(P.ktiles, kt0 + kwin);
-    for (int kt = kt0; kt < kt1; ++kt) {
-      // stage the SP A and SP B digit-plane tiles of this K chunk (TMA)
-      if (tid == 0) {
-        mbar_expect_tx(&bar_tma, SP * (ATILE + BTILE));
-        const char *ga = P.a_planes + ((long long)tm * P.ktiles + kt) * SP * ATILE;
-        const char *gb = P.b_planes + ((long long)tn * P.ktiles + kt) * SP * BTILE;
-        tma_load(sa, ga, SP * ATILE, &bar_tma);
-        tma_load(sb, gb, SP * BTILE, &bar_tma);
-      }
-      ok = __syncthreads_and(mbar_wait(&bar_tma, ph_tma));  // block-uniform
-      ph_tma ^= 1;
-      if (!ok) { if (tid == 0) atomicOr(err, 1); break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (tid == 0) {
-        // digit-plane products with s + t < SP into group accumulator g
-#pragma unroll 1
-        for (int kk = 0; kk < TK / 16; ++kk) {
-#pragma unroll 1
-          for (int s = 0; s < SP; ++s)
-#pragma unroll 1
-            for (int q = 0; q + s < SP; ++q) {
-              const int g = s + q;
-              const uint32_t aaddr = smem_u32(sa + s * ATILE) + kk * 2 * (TM * 16);
-              const uint32_t baddr = smem_u32(sb + q * BTILE) + kk * 2 * (TN * 16);
-              const uint64_t ad = make_desc(aaddr, TM * 16, 128);
-              const uint64_t bd = make_desc(baddr, TN * 16, 128);
-              // first product of this group in the window overwrites
-              const uint32_t accum = (kt > kt0 || kk > 0 || s > 0) ? 1u : 0u;
-              umma(tbase + g * TN, ad, bd, idesc, accum);
+    if (tid == 0 && s_ok) {
+      for (int kt = kt0; kt < kt1; ++kt) {
+        const int q = kt & 1;
+        if (!mbar_wait(&full[q], ph_full[q])) { atomicOr(err, 1); s_ok = 0; break; }
+        ph_full[q] ^= 1;
+        ++waited;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // descriptor(address + offset) = descriptor(address) + offset / 16:
+        // two base descriptors, constant offsets in the unrolled issue loop
+        const uint64_t ad0 = make_desc(smem_u32(sa(q)), TM * 16, 128);
+        const uint64_t bd0 = make_desc(smem_u32(sb(q)), TN * 16, 128);
+        const uint32_t later = kt > kt0 ? 1u : 0u;
+#pragma unroll
+        for (int kk = 0; kk < TK / 16; ++kk)
+#pragma unroll
+          for (int s2 = 0; s2 < SP; ++s2)
+#pragma unroll
+            for (int p2 = 0; p2 + s2 < SP; ++p2) {
+              // the first product of a group in the window overwrites
+              const uint32_t accum = (kk > 0 || s2 > 0) ? 1u : later;
+              umma(tbase + (s2 + p2) * TN, ad0 + (uint64_t)((s2 * ATILE + kk * 2 * (TM * 16)) >> 4),
+                   bd0 + (uint64_t)((p2 * BTILE + kk * 2 * (TN * 16)) >> 4), idesc, accum);
             }
-        }
-        umma_commit(&bar_mma);
+        umma_commit(&empty[q]);
+        if (!mbar_wait(&empty[q], ph_empty[q])) { atomicOr(err, 2); s_ok = 0; break; }
+        ph_empty[q] ^= 1;
+        if (kt + 2 < P.ktiles) load(kt + 2);
       }
-      __syncwarp();
-      ok = __syncthreads_and(mbar_wait(&bar_mma, ph_mma));
-      ph_mma ^= 1;
-      if (!ok) { if (tid == 0) atomicOr(err, 2); break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
-    if (!ok) break;
-    // drain the group sums of this window (exact integers below 2^24) into
-    // the int64 accumulators; integer and conversion pipes only
+    // the window's MMAs are complete (thread 0 waited for every commit)
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_ok) break;
+    // drain the window's exact group sums into the int64 accumulators
     const uint32_t lane_addr =
         tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TH);
 #pragma unroll
@@ -484,6 +498,16 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
+  if (tid == 0 && !s_ok) {
+    // a bounded wait gave up: wait (bounded) for the copies still in flight
+    // before the CTA's shared memory is released
+    for (int kt = waited; kt < issued; ++kt) {
+      const int q = kt & 1;
+      if (!mbar_wait(&full[q], ph_full[q])) break;
+      ph_full[q] ^= 1;
+    }
+  }
+  const bool ok = s_ok != 0;
   // epilogue: C = 2^{e_i + f_j - 30} (H + 2^-32 L) (+ C)
   const int r = tm * TM + (warp & 3) * 32 + (tid & 31);
   if (ok && r < P.M) {
@@ -674,17 +698,18 @@ k_gemm_fused(const FusedProb *__restrict__ probs, int nprob, int *__restrict__ e
       __syncthreads();
       if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
+        const uint64_t ad0 = make_desc(smem_u32(sa), FM * 16, 128);
+        const uint64_t bd0 = make_desc(smem_u32(sb), FN * 16, 128);
+        const uint32_t later = k0 > w0 ? 1u : 0u;
+#pragma unroll
         for (int kk = 0; kk < FK / 16; ++kk)
-#pragma unroll 1
+#pragma unroll
           for (int s2 = 0; s2 < SP; ++s2)
-#pragma unroll 1
+#pragma unroll
             for (int q = 0; q + s2 < SP; ++q) {
-              const uint32_t aaddr = smem_u32(sa + s2 * FATILE) + kk * 2 * (FM * 16);
-              const uint32_t baddr = smem_u32(sb + q * FBTILE) + kk * 2 * (FN * 16);
-              const uint32_t accum = (k0 > w0 || kk > 0 || s2 > 0) ? 1u : 0u;
-              umma(tbase + (s2 + q) * FN, make_desc(aaddr, FM * 16, 128),
-                   make_desc(baddr, FN * 16, 128), idesc, accum);
+              const uint32_t accum = (kk > 0 || s2 > 0) ? 1u : later;
+              umma(tbase + (s2 + q) * FN, ad0 + (uint64_t)((s2 * FATILE + kk * 2 * (FM * 16)) >> 4),
+                   bd0 + (uint64_t)((q * FBTILE + kk * 2 * (FN * 16)) >> 4), idesc, accum);
             }
         umma_commit(&bar);
       }
