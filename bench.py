@@ -212,9 +212,11 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
             t0.record(stream)
             for _ in range(steps):
                 fn()
-                launches += hp.get_stats()["kernel_launches"]
             t1.record(stream)
             torch.cuda.synchronize()
+            # the last call's launch count (each step does the same work),
+            # read after the timed region
+            launches = hp.get_stats()["kernel_launches"] * steps
             return t0.elapsed_time(t1) / steps, launches
         finally:
             hp.restore_config(old)
@@ -440,15 +442,24 @@ def run_ours(args):
             t0.record(stream)
             for _ in range(steps):
                 solve()
-                st = hp.get_stats()
-                launches += st["kernel_launches"]
-                for k in acc:
-                    src = st["stage_" + k]
-                    for s, v in src.items():
-                        acc[k][s] = acc[k].get(s, 0) + v
+                if profile:  # per-step stage times (stats are reset by every call)
+                    st = hp.get_stats()
+                    launches += st["kernel_launches"]
+                    for k in acc:
+                        for s, v in st["stage_" + k].items():
+                            acc[k][s] = acc[k].get(s, 0) + v
             t1.record(stream)
             torch.cuda.synchronize()
             ms = t0.elapsed_time(t1) / steps
+            if not profile:
+                # every step does the same work: the last call's counts, times
+                # the steps (read after the timed region, so that no host work
+                # between steps is timed)
+                st = hp.get_stats()
+                launches = st["kernel_launches"] * steps
+                for k in acc:
+                    for s, v in st["stage_" + k].items():
+                        acc[k][s] = v * steps
             if world > 1:
                 x = torch.tensor([ms], device="cuda")
                 dist.all_reduce(x, op=dist.ReduceOp.MAX)
