@@ -234,6 +234,25 @@ static LevelArrays level_arrays(Ctx &c, int n) {
   return a;
 }
 
+// Host arrays of one phase packed into a single upload: each call of a
+// pageable host->device copy costs microseconds of host time while the GPU
+// waits at a level boundary; one copy per phase replaces a dozen.
+struct Pack {
+  std::vector<char> h;
+  template <class T>
+  size_t add(const std::vector<T> &v) {
+    const size_t off = (h.size() + 15) & ~(size_t)15;
+    h.resize(off + v.size() * sizeof(T));
+    if (!v.empty()) memcpy(h.data() + off, v.data(), v.size() * sizeof(T));
+    return off;
+  }
+  char *upload(Ctx &c, const char *name, cudaStream_t st) {
+    char *d = buf<char>(c, name, std::max<size_t>(h.size(), 16));
+    stage_h2d(d, h.data(), h.size(), st);
+    return d;
+  }
+};
+
 // One of the kd rank-one updates of a banded merge (the loop of MDSBED1,
 // SRC/mdsbed1.f90): z per slot (a column of Z = Q^T W), the coupling rho_in
 // per merge of the group, prepare flags, and the columns of Z still to come,
@@ -257,18 +276,19 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   const int P = (int)ms.size();
   if (P == 0) return;
   // ---- upload the group and prepare (deflation)
-  int *dms = buf<int>(c, "g_ms", P), *dmn = buf<int>(c, "g_mn", P), *dmn1 = buf<int>(c, "g_mn1", P);
-  h2d(dms, ms, st); h2d(dmn, mn, st); h2d(dmn1, mn1, st);
+  int pflags = bu ? bu->flags : 0;
+  std::vector<int> poff(P + 1, 0);
+  for (int m = 0; m < P; ++m) poff[m + 1] = poff[m] + mn[m];
+  Pack pk0;
+  const size_t o_ms = pk0.add(ms), o_mn = pk0.add(mn), o_mn1 = pk0.add(mn1), o_po = pk0.add(poff);
+  char *d0 = pk0.upload(c, "g_pack", st);
+  int *dms = (int *)(d0 + o_ms), *dmn = (int *)(d0 + o_mn), *dmn1 = (int *)(d0 + o_mn1);
   int *dout = buf<int>(c, "g_out", 5 * P);
   double *drho = buf<double>(c, "g_rho", P);
   stage_begin(HSS_ST_PREPARE, st);
-  int pflags = bu ? bu->flags : 0;
   if (!(pflags & PREP_SORTED)) {
     // merged order and z for every position of the level in one wide launch
-    std::vector<int> poff(P + 1, 0);
-    for (int m = 0; m < P; ++m) poff[m + 1] = poff[m] + mn[m];
-    int *dpo = buf<int>(c, "g_poff", P + 1);
-    h2d(dpo, poff, st);
+    int *dpo = (int *)(d0 + o_po);
     launch_merge_front(P, poff[P], dpo, dms, dmn, dmn1, e, Q, ldq, Dp, perm, L.w,
                        bu ? bu->z : nullptr, bu ? bu->rho : nullptr, pflags, st, L.sup);
     pflags |= PREP_FRONT;
@@ -324,11 +344,19 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     stot += (long long)K * K;
   }
   const int PA = (int)as.size();
+  // every array the level's launches read, in one upload
+  std::vector<int> apoff(PA + 1, 0);
+  for (int a = 0; a < PA; ++a) apoff[a + 1] = apoff[a] + an[a];
+  Pack pk;
+  const size_t o_gs = pk.add(gs), o_gn = pk.add(gn), o_gng = pk.add(gng);
+  const size_t o_as = pk.add(as), o_aK = pk.add(aK), o_aoff = pk.add(aoff), o_arho = pk.add(arho),
+               o_apoff = pk.add(apoff);
+  const size_t o_ds = pk.add(ds_), o_dK = pk.add(dK_), o_doff = pk.add(doff), o_drho = pk.add(drho_),
+               o_dn = pk.add(dn_), o_q2 = pk.add(q2off), o_so = pk.add(soff);
+  char *dpk = pk.upload(c, "l_pack", st);
   // ---- Givens rotations of deflation
   if (!gs.empty()) {
-    int *g1 = buf<int>(c, "gv_s", gs.size()), *g2 = buf<int>(c, "gv_n", gs.size()),
-        *g3 = buf<int>(c, "gv_g", gs.size());
-    h2d(g1, gs, st); h2d(g2, gn, st); h2d(g3, gng, st);
+    int *g1 = (int *)(dpk + o_gs), *g2 = (int *)(dpk + o_gn), *g3 = (int *)(dpk + o_gng);
     stage_begin(HSS_ST_GIVENS, st);
     launch_widen((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, L.sup, st);
     launch_givens((int)gs.size(), maxn_g, g1, g2, g3, L.w, Q, ldq, st, bu ? bu->zrest : nullptr,
@@ -340,10 +368,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   }
   if (PA == 0) return;
   // ---- secular equation + Loewner for every active merge
-  int *vs = buf<int>(c, "a_s", PA), *vK = buf<int>(c, "a_K", PA), *voff = buf<int>(c, "a_off", PA + 1),
-      *vn = buf<int>(c, "a_n", PA);
-  double *vrho = buf<double>(c, "a_rho", PA);
-  h2d(vs, as, st); h2d(vK, aK, st); h2d(voff, aoff, st); h2d(vrho, arho, st); h2d(vn, an, st);
+  int *vs = (int *)(dpk + o_as), *vK = (int *)(dpk + o_aK), *voff = (int *)(dpk + o_aoff);
+  double *vrho = (double *)(dpk + o_arho);
   LevelView lv{vs, vK, vrho, voff, PA};
   const int total = aoff.back();
   c.stats.secular_roots += total;
@@ -386,12 +412,10 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   // ---- dense merges: S, gather, GEMM (block structured), scatter
   const int PD = (int)ds_.size();
   if (PD > 0) {
-    int *xs = buf<int>(c, "d_s", PD), *xK = buf<int>(c, "d_K", PD), *xoff = buf<int>(c, "d_off", PD + 1),
-        *xn = buf<int>(c, "d_n", PD);
-    double *xrho = buf<double>(c, "d_rho", PD);
-    long long *xq2 = buf<long long>(c, "d_q2off", PD), *xso = buf<long long>(c, "d_soff", PD);
-    h2d(xs, ds_, st); h2d(xK, dK_, st); h2d(xoff, doff, st); h2d(xrho, drho_, st); h2d(xn, dn_, st);
-    h2d(xq2, q2off, st); h2d(xso, soff, st);
+    int *xs = (int *)(dpk + o_ds), *xK = (int *)(dpk + o_dK), *xoff = (int *)(dpk + o_doff),
+        *xn = (int *)(dpk + o_dn);
+    double *xrho = (double *)(dpk + o_drho);
+    long long *xq2 = (long long *)(dpk + o_q2), *xso = (long long *)(dpk + o_so);
     LevelView dv{xs, xK, xrho, xoff, PD};
     const int dtot = doff.back();
     double *Q2 = buf<double>(c, "Q2", q2tot), *T = buf<double>(c, "T", q2tot);
@@ -449,13 +473,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   }
   // ---- new ascending order and eigenvalues of the rewritten slots
   stage_begin(HSS_ST_FINISH, st);
-  {
-    std::vector<int> apoff(PA + 1, 0);
-    for (int a = 0; a < PA; ++a) apoff[a + 1] = apoff[a] + an[a];
-    int *dapo = buf<int>(c, "a_poff", PA + 1);
-    h2d(dapo, apoff, st);
-    launch_merge_finish_grid(PA, apoff[PA], dapo, vs, vK, L.lam, L.w, perm, Dp, st);
-  }
+  launch_merge_finish_grid(PA, apoff[PA], (int *)(dpk + o_apoff), vs, vK, L.lam, L.w, perm, Dp, st);
   {
     long long nn = 0;
     for (int x : an) nn += x;
