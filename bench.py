@@ -480,7 +480,7 @@ def run_ours(args):
         tuned, tune_ms = {"smlsiz": args.smlsiz, "predictor": 0}, None
     else:
         tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
-                                       predictor=(0, 1) if have_pred else (0,))
+                                       predictor=(0, 1, 2) if have_pred else (0, 2))
     full_cfg.update(tuned)
     plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()
@@ -577,7 +577,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "tridiagonal DC eigensolve n=%d, D,E iid U[-1,1] seed 0, COMPZ='I'"
                    % n, "n": n, "mode": "batched levels, split-BF16 tensor-core products" +
-                           (", learned secular start" if full_cfg.get("predictor") else ""),
+                           ("", ", learned secular start", ", FP32 pre-solved secular start")
+                           [int(full_cfg.get("predictor", 0))],
                    "smlsiz": full_cfg.get("smlsiz"), "autotune_ms": tune_ms,
                    "l2": "no flush: the 8.6 GB eigenvector matrix exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},

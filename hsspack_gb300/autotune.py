@@ -1,10 +1,10 @@
 """Autotuner for the divide-and-conquer configuration.
 
 Chooses, per problem-size bucket (powers of two), the DC leaf size SMLSIZ and
-whether the learned secular start is used, by timing the candidate settings on
-a seeded random tridiagonal of that size (device time from the library's CUDA
-events).  Results are cached in ``_lib/autotune.json`` next to the library and
-applied with :func:`apply`.
+the secular start (standard, learned or FP32 pre-solve), by timing the
+candidate settings on a seeded random tridiagonal of that size (device time
+from the library's CUDA events).  Results are cached in ``_lib/autotune.json``
+next to the library and applied with :func:`apply`.
 """
 import json
 import os
@@ -31,9 +31,10 @@ def load_cache():
 
 
 def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None, predictor=(0,)):
-    """Time MDSTEDC('I') at size n for each DC leaf size and learned-start
-    setting; return the best config dict (and all timings, keyed
-    "smlsiz" or "smlsiz+learned") and cache it under the size bucket."""
+    """Time MDSTEDC('I') at size n for each DC leaf size and secular start
+    (predictor 0 standard, 1 learned, 2 FP32 pre-solve); return the best
+    config dict (and all timings, keyed "smlsiz", "smlsiz+learned" or
+    "smlsiz+fp32") and cache it under the size bucket."""
     import torch
     import hsspack_gb300 as hp
     rng = np.random.default_rng(seed)
@@ -45,7 +46,7 @@ def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None, predictor=(
     results, cfgs = {}, {}
     for pred in predictor:
         for sml in candidates:
-            key = "%d%s" % (sml, "+learned" if pred else "")
+            key = "%d%s" % (sml, ("", "+learned", "+fp32")[int(pred)])
             cfg = dict(base or {}, smlsiz=int(sml), predictor=int(pred))
             old = hp.set_config(**cfg)
             try:

@@ -376,7 +376,16 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   double k2 = 0.0;
   for (int K : aK) k2 += (double)K * K;
   float *guess = nullptr;
-  if (c.cfg.predictor && c.pred_ready) {
+  const int maxK = *std::max_element(aK.begin(), aK.end());
+  if (c.cfg.predictor == 2) {
+    // starts from an FP32 pre-solve of every root
+    guess = buf<float>(c, "guess", L.n);
+    float *d32 = buf<float>(c, "pole_f32", L.n), *z32 = buf<float>(c, "z_f32", L.n);
+    stage_begin(HSS_ST_PREDICT, st);
+    launch_secular_guess32(lv, total, maxK, L.n, L.w.dl, L.w.zw, d32, z32, guess, st);
+    stage_end(HSS_ST_PREDICT, st, 0, 0.0);
+    c.launches += 2;
+  } else if (c.cfg.predictor && c.pred_ready) {
     // features for every position of the level (unused slots carry side = -1)
     float *feat = buf<float>(c, "pred_feat", (size_t)L.n * (mlp_nfeat() + 1));
     guess = buf<float>(c, "guess", L.n);
@@ -389,9 +398,8 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     c.launches += 2;
   }
   stage_begin(HSS_ST_SECULAR, st);
-  launch_secular(lv, total, *std::max_element(aK.begin(), aK.end()), L.w.dl, L.w.zw, L.lam, L.difl,
-                 L.difr, L.iters, status,
-                 (unsigned long long *)(status + 2), guess, st);
+  launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
+                 (unsigned long long *)(status + 2), guess, st, false, c.cfg.predictor == 2);
   // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 8.0 * 4.0 * k2);
   stage_begin(HSS_ST_LOWNER, st);
@@ -1612,7 +1620,11 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     CK(cudaMemsetAsync(status, 0, sizeof(int), st));
     LevelView lv{vs, vK, vr, vo, 1};
     float *guess = nullptr;
-    if (c.cfg.predictor && c.pred_ready) {
+    if (c.cfg.predictor == 2) {
+      guess = buf<float>(c, "x_guess", k);
+      launch_secular_guess32(lv, k, k, k, dlamda, z, buf<float>(c, "x_d32", k),
+                             buf<float>(c, "x_z32", k), guess, st);
+    } else if (c.cfg.predictor && c.pred_ready) {
       float *feat = buf<float>(c, "x_feat", (size_t)k * (mlp_nfeat() + 1));
       guess = buf<float>(c, "x_guess", k);
       launch_secular_mid(lv, k, k, dlamda, z, feat, st);
@@ -1620,7 +1632,8 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     }
     unsigned long long *cnt = (unsigned long long *)buf<char>(c, "x_counts", 16);
     CK(cudaMemsetAsync(cnt, 0, 16, st));
-    launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, cnt, guess, st);
+    launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, cnt, guess, st, false,
+                   c.cfg.predictor == 2);
     unsigned long long hc[2];
     CK(cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
     int hs = 0;

@@ -41,10 +41,16 @@ void set_secular_terms(int t);
 // threads a secular level should reach before lanes per root shrink (0: 152 * 256)
 void set_secular_threads(int t);
 // sq: singular-value mode (poles d_i^2, outputs sigma and DIFL/DIFR = sigma - d)
+// guess: per root start (see root_init), full: its bracket is the whole interval
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st,
-                    bool sq = false);
+                    bool sq = false, bool full = false);
+// starts for the FP64 iteration from an FP32 pre-solve (npos: positions of the
+// level arrays, d32 / z32 their FP32 copies)
+void launch_secular_guess32(const LevelView &lv, int total, int maxk, int npos,
+                            const double *dl, const double *zw, float *d32, float *z32,
+                            float *guess, cudaStream_t st);
 // maxk: the largest K of the launch (lanes per root as the secular kernel;
 // the default keeps a full warp per root)
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,

@@ -126,6 +126,8 @@ struct RootState {
   bool last;
   bool learned;  // started from the learned position; checked at the first step
   bool fell_back;
+  bool fw;       // step model: false middle way, true fixed weight (origin pole exact)
+  double prew;   // residual of the previous step (0: none yet)
 };
 
 __device__ __forceinline__ double pole(const RootState &r, int i) { return __ldg(r.d + i); }
@@ -139,7 +141,12 @@ __device__ __forceinline__ double gap(const RootState &r, int i) { return pdiff(
 
 // First evaluation point: the midpoint of the pole interval (standard guess),
 // or the learned position (phase 1 directly).
-__device__ __forceinline__ void root_init(RootState &r, float guess, double zsq) {
+// guess: signed distance of the start to the nearer pole in units of the
+// interval (|guess| <= 1/2; anything else: the standard midpoint start).
+// full: the start's side is not known (an FP32 pre-solve) -- the bracket is
+// the whole interval; otherwise (a learned start after the FP64 midpoint
+// evaluation) the half interval.
+__device__ __forceinline__ void root_init(RootState &r, float guess, double zsq, bool full) {
   r.rhoinv = 1.0 / r.rho;
   r.iters = 0;
   r.status = HSS_OK;
@@ -151,13 +158,16 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq)
   r.phase = 0;
   r.learned = false;
   r.fell_back = false;
+  r.fw = false;
+  r.prew = 0.0;
   if (!r.last) {
     r.oi = r.j;
     r.tau = 0.5 * r.delta;
     if (guess != 0.0f && fabsf(guess) <= 0.5f) {  // learned signed distance to the nearer pole
       // the midpoint pass already fixed the half interval (one evaluation)
-      if (guess > 0.0f) { r.oi = r.j; r.tau = (double)guess * r.delta; r.lo = 0.0; r.hi = 0.5 * r.delta; }
-      else { r.oi = r.j + 1; r.tau = (double)guess * r.delta; r.lo = -0.5 * r.delta; r.hi = 0.0; }
+      const double half = full ? r.delta : 0.5 * r.delta;
+      if (guess > 0.0f) { r.oi = r.j; r.tau = (double)guess * r.delta; r.lo = 0.0; r.hi = half; }
+      else { r.oi = r.j + 1; r.tau = (double)guess * r.delta; r.lo = -half; r.hi = 0.0; }
       r.phase = 1;
       r.learned = true;
       r.iters = 1;
@@ -217,29 +227,62 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
     r.learned = false;
     if (!(fabs(w / dw) <= 0.45 * r.delta)) {
       r.fell_back = true;
+      r.prew = 0.0;
       r.phase = 0;
       r.oi = r.j;
       r.tau = 0.5 * r.delta;
       return;
     }
   }
+  // a residual that kept its sign and fell by less than 10x: change the model
+  if (!r.last && w * r.prew > 0.0 && fabs(w) > 0.1 * fabs(r.prew)) r.fw = !r.fw;
+  r.prew = w;
   if (w < 0.0) r.lo = fmax(r.lo, r.tau); else r.hi = fmin(r.hi, r.tau);
+  // Two-pole model  c + s_l/(gl - eta) + s_r/(gr - eta)  matching w and dw at
+  // eta = 0; cleared of denominators it is  c eta^2 - a eta + b = 0, and only
+  // c depends on how dw is shared between the two poles.
   const double gl = gap(r, r.jl) - r.tau;
   const double gr = gap(r, r.jr) - r.tau;
   const double a = (gl + gr) * w - gl * gr * dw;
   const double b = gl * gr * w;
-  const double c = w - gl * s.dpsi - gr * s.dphi;
-  double eta;
-  if (c == 0.0) {
-    eta = (a != 0.0) ? b / a : -w / dw;
+  double c;
+  if (!r.fw) {  // middle way: each side's sum on its own pole
+    c = w - gl * s.dpsi - gr * s.dphi;
+  } else if (r.oi == r.j) {  // fixed weight: origin pole exact, the rest on the other
+    const double q = (__ldg(r.z + r.jl) / gl) * (__ldg(r.z + r.jl) / gl);
+    c = w - gr * dw - (gl - gr) * q;
   } else {
+    const double q = (__ldg(r.z + r.jr) / gr) * (__ldg(r.z + r.jr) / gr);
+    c = w - gl * dw - (gr - gl) * q;
+  }
+  double eta;
+  if (r.last) {
+    // the root lies beyond both poles (gl, gr < 0): the larger root of the
+    // quadratic; c < 0 only from rounding
+    c = fabs(c);
+    if (c == 0.0) {
+      eta = r.hi - r.tau;  // no root beyond the poles: bisect
+    } else {
+      double disc = a * a - 4.0 * b * c;
+      if (disc < 0.0) disc = 0.0;
+      eta = (a >= 0.0) ? (a + sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a - sqrt(disc));
+    }
+  } else if (c == 0.0) {
+    eta = (a != 0.0) ? b / a : -w / dw;
+  } else {  // the root between the two poles
     double disc = a * a - 4.0 * b * c;
     if (disc < 0.0) disc = 0.0;
     eta = (a <= 0.0) ? (a - sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a + sqrt(disc));
   }
   if (w * eta >= 0.0) eta = -w / dw;  // model went the wrong way: Newton step
   double tn = r.tau + eta;
-  if (!(tn > r.lo && tn < r.hi)) tn = 0.5 * (r.lo + r.hi);
+  if (!(tn > r.lo && tn < r.hi)) {
+    // bisect; geometrically when the bracket spans decades on one side of the
+    // origin (roots next to a pole sit many decades below the interval)
+    if (r.lo > 0.0 && r.hi > 4096.0 * r.lo) tn = sqrt(r.lo * r.hi);
+    else if (r.hi < 0.0 && r.lo < 4096.0 * r.hi) tn = -sqrt(r.lo * r.hi);
+    else tn = 0.5 * (r.lo + r.hi);
+  }
   const double step = tn - r.tau;
   r.tau = tn;
   if (!r.last) {  // keep the origin at the pole nearer the iterate
@@ -263,7 +306,7 @@ __global__ void __launch_bounds__(256)
 k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
           double *__restrict__ lam, double *__restrict__ difl, double *__restrict__ difr,
           int *__restrict__ iters, int *__restrict__ status, unsigned long long *__restrict__ itsum,
-          const float *__restrict__ guess) {
+          const float *__restrict__ guess, bool full) {
   const int lane = threadIdx.x & 31, gl = lane & (L - 1);
   const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
   const int total = __ldg(lv.rootoff + lv.P);
@@ -287,7 +330,7 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
   for (int i = gl; i < st.K; i += L) zsq += __ldg(st.z + i) * __ldg(st.z + i);
   zsq = group_sum<L>(zsq);
   const bool trivial = !valid || st.K == 1;
-  if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq);
+  if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq, full);
   else st.phase = 2;
   while (__any_sync(HSS_FULL, st.phase != 2)) {
     const SecSums sm = sec_eval<L, SQ>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.oi, st.tau, st.jl,
@@ -507,6 +550,137 @@ __device__ __forceinline__ double logit_u(double u, int side) {
   return side == 0 ? l : -l;
 }
 
+// FP32 copies of a level's poles and weights (for the FP32 pre-solve).
+__global__ void k_to_f32(int n, const double *__restrict__ a, const double *__restrict__ b,
+                         float *__restrict__ fa, float *__restrict__ fb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { fa[i] = (float)a[i]; fb[i] = (float)b[i]; }
+}
+
+template <int L>
+__device__ __forceinline__ float group_sum_f(float v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(HSS_FULL, v, o);
+  return v;
+}
+
+// Starting points of the FP64 iteration from a few steps of the same
+// middle-way iteration in FP32 (this part issues FP32 instructions about sixty
+// times faster than FP64 ones): gaps to the 2 GR nearest poles from FP64
+// differences, the others from FP32 copies; start at the midpoint of
+// (d_j, d_{j+1}), origin kept at the nearer pole, bracket safeguarding, at
+// most 10 evaluations or until a step is below 4e-6 of the distance to the
+// origin pole.  The result (a few 1e-6 of the interval at
+// best) only starts the FP64 iteration, which decides convergence as before;
+// guess[s + j] = signed distance to the nearer pole / interval, 0 for none.
+template <int L>
+__global__ void __launch_bounds__(256)
+k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__restrict__ d32,
+                  const float *__restrict__ z32, float *__restrict__ guess) {
+  constexpr int GR = 4;
+  const int lane = threadIdx.x & 31, gl = lane & (L - 1);
+  const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
+  const int total = __ldg(lv.rootoff + lv.P);
+  int s = 0, j = 0, K = 0;
+  float rhoinv = 1.f;
+  if (r < total) {
+    const int m = find_merge(lv.rootoff, lv.P, r);
+    s = __ldg(lv.s + m);
+    j = r - __ldg(lv.rootoff + m);
+    K = __ldg(lv.K + m);
+    rhoinv = (float)(1.0 / __ldg(lv.rho + m));
+  }
+  const bool active = r < total && K >= 2 && j < K - 1;
+  const int n0 = j - GR + 1;  // first near pole
+  // near gaps d_i - d_o from FP64 differences, for the origin o = j or j + 1
+  float gn[2 * GR];
+  auto near_gaps = [&](int o) {
+    const double dorg = active ? __ldg(dl + s + o) : 0.0;
+#pragma unroll
+    for (int q = 0; q < 2 * GR; ++q) {
+      const int i = n0 + q;
+      gn[q] = (active && i >= 0 && i < K) ? (float)(__ldg(dl + s + i) - dorg) : 0.f;
+    }
+  };
+  near_gaps(j);
+  const float delta = gn[GR];  // d_{j+1} - d_j
+  int o = j;
+  float do32 = active ? __ldg(d32 + s + j) : 0.f;
+  const int Ka = active ? K : 0;
+  float tau = 0.5f * delta, lo = 0.f, hi = delta;
+  bool done = !active;
+#pragma unroll 1
+  for (int it = 0; it < 10; ++it) {
+    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+    if (!done) {
+      for (int i = gl; i < Ka; i += L) {
+        if (i >= n0 && i < n0 + 2 * GR) continue;  // the near poles follow
+        const float zi = __ldg(z32 + s + i);
+        const float t = zi / ((__ldg(d32 + s + i) - do32) - tau);
+        if (i <= j) { a0 = fmaf(zi, t, a0); a1 = fmaf(t, t, a1); }
+        else { b0 = fmaf(zi, t, b0); b1 = fmaf(t, t, b1); }
+      }
+#pragma unroll
+      for (int q = 0; q < 2 * GR; ++q) {
+        const int i = n0 + q;
+        if (i < 0 || i >= Ka || (i & (L - 1)) != gl) continue;
+        const float zi = __ldg(z32 + s + i);
+        const float t = zi / (gn[q] - tau);
+        if (i <= j) { a0 = fmaf(zi, t, a0); a1 = fmaf(t, t, a1); }
+        else { b0 = fmaf(zi, t, b0); b1 = fmaf(t, t, b1); }
+      }
+    }
+    a0 = group_sum_f<L>(a0); a1 = group_sum_f<L>(a1);
+    b0 = group_sum_f<L>(b0); b1 = group_sum_f<L>(b1);
+    if (!done) {
+      const float w = rhoinv + a0 + b0, dw = a1 + b1;
+      if (w == 0.f) {
+        done = true;
+      } else {
+        if (w < 0.f) lo = fmaxf(lo, tau); else hi = fminf(hi, tau);
+        const float gL = gn[GR - 1] - tau, gR = gn[GR] - tau;  // the poles j, j + 1
+        const float A = (gL + gR) * w - gL * gR * dw;
+        const float B = gL * gR * w;
+        const float C = w - gL * a1 - gR * b1;
+        float eta;
+        if (C == 0.f) {
+          eta = A != 0.f ? B / A : -w / dw;
+        } else {
+          const float disc = fmaxf(A * A - 4.f * B * C, 0.f);
+          eta = A <= 0.f ? (A - sqrtf(disc)) / (2.f * C) : (2.f * B) / (A + sqrtf(disc));
+        }
+        if (!(w * eta < 0.f)) eta = -w / dw;  // wrong direction or not finite: Newton
+        if (fabsf(eta) <= 4e-6f * fabsf(tau)) {  // FP32 resolution reached
+          tau += eta;
+          done = true;
+        } else {
+          float tn = tau + eta;
+          if (!(tn > lo && tn < hi)) tn = 0.5f * (lo + hi);
+          tau = tn;
+          // keep the origin at the pole nearer the iterate
+          if (o == j && tau > 0.5f * delta) {
+            o = j + 1; near_gaps(o); do32 = __ldg(d32 + s + o);
+            tau -= delta; lo -= delta; hi -= delta;
+          } else if (o == j + 1 && tau < -0.5f * delta) {
+            o = j; near_gaps(o); do32 = __ldg(d32 + s + o);
+            tau += delta; lo += delta; hi += delta;
+          }
+        }
+      }
+    }
+  }
+  if (r < total && gl == 0) {
+    float g = 0.f;
+    if (active) {
+      g = tau / delta;  // from the origin pole: positive from d_j, negative from d_{j+1}
+      if (g > 0.5f) g -= 1.f;
+      else if (g < -0.5f) g += 1.f;
+      if (!(fabsf(g) > 0.f && fabsf(g) <= 0.5f)) g = 0.f;
+    }
+    guess[s + j] = g;
+  }
+}
+
 template <int L>
 __global__ void __launch_bounds__(256)
 k_secular_mid(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
@@ -592,7 +766,8 @@ static int lanes_per_root(int total, int maxk) {
 
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
-                    unsigned long long *itsum, const float *guess, cudaStream_t st, bool sq) {
+                    unsigned long long *itsum, const float *guess, cudaStream_t st, bool sq,
+                    bool full) {
   if (total <= 0) return;
   const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
@@ -601,11 +776,26 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
 #define SEC_CASE(LL, SQ)                                                                     \
   case LL * 2 + SQ:                                                                          \
     k_secular<LL, SQ><<<grid, tb, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,     \
-                                            itsum, guess);                                   \
+                                            itsum, guess, full);                             \
     break;
     SEC_CASE(1, 0) SEC_CASE(2, 0) SEC_CASE(4, 0) SEC_CASE(8, 0) SEC_CASE(16, 0) SEC_CASE(32, 0)
     SEC_CASE(1, 1) SEC_CASE(2, 1) SEC_CASE(4, 1) SEC_CASE(8, 1) SEC_CASE(16, 1) SEC_CASE(32, 1)
 #undef SEC_CASE
+  }
+}
+void launch_secular_guess32(const LevelView &lv, int total, int maxk, int npos,
+                            const double *dl, const double *zw, float *d32, float *z32,
+                            float *guess, cudaStream_t st) {
+  if (total <= 0) return;
+  k_to_f32<<<(npos + 255) / 256, 256, 0, st>>>(npos, dl, zw, d32, z32);
+  const int L = lanes_per_root(total, maxk);
+  const int tb = root_block((long long)total * L);
+  const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
+  switch (L) {
+#define G32_CASE(LL) \
+  case LL: k_secular_guess32<LL><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess); break;
+    G32_CASE(1) G32_CASE(2) G32_CASE(4) G32_CASE(8) G32_CASE(16) G32_CASE(32)
+#undef G32_CASE
   }
 }
 void launch_secular_mid(const LevelView &lv, int total, int maxk, const double *dl,

@@ -79,3 +79,59 @@ def test_stats_counts():
     st = hp.get_stats()
     assert st["n_merges"] == 127 and st["n_levels"] == 7
     assert st["kernel_launches"] > 0
+
+
+# starts from the FP32 pre-solve (predictor = 2): same acceptance bar, fewer
+# FP64 evaluations per root
+
+
+@pytest.mark.parametrize("n", [3, 26, 257, 2048, 6000])
+def test_fp32_start_random(n):
+    d, e = rand_tridiag(n, seed=n + 7)
+    _check(d, e, predictor=2)
+
+
+@pytest.mark.parametrize("n", [500, 2048])
+def test_fp32_start_toeplitz(n):
+    d, e = toeplitz_tridiag(n)
+    w, _ = _check(d, e, predictor=2)
+    assert np.max(np.abs(w - toeplitz_eigs(n))) <= 4 * EV_TOL
+
+
+def test_fp32_start_clustered_spectrum():
+    # eigenvalues in tight clusters (poles closer than FP32 resolves):
+    # diagonal 1 + 1e-9 noise with weak coupling, plus a few outliers
+    n = 3000
+    rng = np.random.default_rng(31)
+    d = 1.0 + 1e-9 * rng.standard_normal(n)
+    d[::500] += 3.0
+    e = 1e-4 * rng.uniform(0.5, 1.0, n - 1)
+    _check(d, e, predictor=2)
+
+
+@pytest.mark.parametrize("pred", [0, 2])
+@pytest.mark.parametrize("smlsiz", [12, 25])
+def test_glued_wilkinson(pred, smlsiz):
+    # Wilkinson-type blocks (pairs of nearly equal eigenvalues) glued weakly:
+    # every merge has poles with tiny weights sitting on roots of the others,
+    # including the last pole (the root beyond it once needed 40+ steps)
+    m, nb = 21, 60
+    w1 = np.abs(np.arange(m) - (m - 1) / 2.0)
+    d = np.tile(w1, nb)
+    e = np.ones(m * nb - 1)
+    e[m - 1::m] = 1e-8
+    _check(d, e, predictor=pred, smlsiz=smlsiz)
+
+
+def test_fp32_start_saves_evaluations():
+    d, e = rand_tridiag(4096, seed=5)
+    evals = {}
+    for pred in (0, 2):
+        old = hp.set_config(predictor=pred)
+        try:
+            hp.eigh_tridiagonal(d, e)
+            st = hp.get_stats()
+        finally:
+            hp.restore_config(old)
+        evals[pred] = st["secular_iters"] / max(st["secular_roots"], 1)
+    assert evals[2] < evals[0] - 0.5, evals

@@ -55,6 +55,52 @@ def test_secular_vs_dlaed4(k, seed):
     assert it.max() < 40
 
 
+@pytest.mark.parametrize("k,seed", [(2, 1), (50, 3), (1000, 4), (5000, 5)])
+def test_secular_fp32_start_vs_dlaed4(k, seed):
+    """FP32 pre-solved starting points: same roots, fewer FP64 evaluations."""
+    d, z, rho = secular_problem(k, seed)
+    lam_o, difl_o, _ = oracle.secular(d, z, rho)
+    _solve(d, z, rho)
+    base = hp.get_stats()["secular_iters"]
+    old = hp.set_config(predictor=2)
+    try:
+        lam, difl, difr, it = _solve(d, z, rho)
+        fast = hp.get_stats()["secular_iters"]
+    finally:
+        hp.restore_config(old)
+    assert np.max(np.abs(lam - lam_o)) <= 1e-13 * max(1.0, np.abs(d).max())
+    assert np.max(np.abs(difl - difl_o) / np.abs(difl_o)) <= 1e-11
+    assert it.max() < 40
+    if k >= 50:
+        assert fast < base, (fast, base)
+
+
+def _near_root_problem(k, seed, which, wz):
+    """A pole with a tiny weight placed on a root of the other poles'
+    equation: the nearly deflatable case that glued matrices produce in every
+    merge.  The new root sits about wz / sqrt(w') from the pole."""
+    d, z, rho = secular_problem(k, seed)
+    lam, _, _ = oracle.secular(d, z, rho)
+    p = lam[which]
+    dn = np.sort(np.append(d, p))
+    zn = np.insert(z, int(np.searchsorted(dn, p)), wz)
+    return dn, zn / np.linalg.norm(zn), rho
+
+
+@pytest.mark.parametrize("k", [40, 300])
+@pytest.mark.parametrize("where", ["last", "middle", "first"])
+@pytest.mark.parametrize("wz", [1e-7, 3e-11, 3e-14])
+def test_secular_pole_on_a_root(k, where, wz):
+    which = {"last": k - 1, "middle": k // 2, "first": 0}[where]
+    d, z, rho = _near_root_problem(k, 11, which, wz)
+    lam_o, _, _ = oracle.secular(d, z, rho)
+    lam, difl, difr, it = _solve(d, z, rho)
+    assert np.max(np.abs(lam - lam_o)) <= 1e-13 * max(1.0, np.abs(d).max())
+    # the last root beyond a nearly weightless pole took over 40 steps when
+    # its step used the interior root of the model's quadratic
+    assert it.max() <= 15, it.max()
+
+
 @pytest.mark.parametrize("k", [10, 700])
 def test_lowner_alpha(k):
     d, z, rho = secular_problem(k, 7)
