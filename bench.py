@@ -512,15 +512,21 @@ def run_ours(args):
         info = hp.mdstedc("I", n, dn, en, zn, n, work, lw, iwork, liw)
         assert info == 0, info
 
-    e2e_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    t = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 5))
-    for _ in range(e2e_steps):
+    # the same configuration as the device-timed solves
+    old_cfg = hp.set_config(**full_cfg)
+    try:
         e2e_step()
-    e2e_s = (time.perf_counter() - t) / e2e_steps
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 5))
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t) / e2e_steps
+        e2e_solve_ms = hp.get_stats()["ms_total"]  # the last step's device solve
+    finally:
+        hp.restore_config(old_cfg)
     if world > 1:
         x = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(x, op=dist.ReduceOp.MAX)
@@ -583,7 +589,10 @@ def run_ours(args):
                    "l2": "no flush: the 8.6 GB eigenvector matrix exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 16 * n,
-                "d2h_bytes_per_step": 8 * n * n + 8 * n},
+                "d2h_bytes_per_step": 8 * n * n + 8 * n,
+                # the library's event time of the solve inside a step; the
+                # rest is the host<->device copies and the call's host work
+                "device_solve_s": e2e_solve_ms / 1000.0},
         "gpu_launches": int(launches),
         "roofline": roof,
         "cpu_baseline": cpu,
