@@ -114,6 +114,9 @@ static void *pinned(Ctx &c, size_t bytes) {
 }
 
 void *pool_get(const char *name, size_t bytes) { return buf<char>(ctx(), name, bytes); }
+// error word of the tensor-core products (set by a CTA whose bounded wait
+// timed out; reset at the start of every solve, read with its status)
+static int *gemm_flag(Ctx &c) { return buf<int>(c, "gemm_err", 1); }
 
 // Host->device parameter uploads (level views, product descriptors).  Small
 // ones stay pageable copies (measured faster: they travel with the command
@@ -601,6 +604,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   // status[4..5]: 64-bit count of learned starts that fell back
   int *status = buf<int>(c, "status", 6);
   CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
   // no zero fill of Q: every column is tracked with the rows it holds data on
   // (set by the leaves, widened by merges) and read as zero elsewhere
   int2 *sup = buf<int2>(c, "sup", N);
@@ -704,6 +708,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   CK(cudaEventRecord(ev1, st));
   int hst[6] = {0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const int hstatus = hst[0];
   unsigned long long its, fb;
@@ -719,6 +724,10 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   CK(cudaGetLastError());
+  if (hst[1]) {
+    c.err = "tensor-core product: bounded wait timed out";
+    return 1;
+  }
   if (hstatus != 0) {
     c.err = hstatus == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
                                            : "leaf QL iteration did not converge";
@@ -769,6 +778,7 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   int *perm = buf<int>(c, "perm", n);
   int *status = buf<int>(c, "status", 6);
   CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
   CK(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)n * n, st));
   const size_t kk = (size_t)kd * kd;
   double *Uc = buf<double>(c, "band_U", std::max<size_t>(ncut, 1) * kk);
@@ -849,6 +859,7 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   CK(cudaEventRecord(ev1, st));
   int hst[6] = {0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   unsigned long long its, fb;
   memcpy(&its, hst + 2, sizeof its);
@@ -863,6 +874,10 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   CK(cudaGetLastError());
+  if (hst[1]) {
+    c.err = "tensor-core product: bounded wait timed out";
+    return 1;
+  }
   if (hst[0] != 0) {
     c.err = hst[0] == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
                                           : "leaf Jacobi iteration did not converge";
@@ -1068,6 +1083,7 @@ static int svd_core(Ctx &c, int n, const double *d, const double *e, double *Uo,
   int *perm = buf<int>(c, "perm", n);
   int *status = buf<int>(c, "status", 6);
   CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
   CK(cudaMemsetAsync(U, 0, sizeof(double) * (size_t)n * n, st));
   CK(cudaMemsetAsync(V, 0, sizeof(double) * (size_t)n * n, st));
   {
@@ -1113,6 +1129,7 @@ static int svd_core(Ctx &c, int n, const double *d, const double *e, double *Uo,
   CK(cudaEventRecord(ev1, st));
   int hst[6] = {0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   unsigned long long its;
   memcpy(&its, hst + 2, sizeof its);
@@ -1125,6 +1142,10 @@ static int svd_core(Ctx &c, int n, const double *d, const double *e, double *Uo,
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   CK(cudaGetLastError());
+  if (hst[1]) {
+    c.err = "tensor-core product: bounded wait timed out";
+    return 1;
+  }
   if (hst[0] != 0) {
     c.err = hst[0] == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
                                           : "leaf SVD iteration did not converge";

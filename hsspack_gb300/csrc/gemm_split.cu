@@ -25,10 +25,11 @@
 // Kernels: k_split_a / k_split_b write the digit planes pre-tiled in the
 // tcgen05 shared-memory image (K-major, no swizzle, 8x16-byte core matrices),
 // so the GEMM stages each tile with one cp.async.bulk (TMA) copy.  k_gemm_tc:
-// one CTA per 128 x 64 output tile; one elected thread issues
-// tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) into TMEM, 4 warps drain TMEM
-// with tcgen05.ld and accumulate in FP64.  Every mbarrier wait is bounded; a
-// timeout sets an error flag and the CTA still frees its TMEM before exiting.
+// one CTA per 128 x 32 output tile, two CTAs per SM; one thread streams the
+// 16-deep K chunks through three shared-memory stages, another issues
+// tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) into TMEM, and 8 warps drain
+// TMEM with tcgen05.ld into exact int64 sums.  Every mbarrier wait is bounded;
+// a timeout sets an error flag and the CTA still frees its TMEM before exiting.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -42,11 +43,12 @@ namespace hss {
 
 constexpr int SP = 7;        // digit planes
 constexpr int TM = 128;      // output tile rows (tcgen05 M)
-constexpr int TN = 64;       // output tile cols (tcgen05 N)
-constexpr int TK = 32;       // K per staged chunk (two chunks in flight)
+constexpr int TN = 32;       // output tile cols (tcgen05 N)
+constexpr int TK = 16;       // K per staged chunk (one MMA deep)
+constexpr int NST = 3;       // staged chunks in flight
 constexpr int KWIN = 128;    // exactness window for groups 0..2
-constexpr int ATILE = TM * TK * 2;  // bytes of one A digit-plane tile (8 KB)
-constexpr int BTILE = TN * TK * 2;  // bytes of one B digit-plane tile (4 KB)
+constexpr int ATILE = TM * TK * 2;  // bytes of one A digit-plane tile (4 KB)
+constexpr int BTILE = TN * TK * 2;  // bytes of one B digit-plane tile (1 KB)
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
 
 // ------------------------------------------------------------ splitting ---
@@ -185,31 +187,30 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
   __syncthreads();
   // pass 2: thread handles (row, 8 consecutive k) -> 16-byte rows of core matrices
   const int nkt = (P.inner + TK - 1) / TK;
-  for (int kt = 0; kt < nkt; ++kt) {
+  for (int v = tid; v < nkt * TM * (TK / 8); v += 256) {
+    const int kt = v / (TM * (TK / 8)), u = v % (TM * (TK / 8));
     char *tile = (char *)P.dst + ((long long)tm * P.ktiles + kt) * SP * ATILE;
-    for (int u = tid; u < TM * (TK / 8); u += 256) {
-      const int r = u % TM, k8 = u / TM;
-      const int gr = tm * TM + r;
-      __align__(16) __nv_bfloat16 dg[SP][8];
+    const int r = u % TM, k8 = u / TM;
+    const int gr = tm * TM + r;
+    __align__(16) __nv_bfloat16 dg[SP][8];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const int gk = kt * TK + k8 * 8 + c;
-        const double x = (gr < P.rows && gk < P.inner) ? P.src[(long long)gk * P.ld + gr] : 0.0;
-        __nv_bfloat16 d[SP];
-        split_digits(x, sexp[r], d);
+    for (int c = 0; c < 8; ++c) {
+      const int gk = kt * TK + k8 * 8 + c;
+      const double x = (gr < P.rows && gk < P.inner) ? P.src[(long long)gk * P.ld + gr] : 0.0;
+      __nv_bfloat16 d[SP];
+      split_digits(x, sexp[r], d);
 #pragma unroll
-        for (int s = 0; s < SP; ++s) dg[s][c] = d[s];
-      }
-#pragma unroll
-      for (int s = 0; s < SP; ++s)
-        *reinterpret_cast<uint4 *>(tile + s * ATILE + tile_off(r, k8 * 8, TM)) =
-            *reinterpret_cast<uint4 *>(dg[s]);
+      for (int s = 0; s < SP; ++s) dg[s][c] = d[s];
     }
+#pragma unroll
+    for (int s = 0; s < SP; ++s)
+      *reinterpret_cast<uint4 *>(tile + s * ATILE + tile_off(r, k8 * 8, TM)) =
+          *reinterpret_cast<uint4 *>(dg[s]);
   }
 }
 
 // B: K x N (ldb) -> planes [tile_n][tile_k][s] of TN x TK (K-major), column
-// exponents.  One CTA per 64-column panel.
+// exponents.  One CTA per TN-column panel.
 __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
   __shared__ int sexp[TN];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -227,26 +228,25 @@ __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
   }
   __syncthreads();
   const int nkt = (P.inner + TK - 1) / TK;
-  for (int kt = 0; kt < nkt; ++kt) {
+  for (int v = tid; v < nkt * TN * (TK / 8); v += 256) {
+    const int kt = v / (TN * (TK / 8)), u = v % (TN * (TK / 8));
     char *tile = (char *)P.dst + ((long long)tn * P.ktiles + kt) * SP * BTILE;
-    for (int u = tid; u < TN * (TK / 8); u += 256) {
-      const int c = u / (TK / 8), k8 = u % (TK / 8);
-      const int gc = tn * TN + c;
-      __align__(16) __nv_bfloat16 dg[SP][8];
+    const int c = u / (TK / 8), k8 = u % (TK / 8);
+    const int gc = tn * TN + c;
+    __align__(16) __nv_bfloat16 dg[SP][8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int gk = kt * TK + k8 * 8 + q;
-        const double x = (gc < P.rows && gk < P.inner) ? P.src[(long long)gc * P.ld + gk] : 0.0;
-        __nv_bfloat16 d[SP];
-        split_digits(x, sexp[c], d);
+    for (int q = 0; q < 8; ++q) {
+      const int gk = kt * TK + k8 * 8 + q;
+      const double x = (gc < P.rows && gk < P.inner) ? P.src[(long long)gc * P.ld + gk] : 0.0;
+      __nv_bfloat16 d[SP];
+      split_digits(x, sexp[c], d);
 #pragma unroll
-        for (int s = 0; s < SP; ++s) dg[s][q] = d[s];
-      }
-#pragma unroll
-      for (int s = 0; s < SP; ++s)
-        *reinterpret_cast<uint4 *>(tile + s * BTILE + tile_off(c, k8 * 8, TN)) =
-            *reinterpret_cast<uint4 *>(dg[s]);
+      for (int s = 0; s < SP; ++s) dg[s][q] = d[s];
     }
+#pragma unroll
+    for (int s = 0; s < SP; ++s)
+      *reinterpret_cast<uint4 *>(tile + s * BTILE + tile_off(c, k8 * 8, TN)) =
+          *reinterpret_cast<uint4 *>(dg[s]);
   }
 }
 
@@ -373,24 +373,42 @@ struct TcProb {
 };
 
 // 8 warps: warp w drains TMEM lanes 32 (w % 4) .. + 31 (its row quarter) and
-// columns 32 (w / 4) .. + 31 of each group
+// columns TH (w / 4) .. + TH - 1 of each group
 constexpr int GTH = 256;
-// 16 KB of slack keeps every descriptor-addressed byte inside the allocation
-constexpr int STAGE_TC = SP * (ATILE + BTILE);      // one K chunk of both operands
-constexpr int SMEM_TC = 2 * STAGE_TC + 16384;
+constexpr int TMEM_TC = 256;                      // columns: SP groups of TN
+constexpr int STAGE_TC = SP * (ATILE + BTILE);    // one K chunk of both operands (35 KB)
+constexpr int SMEM_TC = NST * STAGE_TC + 1024;    // two CTAs share an SM
+static_assert(SP * TN <= TMEM_TC, "accumulator groups exceed the TMEM allocation");
+static_assert(2 * (SMEM_TC + 1024) <= 227 * 1024, "two CTAs per SM must fit");
 
-__global__ void __launch_bounds__(GTH, 1)
+// One CTA per 128 x 32 output tile, two CTAs per SM (one's drain and
+// epilogue overlap the other's MMAs).  Thread 0 streams the K chunks into
+// NST stages with bulk copies; thread 32 issues the 28 plane products of
+// each chunk as soon as it lands and commits the chunk's MMAs to the stage's
+// "empty" barrier, which thread 0 waits on before refilling the stage, so
+// copies, MMAs and the next copies overlap.  At the end of every 128-deep
+// exactness window all 8 warps drain the group sums into int64 accumulators.
+// Every wait is bounded; after a timeout the CTA waits (bounded) for its
+// copies and MMAs in flight, then frees its TMEM.
+__global__ void __launch_bounds__(GTH, 2)
 k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t full[2], empty[2];
+  __shared__ uint64_t full[NST], empty[NST], wdone;
   __shared__ uint32_t tmem_base;
-  __shared__ int s_ok;
+  __shared__ volatile int s_ok;
+  __shared__ int s_consumed;
   int lo = 0, hi = nprob;
   const int b = blockIdx.x;
   while (hi - lo > 1) {
     int mid = (lo + hi) >> 1;
     if (probs[mid].tile0 <= b) lo = mid; else hi = mid;
   }
+  // another CTA's wait already timed out: the launch is failing, skip the
+  // work (one read, so the whole CTA leaves together)
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = *(volatile int *)err;
+  __syncthreads();
+  if (s_skip) return;
   const TcProb P = probs[lo];
   const int t = b - P.tile0;
   const int ntm = (P.M + TM - 1) / TM;
@@ -402,13 +420,14 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base)),
-                 "r"(512));
+                 "r"(TMEM_TC));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    mbar_init(&full[0], 1); mbar_init(&full[1], 1);
-    mbar_init(&empty[0], 1); mbar_init(&empty[1], 1);
+    for (int q = 0; q < NST; ++q) { mbar_init(&full[q], 1); mbar_init(&empty[q], 1); }
+    mbar_init(&wdone, 1);
     s_ok = 1;
+    s_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -417,62 +436,58 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   const uint32_t tbase = tmem_base;
   const uint32_t idesc = make_idesc(TM, TN);
   constexpr int TH = TN / 2;  // output columns per thread
+  static_assert(TH == 16, "the drain reads 16 TMEM columns per group");
   long long hacc[TH], lacc[TH];
 #pragma unroll
   for (int j = 0; j < TH; ++j) { hacc[j] = 0; lacc[j] = 0; }
-  // thread 0: TMA producer and MMA issuer.  Chunk k lives in stage k & 1;
-  // chunk k + 2 is loaded into it once chunk k's MMAs have completed, so a
-  // chunk's copy overlaps the previous chunk's MMAs.  Every barrier phase is
-  // waited on exactly once, each wait bounded.
-  uint32_t ph_full[2] = {0, 0}, ph_empty[2] = {0, 0};
-  int issued = 0;  // chunks whose copies were started
-  auto load = [&](int kt) {
-    const int q = kt & 1;
-    mbar_expect_tx(&full[q], STAGE_TC);
-    const char *ga = P.a_planes + ((long long)tm * P.ktiles + kt) * SP * ATILE;
-    const char *gb = P.b_planes + ((long long)tn * P.ktiles + kt) * SP * BTILE;
-    tma_load(sa(q), ga, SP * ATILE, &full[q]);
-    tma_load(sb(q), gb, SP * BTILE, &full[q]);
-    ++issued;
-  };
-  if (tid == 0) {
-    if (P.ktiles > 0) load(0);
-    if (P.ktiles > 1) load(1);
-  }
-  const int kwin = KWIN / TK;  // chunks per exactness window
-  int waited = 0;              // chunks whose copies were waited for
-  for (int kt0 = 0; kt0 < P.ktiles; kt0 += kwin) {
-    const int kt1 = min(P.ktiles, kt0 + kwin);
-    if (tid == 0 && s_ok) {
-      for (int kt = kt0; kt < kt1; ++kt) {
-        const int q = kt & 1;
-        if (!mbar_wait(&full[q], ph_full[q])) { atomicOr(err, 1); s_ok = 0; break; }
-        ph_full[q] ^= 1;
-        ++waited;
+  // chunk kt lives in stage kt % NST; it is that stage's (kt / NST)-th use,
+  // so its "full" phase has parity (kt / NST) & 1, and the stage is free for
+  // it once the "empty" phase of use kt / NST - 1 completed
+  const int nk = P.ktiles, kwin = KWIN / TK;
+  int issued = 0;     // thread 0: chunks whose copies were started
+  int consumed = 0;   // thread 32: chunks whose copies were waited for
+  uint32_t ph_w = 0;  // thread 32: parity of the window barrier
+  for (int k0 = 0; k0 < nk; k0 += kwin) {
+    const int k1 = min(nk, k0 + kwin);
+    if (tid == 0) {
+      for (int kt = k0; kt < k1 && s_ok; ++kt) {
+        const int q = kt % NST;
+        if (kt >= NST && !mbar_wait(&empty[q], ((kt / NST) - 1) & 1)) {
+          atomicOr(err, 1); s_ok = 0; break;
+        }
+        mbar_expect_tx(&full[q], STAGE_TC);
+        const char *ga = P.a_planes + ((long long)tm * nk + kt) * SP * ATILE;
+        const char *gb = P.b_planes + ((long long)tn * nk + kt) * SP * BTILE;
+        tma_load(sa(q), ga, SP * ATILE, &full[q]);
+        tma_load(sb(q), gb, SP * BTILE, &full[q]);
+        ++issued;
+      }
+    } else if (tid == 32) {
+      for (int kt = k0; kt < k1 && s_ok; ++kt) {
+        const int q = kt % NST;
+        if (!mbar_wait(&full[q], (kt / NST) & 1)) { atomicOr(err, 2); s_ok = 0; break; }
+        ++consumed;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // descriptor(address + offset) = descriptor(address) + offset / 16:
-        // two base descriptors, constant offsets in the unrolled issue loop
+        // descriptor(address + offset) = descriptor(address) + offset / 16
         const uint64_t ad0 = make_desc(smem_u32(sa(q)), TM * 16, 128);
         const uint64_t bd0 = make_desc(smem_u32(sb(q)), TN * 16, 128);
-        const uint32_t later = kt > kt0 ? 1u : 0u;
+        const uint32_t later = kt > k0 ? 1u : 0u;
+        // the window's first product of a group (s2 = 0) overwrites
+#pragma unroll 1
+        for (int s2 = 0; s2 < SP; ++s2)
 #pragma unroll
-        for (int kk = 0; kk < TK / 16; ++kk)
-#pragma unroll
-          for (int s2 = 0; s2 < SP; ++s2)
-#pragma unroll
-            for (int p2 = 0; p2 + s2 < SP; ++p2) {
-              // the first product of a group in the window overwrites
-              const uint32_t accum = (kk > 0 || s2 > 0) ? 1u : later;
-              umma(tbase + (s2 + p2) * TN, ad0 + (uint64_t)((s2 * ATILE + kk * 2 * (TM * 16)) >> 4),
-                   bd0 + (uint64_t)((p2 * BTILE + kk * 2 * (TN * 16)) >> 4), idesc, accum);
-            }
-        umma_commit(&empty[q]);
-        if (!mbar_wait(&empty[q], ph_empty[q])) { atomicOr(err, 2); s_ok = 0; break; }
-        ph_empty[q] ^= 1;
-        if (kt + 2 < P.ktiles) load(kt + 2);
+          for (int p2 = 0; p2 < SP; ++p2)
+            if (p2 + s2 < SP)
+              umma(tbase + (s2 + p2) * TN, ad0 + (uint64_t)((s2 * ATILE) >> 4),
+                   bd0 + (uint64_t)((p2 * BTILE) >> 4), idesc, s2 > 0 ? 1u : later);
+        umma_commit(&empty[q]);  // stage q is free once these MMAs completed
       }
+      // every MMA issued so far (also before an error) has completed
+      umma_commit(&wdone);
+      if (!mbar_wait(&wdone, ph_w)) { atomicOr(err, 4); s_ok = 0; }
+      ph_w ^= 1;
+      s_consumed = consumed;
     }
-    // the window's MMAs are complete (thread 0 waited for every commit)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -481,17 +496,14 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
     const uint32_t lane_addr =
         tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TH);
 #pragma unroll
-    for (int c = 0; c < TH; c += 16) {
+    for (int g = 0; g < SP; ++g) {
+      float v[16];
+      tmem_ld16(lane_addr + g * TN, v);
 #pragma unroll
-      for (int g = 0; g < SP; ++g) {
-        float v[16];
-        tmem_ld16(lane_addr + g * TN + c, v);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const long long x = (long long)int_of_float(v[i]);
-          if (g < 3) hacc[c + i] += x * (1ll << (8 * (2 - g)));
-          else lacc[c + i] += x * (1ll << (8 * (6 - g)));
-        }
+      for (int i = 0; i < TH; ++i) {
+        const long long x = (long long)int_of_float(v[i]);
+        if (g < 3) hacc[i] += x * (1ll << (8 * (2 - g)));
+        else lacc[i] += x * (1ll << (8 * (6 - g)));
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -501,11 +513,8 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   if (tid == 0 && !s_ok) {
     // a bounded wait gave up: wait (bounded) for the copies still in flight
     // before the CTA's shared memory is released
-    for (int kt = waited; kt < issued; ++kt) {
-      const int q = kt & 1;
-      if (!mbar_wait(&full[q], ph_full[q])) break;
-      ph_full[q] ^= 1;
-    }
+    for (int kt = s_consumed; kt < issued; ++kt)
+      if (!mbar_wait(&full[kt % NST], (kt / NST) & 1)) break;
   }
   const bool ok = s_ok != 0;
   // epilogue: C = 2^{e_i + f_j - 30} (H + 2^-32 L) (+ C)
@@ -525,7 +534,8 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(TMEM_TC));
 }
 
 // ------------------------------------------------- fused split GEMM -----
@@ -623,6 +633,10 @@ k_gemm_fused(const FusedProb *__restrict__ probs, int nprob, int *__restrict__ e
   int lo = 0, hi = nprob;
   const int b = blockIdx.x;
   while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (probs[mid].tile0 <= b) lo = mid; else hi = mid; }
+  __shared__ int s_skip;  // another CTA's wait timed out: the whole CTA skips the work
+  if (threadIdx.x == 0) s_skip = *(volatile int *)err;
+  __syncthreads();
+  if (s_skip) return;
   const FusedProb P = probs[lo];
   const int t = b - P.tile0, ntm = (P.M + FM - 1) / FM;
   const int tm = t % ntm, tn = t / ntm;
