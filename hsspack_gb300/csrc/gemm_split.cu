@@ -45,7 +45,6 @@ constexpr int SP = 7;        // digit planes
 constexpr int TM = 128;      // output tile rows (tcgen05 M)
 constexpr int TN = 32;       // output tile cols (tcgen05 N)
 constexpr int TK = 16;       // K per staged chunk (one MMA deep)
-constexpr int NST = 3;       // staged chunks in flight
 constexpr int KWIN = 128;    // exactness window for groups 0..2
 constexpr int ATILE = TM * TK * 2;  // bytes of one A digit-plane tile (4 KB)
 constexpr int BTILE = TN * TK * 2;  // bytes of one B digit-plane tile (1 KB)
@@ -209,8 +208,10 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
   }
 }
 
-// B: K x N (ldb) -> planes [tile_n][tile_k][s] of TN x TK (K-major), column
-// exponents.  One CTA per TN-column panel.
+// B: K x N (ldb) -> one K-major tile per (tile_n, tile_k) holding the SP
+// planes stacked along N (plane p in rows p TN .. p TN + TN - 1, so the
+// planes 0..P-1 form one operand of N = P TN rows), column exponents.  One
+// CTA per TN-column panel.
 __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
   __shared__ int sexp[TN];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -245,7 +246,7 @@ __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
     }
 #pragma unroll
     for (int s = 0; s < SP; ++s)
-      *reinterpret_cast<uint4 *>(tile + s * BTILE + tile_off(c, k8 * 8, TN)) =
+      *reinterpret_cast<uint4 *>(tile + tile_off(s * TN + c, k8 * 8, SP * TN)) =
           *reinterpret_cast<uint4 *>(dg[s]);
   }
 }
@@ -318,6 +319,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes));
@@ -365,56 +370,47 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 // ---------------------------------------------------------------- GEMM ----
 struct TcProb {
   const char *a_planes;  // [tm][kt][s] ATILE
-  const char *b_planes;  // [tn][kt][s] BTILE
+  const char *b_planes;  // [tn][kt] SP * BTILE, planes stacked along N
   const int *ea, *eb;    // row / column exponents
   double *C;
   int ldc, M, N, ktiles, beta;
   int tile0;             // first flattened tile index
 };
 
-// 8 warps: warp w drains TMEM lanes 32 (w % 4) .. + 31 (its row quarter) and
-// columns TH (w / 4) .. + TH - 1 of each group
-constexpr int GTH = 256;
-constexpr int TMEM_TC = 256;                      // columns: SP groups of TN
+// Persistent kernel, one CTA per SM: warp 0 (one lane) streams the K chunks
+// of the CTA's tiles through NST shared-memory stages with bulk copies;
+// warp 1 (one lane) issues the 28 plane products of every chunk into one of
+// two TMEM accumulator sets, alternating per 128-deep exactness window;
+// warps 2..9 drain a finished set into exact int64 sums (the other set
+// meanwhile takes the next window's MMAs) and write the tile's doubles.  So
+// copies, MMAs and drains of consecutive tiles overlap.  Tiles t = blockIdx.x
+// + i gridDim.x; tprob[t] names the tile's product.  Every wait is bounded;
+// after a timeout every role stops, the CTA waits (bounded) for its copies
+// and MMAs in flight, then frees its TMEM.
+constexpr int NST = 6;                            // staged chunks in flight
+constexpr int GTH = 320;                          // 10 warps
+constexpr int ACC_SET = 256;                      // TMEM columns per accumulator set
+constexpr int TMEM_TC = 2 * ACC_SET;
 constexpr int STAGE_TC = SP * (ATILE + BTILE);    // one K chunk of both operands (35 KB)
-constexpr int SMEM_TC = NST * STAGE_TC + 1024;    // two CTAs share an SM
-static_assert(SP * TN <= TMEM_TC, "accumulator groups exceed the TMEM allocation");
-static_assert(2 * (SMEM_TC + 1024) <= 227 * 1024, "two CTAs per SM must fit");
+constexpr int SMEM_TC = NST * STAGE_TC + 1024;
+static_assert(SP * TN <= ACC_SET, "accumulator groups exceed a TMEM set");
+static_assert(SMEM_TC <= 226 * 1024, "stages exceed the shared memory of a CTA");
 
-// One CTA per 128 x 32 output tile, two CTAs per SM (one's drain and
-// epilogue overlap the other's MMAs).  Thread 0 streams the K chunks into
-// NST stages with bulk copies; thread 32 issues the 28 plane products of
-// each chunk as soon as it lands and commits the chunk's MMAs to the stage's
-// "empty" barrier, which thread 0 waits on before refilling the stage, so
-// copies, MMAs and the next copies overlap.  At the end of every 128-deep
-// exactness window all 8 warps drain the group sums into int64 accumulators.
-// Every wait is bounded; after a timeout the CTA waits (bounded) for its
-// copies and MMAs in flight, then frees its TMEM.
-__global__ void __launch_bounds__(GTH, 2)
-k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
+__global__ void __launch_bounds__(GTH, 1)
+k_gemm_tc(const TcProb *__restrict__ probs, const int *__restrict__ tprob, int ntiles,
+          int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t full[NST], empty[NST], wdone;
+  __shared__ uint64_t full[NST], empty[NST], afull[2], aempty[2], fin;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int s_ok;
-  __shared__ int s_consumed;
-  int lo = 0, hi = nprob;
-  const int b = blockIdx.x;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (probs[mid].tile0 <= b) lo = mid; else hi = mid;
-  }
+  __shared__ long long s_issued, s_consumed;
+  __shared__ int s_skip;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // another CTA's wait already timed out: the launch is failing, skip the
   // work (one read, so the whole CTA leaves together)
-  __shared__ int s_skip;
-  if (threadIdx.x == 0) s_skip = *(volatile int *)err;
+  if (tid == 0) s_skip = *(volatile int *)err;
   __syncthreads();
   if (s_skip) return;
-  const TcProb P = probs[lo];
-  const int t = b - P.tile0;
-  const int ntm = (P.M + TM - 1) / TM;
-  const int tm = t % ntm, tn = t / ntm;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  // stage q: A planes at smem + q * STAGE_TC, B planes after them
   auto sa = [&](int q) { return smem + q * STAGE_TC; };
   auto sb = [&](int q) { return smem + q * STAGE_TC + SP * ATILE; };
   if (warp == 0) {
@@ -425,8 +421,10 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   }
   if (tid == 0) {
     for (int q = 0; q < NST; ++q) { mbar_init(&full[q], 1); mbar_init(&empty[q], 1); }
-    mbar_init(&wdone, 1);
+    for (int a = 0; a < 2; ++a) { mbar_init(&afull[a], 1); mbar_init(&aempty[a], 8); }
+    mbar_init(&fin, 1);
     s_ok = 1;
+    s_issued = 0;
     s_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -434,104 +432,135 @@ k_gemm_tc(const TcProb *__restrict__ probs, int nprob, int *__restrict__ err) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tbase = tmem_base;
-  const uint32_t idesc = make_idesc(TM, TN);
-  constexpr int TH = TN / 2;  // output columns per thread
-  static_assert(TH == 16, "the drain reads 16 TMEM columns per group");
-  long long hacc[TH], lacc[TH];
-#pragma unroll
-  for (int j = 0; j < TH; ++j) { hacc[j] = 0; lacc[j] = 0; }
-  // chunk kt lives in stage kt % NST; it is that stage's (kt / NST)-th use,
-  // so its "full" phase has parity (kt / NST) & 1, and the stage is free for
-  // it once the "empty" phase of use kt / NST - 1 completed
-  const int nk = P.ktiles, kwin = KWIN / TK;
-  int issued = 0;     // thread 0: chunks whose copies were started
-  int consumed = 0;   // thread 32: chunks whose copies were waited for
-  uint32_t ph_w = 0;  // thread 32: parity of the window barrier
-  for (int k0 = 0; k0 < nk; k0 += kwin) {
-    const int k1 = min(nk, k0 + kwin);
-    if (tid == 0) {
-      for (int kt = k0; kt < k1 && s_ok; ++kt) {
-        const int q = kt % NST;
-        if (kt >= NST && !mbar_wait(&empty[q], ((kt / NST) - 1) & 1)) {
-          atomicOr(err, 1); s_ok = 0; break;
+  const int kwin = KWIN / TK;  // chunks per exactness window
+  // Chunk g (counted over the CTA's tiles) lives in stage g % NST, that
+  // stage's (g / NST)-th use: its "full" phase has parity (g / NST) & 1 and
+  // the stage is free for it once "empty" of use g / NST - 1 completed.
+  // Window w (counted likewise) accumulates in set w & 1, that set's
+  // (w / 2)-th use, with the same parity rule for afull / aempty.
+  if (warp == 0) {
+    if (lane == 0) {  // copies
+      long long g = 0;
+      for (int t = blockIdx.x; t < ntiles && s_ok; t += gridDim.x) {
+        const TcProb &P = probs[__ldg(tprob + t)];
+        const int nk = P.ktiles, ntm = (P.M + TM - 1) / TM, tt = t - P.tile0;
+        const char *ga0 = P.a_planes + (long long)(tt % ntm) * nk * SP * ATILE;
+        const char *gb0 = P.b_planes + (long long)(tt / ntm) * nk * SP * BTILE;
+        for (int kt = 0; kt < nk && s_ok; ++kt, ++g) {
+          const int q = (int)(g % NST);
+          if (g >= NST && !mbar_wait(&empty[q], (uint32_t)((g / NST) - 1) & 1)) {
+            atomicOr(err, 1); s_ok = 0; break;
+          }
+          mbar_expect_tx(&full[q], STAGE_TC);
+          tma_load(sa(q), ga0 + (long long)kt * SP * ATILE, SP * ATILE, &full[q]);
+          tma_load(sb(q), gb0 + (long long)kt * SP * BTILE, SP * BTILE, &full[q]);
+          s_issued = g + 1;
         }
-        mbar_expect_tx(&full[q], STAGE_TC);
-        const char *ga = P.a_planes + ((long long)tm * nk + kt) * SP * ATILE;
-        const char *gb = P.b_planes + ((long long)tn * nk + kt) * SP * BTILE;
-        tma_load(sa(q), ga, SP * ATILE, &full[q]);
-        tma_load(sb(q), gb, SP * BTILE, &full[q]);
-        ++issued;
       }
-    } else if (tid == 32) {
-      for (int kt = k0; kt < k1 && s_ok; ++kt) {
-        const int q = kt % NST;
-        if (!mbar_wait(&full[q], (kt / NST) & 1)) { atomicOr(err, 2); s_ok = 0; break; }
-        ++consumed;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMAs
+      long long g = 0, w = 0;
+      for (int t = blockIdx.x; t < ntiles && s_ok; t += gridDim.x) {
+        const int nk = probs[__ldg(tprob + t)].ktiles;
+        for (int k0 = 0; k0 < nk && s_ok; k0 += kwin, ++w) {
+          const int k1 = min(nk, k0 + kwin), a = (int)(w & 1);
+          if (w >= 2 && !mbar_wait(&aempty[a], (uint32_t)((w / 2) - 1) & 1)) {
+            atomicOr(err, 2); s_ok = 0; break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t acc = tbase + (uint32_t)(a * ACC_SET);
+          for (int kt = k0; kt < k1 && s_ok; ++kt, ++g) {
+            const int q = (int)(g % NST);
+            if (!mbar_wait(&full[q], (uint32_t)(g / NST) & 1)) { atomicOr(err, 4); s_ok = 0; break; }
+            s_consumed = g + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // descriptor(address + offset) = descriptor(address) + offset / 16.
+            // A plane s2 times B planes 0 .. SP-1-s2 (stacked along N) is one
+            // MMA of N = (SP - s2) TN whose column block p2 lands on group
+            // s2 + p2; the window's first MMA (s2 = 0) overwrites every group
+            const uint64_t ad0 = make_desc(smem_u32(sa(q)), TM * 16, 128);
+            const uint64_t bd = make_desc(smem_u32(sb(q)), SP * TN * 16, 128);
+            const uint32_t later = kt > k0 ? 1u : 0u;
+#pragma unroll
+            for (int s2 = 0; s2 < SP; ++s2)
+              umma(acc + s2 * TN, ad0 + (uint64_t)((s2 * ATILE) >> 4), bd,
+                   make_idesc(TM, (SP - s2) * TN), s2 > 0 ? 1u : later);
+            umma_commit(&empty[q]);  // stage q is free once these MMAs completed
+          }
+          umma_commit(&afull[a]);    // the window's sums are complete
+        }
+      }
+      // every MMA issued (also before an error) completes before TMEM is freed
+      umma_commit(&fin);
+      if (!mbar_wait(&fin, 0)) { atomicOr(err, 8); s_ok = 0; }
+    }
+  } else {  // warps 2..9: drain and write; TMEM lanes 32 (warp % 4) ..
+    const int quarter = warp & 3, half = (warp - 2) >> 2;
+    constexpr int TH = TN / 2;  // output columns per thread
+    static_assert(TH == 16, "the drain reads 16 TMEM columns per group");
+    long long w = 0;
+    for (int t = blockIdx.x; t < ntiles && s_ok; t += gridDim.x) {
+      const TcProb &P = probs[__ldg(tprob + t)];
+      const int nk = P.ktiles, ntm = (P.M + TM - 1) / TM, tt = t - P.tile0;
+      long long hacc[TH], lacc[TH];
+#pragma unroll
+      for (int j = 0; j < TH; ++j) { hacc[j] = 0; lacc[j] = 0; }
+      bool okt = true;
+      for (int k0 = 0; k0 < nk; k0 += kwin, ++w) {
+        const int a = (int)(w & 1);
+        // one lane waits, the warp follows its verdict (tcgen05.ld is warp-wide)
+        int got = 0;
+        if (lane == 0) got = mbar_wait(&afull[a], (uint32_t)(w / 2) & 1) ? 1 : 0;
+        got = __shfl_sync(HSS_FULL, got, 0);
+        if (!got) {
+          if (lane == 0) { atomicOr(err, 16); s_ok = 0; }
+          okt = false;
+          break;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // descriptor(address + offset) = descriptor(address) + offset / 16
-        const uint64_t ad0 = make_desc(smem_u32(sa(q)), TM * 16, 128);
-        const uint64_t bd0 = make_desc(smem_u32(sb(q)), TN * 16, 128);
-        const uint32_t later = kt > k0 ? 1u : 0u;
-        // the window's first product of a group (s2 = 0) overwrites
-#pragma unroll 1
-        for (int s2 = 0; s2 < SP; ++s2)
+        const uint32_t lane_addr = tbase + (uint32_t)(a * ACC_SET) +
+                                   ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * TH);
 #pragma unroll
-          for (int p2 = 0; p2 < SP; ++p2)
-            if (p2 + s2 < SP)
-              umma(tbase + (s2 + p2) * TN, ad0 + (uint64_t)((s2 * ATILE) >> 4),
-                   bd0 + (uint64_t)((p2 * BTILE) >> 4), idesc, s2 > 0 ? 1u : later);
-        umma_commit(&empty[q]);  // stage q is free once these MMAs completed
+        for (int gq = 0; gq < SP; ++gq) {
+          float v[16];
+          tmem_ld16(lane_addr + gq * TN, v);
+#pragma unroll
+          for (int i = 0; i < TH; ++i) {
+            const long long x = (long long)int_of_float(v[i]);
+            if (gq < 3) hacc[i] += x * (1ll << (8 * (2 - gq)));
+            else lacc[i] += x * (1ll << (8 * (6 - gq)));
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&aempty[a]);  // the set may take new MMAs
       }
-      // every MMA issued so far (also before an error) has completed
-      umma_commit(&wdone);
-      if (!mbar_wait(&wdone, ph_w)) { atomicOr(err, 4); s_ok = 0; }
-      ph_w ^= 1;
-      s_consumed = consumed;
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!s_ok) break;
-    // drain the window's exact group sums into the int64 accumulators
-    const uint32_t lane_addr =
-        tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TH);
+      if (!okt) break;
+      // C = 2^{e_i + f_j - 30} (H + 2^-32 L) (+ C)
+      const int r = (tt % ntm) * TM + quarter * 32 + lane;
+      if (r < P.M) {
+        const int ei = P.ea[r];
 #pragma unroll
-    for (int g = 0; g < SP; ++g) {
-      float v[16];
-      tmem_ld16(lane_addr + g * TN, v);
-#pragma unroll
-      for (int i = 0; i < TH; ++i) {
-        const long long x = (long long)int_of_float(v[i]);
-        if (g < 3) hacc[i] += x * (1ll << (8 * (2 - g)));
-        else lacc[i] += x * (1ll << (8 * (6 - g)));
-      }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  }
-  if (tid == 0 && !s_ok) {
-    // a bounded wait gave up: wait (bounded) for the copies still in flight
-    // before the CTA's shared memory is released
-    for (int kt = s_consumed; kt < issued; ++kt)
-      if (!mbar_wait(&full[kt % NST], (kt / NST) & 1)) break;
-  }
-  const bool ok = s_ok != 0;
-  // epilogue: C = 2^{e_i + f_j - 30} (H + 2^-32 L) (+ C)
-  const int r = tm * TM + (warp & 3) * 32 + (tid & 31);
-  if (ok && r < P.M) {
-    const int ei = P.ea[r];
-#pragma unroll
-    for (int j = 0; j < TH; ++j) {
-      const int c = tn * TN + (warp >> 2) * TH + j;
-      if (c < P.N) {
-        const double v = exact_double(hacc[j], lacc[j], ei + P.eb[c] - 30);
-        double *dst = P.C + (long long)c * P.ldc + r;
-        *dst = P.beta ? *dst + v : v;
+        for (int j = 0; j < TH; ++j) {
+          const int c = (tt / ntm) * TN + half * TH + j;
+          if (c < P.N) {
+            const double v = exact_double(hacc[j], lacc[j], ei + P.eb[c] - 30);
+            double *dst = P.C + (long long)c * P.ldc + r;
+            *dst = P.beta ? *dst + v : v;
+          }
+        }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (tid == 0 && !s_ok) {
+    // a bounded wait gave up: wait (bounded) for the copies still in flight
+    // before the CTA's shared memory is released
+    for (long long g = s_consumed; g < s_issued; ++g)
+      if (!mbar_wait(&full[g % NST], (uint32_t)(g / NST) & 1)) break;
+  }
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
@@ -803,6 +832,7 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
     tiles += ntm * ntn;
     tc.push_back(t);
   }
+  if (tiles == 0) return;  // every product is empty
   char *A = pool<char>("gs_A", abytes + 1024), *B = pool<char>("gs_B", bbytes + 1024);
   int *EA = pool<int>("gs_ea", ea + 1), *EB = pool<int>("gs_eb", eb + 1);
   for (size_t i = 0; i < probs.size(); ++i) {
@@ -813,9 +843,17 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   }
   SplitProb *dsa = pool<SplitProb>("gs_sa", sa.size()), *dsb = pool<SplitProb>("gs_sb", sb.size());
   TcProb *dtc = pool<TcProb>("gs_tc", tc.size());
+  // tile -> product table for the persistent product kernel
+  std::vector<int> tp(tiles);
+  for (size_t i = 0; i < tc.size(); ++i) {
+    const int nt = ((probs[i].M + TM - 1) / TM) * ((probs[i].N + TN - 1) / TN);
+    for (int k = 0; k < nt; ++k) tp[tc[i].tile0 + k] = (int)i;
+  }
+  int *dtp = pool<int>("gs_tp", tp.size());
   stage_h2d(dsa, sa.data(), sa.size() * sizeof(SplitProb), st);
   stage_h2d(dsb, sb.data(), sb.size() * sizeof(SplitProb), st);
   stage_h2d(dtc, tc.data(), tc.size() * sizeof(TcProb), st);
+  stage_h2d(dtp, tp.data(), tp.size() * sizeof(int), st);
   const unsigned gy = (unsigned)std::min<size_t>(sa.size(), 65535);
   k_split_a<<<dim3(maxtm, gy), 256, 0, st>>>(dsa, (int)sa.size());
   k_split_b<<<dim3(maxtn, gy), 256, 0, st>>>(dsb, (int)sb.size());
@@ -824,7 +862,14 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
     cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);
     attr = true;
   }
-  k_gemm_tc<<<tiles, GTH, SMEM_TC, st>>>(dtc, (int)tc.size(), d_err);
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  k_gemm_tc<<<std::min(tiles, sms), GTH, SMEM_TC, st>>>(dtc, dtp, tiles, d_err);
 }
 
 
