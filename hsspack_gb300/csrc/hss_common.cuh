@@ -24,19 +24,18 @@ __device__ __forceinline__ int warp_sum_int(int v) {
   return v;
 }
 
-// 1/x by Newton-Raphson on the reciprocal, y <- y + y (1 - x y), two steps
-// from the estimate of the PTX instruction rcp.approx.ftz.f64; each step
-// doubles the correct bits, so the result is within a few ulp of 1/x for
-// normal, finite, nonzero x (x = 0 or infinite gives NaN).  Five FP64
-// instructions instead of a correctly rounded divide: the pole sums are
-// FP64-pipe bound.
+// 1/x from the estimate y of the PTX instruction rcp.approx.ftz.f64 and one
+// second-order correction: with e = 1 - x y (one fma, exact to ~2^-75),
+// 1/x = y / (1 - e) = y (1 + e + e^2 + e^3 + ...), so y + y (e + e^2)
+// leaves |e|^3 (far below an ulp for the estimate's accuracy) plus the final
+// fma's rounding: within one ulp of 1/x for normal, finite, nonzero x (x = 0
+// or infinite gives NaN).  Four FP64 instructions instead of a correctly
+// rounded divide: the pole sums are FP64-pipe bound.
 __device__ __forceinline__ double rcp_nr(double x) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
+  const double e = fma(-x, y, 1.0);
+  return fma(y, fma(e, e, e), y);
 }
 
 // (value, index) argmax with "first index wins" ties -- Fortran MAXLOC order.

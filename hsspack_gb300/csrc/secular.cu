@@ -128,6 +128,8 @@ struct RootState {
   bool fell_back;
   bool fw;       // step model: false middle way, true fixed weight (origin pole exact)
   double prew;   // residual of the previous step (0: none yet)
+  double prel;   // previous model step / distance to the origin pole (< 0: none)
+  int first;     // evaluation count at the first evaluation of a given start
 };
 
 __device__ __forceinline__ double pole(const RootState &r, int i) { return __ldg(r.d + i); }
@@ -160,6 +162,8 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq,
   r.fell_back = false;
   r.fw = false;
   r.prew = 0.0;
+  r.prel = -1.0;
+  r.first = 0;
   if (!r.last) {
     r.oi = r.j;
     r.tau = 0.5 * r.delta;
@@ -170,7 +174,8 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq,
       else { r.oi = r.j + 1; r.tau = (double)guess * r.delta; r.lo = -half; r.hi = 0.0; }
       r.phase = 1;
       r.learned = true;
-      r.iters = 1;
+      r.iters = full ? 0 : 1;  // the learned start spent one evaluation on the midpoint
+      r.first = r.iters + 1;
     }
   } else {
     r.oi = r.K - 1;
@@ -221,13 +226,14 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   const double erretm = 8.0 * s.eabs + 2.0 * r.rhoinv + 3.0 * fabs(r.tau) * dw;
   if (fabs(w) <= HSS_EPS * erretm) { r.phase = 2; return; }
   if (r.iters > 41) { r.status = HSS_SECULAR_NOCONV; r.phase = 2; return; }
-  if (r.learned && r.iters == 2) {
+  if (r.learned && r.iters == r.first) {
     // residual check of the learned start: a Newton step across most of the
     // half interval means the start is unusable; restart from the standard guess
     r.learned = false;
     if (!(fabs(w / dw) <= 0.45 * r.delta)) {
       r.fell_back = true;
       r.prew = 0.0;
+      r.prel = -1.0;
       r.phase = 0;
       r.oi = r.j;
       r.tau = 0.5 * r.delta;
@@ -276,7 +282,8 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   }
   if (w * eta >= 0.0) eta = -w / dw;  // model went the wrong way: Newton step
   double tn = r.tau + eta;
-  if (!(tn > r.lo && tn < r.hi)) {
+  const bool bisect = !(tn > r.lo && tn < r.hi);
+  if (bisect) {
     // bisect; geometrically when the bracket spans decades on one side of the
     // origin (roots next to a pole sit many decades below the interval)
     if (r.lo > 0.0 && r.hi > 4096.0 * r.lo) tn = sqrt(r.lo * r.hi);
@@ -292,8 +299,20 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
       r.oi = r.j; r.tau += r.delta; r.lo += r.delta; r.hi += r.delta;
     }
   }
-  if (fabs(step) <= 2.0 * HSS_EPS * fabs(r.tau) || r.hi - r.lo <= 2.0 * HSS_EPS * fabs(r.tau))
+  if (fabs(step) <= 2.0 * HSS_EPS * fabs(r.tau) || r.hi - r.lo <= 2.0 * HSS_EPS * fabs(r.tau)) {
     r.phase = 2;
+    return;
+  }
+  // Quadratic convergence seen (a model step of at most 1e-10 of the
+  // distance to the origin pole, and at most 100 x the square of the
+  // previous relative step): the new iterate's error is below 1e-18 of that
+  // distance, so it is final without another evaluation.
+  const double rel = fabs(step) / fmax(fabs(r.tau), 1e-300);
+  if (!bisect && r.prel >= 0.0 && rel <= 1e-10 && rel <= 100.0 * r.prel * r.prel) {
+    r.phase = 2;
+    return;
+  }
+  r.prel = bisect ? -1.0 : rel;
 }
 
 // ------------------------------------------------------------- kernels -----
@@ -616,7 +635,7 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
       for (int i = gl; i < Ka; i += L) {
         if (i >= n0 && i < n0 + 2 * GR) continue;  // the near poles follow
         const float zi = __ldg(z32 + s + i);
-        const float t = zi / ((__ldg(d32 + s + i) - do32) - tau);
+        const float t = __fdividef(zi, (__ldg(d32 + s + i) - do32) - tau);
         if (i <= j) { a0 = fmaf(zi, t, a0); a1 = fmaf(t, t, a1); }
         else { b0 = fmaf(zi, t, b0); b1 = fmaf(t, t, b1); }
       }
@@ -625,7 +644,7 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
         const int i = n0 + q;
         if (i < 0 || i >= Ka || (i & (L - 1)) != gl) continue;
         const float zi = __ldg(z32 + s + i);
-        const float t = zi / (gn[q] - tau);
+        const float t = __fdividef(zi, gn[q] - tau);
         if (i <= j) { a0 = fmaf(zi, t, a0); a1 = fmaf(t, t, a1); }
         else { b0 = fmaf(zi, t, b0); b1 = fmaf(t, t, b1); }
       }

@@ -133,10 +133,10 @@ def test_cauchylike_host_entry():
     assert np.allclose(A, u[:, None] * v[None, :] / (D[:, None] - F[None, :]), rtol=1e-15, atol=0)
 
 
-def test_reciprocal_within_two_ulp_of_ieee_division():
-    # the pole sums divide by Newton-Raphson reciprocals instead of IEEE
-    # division; over 25 decades of magnitude and both signs they stay within
-    # 2 ulp of the correctly rounded 1/x
+def test_reciprocal_within_one_ulp_of_ieee_division():
+    # the pole sums divide by refined reciprocal estimates instead of IEEE
+    # division; over 300 decades of magnitude and both signs they stay within
+    # 1 ulp of the correctly rounded 1/x
     import ctypes
     rng = np.random.default_rng(9)
     x = rng.uniform(1.0, 2.0, 200000) * 10.0 ** rng.integers(-150, 150, 200000)
@@ -149,4 +149,4 @@ def test_reciprocal_within_two_ulp_of_ieee_division():
     y = yd.cpu().numpy()
     ref = 1.0 / x
     ulp = np.abs(y - ref) / np.spacing(np.abs(ref))
-    assert ulp.max() <= 2.0, ulp.max()
+    assert ulp.max() <= 1.0, ulp.max()
