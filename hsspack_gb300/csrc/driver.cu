@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <mutex>
 #include <string>
@@ -55,8 +56,14 @@ struct Ctx {
   bool pred_ready = false;  // learned secular predictor installed
   void *pinned = nullptr;
   size_t pinned_cap = 0;
-  char *ring = nullptr;  // pinned staging ring for small parameter uploads
+  char *ring = nullptr;  // pinned staging ring for parameter uploads
   size_t ring_cap = 0, ring_head = 0;
+  struct RingUse {  // ring bytes [a, b) are read by copies before event ev
+    size_t a, b;
+    cudaEvent_t ev;
+  };
+  std::deque<RingUse> ring_uses;     // in allocation order
+  std::vector<cudaEvent_t> ring_ev;  // free events
   long long launches = 0;
   Ctx() {
     hss_default_config(&cfg);
@@ -121,14 +128,14 @@ static int *gemm_flag(Ctx &c) { return buf<int>(c, "gemm_err", 1); }
 // Host->device parameter uploads (level views, product descriptors).  Small
 // ones stay pageable copies (measured faster: they travel with the command
 // stream); the larger lists of the batched levels go through a pinned ring --
-// a host memcpy plus an asynchronous copy, instead of a pageable copy staged
-// by the driver on the host while the GPU waits.  A ring region is reused
-// only after a device synchronisation.
+// a host memcpy plus an asynchronous copy, instead of a pageable copy that the
+// driver may serialise with the stream.  Each ring region is reused only
+// after the event recorded behind the copy that read it, normally long done.
 void stage_h2d(void *dst, const void *src, size_t bytes, void *stream) {
   if (bytes == 0) return;
   Ctx &c = ctx();
   cudaStream_t st = (cudaStream_t)stream;
-  constexpr size_t RING = 16u << 20;
+  constexpr size_t RING = 64u << 20;
   if (bytes <= (64u << 10) || bytes > RING / 4) {
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     return;
@@ -138,14 +145,28 @@ void stage_h2d(void *dst, const void *src, size_t bytes, void *stream) {
     c.ring_cap = RING;
     c.ring_head = 0;
   }
-  if (c.ring_head + bytes > c.ring_cap) {
-    CK(cudaDeviceSynchronize());
-    c.ring_head = 0;
+  const size_t need = (bytes + 255) & ~(size_t)255;
+  if (c.ring_head + need > c.ring_cap) c.ring_head = 0;
+  const size_t a = c.ring_head, b = a + need;
+  // the oldest uses come first; wait for (and retire) those [a, b) overlaps
+  while (!c.ring_uses.empty() && c.ring_uses.front().a < b && a < c.ring_uses.front().b) {
+    CK(cudaEventSynchronize(c.ring_uses.front().ev));
+    c.ring_ev.push_back(c.ring_uses.front().ev);
+    c.ring_uses.pop_front();
   }
-  char *p = c.ring + c.ring_head;
+  char *p = c.ring + a;
   memcpy(p, src, bytes);
   CK(cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, st));
-  c.ring_head += (bytes + 255) & ~(size_t)255;
+  cudaEvent_t ev;
+  if (c.ring_ev.empty()) {
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  } else {
+    ev = c.ring_ev.back();
+    c.ring_ev.pop_back();
+  }
+  CK(cudaEventRecord(ev, st));
+  c.ring_uses.push_back({a, b, ev});
+  c.ring_head = b;
 }
 
 static cudaEvent_t next_event(Ctx &c) {
@@ -320,6 +341,9 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   std::vector<double> drho_;
   std::vector<long long> q2off, soff, toff;
   std::vector<int> hsel;  // HSS merges (index into active arrays)
+  for (auto *v : {&as, &an, &aK, &aoff, &gs, &gn, &gng, &ds_, &dn_, &dK_, &doff}) v->reserve(P + 1);
+  for (auto *v : {&arho, &drho_}) v->reserve(P);
+  for (auto *v : {&q2off, &soff}) v->reserve(P);
   long long q2tot = 0, stot = 0;
   int maxn = 0, maxn_g = 0;
   for (int m = 0; m < P; ++m) {
@@ -493,6 +517,21 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   c.launches++;
 }
 
+// MDSTEDC's split test (mdstedc.f90: |E(i)| <= EPS sqrt|D(i)| sqrt|D(i+1)|).
+// Squares decide it without square roots unless they are within a relative
+// 1e-12 of the boundary or outside the range where they are exact enough;
+// those cases take the reference's own expression, so the decision is the
+// same.
+static inline bool negligible(double e, double a, double b) {
+  const double ae = std::fabs(e), aa = std::fabs(a), ab = std::fabs(b);
+  if (ae > 1e-100 && ae < 1e100 && aa > 1e-100 && aa < 1e100 && ab > 1e-100 && ab < 1e100) {
+    const double lhs = ae * ae, rhs = (HSS_EPS * HSS_EPS) * (aa * ab);
+    if (lhs > rhs * (1.0 + 1e-12)) return false;
+    if (lhs < rhs * (1.0 - 1e-12)) return true;
+  }
+  return !(ae > HSS_EPS * std::sqrt(aa) * std::sqrt(ab));
+}
+
 // Eigen-decomposition of many unreduced, scaled blocks at once.  Block b
 // covers global positions bs[b] .. bs[b] + bm[b] - 1 of d, e, Dp, perm and the
 // same rows and columns of Q (leading dim ldq); e is zero at every block's last
@@ -625,10 +664,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
     int start = o;
     while (start < o + n) {
       int finish = start;
-      while (finish < o + n - 1) {
-        const double tiny = EPS * std::sqrt(std::fabs(hd[finish])) * std::sqrt(std::fabs(hd[finish + 1]));
-        if (std::fabs(he[finish]) > tiny) ++finish; else break;
-      }
+      while (finish < o + n - 1 && !negligible(he[finish], hd[finish], hd[finish + 1])) ++finish;
       he[finish] = 0.0;
       double nrm = 0.0;
       for (int i = start; i <= finish; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
@@ -1281,6 +1317,10 @@ int hss_finalize(void) {
   if (c.ring) cudaFreeHost(c.ring);
   c.ring = nullptr;
   c.ring_cap = c.ring_head = 0;
+  for (auto &u : c.ring_uses) cudaEventDestroy(u.ev);
+  c.ring_uses.clear();
+  for (auto ev : c.ring_ev) cudaEventDestroy(ev);
+  c.ring_ev.clear();
   return 0;
 }
 
