@@ -477,7 +477,7 @@ def run_ours(args):
     # outside the measured region)
     from hsspack_gb300 import autotune
     if args.smlsiz > 0:
-        tuned, tune_ms = {"smlsiz": args.smlsiz, "predictor": 0}, None
+        tuned, tune_ms = {"smlsiz": args.smlsiz, "predictor": args.predictor}, None
     else:
         tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
                                        predictor=(0, 1, 2) if have_pred else (0, 2))
@@ -485,13 +485,16 @@ def run_ours(args):
     plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()
     clocks.start()
-    ms, acc, launches, st = timed(args.steps, args.warmup, True, full_cfg)
+    # the headline: no per-stage events, statistics read after the timed region
+    ms, _, launches, st = timed(args.steps, args.warmup, False, full_cfg)
     clk = clocks.stop()
     if args.profile_only:  # solves only: the command the ncu launch list wraps
         if rank == 0:
-            print(json.dumps({"profile_only": True, "ms_per_step": ms, "launches": launches,
-                              "stages_ms": {k: v for k, v in acc["ms"].items() if v > 0}}))
+            print(json.dumps({"profile_only": True, "ms_per_step": ms, "launches": launches}))
         return
+    # stage times (CUDA events per stage) from a separate, shorter run
+    prof_steps = max(1, min(3, args.steps))
+    _, acc, _, _ = timed(prof_steps, 1, True, full_cfg)
     # plain GPU merge (per-merge launches), fewer steps
     ms_plain, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, plain_cfg)
     ms_fp64, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, {"batched": 1, "precision": 0})
@@ -543,22 +546,33 @@ def run_ours(args):
     # dominant stage -> roofline (contract object), plus every stage against
     # the bound that applies to it
     pk = peaks()
-    top = max(acc["ms"], key=lambda s: acc["ms"][s])
+    # the dominant kernel: the longest stage among those that are one kernel
+    # (the product stage is a split pass plus tensor-core and FP64 kernels)
+    single = [s for s in ("final_gather", "secular", "build_S", "lowner", "leaf", "gather",
+                          "scatter") if acc["ms"].get(s, 0) > 0]
+    top = max(single, key=lambda s: acc["ms"][s])
     calls = max(1, acc["calls"][top])
     per_launch_ms = acc["ms"][top] / calls
     per_launch_bytes = acc["bytes"][top] / calls
-    achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_%s.json" % top)
     if os.path.exists(tpath):
         traffic = json.load(open(tpath)).get("bytes_per_launch")
     stage_roof = stage_rooflines(acc, pk)
-    roof = {"bound": "hbm", "kernel_stage": top, "achieved": achieved, "peak": pk["hbm_gbs"],
-            "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-            "peak_source": pk["source"], "per_launch_ms": per_launch_ms,
-            "algorithmic_bytes_per_launch": per_launch_bytes,
-            "pipe_bound": stage_roof.get(top, {}).get("bound"),
-            "pipe_roofline": stage_roof.get(top)}
+    if STAGE_BOUND[top] == "hbm":
+        achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel_stage": top, "achieved": achieved,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                "traffic": traffic, "peak_source": pk["source"],
+                "algorithmic_bytes_per_launch": per_launch_bytes}
+    else:  # an FP64-pipe kernel: its algorithmic flops against the FP64 rate
+        per_launch_flops = acc["flops"][top] / calls
+        achieved = per_launch_flops / (per_launch_ms * 1e-3) / 1e12
+        roof = {"bound": STAGE_BOUND[top], "kernel_stage": top, "achieved": achieved,
+                "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": traffic,
+                "peak_source": "nominal FP64 rate", "algorithmic_flops_per_launch": per_launch_flops}
+    roof.update({"per_launch_ms": per_launch_ms, "launches_per_step": calls})
     if rank != 0:
         return
     cpu = None
@@ -604,7 +618,7 @@ def run_ours(args):
         "batch": batch,
         "stage_rooflines": stage_roof,
         "other_workloads": extra,
-        "stages_ms_per_step": {k: v / args.steps for k, v in acc["ms"].items() if v > 0},
+        "stages_ms_per_step": {k: v / prof_steps for k, v in acc["ms"].items() if v > 0},
         "profiled_stage_share": {k: v / total_ms for k, v in acc["ms"].items() if v > 0},
         "stats": {k: st[k] for k in ("n_levels", "n_merges", "n_hss_merges", "n_dense_merges",
                                      "max_k", "max_rank", "total_k", "secular_iters",
@@ -628,6 +642,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
     ap.add_argument("--smlsiz", type=int, default=0,
                     help="fixed DC leaf size instead of the autotuner (profiling runs)")
+    ap.add_argument("--predictor", type=int, default=2, choices=[0, 1, 2],
+                    help="secular start when --smlsiz bypasses the autotuner (0 standard, "
+                         "1 learned, 2 FP32 pre-solve)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warmup + timed solves (for ncu launch lists)")
     args = ap.parse_args()
