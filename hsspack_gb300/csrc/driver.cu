@@ -428,7 +428,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
                  (unsigned long long *)(status + 2), guess, st, false, c.cfg.predictor == 2);
   // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
-  stage_end(HSS_ST_SECULAR, st, 40LL * total, 8.0 * 4.0 * k2);
+  stage_end(HSS_ST_SECULAR, st, 40LL * total, 0.0);  // flops from the pole-term count
   stage_begin(HSS_ST_LOWNER, st);
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, false,
                 *std::max_element(aK.begin(), aK.end()));
@@ -640,9 +640,10 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   double *d = buf<double>(c, "d_in", N), *e = buf<double>(c, "e_in", N);
   long long *dP = nullptr;
   // status[0]: error code, status[2..3]: 64-bit sum of secular iterations,
-  // status[4..5]: 64-bit count of learned starts that fell back
-  int *status = buf<int>(c, "status", 6);
-  CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  // status[4..5]: 64-bit count of learned starts that fell back, status[6..7]:
+  // 64-bit sum over roots of iterations x K (pole terms evaluated)
+  int *status = buf<int>(c, "status", 8);
+  CK(cudaMemsetAsync(status, 0, 8 * sizeof(int), st));
   CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
   // no zero fill of Q: every column is tracked with the rows it holds data on
   // (set by the leaves, widened by merges) and read as zero elsewhere
@@ -742,7 +743,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   }
   c.launches++;
   CK(cudaEventRecord(ev1, st));
-  int hst[6] = {0, 0, 0, 0, 0, 0};
+  int hst[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -752,6 +753,13 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   memcpy(&fb, hst + 4, sizeof fb);
   c.stats.secular_iters = (long long)its;
   c.stats.predictor_fallbacks = (long long)fb;
+  {
+    // per pole term per evaluation: 2 subtractions, a reciprocal (estimate +
+    // 3 fma = 6 flops), a multiply and 2 fma
+    unsigned long long terms;
+    memcpy(&terms, hst + 6, sizeof terms);
+    c.stats.stage_flops[HSS_ST_SECULAR] = 13.0 * (double)terms;
+  }
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   c.stats.ms_total = ms;
@@ -812,8 +820,8 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   double *Q = buf<double>(c, "Q", (size_t)n * n);
   double *Dp = buf<double>(c, "Dp", n);
   int *perm = buf<int>(c, "perm", n);
-  int *status = buf<int>(c, "status", 6);
-  CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  int *status = buf<int>(c, "status", 8);
+  CK(cudaMemsetAsync(status, 0, 8 * sizeof(int), st));
   CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
   CK(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)n * n, st));
   const size_t kk = (size_t)kd * kd;
@@ -893,7 +901,7 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   stage_end(HSS_ST_FINAL, st, 16LL * n * n + 20LL * n, 0.0);
   c.launches++;
   CK(cudaEventRecord(ev1, st));
-  int hst[6] = {0, 0, 0, 0, 0, 0};
+  int hst[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -902,6 +910,13 @@ static int band_core(Ctx &c, int n, int kd, const double *ab, long long ldab, do
   memcpy(&fb, hst + 4, sizeof fb);
   c.stats.secular_iters = (long long)its;
   c.stats.predictor_fallbacks = (long long)fb;
+  {
+    // per pole term per evaluation: 2 subtractions, a reciprocal (estimate +
+    // 3 fma = 6 flops), a multiply and 2 fma
+    unsigned long long terms;
+    memcpy(&terms, hst + 6, sizeof terms);
+    c.stats.stage_flops[HSS_ST_SECULAR] = 13.0 * (double)terms;
+  }
   float ms_ = 0.f;
   CK(cudaEventElapsedTime(&ms_, ev0, ev1));
   c.stats.ms_total = ms_;
@@ -999,7 +1014,7 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
   stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
                  (unsigned long long *)(status + 2), nullptr, st, true);
-  stage_end(HSS_ST_SECULAR, st, 40LL * total, 12.0 * 4.0 * k2);
+  stage_end(HSS_ST_SECULAR, st, 40LL * total, 0.0);  // flops from the pole-term count
   stage_begin(HSS_ST_LOWNER, st);
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true, maxK);
   stage_end(HSS_ST_LOWNER, st, 40LL * total, 8.0 * k2);
@@ -1117,8 +1132,8 @@ static int svd_core(Ctx &c, int n, const double *d, const double *e, double *Uo,
   double *V = buf<double>(c, "sv_V", (size_t)n * n);
   double *Dp = buf<double>(c, "Dp", n);
   int *perm = buf<int>(c, "perm", n);
-  int *status = buf<int>(c, "status", 6);
-  CK(cudaMemsetAsync(status, 0, 6 * sizeof(int), st));
+  int *status = buf<int>(c, "status", 8);
+  CK(cudaMemsetAsync(status, 0, 8 * sizeof(int), st));
   CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
   CK(cudaMemsetAsync(U, 0, sizeof(double) * (size_t)n * n, st));
   CK(cudaMemsetAsync(V, 0, sizeof(double) * (size_t)n * n, st));
@@ -1163,13 +1178,16 @@ static int svd_core(Ctx &c, int n, const double *d, const double *e, double *Uo,
   stage_end(HSS_ST_FINAL, st, vectors ? 32LL * n * n : 16LL * n, 0.0);
   c.launches += 2;
   CK(cudaEventRecord(ev1, st));
-  int hst[6] = {0, 0, 0, 0, 0, 0};
+  int hst[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  unsigned long long its;
+  unsigned long long its, terms;
   memcpy(&its, hst + 2, sizeof its);
+  memcpy(&terms, hst + 6, sizeof terms);
   c.stats.secular_iters = (long long)its;
+  // squared poles: one more multiply and add per term
+  c.stats.stage_flops[HSS_ST_SECULAR] = 15.0 * (double)terms;
   float ms_ = 0.f;
   CK(cudaEventElapsedTime(&ms_, ev0, ev1));
   c.stats.ms_total = ms_;
@@ -1691,8 +1709,8 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
       launch_secular_mid(lv, k, k, dlamda, z, feat, st);
       launch_predict(k, feat, buf<char>(c, "pred_wb", 0), buf<float>(c, "pred_norm", 0), guess, st);
     }
-    unsigned long long *cnt = (unsigned long long *)buf<char>(c, "x_counts", 16);
-    CK(cudaMemsetAsync(cnt, 0, 16, st));
+    unsigned long long *cnt = (unsigned long long *)buf<char>(c, "x_counts", 24);
+    CK(cudaMemsetAsync(cnt, 0, 24, st));
     launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, cnt, guess, st, false,
                    c.cfg.predictor == 2);
     unsigned long long hc[2];

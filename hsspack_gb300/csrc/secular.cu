@@ -396,6 +396,7 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
     if (itsum) {
       atomicAdd(itsum, (unsigned long long)st.iters);
       if (st.fell_back) atomicAdd(itsum + 1, 1ull);
+      atomicAdd(itsum + 2, (unsigned long long)st.iters * (unsigned long long)st.K);  // pole terms
     }
     if (st.status) atomicMax(status, st.status);
   }
