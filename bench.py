@@ -7,14 +7,16 @@ eigenvector matrix (8.6 GB) is far larger than L2, so no flush is needed
 between steps.
 
 value: device-resident seconds per solve (inputs already in HBM, CUDA events
-on the launching stream over exactly K steps).  batch: the second half of the
-metric, 512 uneven tridiagonals (n log-uniform in [256, 4096]) solved in one
-batched call, as solves/s, beside one call per problem and the plain GPU merge.  e2e: the same solve through the
-Fortran drop-in ``mdstedc_`` with pinned host buffers (D/E host->device and
-Z/W device->host inside the timed region).  roofline: the stage that takes the
-most device time, its algorithmic bytes (or flops) over its event-timed
-duration.  cpu_baseline / --impl reference: the CPU oracle (C++ restatement of
-HSSPACK's MDSTEDC + LAPACK from OpenBLAS) on the host cores.
+on the launching stream over exactly K steps, no per-stage events).  batch: the
+second half of the metric, 512 uneven tridiagonals (n log-uniform in
+[256, 4096]) solved in one batched call, as solves/s, beside one call per
+problem and the plain GPU merge.  e2e: the same solve through the Fortran
+drop-in ``mdstedc_`` with pinned host buffers (D/E host->device, the
+eigenvectors and eigenvalues device->host and the host-side zero fill of Z
+inside the timed region).  roofline: the final gather, the longest single
+launch, its algorithmic bytes over its event-timed duration.  cpu_baseline /
+--impl reference: the CPU oracle (C++ restatement of HSSPACK's MDSTEDC +
+LAPACK from OpenBLAS) on the host cores.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -527,7 +529,8 @@ def run_ours(args):
         for _ in range(e2e_steps):
             e2e_step()
         e2e_s = (time.perf_counter() - t) / e2e_steps
-        e2e_solve_ms = hp.get_stats()["ms_total"]  # the last step's device solve
+        e2e_st = hp.get_stats()  # the last step's device solve and its copies
+        e2e_solve_ms = e2e_st["ms_total"]
     finally:
         hp.restore_config(old_cfg)
     if world > 1:
@@ -604,8 +607,10 @@ def run_ours(args):
                    "smlsiz": full_cfg.get("smlsiz"), "autotune_ms": tune_ms,
                    "l2": "no flush: the 8.6 GB eigenvector matrix exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 16 * n,
-                "d2h_bytes_per_step": 8 * n * n + 8 * n,
+        # bytes the call copied: D, E in; eigenvalues and either Z or only the
+        # rows each column holds data on (the call zero-fills Z on the host)
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": e2e_st["host_h2d_bytes"],
+                "d2h_bytes_per_step": e2e_st["host_d2h_bytes"],
                 # the library's event time of the solve inside a step; the
                 # rest is the host<->device copies and the call's host work
                 "device_solve_s": e2e_solve_ms / 1000.0},

@@ -59,7 +59,8 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_longlong), ("ms_total", ctypes.c_double),
                 ("stage_ms", ctypes.c_double * 16), ("stage_calls", ctypes.c_longlong * 16),
                 ("stage_bytes", ctypes.c_longlong * 16), ("stage_flops", ctypes.c_double * 16),
-                ("reserved", ctypes.c_int * 8)]
+                ("host_h2d_bytes", ctypes.c_longlong), ("host_d2h_bytes", ctypes.c_longlong),
+                ("reserved", ctypes.c_int * 4)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

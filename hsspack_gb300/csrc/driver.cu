@@ -19,6 +19,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/hsspack_gb300.h"
@@ -43,6 +44,19 @@ struct TimedRange {
   double flops;
 };
 
+// Eigenvectors bound for host memory (mdstedc_): when the columns' supports
+// cover little of Z, the solve leaves them packed on the device (the
+// supported rows of every output column back to back) instead of writing the
+// full n x n matrix; the host zero-fills Z meanwhile and scatters the segments.
+struct PackedZ {
+  bool want = false;           // request (single problem, supports tracked)
+  bool packed = false;         // result: the packed form was produced
+  long long total = 0;         // packed doubles
+  std::vector<int2> seg;       // per output column: rows [x, y)
+  std::vector<long long> off;  // per output column: offset into the packed data
+  double *dbuf = nullptr;      // device packed data
+};
+
 struct Ctx {
   std::recursive_mutex mu;
   std::vector<cudaEvent_t> evpool;
@@ -64,6 +78,9 @@ struct Ctx {
   };
   std::deque<RingUse> ring_uses;     // in allocation order
   std::vector<cudaEvent_t> ring_ev;  // free events
+  PackedZ *pz = nullptr;             // packed-output request of the running solve
+  double *zstage = nullptr;          // pinned staging of packed eigenvectors
+  size_t zstage_cap = 0;
   long long launches = 0;
   Ctx() {
     hss_default_config(&cfg);
@@ -107,6 +124,93 @@ static T *buf(Ctx &c, const char *name, size_t count) {
     b.cap = cap;
   }
   return (T *)b.p;
+}
+
+// Host threads for the output work of the host entry points: all cores but
+// two (the solve's own host thread keeps running meanwhile).
+static int host_threads() {
+  const unsigned h = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(16u, h > 2 ? h - 2 : 1u));
+}
+
+// Zeroes rows 0..n-1 of the n columns of a host matrix (leading dimension ld)
+// on worker threads; join() (also the destructor) waits for them.
+class HostFill {
+ public:
+  HostFill(double *z, int n, long long ld, bool on) {
+    if (!on) return;
+    const int T = host_threads();
+    auto work = [z, n, ld, T](int t) {
+      if (ld == n) {
+        const size_t tot = (size_t)n * n, a = tot * t / T, b = tot * (t + 1) / T;
+        memset(z + a, 0, (b - a) * sizeof(double));
+      } else {
+        for (long long j = (long long)n * t / T; j < (long long)n * (t + 1) / T; ++j)
+          memset(z + j * ld, 0, (size_t)n * sizeof(double));
+      }
+    };
+    for (int t = 0; t < T; ++t) {
+      try {
+        th_.emplace_back(work, t);
+      } catch (...) {
+        work(t);  // no thread available: do this share here
+      }
+    }
+    on_ = true;
+  }
+  bool active() const { return on_; }
+  void join() {
+    for (auto &x : th_)
+      if (x.joinable()) x.join();
+    th_.clear();
+  }
+  ~HostFill() { join(); }
+
+ private:
+  std::vector<std::thread> th_;
+  bool on_ = false;
+};
+
+// the packed segments into their columns of the (zeroed) host matrix
+static void scatter_columns(double *z, long long ld, int n, const PackedZ &pz, const double *src) {
+  const int T = host_threads();
+  auto work = [&](int t) {
+    for (long long j = (long long)n * t / T; j < (long long)n * (t + 1) / T; ++j) {
+      const int2 r = pz.seg[j];
+      if (r.y > r.x)
+        memcpy(z + j * ld + r.x, src + pz.off[j], (size_t)(r.y - r.x) * sizeof(double));
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; ++t) {
+    try {
+      th.emplace_back(work, t);
+    } catch (...) {
+      work(t);
+    }
+  }
+  work(0);
+  for (auto &x : th) x.join();
+}
+
+// sets the packed-output request for the duration of one solve
+struct PzScope {
+  Ctx &c;
+  PzScope(Ctx &c_, PackedZ *p) : c(c_) { c.pz = p; }
+  ~PzScope() { c.pz = nullptr; }
+};
+
+// pinned staging for packed eigenvectors (grows, kept)
+static double *zstage(Ctx &c, size_t count) {
+  if (c.zstage_cap < count) {
+    if (c.zstage) CK(cudaFreeHost(c.zstage));
+    c.zstage = nullptr;
+    c.zstage_cap = 0;
+    const size_t cap = count + count / 8;
+    CK(cudaMallocHost((void **)&c.zstage, cap * sizeof(double)));
+    c.zstage_cap = cap;
+  }
+  return c.zstage;
 }
 
 static void *pinned(Ctx &c, size_t bytes) {
@@ -723,7 +827,36 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
     h2d(fperm, hp, st);
   }
   stage_begin(HSS_ST_FINAL, st);
-  if (np == 1) {
+  long long final_bytes = 0;
+  bool packed = false;
+  if (np == 1 && c.pz && c.pz->want && sup) {
+    // output column i is slot fperm[i], holding data on rows sup[slot]
+    PackedZ &pz = *c.pz;
+    std::vector<int> hp(N);
+    std::vector<int2> hs(N);
+    CK(cudaMemcpyAsync(hp.data(), fperm, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hs.data(), sup, sizeof(int2) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    pz.seg.resize(N);
+    pz.off.assign(N + 1, 0);
+    for (int i = 0; i < N; ++i) {
+      const int2 r = hs[hp[i]];
+      pz.seg[i] = r;
+      pz.off[i + 1] = pz.off[i] + std::max(0, r.y - r.x);
+    }
+    pz.total = pz.off[N];
+    if (pz.total * 5 <= (long long)N * N * 3) {  // supports cover at most 60 % of Z
+      long long *doff = buf<long long>(c, "pz_off", N + 1);
+      stage_h2d(doff, pz.off.data(), sizeof(long long) * (N + 1), st);
+      pz.dbuf = buf<double>(c, "pz_data", (size_t)std::max<long long>(pz.total, 1));
+      launch_pack_columns(N, fperm, Dp, Q, L, sup, doff, pz.dbuf, pr[0].w, st);
+      pz.packed = packed = true;
+      final_bytes = 16LL * pz.total + 20LL * N;
+    }
+  }
+  if (packed) {
+    // the packed segments replace the n x n write
+  } else if (np == 1) {
     launch_final_gather(N, fperm, Dp, Q, L, pr[0].z, pr[0].ldz, pr[0].w, st, sup);
   } else {
     std::vector<double *> hz(np), hw(np);
@@ -739,7 +872,7 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
     for (auto &q : pr) nn += (long long)q.n * q.n;
     // compulsory traffic: the n^2 output write and the slot/eigenvalue
     // vectors; the Q reads cover only the columns' supports (data dependent)
-    stage_end(HSS_ST_FINAL, st, 8LL * nn + 20LL * N, 0.0);
+    stage_end(HSS_ST_FINAL, st, packed ? final_bytes : 8LL * nn + 20LL * N, 0.0);
   }
   c.launches++;
   CK(cudaEventRecord(ev1, st));
@@ -1339,6 +1472,9 @@ int hss_finalize(void) {
   c.ring_uses.clear();
   for (auto ev : c.ring_ev) cudaEventDestroy(ev);
   c.ring_ev.clear();
+  if (c.zstage) cudaFreeHost(c.zstage);
+  c.zstage = nullptr;
+  c.zstage_cap = 0;
   return 0;
 }
 
@@ -1669,12 +1805,34 @@ void mdstedc_(const char *compz, const int *n_, double *d, double *e, double *z,
       // calls DSTERF here, mdstedc.f90:264-267)
       *info = mdstedc_core(c, n, hd, he, dz, n, dw, st);
     } else {
-      *info = mdstedc_core(c, n, hd, he, dz, n, dw, st);
-      CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n, n,
-                           cudaMemcpyDeviceToHost, st));
+      // large problems: Z is zeroed on host threads while the GPU solves, and
+      // only the columns' supported rows come back (unless they fill Z)
+      HostFill fill(z, n, ldz, n >= 2048);
+      PackedZ pz;
+      pz.want = fill.active();
+      {
+        PzScope scope(c, &pz);
+        *info = mdstedc_core(c, n, hd, he, dz, n, dw, st);
+      }
+      if (pz.packed) {
+        double *hz = zstage(c, (size_t)std::max<long long>(pz.total, 1));
+        CK(cudaMemcpyAsync(hz, pz.dbuf, sizeof(double) * pz.total, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        fill.join();
+        scatter_columns(z, ldz, n, pz, hz);
+        // packed rows plus the slot and row-range tables read on the host
+        c.stats.host_d2h_bytes = 8LL * pz.total + 12LL * n;
+      } else {
+        fill.join();
+        CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n, n,
+                             cudaMemcpyDeviceToHost, st));
+        c.stats.host_d2h_bytes = 8LL * n * n;
+      }
     }
     CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    c.stats.host_d2h_bytes += 8LL * n;
+    c.stats.host_h2d_bytes = 16LL * n;
     if (work) work[0] = (double)lwmin;
     if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
   } catch (CudaError &ex) {

@@ -119,6 +119,11 @@ void launch_merge_finish_grid(int P, int total, const int *poff, const int *ms, 
 void launch_final_gather(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          double *Z, long long ldz, double *wout, cudaStream_t st,
                          const int2 *sup = nullptr);
+// packed final permutation: the supported rows of every output column back to
+// back at out + off[c] (off from the host), w(c) = Dp(perm(c))
+void launch_pack_columns(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
+                         const int2 *sup, const long long *off, double *out, double *wout,
+                         cudaStream_t st);
 // many problems per call: P = global start of each problem (np + 1 entries),
 // total = P[np]; problem p's block is Q + P[p] * (ldq + 1), leading dim ldq
 void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,

@@ -561,6 +561,24 @@ __global__ void k_final_gather(int n, const int *__restrict__ perm, const double
   if (threadIdx.x == 0) wout[c] = Dp[p];
 }
 
+// Packed form of the final permutation for host outputs: output column c
+// (slot perm[c]) holds data only on rows sup[slot] = [x, y); those rows go to
+// out[off[c] ..] back to back (off: prefix sum of y - x, computed on the host
+// from the same sup), w(c) = Dp(perm(c)).  One CTA per column.
+__global__ void k_pack_columns(int n, const int *__restrict__ perm, const double *__restrict__ Dp,
+                               const double *__restrict__ Q, long long ldq,
+                               const int2 *__restrict__ sup, const long long *__restrict__ off,
+                               double *__restrict__ out, double *__restrict__ wout) {
+  const int c = blockIdx.x;
+  if (c >= n) return;
+  const long long p = perm[c];
+  const int2 r = sup[p];
+  const double *src = Q + p * ldq;
+  double *dst = out + off[c];
+  for (int i = r.x + threadIdx.x; i < r.y; i += blockDim.x) dst[i - r.x] = src[i];
+  if (threadIdx.x == 0) wout[c] = Dp[p];
+}
+
 // ------------------------------------------------ many problems per call --
 // Problems of one call sit at global positions P[p] .. P[p+1]-1 and share one
 // Q with leading dimension ldq >= max n_p: problem p's eigenvector block is the
@@ -704,6 +722,11 @@ void launch_final_gather(int n, const int *perm, const double *Dp, const double 
                          double *Z, long long ldz, double *wout, cudaStream_t st,
                          const int2 *sup) {
   if (n > 0) k_final_gather<<<n, 256, 0, st>>>(n, perm, Dp, Q, ldq, Z, ldz, wout, sup);
+}
+void launch_pack_columns(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
+                         const int2 *sup, const long long *off, double *out, double *wout,
+                         cudaStream_t st) {
+  if (n > 0) k_pack_columns<<<n, 128, 0, st>>>(n, perm, Dp, Q, ldq, sup, off, out, wout);
 }
 void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
                         cudaStream_t st) {

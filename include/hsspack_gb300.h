@@ -68,7 +68,9 @@ typedef struct hss_stats {
   long long stage_calls[16];    /* timed launches per stage                 */
   long long stage_bytes[16];    /* algorithmic bytes moved per stage        */
   double stage_flops[16];       /* algorithmic flops per stage              */
-  int reserved[8];
+  long long host_h2d_bytes;     /* host entries: bytes copied host -> device */
+  long long host_d2h_bytes;     /* host entries: bytes copied device -> host */
+  int reserved[4];
 } hss_stats;
 
 void hss_default_config(hss_config *cfg);

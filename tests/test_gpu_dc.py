@@ -135,3 +135,36 @@ def test_fp32_start_saves_evaluations():
             hp.restore_config(old)
         evals[pred] = st["secular_iters"] / max(st["secular_roots"], 1)
     assert evals[2] < evals[0] - 0.5, evals
+
+
+# The host entry (MDSTEDC) zero-fills Z on host threads during the solve and
+# copies back only each column's supported rows when they cover at most 60 %
+# of Z; the result must be the device entry's Z bit for bit, also with
+# LDZ > N (rows N..LDZ-1 untouched) and when the supports fill Z (dense path).
+@pytest.mark.parametrize("kind,n,extra", [("random", 4096, 0), ("random", 2500, 37),
+                                          ("toeplitz", 2048, 0)])
+def test_host_entry_packed_output_matches_device(kind, n, extra):
+    import torch
+    d, e = rand_tridiag(n, seed=3) if kind == "random" else toeplitz_tridiag(n)
+    old = hp.set_config(precision=1, smlsiz=12)
+    try:
+        dd = torch.tensor(d, device="cuda")
+        ee = torch.tensor(np.append(e, 0.0), device="cuda")
+        zd = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        hp.mdstedc_dev(dd, ee, zd)
+        zdev = zd.cpu().numpy().reshape(n, n).T
+        ldz = n + extra
+        Z = np.full((ldz, n), 7.0, order="F")
+        w = np.array(d, dtype=np.float64)
+        ew = np.zeros(n)
+        ew[: n - 1] = e
+        work = np.zeros(1)
+        iwork = np.zeros(1, dtype=np.int32)
+        info = hp.mdstedc("I", n, w, ew, Z, ldz, work, 1 + 4 * n + n * n, iwork, 3 + 5 * n)
+    finally:
+        hp.restore_config(old)
+    assert info == 0
+    assert np.array_equal(w, dd.cpu().numpy())
+    assert np.array_equal(Z[:n], zdev)
+    if extra:
+        assert np.all(Z[n:] == 7.0)
