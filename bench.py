@@ -65,13 +65,18 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
             return
         self.th = threading.Thread(target=self._read, daemon=True)
         self.th.start()
+        # nvidia-smi takes a moment to start: let it, so the samples cover the
+        # warm-up and timed solves that follow
+        t0 = time.time()
+        while not self.rows and time.time() - t0 < 2.0:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
