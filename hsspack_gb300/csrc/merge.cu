@@ -113,35 +113,33 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     return;
   }
   // ---- candidates: z large enough (deflation by small z, mdlaed2.f90:304-313)
-  const int chunk = (n + MT - 1) / MT;
-  const int b0 = min(n, tid * chunk), b1 = min(n, b0 + chunk);
-  // The chunk loops take PB positions per step, loads first: each thread's
-  // chunk is contiguous (order-preserving compaction from one block scan),
-  // so the loads are not coalesced, and batching them hides the latency.
-  constexpr int PB = 8;
+  // Warp w scans the contiguous positions [w0, w1) in steps of 32 consecutive
+  // positions (coalesced); ballots rank a position among its warp's, and a
+  // scan over the warps' totals orders the warps, so every compaction keeps
+  // the position order.
+  constexpr int NW = MT / 32;
+  const int lane = tid & 31, wid = tid >> 5;
+  const int seg = (((n + NW - 1) / NW) + 31) & ~31;
+  const int w0 = min(n, wid * seg), w1 = min(n, w0 + seg);
+  const unsigned below = (1u << lane) - 1u;  // lanes ahead of this one
   int cnt = 0;
-  for (int i0 = b0; i0 < b1; i0 += PB) {
-    double zv[PB];
-#pragma unroll
-    for (int u = 0; u < PB; ++u) zv[u] = i0 + u < b1 ? w.zs[s + i0 + u] : 0.0;
-#pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      if (i0 + u >= b1) break;
-      const bool big = rho * fabs(zv[u]) > tol;  // typ 4: deflated, small z
-      cnt += big;
-      if (!big) w.typ[s + i0 + u] = 4;
-    }
+  for (int i0 = w0; i0 < w1; i0 += 32) {
+    const int i = i0 + lane;
+    const bool in = i < w1;
+    const bool big = in && rho * fabs(w.zs[s + i]) > tol;
+    if (in && !big) w.typ[s + i] = 4;  // deflated, small z
+    cnt += __popc(__ballot_sync(HSS_FULL, big));
   }
   unsigned long long tot;
-  int pos = (int)block_scan64<MT>((unsigned long long)cnt, &tot);
+  int pos = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)cnt : 0ull, &tot);
+  pos = __shfl_sync(HSS_FULL, pos, 0);
   const int nc = (int)tot;
-  for (int i0 = b0; i0 < b1; i0 += PB) {
-    unsigned char tv[PB];
-#pragma unroll
-    for (int u = 0; u < PB; ++u) tv[u] = i0 + u < b1 ? w.typ[s + i0 + u] : 4;
-#pragma unroll
-    for (int u = 0; u < PB; ++u)
-      if (tv[u] != 4) w.cand[s + pos++] = i0 + u;
+  for (int i0 = w0; i0 < w1; i0 += 32) {
+    const int i = i0 + lane;
+    const bool big = i < w1 && w.typ[s + i] != 4;
+    const unsigned m = __ballot_sync(HSS_FULL, big);
+    if (big) w.cand[s + pos + __popc(m & below)] = i;
+    pos += __popc(m);
   }
   __syncthreads();
   // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371): a
@@ -229,66 +227,58 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     __syncthreads();
   }
   // ---- compact non-deflated (poles, weights, slots, block-structure groups)
-  //      and deflated (slots, values) lists
-  unsigned long long pk = 0;
+  //      and deflated (slots, values) lists; same warp segments and ranks
+  unsigned long long pk = 0;  // types 1, 2, 3 counted in 21-bit fields
   int n5 = 0;
-  for (int i0 = b0; i0 < b1; i0 += PB) {
-    unsigned char tv[PB];
-#pragma unroll
-    for (int u = 0; u < PB; ++u) tv[u] = i0 + u < b1 ? w.typ[s + i0 + u] : 4;
-#pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      const int t = tv[u];
-      if (t <= 3) pk += 1ull << (21 * (t == 1 ? 0 : t == 2 ? 1 : 2));
-      n5 += (t == 5);
-    }
+  for (int i0 = w0; i0 < w1; i0 += 32) {
+    const int i = i0 + lane;
+    const int t = i < w1 ? w.typ[s + i] : 0;
+    pk += (unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 1)) +
+          ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 2)) << 21) +
+          ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 3)) << 42);
+    n5 += __popc(__ballot_sync(HSS_FULL, t == 5));
   }
   unsigned long long ptot, t5;
-  unsigned long long pre = block_scan64<MT>(pk, &ptot);
-  int r5 = (int)block_scan64<MT>((unsigned long long)n5, &t5);
+  unsigned long long pre = block_scan64<MT>(lane == 0 ? pk : 0ull, &ptot);
+  int r5 = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)n5 : 0ull, &t5);
+  pre = __shfl_sync(HSS_FULL, pre, 0);
+  r5 = __shfl_sync(HSS_FULL, r5, 0);
   const int c1 = (int)(ptot & 0x1fffff), c2 = (int)((ptot >> 21) & 0x1fffff),
             c3 = (int)((ptot >> 42) & 0x1fffff);
   const int K = c1 + c2 + c3;
   const int nrot = (int)t5;
   int r1 = (int)(pre & 0x1fffff), r2 = (int)((pre >> 21) & 0x1fffff),
       r3 = (int)((pre >> 42) & 0x1fffff);
-  for (int i0 = b0; i0 < b1; i0 += PB) {
-    unsigned char tv[PB];
-    double dv[PB], zv[PB];
-    int sv[PB];
-#pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      const bool in = i0 + u < b1;
-      tv[u] = in ? w.typ[s + i0 + u] : 0;
-      dv[u] = in ? w.ds[s + i0 + u] : 0.0;
-      zv[u] = in ? w.zs[s + i0 + u] : 0.0;
-      sv[u] = in ? w.srt[s + i0 + u] : 0;
-    }
-#pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      const int i = i0 + u;
-      if (i >= b1) break;
-      const int t = tv[u];
-      const int j = r1 + r2 + r3;  // non-deflated before position i
+  for (int i0 = w0; i0 < w1; i0 += 32) {
+    const int i = i0 + lane;
+    const bool in = i < w1;
+    const int t = in ? w.typ[s + i] : 0;
+    const double dv = in ? w.ds[s + i] : 0.0, zv = in ? w.zs[s + i] : 0.0;
+    const int sv = in ? w.srt[s + i] : 0;
+    const unsigned m1 = __ballot_sync(HSS_FULL, t == 1), m2 = __ballot_sync(HSS_FULL, t == 2),
+                   m3 = __ballot_sync(HSS_FULL, t == 3), m5 = __ballot_sync(HSS_FULL, t == 5);
+    if (in) {
+      // this position's rank among the non-deflated of each type and the rotated
+      const int e1 = r1 + __popc(m1 & below), e2 = r2 + __popc(m2 & below),
+                e3 = r3 + __popc(m3 & below), e5 = r5 + __popc(m5 & below);
+      const int j = e1 + e2 + e3;  // non-deflated before position i
       if (t <= 3) {
-        w.dl[s + j] = dv[u];
-        w.zw[s + j] = zv[u];
-        w.ndslot[s + j] = sv[u];
-        w.grp[s + j] = (t == 1) ? r1 : (t == 2) ? c1 + r2 : c1 + c2 + r3;
-        if (t == 1) ++r1; else if (t == 2) ++r2; else ++r3;
+        w.dl[s + j] = dv;
+        w.zw[s + j] = zv;
+        w.ndslot[s + j] = sv;
+        w.grp[s + j] = (t == 1) ? e1 : (t == 2) ? c1 + e2 : c1 + c2 + e3;
       } else {
         const int a = i - j;  // deflated before position i
-        const int slot = sv[u];
-        const double v = dv[u];
-        Dp[slot] = v;
+        Dp[sv] = dv;
         if (t == 5) {
-          w.l2slot[s + r5] = slot; w.l2val[s + r5] = v; ++r5;
+          w.l2slot[s + e5] = sv; w.l2val[s + e5] = dv;
         } else {
-          const int a1 = a - r5;  // small-z deflated before position i
-          w.l1slot[s + a1] = slot; w.l1val[s + a1] = v;
+          const int a1 = a - e5;  // small-z deflated before position i
+          w.l1slot[s + a1] = sv; w.l1val[s + a1] = dv;
         }
       }
     }
+    r1 += __popc(m1); r2 += __popc(m2); r3 += __popc(m3); r5 += __popc(m5);
   }
   __syncthreads();
   // The small-z list is ascending; rotated poles moved inside their gap
