@@ -568,6 +568,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     stage_end(HSS_ST_GATHER, st, 16LL * q2tot, 0.0);
     // GEMM problems: top rows use type 1,2 columns, bottom rows type 2,3
     std::vector<GemmDesc> probs;
+    probs.reserve(2 * (size_t)PD);
     int tiles = 0;
     int di = 0;
     for (int m = 0; m < P; ++m) {

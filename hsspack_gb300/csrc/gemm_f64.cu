@@ -132,32 +132,28 @@ void launch_gemm_f64(int nprob, int total_tiles, const GemmDesc *d_probs, cudaSt
   k_gemm_f64<<<total_tiles, GT, 0, st>>>(nprob, d_probs);
 }
 
-void launch_gemm(const std::vector<GemmDesc> &probs_in, int precision, cudaStream_t st) {
-  if (probs_in.empty()) return;
-  std::vector<GemmDesc> probs;
-  if (precision == 1) {
-    // tensor-core splitting pays off once a product has enough MACs per
-    // operand byte; small products stay on the FP64 pipe
-    std::vector<GemmDesc> big;
-    for (const auto &p : probs_in) {
-      if ((double)p.M * p.N * p.K >= ldexp(1.0, g_split_log2) && p.M >= g_split_m) big.push_back(p);
-      else probs.push_back(p);
-    }
-    int *err = pool<int>("gemm_err", 1);
-    if (!big.empty()) {
-      if (g_gemm_path == 1) launch_gemm_fused(big, err, st);
-      else launch_gemm_split(big, err, st);
-    }
-    if (probs.empty()) return;
-  } else {
-    probs = probs_in;
+void launch_gemm(const std::vector<GemmDesc> &probs, int precision, cudaStream_t st) {
+  if (probs.empty()) return;
+  // one pass: tensor-core splitting pays off once a product has enough MACs
+  // per operand byte (precision 1); the rest stay on the FP64 pipe, small
+  // ones (N, K <= g_small_nk) by the element kernel, others by 64 x 64 tiles
+  const double big_macs = ldexp(1.0, g_split_log2);
+  std::vector<GemmDesc> big, tiny, tiled;
+  tiny.reserve(probs.size());
+  for (const auto &p : probs) {
+    if (precision == 1 && (double)p.M * p.N * p.K >= big_macs && p.M >= g_split_m) big.push_back(p);
+    else if (p.N <= g_small_nk && p.K <= g_small_nk) tiny.push_back(p);
+    else tiled.push_back(p);
   }
-  // small products (N, K <= g_small_nk) by the element kernel, the rest by 64 x 64 tiles
-  std::vector<GemmDesc> tiny, tiled;
-  for (const auto &p : probs) (p.N <= g_small_nk && p.K <= g_small_nk ? tiny : tiled).push_back(p);
+  if (!big.empty()) {
+    int *err = pool<int>("gemm_err", 1);
+    if (g_gemm_path == 1) launch_gemm_fused(big, err, st);
+    else launch_gemm_split(big, err, st);
+  }
   if (!tiny.empty()) {
-    std::vector<long long> eoff(1, 0);
-    for (const auto &p : tiny) eoff.push_back(eoff.back() + (long long)p.M * p.N);
+    std::vector<long long> eoff(tiny.size() + 1);
+    eoff[0] = 0;
+    for (size_t i = 0; i < tiny.size(); ++i) eoff[i + 1] = eoff[i] + (long long)tiny[i].M * tiny[i].N;
     GemmDesc *d = pool<GemmDesc>("gemm_small_probs", tiny.size());
     long long *de = pool<long long>("gemm_small_eoff", eoff.size());
     stage_h2d(d, tiny.data(), tiny.size() * sizeof(GemmDesc), st);
