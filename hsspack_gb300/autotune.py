@@ -14,7 +14,7 @@ import numpy as np
 from . import build as _build
 
 CACHE = os.path.join(os.path.dirname(_build.LIB), "autotune.json")
-SMLSIZ_CANDIDATES = (6, 12, 25)
+SMLSIZ_CANDIDATES = (6, 12, 16, 25)
 
 
 def _bucket(n):
