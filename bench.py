@@ -182,6 +182,33 @@ def batch_cpu_sample(sizes, probs, threads, count=12):
     return t, t * scale, scale
 
 
+def profile_batch(args, torch, hp, full_cfg):
+    """Only the batched solves of the uneven batch (warm-up + steps): the
+    command an ncu launch list of the batch wraps."""
+    sizes, probs = batch_inputs()
+    _, D, E = hp.pack_batch(probs)
+    o, oz = hp.batch_offsets(sizes)
+    d0 = torch.tensor(D, device="cuda")
+    e0 = torch.tensor(E, device="cuda")
+    d, e = d0.clone(), e0.clone()
+    z = torch.empty(int(oz[-1]), dtype=torch.float64, device="cuda")
+    old = hp.set_config(**full_cfg)
+    try:
+        for it in range(args.warmup + args.steps):
+            if it == args.warmup:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+            d.copy_(d0)
+            e.copy_(e0)
+            hp.mdstedc_batch_dev(sizes, d, e, z)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps)
+        return {"profile_batch": True, "ms_per_batch": ms, "launches_per_batch":
+                hp.get_stats()["kernel_launches"], "config": full_cfg}
+    finally:
+        hp.restore_config(old)
+
+
 def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
     """The uneven batch: solves/s batched (one call), one call per problem, and
     with the plain GPU merge; residual of every problem on the device."""
@@ -489,6 +516,10 @@ def run_ours(args):
         tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
                                        predictor=(0, 1, 2) if have_pred else (0, 2))
     full_cfg.update(tuned)
+    if args.profile_batch:  # the batch's solves only (ncu launch lists)
+        if rank == 0:
+            print(json.dumps(profile_batch(args, torch, hp, full_cfg)))
+        return
     plain_cfg = {"batched": 0, "precision": 0, "predictor": 0}
     clocks = ClockSampler()
     clocks.start()
@@ -657,6 +688,8 @@ def main():
     ap.add_argument("--predictor", type=int, default=2, choices=[0, 1, 2],
                     help="secular start when --smlsiz bypasses the autotuner (0 standard, "
                          "1 learned, 2 FP32 pre-solve)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="run only the batch's warmup + timed batched solves (ncu launch lists)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warmup + timed solves (for ncu launch lists)")
     args = ap.parse_args()
