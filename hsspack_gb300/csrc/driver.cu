@@ -19,6 +19,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <condition_variable>
 #include <thread>
 #include <vector>
 
@@ -134,64 +135,76 @@ static int host_threads() {
 }
 
 // Zeroes rows 0..n-1 of the n columns of a host matrix (leading dimension ld)
-// on worker threads; join() (also the destructor) waits for them.
+// on worker threads, each owning a range of columns; finish() hands them the
+// packed segments (or none), which each worker copies into its own columns
+// once they are zeroed, and waits for them (the destructor releases and
+// joins them on any other path).
 class HostFill {
  public:
-  HostFill(double *z, int n, long long ld, bool on) {
+  HostFill(double *z, int n, long long ld, bool on) : z_(z), n_(n), ld_(ld) {
     if (!on) return;
-    const int T = host_threads();
-    auto work = [z, n, ld, T](int t) {
-      if (ld == n) {
-        const size_t tot = (size_t)n * n, a = tot * t / T, b = tot * (t + 1) / T;
-        memset(z + a, 0, (b - a) * sizeof(double));
-      } else {
-        for (long long j = (long long)n * t / T; j < (long long)n * (t + 1) / T; ++j)
-          memset(z + j * ld, 0, (size_t)n * sizeof(double));
-      }
-    };
-    for (int t = 0; t < T; ++t) {
+    nt_ = host_threads();
+    for (int t = 0; t < nt_; ++t) {
       try {
-        th_.emplace_back(work, t);
+        th_.emplace_back([this, t] { run(t); });
       } catch (...) {
-        work(t);  // no thread available: do this share here
+        inline_.push_back(t);  // no thread available: finish() runs this share
       }
     }
     on_ = true;
   }
   bool active() const { return on_; }
-  void join() {
+  void finish(const PackedZ *pz, const double *src) {
+    if (!on_ || done_) return;
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      pz_ = pz;
+      src_ = src;
+      ready_ = true;
+    }
+    cv_.notify_all();
+    for (int t : inline_) run(t);
     for (auto &x : th_)
       if (x.joinable()) x.join();
-    th_.clear();
+    done_ = true;
   }
-  ~HostFill() { join(); }
+  ~HostFill() { finish(nullptr, nullptr); }
 
  private:
-  std::vector<std::thread> th_;
-  bool on_ = false;
-};
-
-// the packed segments into their columns of the (zeroed) host matrix
-static void scatter_columns(double *z, long long ld, int n, const PackedZ &pz, const double *src) {
-  const int T = host_threads();
-  auto work = [&](int t) {
-    for (long long j = (long long)n * t / T; j < (long long)n * (t + 1) / T; ++j) {
-      const int2 r = pz.seg[j];
-      if (r.y > r.x)
-        memcpy(z + j * ld + r.x, src + pz.off[j], (size_t)(r.y - r.x) * sizeof(double));
+  void run(int t) {
+    const long long j0 = (long long)n_ * t / nt_, j1 = (long long)n_ * (t + 1) / nt_;
+    if (ld_ == n_) {
+      memset(z_ + j0 * n_, 0, (size_t)(j1 - j0) * n_ * sizeof(double));
+    } else {
+      for (long long j = j0; j < j1; ++j) memset(z_ + j * ld_, 0, (size_t)n_ * sizeof(double));
     }
-  };
-  std::vector<std::thread> th;
-  for (int t = 1; t < T; ++t) {
-    try {
-      th.emplace_back(work, t);
-    } catch (...) {
-      work(t);
+    const PackedZ *pz;
+    const double *src;
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_.wait(lk, [this] { return ready_; });
+      pz = pz_;
+      src = src_;
+    }
+    if (!pz) return;
+    for (long long j = j0; j < j1; ++j) {
+      const int2 r = pz->seg[j];
+      if (r.y > r.x)
+        memcpy(z_ + j * ld_ + r.x, src + pz->off[j], (size_t)(r.y - r.x) * sizeof(double));
     }
   }
-  work(0);
-  for (auto &x : th) x.join();
-}
+  double *z_;
+  int n_;
+  long long ld_;
+  int nt_ = 0;
+  std::vector<std::thread> th_;
+  std::vector<int> inline_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  bool ready_ = false, on_ = false, done_ = false;
+  const PackedZ *pz_ = nullptr;
+  const double *src_ = nullptr;
+};
 
 // sets the packed-output request for the duration of one solve
 struct PzScope {
@@ -1819,12 +1832,11 @@ void mdstedc_(const char *compz, const int *n_, double *d, double *e, double *z,
         double *hz = zstage(c, (size_t)std::max<long long>(pz.total, 1));
         CK(cudaMemcpyAsync(hz, pz.dbuf, sizeof(double) * pz.total, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        fill.join();
-        scatter_columns(z, ldz, n, pz, hz);
+        fill.finish(&pz, hz);  // each worker fills in its columns once they are zeroed
         // packed rows plus the slot and row-range tables read on the host
         c.stats.host_d2h_bytes = 8LL * pz.total + 12LL * n;
       } else {
-        fill.join();
+        fill.finish(nullptr, nullptr);
         CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n, n,
                              cudaMemcpyDeviceToHost, st));
         c.stats.host_d2h_bytes = 8LL * n * n;
