@@ -255,8 +255,15 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
         finally:
             hp.restore_config(old)
 
+    # the batch's own leaf size (its problems are far smaller than n = 32768):
+    # one warm and one timed call per candidate, outside the measured region
+    bcfg, tune_ms = dict(full_cfg), {}
+    if args.smlsiz <= 0:
+        for sml in (8, 12, 16):
+            tune_ms[str(sml)] = timed(batched, 1, 1, dict(full_cfg, smlsiz=sml))[0]
+        bcfg["smlsiz"] = int(min(tune_ms, key=tune_ms.get))
     steps = max(1, min(args.steps, 5))
-    ms, launches = timed(batched, steps, max(3, args.warmup), full_cfg)
+    ms, launches = timed(batched, steps, max(3, args.warmup), bcfg)
     # every problem's residual ||TQ - QW||_F / (n ||T||) from the last solve
     res = 0.0
     for p, n in enumerate(sizes):
@@ -269,7 +276,7 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
         R[1:] += ee[:, None] * Q[:-1]
         tn = float(dd.abs().max() + 2 * ee.abs().max())
         res = max(res, float(torch.linalg.norm(R)) / (n * tn))
-    ms_loop, _ = timed(loop, 1, 1, full_cfg)
+    ms_loop, _ = timed(loop, 1, 1, bcfg)
     ms_plain, _ = timed(batched, 1, 0, plain_cfg)
     out = {"workload": "512 tridiagonals, n log-uniform in [256, 4096] (seed 2), D,E iid U[-1,1]",
            "sum_n": int(o[-1]), "sum_n2": int(oz[-1]),
@@ -278,7 +285,7 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
            "loop_solves_per_s": len(sizes) * 1000.0 / ms_loop,
            "plain_solves_per_s": len(sizes) * 1000.0 / ms_plain,
            "full_vs_plain": ms_plain / ms, "batched_vs_loop": ms_loop / ms,
-           "resid_max": res}
+           "resid_max": res, "smlsiz": bcfg.get("smlsiz"), "autotune_ms": tune_ms or None}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_s, scaled, scale = batch_cpu_sample(sizes, probs, threads)
