@@ -23,13 +23,15 @@
 // (s + t >= 7) weigh below 2^-56 of sum_k |A_ik||B_kj|.
 //
 // Kernels: k_split_a / k_split_b write the digit planes pre-tiled in the
-// tcgen05 shared-memory image (K-major, no swizzle, 8x16-byte core matrices),
-// so the GEMM stages each tile with one cp.async.bulk (TMA) copy.  k_gemm_tc:
-// one CTA per 128 x 32 output tile, two CTAs per SM; one thread streams the
-// 16-deep K chunks through three shared-memory stages, another issues
-// tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) into TMEM, and 8 warps drain
-// TMEM with tcgen05.ld into exact int64 sums.  Every mbarrier wait is bounded;
-// a timeout sets an error flag and the CTA still frees its TMEM before exiting.
+// tcgen05 shared-memory image (K-major, no swizzle, 8x16-byte core matrices;
+// B's planes stacked along N), so the GEMM stages each 16-deep K chunk with two
+// cp.async.bulk (TMA) copies.  k_gemm_tc is persistent, one CTA per SM over
+// 128 x 32 output tiles: a copy warp streams the chunks through six
+// shared-memory stages, an MMA warp issues one tcgen05.mma.kind::f16 (BF16 x
+// BF16 -> FP32) per A plane into one of two TMEM accumulator sets, and 8 warps
+// drain a finished set with tcgen05.ld into exact int64 sums and write the
+// tile.  Every mbarrier wait is bounded; a timeout sets an error flag and the
+// CTA still waits for its copies and MMAs in flight and frees its TMEM.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
