@@ -859,7 +859,8 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
       pz.off[i + 1] = pz.off[i] + std::max(0, r.y - r.x);
     }
     pz.total = pz.off[N];
-    if (pz.total * 5 <= (long long)N * N * 3) {  // supports cover at most 60 % of Z
+    // supports cover at most 60 % of Z, and the pinned staging stays <= 4 GB
+    if (pz.total * 5 <= (long long)N * N * 3 && pz.total <= (4LL << 30) / 8) {
       long long *doff = buf<long long>(c, "pz_off", N + 1);
       stage_h2d(doff, pz.off.data(), sizeof(long long) * (N + 1), st);
       pz.dbuf = buf<double>(c, "pz_data", (size_t)std::max<long long>(pz.total, 1));
