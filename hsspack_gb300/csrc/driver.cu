@@ -741,7 +741,6 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   CK(cudaEventCreate(&ev0));
   CK(cudaEventCreate(&ev1));
   CK(cudaEventRecord(ev0, st));
-  const double EPS = 1.1102230246251565e-16;
   const int np = (int)pr.size();
   std::vector<long long> P(np + 1, 0);
   long long L = 1;
