@@ -10,6 +10,12 @@
 * hss_grid.npz -- the interlacing Cauchy grid of TEST/testCauchyHss_serial.f90
   (F_i = 0.1 + (2i-1)g, D_i = F_i + g) with random generators and a dense
   product C @ B computed in numpy, for the standalone Cauchy/HSS APIs.
+* secular_edge_mp.npz -- nearly deflatable secular problems (a pole with a tiny
+  weight placed on a root of the other poles' equation, as glued matrices
+  produce) with roots to 50 digits.
+
+``python tests/golden/make_golden.py [secular dc hss edge]`` writes the named
+fixtures only (default: all).
 
 The reference ships no golden vectors of its own (its test drivers only print
 errors against LAPACK), so these are the pins.
@@ -57,7 +63,26 @@ def mp_roots(d, z, rho, dps=50):
     return np.array(lam), np.array(difl), np.array(difr)
 
 
-def main():
+def edge():
+    """Pole of weight wz inserted at root `which` of a 40-pole problem
+    (seed 11), z renormalised; roots of the new problem to 50 digits."""
+    out = {}
+    d0, z0, rho = secular_problem(40, 11)
+    lam0, _, _ = oracle.secular(d0, z0, rho)
+    for name, which in (("last", 39), ("middle", 20), ("first", 0)):
+        for wname, wz in (("w7", 1e-7), ("w14", 3e-14)):
+            p = lam0[which]
+            d = np.sort(np.append(d0, p))
+            z = np.insert(z0, int(np.searchsorted(d, p)), wz)
+            z = z / np.linalg.norm(z)
+            lam, difl, difr = mp_roots(d, z, rho)
+            key = "%s_%s" % (name, wname)
+            out[key + "_d"], out[key + "_z"], out[key + "_rho"] = d, z, np.array(rho)
+            out[key + "_lam"], out[key + "_difl"], out[key + "_difr"] = lam, difl, difr
+    np.savez_compressed(os.path.join(HERE, "secular_edge_mp.npz"), **out)
+
+
+def secular_fixture():
     out = {}
     for k, seed in [(3, 11), (40, 12), (200, 13)]:
         d, z, rho = secular_problem(k, seed)
@@ -66,6 +91,8 @@ def main():
         out["k%d_lam" % k], out["k%d_difl" % k], out["k%d_difr" % k] = lam, difl, difr
     np.savez_compressed(os.path.join(HERE, "secular_mp.npz"), **out)
 
+
+def dc_fixture():
     dc = {}
     cases = [("rand64", rand_tridiag(64, seed=64)), ("rand200", rand_tridiag(200, seed=200)),
              ("rand512", rand_tridiag(512, seed=512)), ("toep100", toeplitz_tridiag(100))]
@@ -79,6 +106,8 @@ def main():
             dc[name + "_Q"] = Q
     np.savez_compressed(os.path.join(HERE, "dc_small.npz"), **dc)
 
+
+def hss_fixture():
     n = 300
     F, D = interlace_grid(n)
     rng = np.random.default_rng(300)
@@ -86,8 +115,14 @@ def main():
     B = rng.uniform(0, 1, (n, 8))
     C = u[:, None] * v[None, :] / (D[:, None] - F[None, :])
     np.savez_compressed(os.path.join(HERE, "hss_grid.npz"), F=F, D=D, u=u, v=v, B=B, CB=C @ B)
-    print("fixtures written to", HERE)
+
+
+def main(which):
+    makers = {"secular": secular_fixture, "dc": dc_fixture, "hss": hss_fixture, "edge": edge}
+    for name in which:
+        makers[name]()
+    print("fixtures written to", HERE, ":", ", ".join(which))
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]) or ("secular", "dc", "hss", "edge"))

@@ -44,6 +44,19 @@ def test_oracle_secular_vs_mp_roots():
         assert np.max(np.abs(difl - g["k%d_difl" % k]) / np.abs(g["k%d_difl" % k])) <= 1e-10
 
 
+def test_oracle_secular_vs_mp_roots_nearly_deflatable():
+    # a pole of weight 1e-7 or 3e-14 sitting on a root of the other poles'
+    # equation (the merges of glued matrices): LAPACK DLAED4, which the GPU
+    # pole-on-a-root tests compare with, stays within its 1e-13 on every root
+    g = np.load(os.path.join(GOLD, "secular_edge_mp.npz"))
+    for where in ("last", "middle", "first"):
+        for w in ("w7", "w14"):
+            key = "%s_%s" % (where, w)
+            d, z, rho = g[key + "_d"], g[key + "_z"], float(g[key + "_rho"])
+            lam, difl, difr = oracle.secular(d, z, rho)
+            assert np.max(np.abs(lam - g[key + "_lam"])) <= 1e-13, key
+
+
 def test_oracle_matches_golden_dc():
     g = np.load(os.path.join(GOLD, "dc_small.npz"))
     for name in ("rand64", "rand200", "rand512", "toep100"):
