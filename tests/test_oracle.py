@@ -57,6 +57,19 @@ def test_oracle_secular_vs_mp_roots_nearly_deflatable():
             assert np.max(np.abs(lam - g[key + "_lam"])) <= 1e-13, key
 
 
+def test_oracle_glued_wilkinson():
+    # Wilkinson-type blocks glued by 1e-8: every merge has nearly deflatable
+    # poles; the restated MDSTEDC (HSS merges from K >= 40) holds the bar
+    m, nb = 21, 60
+    d = np.tile(np.abs(np.arange(m) - (m - 1) / 2.0), nb)
+    e = np.ones(m * nb - 1)
+    e[m - 1::m] = 1e-8
+    w, Q = oracle.eigh_tridiagonal(d, e, hss_leaf=64, bsmlz=40, tol=1e-14)
+    wl, _ = oracle.dstedc_lapack(d, e)
+    ev, res, orth = eig_metrics(d, e, w, Q, wl)
+    assert ev <= 1e-13 and res <= 1e-12 and orth <= 1e-12, (ev, res, orth)
+
+
 def test_oracle_matches_golden_dc():
     g = np.load(os.path.join(GOLD, "dc_small.npz"))
     for name in ("rand64", "rand200", "rand512", "toep100"):
