@@ -29,6 +29,7 @@
 #include "hss_hss.h"
 #include "hss_kernels.h"
 #include "hss_pool.h"
+#include "host_util.h"
 
 namespace hss {
 
@@ -43,19 +44,6 @@ struct TimedRange {
   cudaEvent_t a, b;
   long long bytes;
   double flops;
-};
-
-// Eigenvectors bound for host memory (mdstedc_): when the columns' supports
-// cover little of Z, the solve leaves them packed on the device (the
-// supported rows of every output column back to back) instead of writing the
-// full n x n matrix; the host zero-fills Z meanwhile and scatters the segments.
-struct PackedZ {
-  bool want = false;           // request (single problem, supports tracked)
-  bool packed = false;         // result: the packed form was produced
-  long long total = 0;         // packed doubles
-  std::vector<int2> seg;       // per output column: rows [x, y)
-  std::vector<long long> off;  // per output column: offset into the packed data
-  double *dbuf = nullptr;      // device packed data
 };
 
 struct Ctx {
@@ -126,85 +114,6 @@ static T *buf(Ctx &c, const char *name, size_t count) {
   }
   return (T *)b.p;
 }
-
-// Host threads for the output work of the host entry points: all cores but
-// two (the solve's own host thread keeps running meanwhile).
-static int host_threads() {
-  const unsigned h = std::thread::hardware_concurrency();
-  return (int)std::max(1u, std::min(16u, h > 2 ? h - 2 : 1u));
-}
-
-// Zeroes rows 0..n-1 of the n columns of a host matrix (leading dimension ld)
-// on worker threads, each owning a range of columns; finish() hands them the
-// packed segments (or none), which each worker copies into its own columns
-// once they are zeroed, and waits for them (the destructor releases and
-// joins them on any other path).
-class HostFill {
- public:
-  HostFill(double *z, int n, long long ld, bool on) : z_(z), n_(n), ld_(ld) {
-    if (!on) return;
-    nt_ = host_threads();
-    for (int t = 0; t < nt_; ++t) {
-      try {
-        th_.emplace_back([this, t] { run(t); });
-      } catch (...) {
-        inline_.push_back(t);  // no thread available: finish() runs this share
-      }
-    }
-    on_ = true;
-  }
-  bool active() const { return on_; }
-  void finish(const PackedZ *pz, const double *src) {
-    if (!on_ || done_) return;
-    {
-      std::lock_guard<std::mutex> g(mu_);
-      pz_ = pz;
-      src_ = src;
-      ready_ = true;
-    }
-    cv_.notify_all();
-    for (int t : inline_) run(t);
-    for (auto &x : th_)
-      if (x.joinable()) x.join();
-    done_ = true;
-  }
-  ~HostFill() { finish(nullptr, nullptr); }
-
- private:
-  void run(int t) {
-    const long long j0 = (long long)n_ * t / nt_, j1 = (long long)n_ * (t + 1) / nt_;
-    if (ld_ == n_) {
-      memset(z_ + j0 * n_, 0, (size_t)(j1 - j0) * n_ * sizeof(double));
-    } else {
-      for (long long j = j0; j < j1; ++j) memset(z_ + j * ld_, 0, (size_t)n_ * sizeof(double));
-    }
-    const PackedZ *pz;
-    const double *src;
-    {
-      std::unique_lock<std::mutex> lk(mu_);
-      cv_.wait(lk, [this] { return ready_; });
-      pz = pz_;
-      src = src_;
-    }
-    if (!pz) return;
-    for (long long j = j0; j < j1; ++j) {
-      const int2 r = pz->seg[j];
-      if (r.y > r.x)
-        memcpy(z_ + j * ld_ + r.x, src + pz->off[j], (size_t)(r.y - r.x) * sizeof(double));
-    }
-  }
-  double *z_;
-  int n_;
-  long long ld_;
-  int nt_ = 0;
-  std::vector<std::thread> th_;
-  std::vector<int> inline_;
-  std::mutex mu_;
-  std::condition_variable cv_;
-  bool ready_ = false, on_ = false, done_ = false;
-  const PackedZ *pz_ = nullptr;
-  const double *src_ = nullptr;
-};
 
 // sets the packed-output request for the duration of one solve
 struct PzScope {
@@ -633,21 +542,6 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
     stage_end(HSS_ST_FINISH, st, 24 * nn, 0.0);
   }
   c.launches++;
-}
-
-// MDSTEDC's split test (mdstedc.f90: |E(i)| <= EPS sqrt|D(i)| sqrt|D(i+1)|).
-// Squares decide it without square roots unless they are within a relative
-// 1e-12 of the boundary or outside the range where they are exact enough;
-// those cases take the reference's own expression, so the decision is the
-// same.
-static inline bool negligible(double e, double a, double b) {
-  const double ae = std::fabs(e), aa = std::fabs(a), ab = std::fabs(b);
-  if (ae > 1e-100 && ae < 1e100 && aa > 1e-100 && aa < 1e100 && ab > 1e-100 && ab < 1e100) {
-    const double lhs = ae * ae, rhs = (HSS_EPS * HSS_EPS) * (aa * ab);
-    if (lhs > rhs * (1.0 + 1e-12)) return false;
-    if (lhs < rhs * (1.0 - 1e-12)) return true;
-  }
-  return !(ae > HSS_EPS * std::sqrt(aa) * std::sqrt(ab));
 }
 
 // Eigen-decomposition of many unreduced, scaled blocks at once.  Block b
