@@ -11,7 +11,7 @@ on the launching stream over exactly K steps, no per-stage events).  batch: the
 second half of the metric, 512 uneven tridiagonals (n log-uniform in
 [256, 4096]) solved in one batched call, as solves/s, beside one call per
 problem and the plain GPU merge.  e2e: the same solve through the Fortran
-drop-in ``mdstedc_`` with pinned host buffers (D/E host->device, the
+drop-in ``mdstedc_`` with pageable host arrays (D/E host->device, the
 eigenvectors and eigenvalues device->host and the host-side zero fill of Z
 inside the timed region).  roofline: the final gather, the longest single
 launch, its algorithmic bytes over its event-timed duration.  cpu_baseline /
@@ -127,32 +127,26 @@ def check_accuracy(torch, d, e, w, Z, n):
     return {"resid": (res2 ** 0.5) / (n * tn), "orth_est": orth}
 
 
-def cpu_reference_sample(n_sample, n_target, threads):
-    """Time the CPU oracle (restated HSSPACK MDSTEDC + OpenBLAS) on one solve of
-    size n_sample with `threads` host threads; scale to n_target by the
-    O(n^2 log n) cost of DC with localized eigenvectors (every level moves the
-    n x n eigenvector matrix)."""
+def cpu_reference_solve(n, threads):
+    """One solve of the n x n benchmark matrix by the CPU oracle (the restated
+    HSSPACK MDSTEDC('I') + OpenBLAS LAPACK) on `threads` host threads; seconds."""
     import oracle
     oracle.set_threads(threads)
-    d, e = inputs(n_sample, seed=0)
+    d, e = inputs(n, seed=0)
     t = time.perf_counter()
     oracle.eigh_tridiagonal(d, e)
-    t = time.perf_counter() - t
-    scale = (n_target / n_sample) ** 2 * (np.log2(n_target) / np.log2(n_sample))
-    return t, t * scale, scale
+    return time.perf_counter() - t
 
 
-def cpu_lapack_sample(n_sample, n_target, threads):
-    """LAPACK DSTEDC (OpenBLAS, the oracle's accuracy reference) on one solve of
-    size n_sample, scaled like cpu_reference_sample."""
+def cpu_lapack_solve(n, threads):
+    """LAPACK DSTEDC('I') (OpenBLAS, the oracle's accuracy reference) on the
+    same matrix; seconds."""
     import oracle
     oracle.set_threads(threads)
-    d, e = inputs(n_sample, seed=0)
+    d, e = inputs(n, seed=0)
     t = time.perf_counter()
     oracle.dstedc_lapack(d, e)
-    t = time.perf_counter() - t
-    scale = (n_target / n_sample) ** 2 * (np.log2(n_target) / np.log2(n_sample))
-    return t, t * scale, scale
+    return time.perf_counter() - t
 
 
 BATCH_COUNT, BATCH_LO, BATCH_HI = 512, 256, 4096
@@ -168,18 +162,15 @@ def batch_inputs(seed=2):
     return sizes, probs
 
 
-def batch_cpu_sample(sizes, probs, threads, count=12):
-    """CPU oracle on the first `count` problems of the batch, scaled to all 512
-    by sum n^2 log n."""
+def batch_cpu_solve(probs, threads):
+    """The CPU oracle on every problem of the batch, one after the other (the
+    reference solves independent problems serially); seconds."""
     import oracle
     oracle.set_threads(threads)
     t = time.perf_counter()
-    for p in range(count):
-        oracle.eigh_tridiagonal(*probs[p])
-    t = time.perf_counter() - t
-    w = sizes.astype(np.float64) ** 2 * np.log2(sizes.astype(np.float64))
-    scale = float(w.sum() / w[:count].sum())
-    return t, t * scale, scale
+    for d, e in probs:
+        oracle.eigh_tridiagonal(d, e)
+    return time.perf_counter() - t
 
 
 def profile_batch(args, torch, hp, full_cfg):
@@ -276,27 +267,34 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
         R[1:] += ee[:, None] * Q[:-1]
         tn = float(dd.abs().max() + 2 * ee.abs().max())
         res = max(res, float(torch.linalg.norm(R)) / (n * tn))
-    ms_loop, _ = timed(loop, 1, 1, bcfg)
-    ms_plain, _ = timed(batched, 1, 0, plain_cfg)
+    # the other arms, each warmed once: one call per problem, batched levels
+    # with FP64 products (no tensor cores), and the plain GPU merge (per-merge
+    # launches, FP64 products, standard start)
+    ms_loop, _ = timed(loop, 2, 1, bcfg)
+    ms_fp64, _ = timed(batched, 2, 1, dict(bcfg, precision=0))
+    ms_std, _ = timed(batched, 2, 1, dict(bcfg, predictor=0))
+    ms_plain, _ = timed(batched, 1, 1, dict(plain_cfg, smlsiz=bcfg.get("smlsiz", 0)))
     out = {"workload": "512 tridiagonals, n log-uniform in [256, 4096] (seed 2), D,E iid U[-1,1]",
            "sum_n": int(o[-1]), "sum_n2": int(oz[-1]),
            "solves_per_s": len(sizes) * 1000.0 / ms, "ms_per_batch": ms,
            "gpu_launches_per_batch": launches / steps,
            "loop_solves_per_s": len(sizes) * 1000.0 / ms_loop,
+           "batched_fp64_solves_per_s": len(sizes) * 1000.0 / ms_fp64,
+           "standard_start_solves_per_s": len(sizes) * 1000.0 / ms_std,
            "plain_solves_per_s": len(sizes) * 1000.0 / ms_plain,
-           "full_vs_plain": ms_plain / ms, "batched_vs_loop": ms_loop / ms,
+           "full_vs_plain": ms_plain / ms, "full_vs_batched_fp64": ms_fp64 / ms,
+           "full_vs_standard_start": ms_std / ms, "batched_vs_loop": ms_loop / ms,
            "resid_max": res, "smlsiz": bcfg.get("smlsiz"), "autotune_ms": tune_ms or None}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        t_s, scaled, scale = batch_cpu_sample(sizes, probs, threads)
-        out["cpu_baseline"] = {"value": len(sizes) / scaled, "unit": "solves/s", "cores": threads,
+        t_s = batch_cpu_solve(probs, threads)
+        out["cpu_baseline"] = {"value": len(sizes) / t_s, "unit": "solves/s", "cores": threads,
                                "kind": "port",
-                               "sample": "first 12 problems (%.2f s), x%.1f (sum n^2 log n) to 512"
-                                         % (t_s, scale)}
+                               "sample": "all 512 problems once (%.2f s)" % t_s}
     return out
 
 
-FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (CUDA cores) rate
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (CUDA cores) rate, nominal: context only
 # per stage: the unit that bounds it on GB300
 STAGE_BOUND = {"secular": "fp64", "lowner": "fp64", "build_S": "fp64", "leaf": "fp64",
                "gemm": "fp64-equivalent", "final_gather": "hbm", "prepare": "hbm",
@@ -306,8 +304,9 @@ STAGE_BOUND = {"secular": "fp64", "lowner": "fp64", "build_S": "fp64", "leaf": "
 def stage_rooflines(acc, pk):
     """Achieved rate of every timed stage from its algorithmic bytes / flops:
     HBM stages against the measured copy bandwidth, FP64 stages against the
-    nominal FP64 rate, the products as FP64-equivalent TFLOP/s (the split-BF16
-    path is meant to exceed the FP64 rate)."""
+    FP64 FMA rate measured in this run (hss_fp64_fma_rate), the products as
+    FP64-equivalent TFLOP/s (the split-BF16 path is meant to exceed the FP64
+    rate)."""
     out = {}
     for st, ms in acc["ms"].items():
         if ms <= 0 or st not in STAGE_BOUND:
@@ -319,8 +318,8 @@ def stage_rooflines(acc, pk):
                        "frac": a / pk["hbm_gbs"], "peak_source": pk["source"]}
         else:
             a = acc["flops"][st] / (ms * 1e-3) / 1e12
-            out[st] = {"bound": b, "achieved": a, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                       "frac": a / FP64_NOMINAL_TFLOPS, "peak_source": "nominal FP64 rate"}
+            out[st] = {"bound": b, "achieved": a, "peak": pk["fp64_tflops"], "unit": "TFLOP/s",
+                       "frac": a / pk["fp64_tflops"], "peak_source": pk["fp64_source"]}
     return out
 
 
@@ -416,18 +415,22 @@ def run_extra(torch, hp, full_cfg):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of HSSPACK's MDSTEDC('I') (with
+    OpenBLAS LAPACK for the routines the reference calls but does not ship) on
+    all host cores; each step is one full solve of the same n = 32768 matrix
+    as our arm (no scaling, no sampling)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import oracle
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
-    n_s = args.cpu_sample
     times = []
+    t_run = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        t, scaled, scale = cpu_reference_sample(n_s, args.n, threads)
+        t = cpu_reference_solve(args.n, threads)
         if i >= args.warmup:
-            times.append(scaled)
+            times.append(t)
     v = float(np.mean(times))
     line = {
         "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
@@ -437,9 +440,10 @@ def run_reference(args):
         "config": {"workload": "tridiagonal DC eigensolve n=%d, D,E iid U[-1,1] seed 0, COMPZ='I'"
                    % args.n, "n": args.n, "l2": "eigenvector matrix 8.6 GB >> L2"},
         "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port",
-                         "sample": "one n=%d solve per step, x%.2f (n^2 log n) to n=%d"
-                                   % (n_s, scale, args.n)},
+                         "sample": "one full n=%d solve per step (min %.2f s, max %.2f s)"
+                                   % (args.n, min(times), max(times))},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "run_s": time.perf_counter() - t_run,
     }
     print(json.dumps(line), flush=True)
 
@@ -542,16 +546,27 @@ def run_ours(args):
     _, acc, _, _ = timed(prof_steps, 1, True, full_cfg)
     # plain GPU merge (per-merge launches), fewer steps
     ms_plain, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, plain_cfg)
-    ms_fp64, _, _, _ = timed(max(1, min(3, args.steps)), 1, False, {"batched": 1, "precision": 0})
+    ms_fp64, _, _, _ = timed(max(1, min(3, args.steps)), 1, False,
+                             dict(full_cfg, precision=0))
+    # the secular start A/B at the tuned leaf size: standard (midpoint), learned
+    # MLP, FP32 pre-solve; time per solve and FP64 evaluations per root
+    start_ab = {}
+    for pred, name in ((0, "standard"), (1, "learned"), (2, "fp32_presolve")):
+        if pred == 1 and not have_pred:
+            continue
+        m_ab, _, _, st_ab = timed(max(1, min(3, args.steps)), 1, False,
+                                  dict(full_cfg, predictor=pred))
+        start_ab[name] = {"ms": m_ab,
+                          "evals_per_root": st_ab["secular_iters"] / max(1, st_ab["secular_roots"]),
+                          "fallbacks": st_ab["predictor_fallbacks"]}
     acc_chk = check_accuracy(torch, d, e, dw, Z, n)
 
-    # end to end through the Fortran drop-in with pinned host buffers
-    hd = torch.empty(n, dtype=torch.float64).pin_memory()
-    he = torch.empty(n, dtype=torch.float64).pin_memory()
-    hz = torch.empty(n * n, dtype=torch.float64).pin_memory()
+    # end to end through the Fortran drop-in with ordinary (pageable) host
+    # arrays, as a Fortran caller passes them
     work = np.zeros(1)
     iwork = np.zeros(1, dtype=np.int32)
-    dn, en, zn = hd.numpy(), he.numpy(), hz.numpy().reshape(n, n).T  # Fortran view
+    dn, en = np.empty(n), np.empty(n)
+    zn = np.empty((n, n), order="F")
     lw, liw = 1 + 4 * n + n * n, 3 + 5 * n
 
     def e2e_step():
@@ -592,6 +607,10 @@ def run_ours(args):
     # dominant stage -> roofline (contract object), plus every stage against
     # the bound that applies to it
     pk = peaks()
+    # the FP64 rate is not in the measured-peaks file: measure it here (best of
+    # three launches of the FMA-chain kernel)
+    pk["fp64_tflops"] = max(hp.fp64_fma_rate()[0] for _ in range(3))
+    pk["fp64_source"] = "measured in this run (FP64 FMA chains, hss_fp64_fma_rate)"
     # the dominant kernel: the longest single launch of the solve, the final
     # gather (8.6 GB written once; the secular kernel's 12 launches together
     # take a similar share and appear, FP64-bound, in stage_rooflines); else
@@ -617,27 +636,22 @@ def run_ours(args):
         per_launch_flops = acc["flops"][top] / calls
         achieved = per_launch_flops / (per_launch_ms * 1e-3) / 1e12
         roof = {"bound": STAGE_BOUND[top], "kernel_stage": top, "achieved": achieved,
-                "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": traffic,
-                "peak_source": "nominal FP64 rate", "algorithmic_flops_per_launch": per_launch_flops}
+                "peak": pk["fp64_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["fp64_tflops"], "traffic": traffic,
+                "peak_source": pk["fp64_source"], "algorithmic_flops_per_launch": per_launch_flops}
     roof.update({"per_launch_ms": per_launch_ms, "launches_per_step": calls})
     if rank != 0:
         return
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        t_s, scaled, scale = cpu_reference_sample(args.cpu_sample, n, threads)
-        cpu = {"value": scaled, "unit": "s", "cores": threads, "kind": "port",
-               "sample": "one n=%d solve (%.2f s), x%.2f (n^2 log n) to n=%d"
-                         % (args.cpu_sample, t_s, scale, n)}
-        # the same restatement on one thread, and LAPACK's own DSTEDC (the
-        # accuracy oracle) on all threads, both on smaller samples
-        t1, s1, sc1 = cpu_reference_sample(4096, n, 1)
-        cpu["one_thread"] = {"value": s1, "unit": "s", "cores": 1,
-                             "sample": "one n=4096 solve (%.2f s), x%.1f to n=%d" % (t1, sc1, n)}
-        t2, s2, sc2 = cpu_lapack_sample(8192, n, threads)
-        cpu["lapack_dstedc"] = {"value": s2, "unit": "s", "cores": threads,
-                                "sample": "one n=8192 DSTEDC (%.2f s), x%.1f to n=%d" % (t2, sc2, n)}
+        t_s = cpu_reference_solve(n, threads)
+        cpu = {"value": t_s, "unit": "s", "cores": threads, "kind": "port",
+               "sample": "one full n=%d solve of the same matrix" % n}
+        # LAPACK's own DSTEDC (the accuracy oracle) on the same matrix and cores
+        t2 = cpu_lapack_solve(n, threads)
+        cpu["lapack_dstedc"] = {"value": t2, "unit": "s", "cores": threads,
+                                "sample": "one full n=%d DSTEDC('I') of the same matrix" % n}
     total_ms = sum(acc["ms"].values())
     line = {
         "metric": METRIC, "value": ms / 1000.0, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -664,9 +678,12 @@ def run_ours(args):
         "plain_gpu_s": ms_plain / 1000.0,
         "batched_fp64_s": ms_fp64 / 1000.0,
         "full_vs_plain": ms_plain / ms,
+        "full_vs_batched_fp64": ms_fp64 / ms,
+        "secular_start_ab": start_ab,
         "accuracy": acc_chk,
         "batch": batch,
         "stage_rooflines": stage_roof,
+        "fp64_peak_tflops": pk["fp64_tflops"],
         "other_workloads": extra,
         "stages_ms_per_step": {k: v / prof_steps for k, v in acc["ms"].items() if v > 0},
         "profiled_stage_share": {k: v / total_ms for k, v in acc["ms"].items() if v > 0},
@@ -686,7 +703,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batch figures")
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")

@@ -108,6 +108,7 @@ SIGNATURES = {
                                       ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                       _V, _V]),
     "hss_rcp_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V]),
+    "hss_fp64_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, _V, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
@@ -540,6 +541,18 @@ def gemm_dev(A, B, C, m, n, k, lda, ldb, ldc, beta=0, precision=0, stream=None):
     if rc != 0:
         raise HssError("hss_gemm_dev rc=%d: %s" % (rc, _err()))
     return rc
+
+
+def fp64_fma_rate(blocks=152 * 8, iters=8192, stream=None):
+    """The GPU's FP64 FMA rate in TFLOP/s, measured by one timed launch
+    (:c:func:`hss_fp64_fma_rate`); returns (tflops, ms)."""
+    ms = ctypes.c_float(0.0)
+    tf = ctypes.c_double(0.0)
+    rc = load().hss_fp64_fma_rate(int(blocks), int(iters), ctypes.byref(ms), ctypes.byref(tf),
+                                  _stream(stream))
+    if rc != 0:
+        raise HssError("hss_fp64_fma_rate rc=%d" % rc)
+    return tf.value, ms.value
 
 
 def dhssevc_dev(F, u, v, difl, difr, Q, ldq, nrows, ni=200, tol=1e-17, stream=None):

@@ -15,6 +15,8 @@
 // Positions are measured from the nearer pole ("origin") so that the gaps
 // d_i - x near the root keep full relative accuracy; DIFL/DIFR are formed from
 // those gaps exactly as LAPACK's DELTA output is used at mdlaed3.f90:215-216.
+#include <atomic>
+
 #include "hss_common.cuh"
 #include "hss_kernels.h"
 
@@ -764,11 +766,16 @@ static inline int root_block(long long threads) { return threads >= 152LL * 256 
 static inline int warp_grid(int total, int threads) {
   return (int)(((long long)total * 32 + threads - 1) / threads);
 }
-// Pole terms per lane the lane-group width aims at (hss_config.sec_terms).
-static int g_sec_terms = 8;
-void set_secular_terms(int t) { g_sec_terms = t > 0 ? t : 8; }
-static long long g_sec_threads = 152LL * 256;
-void set_secular_threads(int t) { g_sec_threads = t > 0 ? t : 152LL * 256; }
+// Pole terms per lane the lane-group width aims at (hss_config.sec_terms), and
+// the thread count a level should reach.  Written by hss_set_config under the
+// library lock but read by entry points that hold only their own lock (the
+// no-allocation Loewner entry), hence relaxed atomics.
+static std::atomic<int> g_sec_terms{8};
+void set_secular_terms(int t) { g_sec_terms.store(t > 0 ? t : 8, std::memory_order_relaxed); }
+static std::atomic<long long> g_sec_threads{152LL * 256};
+void set_secular_threads(int t) {
+  g_sec_threads.store(t > 0 ? t : 152LL * 256, std::memory_order_relaxed);
+}
 
 // Lanes per root of a level with `total` roots and largest merge maxk: the
 // fewest lanes that (a) keep a lane's share at or below 64 pole terms and
@@ -777,10 +784,12 @@ void set_secular_threads(int t) { g_sec_threads = t > 0 ? t : 152LL * 256; }
 // A level with many roots runs one lane per root (no per-root reduction or
 // replicated step work); a level with few roots spreads each root.
 static int lanes_per_root(int total, int maxk) {
+  const int terms = g_sec_terms.load(std::memory_order_relaxed);
+  const long long want = g_sec_threads.load(std::memory_order_relaxed);
   int cap = 1;
-  while (cap < 32 && cap * g_sec_terms < maxk) cap *= 2;
+  while (cap < 32 && cap * terms < maxk) cap *= 2;
   int L = 1;
-  while (L < cap && (L * 64 < maxk || (long long)total * L < g_sec_threads)) L *= 2;
+  while (L < cap && (L * 64 < maxk || (long long)total * L < want)) L *= 2;
   return L;
 }
 

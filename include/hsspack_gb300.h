@@ -209,10 +209,12 @@ int hss_lowner_dev(int k, const double *dlamda, const double *difl,
  * reference.  For callers that cannot let a library allocate device memory
  * (all of it reserved by their own allocator, or allocation forbidden after
  * start-up): the scratch is a static device array of 65536 doubles, so
- * k <= 65536 (larger k returns -1 and sets hss_last_error()).  The first call
- * on a device resolves the scratch address and should come at set-up, before
- * any stream capture.  All calls share the scratch; calls are serialised and
- * wait for their stream, since overlapping ones would race on it. */
+ * k <= 65536 (larger k returns -1 and sets hss_last_error()).  Every call
+ * looks the scratch address up in the current context; the first call on a
+ * device (and the first after cudaDeviceReset) may also load the module there
+ * and should come at set-up, before any stream capture.  All calls share the
+ * scratch; calls are serialised and wait for their stream, since overlapping
+ * ones would race on it. */
 int hss_lowner_noalloc_dev(int k, const double *dlamda, const double *difl,
                            const double *difr, double *z, double *alpha,
                            void *stream);
@@ -251,6 +253,13 @@ int hss_cauchy_eig_dev(int k, const double *F, const double *u, const double *v,
  * a correctly rounded divide (two Newton-Raphson steps from the hardware
  * estimate; within a few ulp for normal x), so its accuracy can be checked. */
 int hss_rcp_dev(int n, const double *x, double *y, void *stream);
+
+/* Measurement helper (no counterpart in the reference): the GPU's FP64 FMA
+ * rate.  One launch of `blocks` CTAs x 256 threads, each thread running eight
+ * independent chains of `iters` FMAs, timed with CUDA events on `stream`
+ * after one untimed launch; *ms = its duration, *tflops = 2 flops per FMA
+ * over it.  Returns 0, -1 for bad arguments, 1000000 on a CUDA error. */
+int hss_fp64_fma_rate(int blocks, int iters, float *ms, double *tflops, void *stream);
 
 /* C(m x n, ldc) = A(m x k, lda) * B(k x n, ldb) [+ C if beta != 0], FP64
  * column-major device arrays; precision 0 = FP64 CUDA cores, 1 = split-BF16

@@ -1,7 +1,9 @@
 """Cauchy-like HSS products on the GPU: CauchyHssMM (generic Cauchy matrix,
 SRC/cauchyhssmm.f90) against the dense product, and the n = 8192 Cauchy merge
 (secular roots, Loewner z, HSS compression of the eigenvector matrix, product
-with a dense orthogonal Q) against the dense eigenvector matrix.
+with a dense orthogonal Q) against the oracle: roots, DIFL/DIFR against
+LAPACK DLAED4, the Loewner vectors and the dense eigenvector block against the
+restated MDLAED3/CauchylikeEig.
 
 Tolerances: the HSS products within 1e-11 (relative Frobenius) of the dense
 products at HSS tolerance 1e-14; orthogonality of Q C within 1e-12 * n."""
@@ -9,6 +11,7 @@ import numpy as np
 import pytest
 import torch
 
+import oracle
 import hsspack_gb300 as hp
 from helpers import interlace_grid
 
@@ -54,11 +57,12 @@ def test_cauchyhssmm_fortran_entry():
     assert t[0] > 0 and t[1] > 0
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_cauchy_merge_8192(precision):
-    # the Cauchy merge workload: d sorted U[0,1], z ~ N(0,1)/sqrt(n), rho = 1;
-    # C_ij = zhat_i alpha_j / (d_i - lambda_j), HSS leaf 128, tol 1e-14, times a
-    # dense random orthogonal Q (8192 x 8192)
+@pytest.fixture(scope="module")
+def merge_8192():
+    """The Cauchy merge workload: d sorted U[0,1], z ~ N(0,1)/sqrt(n), rho = 1
+    (seed 0), n = 8192; the GPU's roots, DIFL/DIFR, z-hat and alpha, checked
+    against the oracle (LAPACK DLAED4 per root and the restated MDLAED3 steps,
+    SRC/mdlaed3.f90:207-249) before any product uses them."""
     n = 8192
     rng = np.random.default_rng(0)
     d = np.sort(rng.uniform(0.0, 1.0, n))
@@ -68,20 +72,46 @@ def test_cauchy_merge_8192(precision):
     hp.secular_dev(dd, zz, 1.0, lam, difl, difr)
     zh, al = zz.clone(), torch.zeros(n, dtype=torch.float64, device="cuda")
     hp.lowner_dev(dd, difl, difr, zh, al)
+    return n, d, z, dd, lam, difl, difr, zh, al
+
+
+def test_cauchy_merge_8192_secular_vs_dlaed4(merge_8192):
+    n, d, z, dd, lam, difl, difr, zh, al = merge_8192
+    lam_o, difl_o, difr_o = oracle.secular(d, z, 1.0)
+    lam_g, difl_g, difr_g = (t.cpu().numpy() for t in (lam, difl, difr))
+    # the secular tests' bar: roots within 1e-13 * max|d|, gaps to 1e-11
+    assert np.max(np.abs(lam_g - lam_o)) <= 1e-13 * max(1.0, np.abs(d).max())
+    assert np.max(np.abs(difl_g - difl_o) / np.abs(difl_o)) <= 1e-11
+    assert np.max(np.abs(difr_g[:-1] - difr_o[:-1]) / np.abs(difr_o[:-1])) <= 1e-11
+    # Loewner z-hat and alpha from the oracle's roots (the restated MDLAED3)
+    zh_o, al_o = oracle.lowner(d, difl_o, difr_o, z)
+    assert np.max(np.abs(zh.cpu().numpy() - zh_o) / np.abs(zh_o)) <= 1e-12
+    assert np.max(np.abs(al.cpu().numpy() - al_o) / np.abs(al_o)) <= 1e-12
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cauchy_merge_8192(merge_8192, precision):
+    # HSS leaf 128, tol 1e-14, times a dense random orthogonal Q (8192 x 8192);
+    # reference: the oracle's dense eigenvector block (CauchylikeEig restated,
+    # SRC/CauchyHssEig.f90:1688-1765) from the oracle's own roots and Loewner
+    # vectors, multiplied in FP64 on the host on 512 rows of Q
+    n, d, z, dd, lam, difl, difr, zh, al = merge_8192
+    lam_o, difl_o, difr_o = oracle.secular(d, z, 1.0)
+    zh_o, al_o = oracle.lowner(d, difl_o, difr_o, z)
+    C_o = oracle.cauchy_eig_dense(d, zh_o, al_o, difl_o, difr_o)
     gen = torch.Generator(device="cuda").manual_seed(1)
     Qf, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device="cuda", generator=gen))
+    rows = np.random.default_rng(3).choice(n, 512, replace=False)
+    ref = Qf[torch.tensor(rows, device="cuda")].cpu().numpy() @ C_o
     Q = Qf.T.contiguous()  # memory = column-major Qf
-    C = torch.zeros(n * n, dtype=torch.float64, device="cuda")
-    hp.cauchy_eig_dev(dd, zh, al, difl, difr, C)
-    Cm = C.view(n, n).T  # C[i, j]
-    ref = Qf @ Cm
     old = hp.set_config(precision=precision)
     try:
         hp.dhssevc_dev(dd, zh, al, difl, difr, Q, n, n, ni=128, tol=1e-14)
     finally:
         hp.restore_config(old)
     out = Q.T  # Q C
-    err = float(torch.linalg.norm(out - ref) / torch.linalg.norm(ref))
+    got = out[torch.tensor(rows, device="cuda")].cpu().numpy()
+    err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
     assert err <= 1e-11, err
     g = torch.randn(n, 8, dtype=torch.float64, device="cuda", generator=gen)
     y = out.T @ (out @ g) - g

@@ -60,6 +60,29 @@ def test_noalloc_matches_pool_version_two_calls():
     _compare(700, 42)
 
 
+def test_noalloc_leaves_free_device_memory_unchanged():
+    # after a first (set-up) call, a call must not change the device's free
+    # memory: everything it needs is in the static scratch and the caller's
+    # buffers, all allocated before the measurement
+    L = hp.load()
+    dd, zz, difl, difr = _inputs(3000, 44)
+    k = dd.numel()
+    z = zz.clone()
+    alpha = torch.zeros(k, dtype=torch.float64, device="cuda")
+    args = (k, hp._ptr(dd), hp._ptr(difl), hp._ptr(difr), hp._ptr(z), hp._ptr(alpha),
+            hp._stream(None))
+    z.copy_(zz)
+    assert L.hss_lowner_noalloc_dev(*args) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        z.copy_(zz)
+        assert L.hss_lowner_noalloc_dev(*args) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_noalloc_limit():
     _compare(MAX_K, 43)
     L = hp.load()
