@@ -202,8 +202,17 @@ def profile_batch(args, torch, hp, full_cfg):
 
 def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
     """The uneven batch: solves/s batched (one call), one call per problem, and
-    with the plain GPU merge; residual of every problem on the device."""
-    sizes, probs = batch_inputs()
+    with the plain GPU merge; residual of every problem on the device.  With
+    several ranks every rank solves its share of the 512 problems (greedy n^3
+    partition, no collective on the data path) and the time is the slowest
+    rank's."""
+    sizes_all, probs_all = batch_inputs()
+    sizes, probs = sizes_all, probs_all
+    if world > 1:
+        from hsspack_gb300 import shard
+        mine = shard.partition(sizes_all, world)[rank]
+        sizes = sizes_all[mine]
+        probs = [probs_all[int(i)] for i in mine]
     _, D, E = hp.pack_batch(probs)
     o, oz = hp.batch_offsets(sizes)
     d0 = torch.tensor(D, device="cuda")
@@ -242,7 +251,12 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
             # the last call's launch count (each step does the same work),
             # read after the timed region
             launches = hp.get_stats()["kernel_launches"] * steps
-            return t0.elapsed_time(t1) / steps, launches
+            ms = t0.elapsed_time(t1) / steps
+            if world > 1:  # the slowest rank's time
+                x = torch.tensor([ms], device="cuda")
+                dist.all_reduce(x, op=dist.ReduceOp.MAX)
+                ms = float(x)
+            return ms, launches
         finally:
             hp.restore_config(old)
 
@@ -276,19 +290,20 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
     ms_plain, _ = timed(batched, 1, 1, dict(plain_cfg, smlsiz=bcfg.get("smlsiz", 0)))
     out = {"workload": "512 tridiagonals, n log-uniform in [256, 4096] (seed 2), D,E iid U[-1,1]",
            "sum_n": int(o[-1]), "sum_n2": int(oz[-1]),
-           "solves_per_s": len(sizes) * 1000.0 / ms, "ms_per_batch": ms,
+           "solves_per_s": len(sizes_all) * 1000.0 / ms, "ms_per_batch": ms,
+           "problems_this_rank": int(len(sizes)), "ranks": world,
            "gpu_launches_per_batch": launches / steps,
-           "loop_solves_per_s": len(sizes) * 1000.0 / ms_loop,
-           "batched_fp64_solves_per_s": len(sizes) * 1000.0 / ms_fp64,
-           "standard_start_solves_per_s": len(sizes) * 1000.0 / ms_std,
-           "plain_solves_per_s": len(sizes) * 1000.0 / ms_plain,
+           "loop_solves_per_s": len(sizes_all) * 1000.0 / ms_loop,
+           "batched_fp64_solves_per_s": len(sizes_all) * 1000.0 / ms_fp64,
+           "standard_start_solves_per_s": len(sizes_all) * 1000.0 / ms_std,
+           "plain_solves_per_s": len(sizes_all) * 1000.0 / ms_plain,
            "full_vs_plain": ms_plain / ms, "full_vs_batched_fp64": ms_fp64 / ms,
            "full_vs_standard_start": ms_std / ms, "batched_vs_loop": ms_loop / ms,
            "resid_max": res, "smlsiz": bcfg.get("smlsiz"), "autotune_ms": tune_ms or None}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        t_s = batch_cpu_solve(probs, threads)
-        out["cpu_baseline"] = {"value": len(sizes) / t_s, "unit": "solves/s", "cores": threads,
+        t_s = batch_cpu_solve(probs_all, threads)
+        out["cpu_baseline"] = {"value": len(sizes_all) / t_s, "unit": "solves/s", "cores": threads,
                                "kind": "port",
                                "sample": "all 512 problems once (%.2f s)" % t_s}
     return out

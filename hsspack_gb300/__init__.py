@@ -110,6 +110,7 @@ SIGNATURES = {
     "hss_rcp_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V]),
     "hss_fp64_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, _V, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
+    "hss_mdstedc_v_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
     "hss_mdstedc_batch_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V]),
     "hss_secular_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, ctypes.c_double, _V, _V, _V, _V, _V]),
     "hss_lowner_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, _V, _V]),
@@ -457,6 +458,16 @@ def mdstedc_dev(d, e, z, stream=None):
     info = load().hss_mdstedc_dev(n, _ptr(d), _ptr(e), _ptr(z), max(1, n), _stream(stream))
     if info != 0:
         raise HssError("hss_mdstedc_dev INFO=%d: %s" % (info, _err()))
+    return info
+
+
+def mdstedc_v_dev(d, e, z, stream=None):
+    """Device MDSTEDC('V'): z (n x n column-major storage) holds Q0 on entry and
+    Q0 times the tridiagonal's eigenvectors on exit; d -> eigenvalues."""
+    n = d.numel()
+    info = load().hss_mdstedc_v_dev(n, _ptr(d), _ptr(e), _ptr(z), max(1, n), _stream(stream))
+    if info != 0:
+        raise HssError("hss_mdstedc_v_dev INFO=%d: %s" % (info, _err()))
     return info
 
 

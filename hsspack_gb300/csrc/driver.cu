@@ -1294,8 +1294,56 @@ static int svd_solve(Ctx &c, bool lower, int n, std::vector<double> hd, std::vec
 // Symmetric band eigensolve from device arrays: ab upper band storage
 // (ldab >= kd + 1).  kd <= 1 is a tridiagonal and goes through the
 // tridiagonal solver; 2 <= kd <= 32 through band_core.
+// Band -> tridiagonal on the device (band_sbr.cu), then the tridiagonal
+// divide and conquer; with eigenvectors, Z = Q Z_T by applying the reduction's
+// reflectors to the tridiagonal's eigenvectors.  The reference takes this
+// route (LAPACK DSBTRD + DSTERF / DSBEVD) for eigenvalues only and for KD > 16
+// (SRC/mdsbedc.f90:274-276, :311-318); here it serves eigenvalues only and the
+// bandwidths above the band divide and conquer's limit.  ab: upper storage.
+static int band_sbr_solve(Ctx &c, int n, int kd, const double *ab, long long ldab, double *z,
+                          long long ldz, double *w, bool wantz, cudaStream_t st) {
+  const int b = std::min(kd, n - 1);
+  if (b > 4096) {
+    c.err = "band reduction: bandwidth above 4096";
+    return -4;
+  }
+  const int ldb = 2 * b;
+  double *LB = buf<double>(c, "sbr_band", (size_t)ldb * n);
+  launch_sbr_load(n, kd, b, ab, ldab, LB, ldb, st);
+  std::vector<long long> roff;
+  const long long nref = sbr_reflectors(n, b, &roff);
+  double *R = nullptr, *rtau = nullptr;
+  long long *droff = nullptr;
+  if (wantz && nref > 0) {
+    R = buf<double>(c, "sbr_v", (size_t)nref * b);
+    rtau = buf<double>(c, "sbr_tau", (size_t)nref);
+    droff = buf<long long>(c, "sbr_roff", roff.size());
+    stage_h2d(droff, roff.data(), sizeof(long long) * roff.size(), st);
+  }
+  const int nl = launch_sbr_reduce(n, b, LB, ldb, R, droff, rtau, st);
+  double *dd = buf<double>(c, "sbr_d", n), *de = buf<double>(c, "sbr_e", n);
+  launch_sbr_tri(n, LB, ldb, dd, de, st);
+  std::vector<double> hd(n), he(n, 0.0);
+  CK(cudaMemcpyAsync(hd.data(), dd, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(he.data(), de, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  double *zt = wantz ? z : buf<double>(c, "z_scratch", (size_t)n * n);
+  const int info = mdstedc_core(c, n, hd, he, zt, wantz ? ldz : n, w, st);
+  if (info != 0) return info;
+  int nb = 0;
+  if (wantz && nref > 0) nb = launch_sbr_back(n, b, R, droff, rtau, z, ldz, st);
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  c.launches += nl + nb + 2;
+  c.stats.kernel_launches = c.launches;
+  return 0;
+}
+
 static int band_solve(Ctx &c, int n, int kd, const double *ab, long long ldab, double *z,
-                      long long ldz, double *w, cudaStream_t st) {
+                      long long ldz, double *w, cudaStream_t st, bool wantz = true) {
+  if (kd >= 2 && n > 2 && (kd > HSS_BAND_KD_MAX || !wantz))
+    return band_sbr_solve(c, n, kd, ab, ldab, z, ldz, w, wantz, st);
   if (kd <= 1 || n <= 2) {
     std::vector<double> hab((size_t)ldab * n);
     CK(cudaMemcpyAsync(hab.data(), ab, sizeof(double) * hab.size(), cudaMemcpyDeviceToHost, st));
@@ -1313,6 +1361,92 @@ static int band_solve(Ctx &c, int n, int kd, const double *ab, long long ldab, d
 static int mdstedc_core(Ctx &c, int n, const std::vector<double> &hd, const std::vector<double> &he,
                         double *dz, long long ldz, double *dw, cudaStream_t st) {
   return solve_core(c, {Problem{n, hd.data(), he.data(), dz, ldz, dw}}, st);
+}
+
+// MDSTEDC('V') of one matrix: on entry z (n x n, ldz, device) holds the
+// orthogonal matrix Q0 that reduced the original matrix to the tridiagonal
+// (d, e) (DSYTRD + DORGTR, say); on exit Q0 * Q_T, Q_T the tridiagonal's
+// eigenvectors in ascending eigenvalue order.  The reference multiplies Q0 into
+// each split block's eigenvector matrix (SRC/mdstedc.f90:341-372: MDLAED0 with
+// ICOMPQ = 1, or DSTEQR + DGEMM on small blocks) before its final ordering.
+// Here the tridiagonal is solved once as for 'I', and Q0 is applied through
+// the supports of the DC eigenvectors: output column c of Q_T holds data only
+// on rows [x_c, y_c) (the range of the last merge that rewrote it), so columns
+// sharing a range form one product Q0(:, x:y) * Q_T(x:y, cols); the products
+// go to a scratch matrix in group order and are scattered back into z.  When
+// the supports fill most of Q_T, one dense product Q0 * Q_T is used instead.
+static int mdstedc_v_core(Ctx &c, int n, const std::vector<double> &hd,
+                          const std::vector<double> &he, double *z, long long ldz, double *dw,
+                          cudaStream_t st) {
+  double *T = buf<double>(c, "v_prod", (size_t)n * n);
+  PackedZ pz;
+  pz.want = true;
+  int info;
+  {
+    PzScope scope(c, &pz);
+    // packed output when the supports are sparse; else Q_T itself lands in T
+    info = mdstedc_core(c, n, hd, he, T, n, dw, st);
+  }
+  if (info != 0) return info;
+  int *err = gemm_flag(c);
+  CK(cudaMemsetAsync(err, 0, sizeof(int), st));
+  if (!pz.packed) {
+    double *P = buf<double>(c, "v_dense", (size_t)n * n);
+    std::vector<GemmDesc> p{{z, T, P, (int)ldz, n, n, n, n, n, 0, 0}};
+    launch_gemm(p, c.cfg.precision, st);
+    c.launches++;
+    CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, P, sizeof(double) * n, sizeof(double) * n, n,
+                         cudaMemcpyDeviceToDevice, st));
+  } else {
+    // output columns grouped by support segment (stable: output order within a group)
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      const int2 &ra = pz.seg[a], &rb = pz.seg[b];
+      return ra.x != rb.x ? ra.x < rb.x : ra.y < rb.y;
+    });
+    std::vector<long long> doff(n + 1, 0);
+    for (int j = 0; j < n; ++j) {
+      const int2 r = pz.seg[order[j]];
+      doff[j + 1] = doff[j] + std::max(0, r.y - r.x);
+    }
+    int *dorder = buf<int>(c, "v_order", n);
+    long long *dsoff = buf<long long>(c, "v_soff", n + 1);
+    long long *ddoff = buf<long long>(c, "v_doff", n + 1);
+    double *B2 = buf<double>(c, "v_packed", (size_t)std::max<long long>(pz.total, 1));
+    stage_h2d(dorder, order.data(), sizeof(int) * n, st);
+    stage_h2d(dsoff, pz.off.data(), sizeof(long long) * (n + 1), st);
+    stage_h2d(ddoff, doff.data(), sizeof(long long) * (n + 1), st);
+    launch_repack_columns(n, dorder, dsoff, ddoff, pz.dbuf, B2, st);
+    c.launches++;
+    std::vector<GemmDesc> prods;
+    for (int j0 = 0; j0 < n;) {
+      const int2 r = pz.seg[order[j0]];
+      int j1 = j0 + 1;
+      while (j1 < n && pz.seg[order[j1]].x == r.x && pz.seg[order[j1]].y == r.y) ++j1;
+      const int m = r.y - r.x;
+      if (m > 0)
+        prods.push_back(GemmDesc{z + (long long)r.x * ldz, B2 + doff[j0], T + (long long)j0 * n,
+                                 (int)ldz, m, n, n, j1 - j0, m, 0, 0});
+      else  // a column without support rows (cannot occur for an eigenvector)
+        CK(cudaMemsetAsync(T + (long long)j0 * n, 0, sizeof(double) * n * (j1 - j0), st));
+      j0 = j1;
+    }
+    launch_gemm(prods, c.cfg.precision, st);
+    c.launches++;
+    // z is free once the products have read it
+    launch_scatter_columns(n, n, dorder, T, n, z, ldz, st);
+    c.launches++;
+  }
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  if (herr) {
+    c.err = "tensor-core product: bounded wait timed out";
+    return 1;
+  }
+  return 0;
 }
 
 // Message for hss_last_error() from entry points that live outside this file.
@@ -1409,6 +1543,35 @@ int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *strea
   }
 }
 
+int hss_mdstedc_v_dev(int n, double *d, double *e, double *z, int ldz, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -2;
+  if (ldz < std::max(1, n)) return -6;
+  if (n == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    if (n == 1) {  // SRC/mdstedc.f90:248-251: Z(1,1) = 1
+      const double one = 1.0;
+      CK(cudaMemcpyAsync(z, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      return 0;
+    }
+    std::vector<double> hd(n), he(n, 0.0);
+    CK(cudaMemcpyAsync(hd.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(he.data(), e, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double *dw = buf<double>(c, "w_out", n);
+    int info = mdstedc_v_core(c, n, hd, he, z, ldz, dw, st);
+    CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return info;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  }
+}
+
 int hss_mdstedc_batch_dev(int nprob, const int *n, double *d, double *e, double *z, void *stream) {
   Ctx &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
@@ -1459,8 +1622,8 @@ int hss_mdsbevd_dev(int n, int kd, const double *ab, int ldab, double *w, double
   Ctx &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
   if (n < 0) return -1;
-  if (kd < 0 || kd > HSS_BAND_KD_MAX) {
-    c.err = "hss_mdsbevd_dev: kd must be in 0.." + std::to_string(HSS_BAND_KD_MAX);
+  if (kd < 0) {
+    c.err = "hss_mdsbevd_dev: kd < 0";
     return -2;
   }
   if (ldab < kd + 1) return -4;
@@ -1568,7 +1731,7 @@ static int band_host(Ctx &c, bool lower, int n, int kd, const double *ab, int ld
   double *dz = buf<double>(c, "z_out", (size_t)n * n);
   double *dw = buf<double>(c, "w_out", n);
   CK(cudaMemcpyAsync(dab, hu.data(), sizeof(double) * hu.size(), cudaMemcpyHostToDevice, st));
-  const int info = band_solve(c, n, kd, dab, ldu, dz, n, dw, st);
+  const int info = band_solve(c, n, kd, dab, ldu, dz, n, dw, st, wantz);
   if (wantz)
     CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n, n,
                          cudaMemcpyDeviceToHost, st));
@@ -1593,7 +1756,7 @@ void mdsbevd_(const char *compz, const char *uplo, const int *n_, const int *kd_
   else if (ldq < 1 || (icompz > 0 && ldq < std::max(1, n))) *info = -6;
   long long lwmin = 1, liwmin = 1;
   if (*info == 0) {
-    const int smlsiz = c.cfg.smlsiz;
+    const int smlsiz = 25;  // ILAENV(9, 'DSTEDC') as the reference (mdsbevd.f90:255)
     if (n <= 1 || icompz == 0) { lwmin = 1; liwmin = 1; }
     else if (n <= smlsiz) { lwmin = 2LL * (n - 1); liwmin = 1; }
     else { lwmin = 1 + 4LL * n + (long long)n * n; liwmin = 3 + 5LL * n; }
@@ -1602,7 +1765,7 @@ void mdsbevd_(const char *compz, const char *uplo, const int *n_, const int *kd_
     if (lwork < lwmin && !lquery) *info = -8;
     else if (liwork < liwmin && !lquery) *info = -10;
   }
-  if (*info == 0 && (kd < 0 || kd > HSS_BAND_KD_MAX || ldab < kd + 1)) *info = -4;
+  if (*info == 0 && (kd < 0 || ldab < kd + 1)) *info = -4;
   if (*info != 0) {
     c.err = "MDSBEVD: illegal argument " + std::to_string(-*info);
     return;
@@ -1651,7 +1814,6 @@ void mdsbedc_(const char *jobz, const char *uplo, const int *n_, const int *kd_,
     if (lwork < lwmin && !lquery) *info = -11;
     else if (liwork < liwmin && !lquery) *info = -13;
   }
-  if (*info == 0 && kd > HSS_BAND_KD_MAX) *info = -4;
   if (*info != 0) {
     c.err = "MDSBEDC: illegal argument " + std::to_string(-*info);
     return;
@@ -1680,15 +1842,22 @@ void mdstedc_(const char *compz, const int *n_, double *d, double *e, double *z,
   int icompz = (cz == 'N' || cz == 'n') ? 0 : (cz == 'V' || cz == 'v') ? 1 : (cz == 'I' || cz == 'i') ? 2 : -1;
   *info = 0;
   const bool lquery = (lwork == -1 || liwork == -1);
-  if (icompz < 0 || icompz == 1) *info = -1;
+  if (icompz < 0) *info = -1;
   else if (n < 0) *info = -2;
   else if (ldz < 1 || (icompz > 0 && ldz < std::max(1, n))) *info = -6;
   long long lwmin = 1, liwmin = 1;
   if (*info == 0) {
-    const int smlsiz = c.cfg.smlsiz;
+    // the reference's workspace formulas (SRC/mdstedc.f90:211-229), with its
+    // SMLSIZ = ILAENV(9, 'DSTEDC') = 25 (the GPU's own leaf size is separate)
+    const int smlsiz = 25;
     if (n <= 1 || icompz == 0) { lwmin = 1; liwmin = 1; }
     else if (n <= smlsiz) { lwmin = 2LL * (n - 1); liwmin = 1; }
-    else { lwmin = 1 + 4LL * n + (long long)n * n; liwmin = 3 + 5LL * n; }
+    else if (icompz == 1) {
+      int lgn = 0;
+      while ((1LL << lgn) < n) ++lgn;  // ceil(log2 n), as LGN there
+      lwmin = 1 + 3LL * n + 2LL * n * lgn + 4LL * n * n;
+      liwmin = 6 + 6LL * n + 5LL * n * lgn;
+    } else { lwmin = 1 + 4LL * n + (long long)n * n; liwmin = 3 + 5LL * n; }
     if (work) work[0] = (double)lwmin;
     if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
     if (lwork < lwmin && !lquery) *info = -8;
@@ -1712,6 +1881,15 @@ void mdstedc_(const char *compz, const int *n_, double *d, double *e, double *z,
       // eigenvalues only: the same solve, vectors discarded (the reference
       // calls DSTERF here, mdstedc.f90:264-267)
       *info = mdstedc_core(c, n, hd, he, dz, n, dw, st);
+    } else if (icompz == 1) {
+      // Z holds Q0 on entry: copied in, multiplied on the device, copied out
+      CK(cudaMemcpy2DAsync(dz, sizeof(double) * n, z, sizeof(double) * ldz, sizeof(double) * n, n,
+                           cudaMemcpyHostToDevice, st));
+      *info = mdstedc_v_core(c, n, hd, he, dz, n, dw, st);
+      if (*info == 0)
+        CK(cudaMemcpy2DAsync(z, sizeof(double) * ldz, dz, sizeof(double) * n, sizeof(double) * n,
+                             n, cudaMemcpyDeviceToHost, st));
+      c.stats.host_d2h_bytes = 8LL * n * n;
     } else {
       // large problems: Z is zeroed on host threads while the GPU solves, and
       // only the columns' supported rows come back (unless they fill Z)
@@ -1739,7 +1917,7 @@ void mdstedc_(const char *compz, const int *n_, double *d, double *e, double *z,
     CK(cudaMemcpyAsync(d, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     c.stats.host_d2h_bytes += 8LL * n;
-    c.stats.host_h2d_bytes = 16LL * n;
+    c.stats.host_h2d_bytes = 16LL * n + (icompz == 1 ? 8LL * n * n : 0LL);
     if (work) work[0] = (double)lwmin;
     if (iwork) iwork[0] = (int)std::min<long long>(liwmin, 2147483647LL);
   } catch (CudaError &ex) {

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <string>
+#include <vector>
 
 namespace hss {
 
@@ -124,6 +125,10 @@ void launch_final_gather(int n, const int *perm, const double *Dp, const double 
 void launch_pack_columns(int n, const int *perm, const double *Dp, const double *Q, long long ldq,
                          const int2 *sup, const long long *off, double *out, double *wout,
                          cudaStream_t st);
+void launch_repack_columns(int n, const int *order, const long long *soff, const long long *doff,
+                           const double *src, double *dst, cudaStream_t st);
+void launch_scatter_columns(int n, int m, const int *order, const double *T, long long ldt,
+                            double *out, long long ldo, cudaStream_t st);
 // many problems per call: P = global start of each problem (np + 1 entries),
 // total = P[np]; problem p's block is Q + P[p] * (ldq + 1), leading dim ldq
 void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
@@ -195,5 +200,17 @@ void launch_rows_rotate_back(int n, int ncols, const double *cs, const double *s
 
 // driver.cu: set the message hss_last_error() returns
 void set_last_error(const std::string &msg);
+
+// band -> tridiagonal reduction (band_sbr.cu): working band in lower storage
+// with ldb = 2b diagonals; reflectors (b doubles each) of step j of sweep s
+// at roff[s] + j when R is not null.
+long long sbr_reflectors(int n, int b, std::vector<long long> *roff);
+void launch_sbr_load(int n, int kd, int b, const double *AB, long long ldab, double *LB, int ldb,
+                     cudaStream_t st);
+int launch_sbr_reduce(int n, int b, double *LB, int ldb, double *R, const long long *droff,
+                      double *rtau, cudaStream_t st);
+void launch_sbr_tri(int n, const double *LB, int ldb, double *d, double *e, cudaStream_t st);
+int launch_sbr_back(int n, int b, const double *R, const long long *droff, const double *rtau,
+                    double *Z, long long ldz, cudaStream_t st);
 
 }  // namespace hss

@@ -569,6 +569,35 @@ __global__ void k_pack_columns(int n, const int *__restrict__ perm, const double
   if (threadIdx.x == 0) wout[c] = Dp[p];
 }
 
+// COMPZ = 'V': the packed columns (output order, column c at soff[c] with
+// soff[c+1] - soff[c] rows) rewritten in the order of `order` (dst column j =
+// source column order[j], at doff[j]), so that columns sharing a support
+// segment sit back to back as one dense m x k operand.  One CTA per column.
+__global__ void k_repack_columns(int n, const int *__restrict__ order,
+                                 const long long *__restrict__ soff,
+                                 const long long *__restrict__ doff,
+                                 const double *__restrict__ src, double *__restrict__ dst) {
+  const int j = blockIdx.x;
+  if (j >= n) return;
+  const int c = order[j];
+  const long long s = soff[c], len = soff[c + 1] - soff[c], d = doff[j];
+  for (long long i = threadIdx.x; i < len; i += blockDim.x) dst[d + i] = src[s + i];
+}
+
+// out(:, order[j]) = T(:, j) for j < n, rows 0..m-1 (T leading dimension ldt,
+// out ldo): the products of the support groups put back in output order.
+// Grid (n columns, row chunks of 2048); 16 bytes per element.
+__global__ void k_scatter_columns(int n, int m, const int *__restrict__ order,
+                                  const double *__restrict__ T, long long ldt,
+                                  double *__restrict__ out, long long ldo) {
+  const int j = blockIdx.x;
+  if (j >= n) return;
+  const double *src = T + (long long)j * ldt;
+  double *dst = out + (long long)order[j] * ldo;
+  const int r0 = blockIdx.y * 2048, r1 = min(m, r0 + 2048);
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = src[i];
+}
+
 // ------------------------------------------------ many problems per call --
 // Problems of one call sit at global positions P[p] .. P[p+1]-1 and share one
 // Q with leading dimension ldq >= max n_p: problem p's eigenvector block is the
@@ -717,6 +746,15 @@ void launch_pack_columns(int n, const int *perm, const double *Dp, const double 
                          const int2 *sup, const long long *off, double *out, double *wout,
                          cudaStream_t st) {
   if (n > 0) k_pack_columns<<<n, 128, 0, st>>>(n, perm, Dp, Q, ldq, sup, off, out, wout);
+}
+void launch_repack_columns(int n, const int *order, const long long *soff, const long long *doff,
+                           const double *src, double *dst, cudaStream_t st) {
+  if (n > 0) k_repack_columns<<<n, 128, 0, st>>>(n, order, soff, doff, src, dst);
+}
+void launch_scatter_columns(int n, int m, const int *order, const double *T, long long ldt,
+                            double *out, long long ldo, cudaStream_t st) {
+  if (n > 0 && m > 0)
+    k_scatter_columns<<<dim3(n, (m + 2047) / 2048), 256, 0, st>>>(n, m, order, T, ldt, out, ldo);
 }
 void launch_zero_blocks(int np, long long total, const long long *P, double *Q, long long ldq,
                         cudaStream_t st) {

@@ -83,10 +83,13 @@ int hss_finalize(void);                           /* frees the device pool */
 /* ------------------------------------------ Fortran drop-ins (host) ---- */
 /* MDSTEDC(COMPZ,N,D,E,Z,LDZ,WORK,LWORK,IWORK,LIWORK,INFO)
  * replaces SRC/mdstedc.f90:139.  COMPZ = 'I' runs the GPU merge; 'N' returns
- * eigenvalues only; 'V' is rejected with INFO = -1 (the reference routes it
- * through LAPACK DLAED7, outside the HSS path).  LWORK = -1 or LIWORK = -1 is
- * a workspace query returning WORK(1) = 1+4N+N^2 and IWORK(1) = 3+5N as the
- * reference does (mdstedc.f90:226-227). */
+ * eigenvalues only; 'V' takes in Z the orthogonal matrix that reduced a
+ * symmetric matrix to (D, E) and returns Z times the tridiagonal's
+ * eigenvectors (the reference's ICOMPQ = 1 path, mdstedc.f90:341-372; here the
+ * tridiagonal solve of 'I' followed by the product on the device).
+ * LWORK = -1 or LIWORK = -1 is a workspace query returning the reference's
+ * sizes (mdstedc.f90:211-229: 'I' 1+4N+N^2 and 3+5N; 'V' 1+3N+2N lg N+4N^2
+ * and 6+6N+5N lg N; 2(N-1) and 1 for N <= 25). */
 void mdstedc_(const char *compz, const int *n, double *d, double *e, double *z,
               const int *ldz, double *work, const int *lwork, int *iwork,
               const int *liwork, int *info, size_t compz_len);
@@ -133,15 +136,19 @@ void dhssmml_(const double *A, const int *lda, const int *m, const int *n, doubl
               const int *ni, const int *ncol, double *time, int *info);
 
 /* Largest band half-width of the banded divide and conquer (leaves of up to
- * 2 kd rows are solved by one warp each). */
+ * 2 kd rows are solved by one warp each).  Wider bands, and every
+ * eigenvalues-only band call, are reduced to tridiagonal form on the device
+ * (Householder bulge chasing, the role of LAPACK DSBTRD in the reference) and
+ * solved by the tridiagonal divide and conquer. */
 #define HSS_BAND_KD_MAX 32
 
 /* MDSBEVD(COMPZ,UPLO,N,KD,AB,LDAB,D,Q,LDQ,WORK,LWORK,IWORK,LIWORK,INFO)
  * replaces SRC/mdsbevd.f90:183: eigenpairs of the symmetric band matrix in
  * upper band storage AB (the reference reads the upper band whatever UPLO
  * says); COMPZ = 'I' computes Q, 'N' eigenvalues only.  Argument errors and
- * workspace queries as the reference (INFO = -1, -2, -6, -8, -10); KD outside
- * 0..HSS_BAND_KD_MAX or LDAB < KD+1 gives INFO = -4. */
+ * workspace queries as the reference (INFO = -1, -2, -6, -8, -10); KD < 0 or
+ * LDAB < KD+1 gives INFO = -4.  KD > HSS_BAND_KD_MAX and COMPZ = 'N' go
+ * through the device band-to-tridiagonal reduction. */
 void mdsbevd_(const char *compz, const char *uplo, const int *n, const int *kd,
               double *ab, const int *ldab, double *d, double *q, const int *ldq,
               double *work, const int *lwork, int *iwork, const int *liwork,
@@ -150,8 +157,10 @@ void mdsbevd_(const char *compz, const char *uplo, const int *n, const int *kd,
 /* MDSBEDC(JOBZ,UPLO,N,KD,AB,LDAB,W,Z,LDZ,WORK,LWORK,IWORK,LIWORK,INFO)
  * replaces SRC/mdsbedc.f90:166: JOBZ = 'V' / 'N', UPLO = 'U' / 'L' (lower
  * storage is converted; the reference passes it on as upper).  Workspace
- * LWMIN = 1+5N+2N^2, LIWMIN = 3+5N (JOBZ = 'V') as mdsbedc.f90:190-201;
- * KD > HSS_BAND_KD_MAX gives INFO = -4. */
+ * LWMIN = 1+5N+2N^2, LIWMIN = 3+5N (JOBZ = 'V') as mdsbedc.f90:190-201.
+ * JOBZ = 'N' (the reference's DSBTRD + DSTERF, mdsbedc.f90:311-318) and
+ * KD > HSS_BAND_KD_MAX (its DSBEVD fallback for KD > 16, :274-276) reduce
+ * the band to tridiagonal form on the device first. */
 void mdsbedc_(const char *jobz, const char *uplo, const int *n, const int *kd,
               double *ab, const int *ldab, double *w, double *z, const int *ldz,
               double *work, const int *lwork, int *iwork, const int *liwork,
@@ -168,6 +177,15 @@ void cauchylike_(double *A, const double *D, const double *F, const double *u,
  * (destroyed); z(ldz, n) out: eigenvectors.  stream may be NULL. */
 int hss_mdstedc_dev(int n, double *d, double *e, double *z, int ldz, void *stream);
 
+/* Device MDSTEDC('V') (SRC/mdstedc.f90:139 with COMPZ = 'V'): z (n x n,
+ * column-major, leading dimension ldz, device) holds on entry the orthogonal
+ * matrix Q0 of a reduction to tridiagonal form and on exit Q0 times the
+ * eigenvectors of (d, e); d returns the eigenvalues ascending.  Q0 is applied
+ * column group by column group over the supports of the divide-and-conquer
+ * eigenvectors (grouped tensor-core products under precision = 1).  Returns
+ * as hss_mdstedc_dev. */
+int hss_mdstedc_v_dev(int n, double *d, double *e, double *z, int ldz, void *stream);
+
 /* SVD of the upper bidiagonal (d, e) in HBM (the MDBDSDC path, COMPQ = 'I'):
  * d(n) in: diagonal, out: singular values descending; e(n-1) superdiagonal;
  * u(ldu, n), vt(ldvt, n) out.  Returns 0, -i for a bad i-th argument, > 0 on
@@ -176,7 +194,8 @@ int hss_mdbdsdc_dev(int n, double *d, double *e, double *u, int ldu, double *vt,
                     void *stream);
 
 /* Symmetric band eigensolve in HBM (the MDSBEVD path): ab(ldab, n) upper band
- * storage, 0 <= kd <= HSS_BAND_KD_MAX; w(n) eigenvalues ascending, z(ldz, n)
+ * storage, kd >= 0 (band divide and conquer up to HSS_BAND_KD_MAX, device
+ * reduction to tridiagonal form above); w(n) eigenvalues ascending, z(ldz, n)
  * eigenvectors.  Returns 0, -i for a bad i-th argument, > 0 on failure. */
 int hss_mdsbevd_dev(int n, int kd, const double *ab, int ldab, double *w, double *z,
                     int ldz, void *stream);

@@ -13,8 +13,10 @@
 * secular_edge_mp.npz -- nearly deflatable secular problems (a pole with a tiny
   weight placed on a root of the other poles' equation, as glued matrices
   produce) with roots to 50 digits.
+* merge8192_mp.npz -- eight roots (the last included) of the n = 8192
+  Cauchy-merge problem to 50 digits.
 
-``python tests/golden/make_golden.py [secular dc hss edge]`` writes the named
+``python tests/golden/make_golden.py [secular dc hss edge merge8192]`` writes the named
 fixtures only (default: all).
 
 The reference ships no golden vectors of its own (its test drivers only print
@@ -82,6 +84,42 @@ def edge():
     np.savez_compressed(os.path.join(HERE, "secular_edge_mp.npz"), **out)
 
 
+def merge8192():
+    """The n = 8192 Cauchy-merge problem (d sorted U[0,1], z ~ N(0,1)/sqrt(n),
+    rho = 1, seed 0): roots 0, 1, 4095, 8190, 8191 and three seeded others to
+    50 digits (bisection on the full 8192-term equation).  DLAED4's last root is
+    1.5e-13 off on this problem, so its parity test pins that root here."""
+    n = 8192
+    rng = np.random.default_rng(0)
+    d = np.sort(rng.uniform(0.0, 1.0, n))
+    z = rng.standard_normal(n) / np.sqrt(n)
+    idx = np.array(sorted({0, 1, 4095, 8190, 8191} |
+                          set(np.random.default_rng(5).choice(n, 3, replace=False).tolist())))
+    mp.mp.dps = 50
+    dm = [mp.mpf(float(x)) for x in d]
+    z2 = [mp.mpf(float(x)) ** 2 for x in z]
+
+    def f(x):
+        return 1 + mp.fsum(zz / (di - x) for di, zz in zip(dm, z2))
+
+    lam, difl, difr = [], [], []
+    for j in idx:
+        lo = dm[j]
+        hi = dm[j + 1] if j + 1 < n else dm[j] + mp.fsum(z2)
+        for _ in range(120):
+            mid = (lo + hi) / 2
+            if f(mid) < 0:
+                lo = mid
+            else:
+                hi = mid
+        x = (lo + hi) / 2
+        lam.append(float(x))
+        difl.append(float(x - dm[j]))
+        difr.append(float(x - dm[j + 1]) if j + 1 < n else 0.0)
+    np.savez_compressed(os.path.join(HERE, "merge8192_mp.npz"), idx=idx, lam=np.array(lam),
+                        difl=np.array(difl), difr=np.array(difr))
+
+
 def secular_fixture():
     out = {}
     for k, seed in [(3, 11), (40, 12), (200, 13)]:
@@ -118,11 +156,12 @@ def hss_fixture():
 
 
 def main(which):
-    makers = {"secular": secular_fixture, "dc": dc_fixture, "hss": hss_fixture, "edge": edge}
+    makers = {"secular": secular_fixture, "dc": dc_fixture, "hss": hss_fixture, "edge": edge,
+              "merge8192": merge8192}
     for name in which:
         makers[name]()
     print("fixtures written to", HERE, ":", ", ".join(which))
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("secular", "dc", "hss", "edge"))
+    main(tuple(sys.argv[1:]) or ("secular", "dc", "hss", "edge", "merge8192"))

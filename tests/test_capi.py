@@ -52,11 +52,25 @@ def test_mdstedc_workspace_query():
     assert lw == 1 + 4 * n + n * n and liw == 3 + 5 * n
     info, lw, liw = _call("I", 20, 20, -1, -1)  # N <= SMLSIZ
     assert info == 0 and lw == 2 * 19 and liw == 1
+    # COMPZ = 'V' (SRC/mdstedc.f90:222-224), LGN = ceil(log2 N)
+    info, lw, liw = _call("V", n, n, -1, -1)
+    assert info == 0
+    assert lw == 1 + 3 * n + 2 * n * 10 + 4 * n * n and liw == 6 + 6 * n + 5 * n * 10
+    info, lw, liw = _call("V", 1024, 1024, -1, -1)
+    assert lw == 1 + 3 * 1024 + 2 * 1024 * 10 + 4 * 1024 * 1024
+    # the reference's SMLSIZ (25) decides the small case, whatever the GPU's leaf size
+    old = hp.set_config(smlsiz=12)
+    try:
+        info, lw, liw = _call("I", 20, 20, -1, -1)
+    finally:
+        hp.restore_config(old)
+    assert info == 0 and lw == 2 * 19 and liw == 1
 
 
 def test_mdstedc_argument_errors():
     assert _call("X", 10, 10, 1000, 1000)[0] == -1
-    assert _call("V", 10, 10, 1000, 1000)[0] == -1  # COMPZ='V' is outside the HSS path
+    assert _call("V", 10, 5, 1000, 1000)[0] == -6
+    assert _call("V", 100, 100, 1 + 4 * 100 + 100 * 100, 10000)[0] == -8  # 'I' size is short
     assert _call("I", -1, 10, 1000, 1000)[0] == -2
     assert _call("I", 10, 5, 1000, 1000)[0] == -6
     assert _call("I", 100, 100, 10, 10000)[0] == -8
@@ -93,7 +107,9 @@ def test_mdsbedc_arguments_and_workspace():
     info, lw, liw = _band_call(hp.mdsbedc, "N", "L", n, 4, 5, 1, -1, -1)
     assert info == 0 and lw == 2 * n and liw == 1
     assert _band_call(hp.mdsbedc, "V", "U", n, 4, 5, n, 10, 10)[0] == -11
-    assert _band_call(hp.mdsbedc, "V", "U", n, 40, 41, n, -1, -1)[0] == -4  # beyond 32
+    # wide bands are accepted (reduced to tridiagonal form on the device)
+    assert _band_call(hp.mdsbedc, "V", "U", n, 40, 41, n, -1, -1)[0] == 0
+    assert _band_call(hp.mdsbedc, "V", "U", n, 40, 40, n, -1, -1)[0] == -6
 
 
 def test_mdsbevd_arguments_and_workspace():

@@ -135,3 +135,55 @@ def test_band_16384_kd4_full_size():
     from scipy.linalg import eig_banded
     wl = eig_banded(ab, eigvals_only=True)
     assert float(np.max(np.abs(w.cpu().numpy() - wl))) / na <= EV_TOL
+
+
+# Bandwidths above the band divide and conquer's limit and eigenvalue-only
+# calls go through the device reduction to tridiagonal form (Householder
+# bulge chasing; the reference's LAPACK DSBTRD route, SRC/mdsbedc.f90:274-276
+# and :311-318): same acceptance bar against LAPACK DSBEVD.
+
+
+@pytest.mark.parametrize("n,kd", [(50, 33), (300, 40), (700, 64), (257, 100), (40, 39),
+                                  (30, 45)])
+@pytest.mark.parametrize("lower", [False, True])
+def test_band_wide_reduction(n, kd, lower):
+    ab = _band(n, kd, seed=n + 3 * kd)
+    if lower:  # the same matrix in lower storage
+        A = band_ref.band_to_dense(ab)
+        ab = np.zeros_like(ab)
+        for j in range(n):
+            for i in range(j, min(n, j + kd + 1)):
+                ab[i - j, j] = A[i, j]
+        ab = np.asfortranarray(ab)
+    w, Q = hp.eigh_banded(ab, lower=lower)
+    _check(ab, w, Q, lower=lower)
+
+
+@pytest.mark.parametrize("n,kd", [(300, 2), (1000, 4), (500, 16), (600, 48), (2048, 4)])
+def test_band_eigenvalues_only_reduction(n, kd):
+    ab = _band(n, kd, seed=2 * n + kd)
+    w = np.zeros(n)
+    z = np.zeros((1, 1), order="F")
+    work, iwork = np.zeros(1), np.zeros(1, dtype=np.int32)
+    info = hp.mdsbedc("N", "U", n, kd, ab.copy(order="F"), kd + 1, w, z, 1, work, -1, iwork, -1)
+    assert info == 0 and work[0] == 2 * n and iwork[0] == 1
+    info = hp.mdsbedc("N", "U", n, kd, ab.copy(order="F"), kd + 1, w, z, 1, work, 2 * n, iwork, 1)
+    assert info == 0
+    wl, _ = band_ref.eig_banded_lapack(ab)
+    na = np.abs(band_ref.band_to_dense(ab)).sum(axis=1).max()
+    assert np.all(np.diff(w) >= 0)
+    assert np.max(np.abs(w - wl)) / na <= EV_TOL
+    # the eigenvalues-only path of MDSBEVD as well
+    d = np.zeros(n)
+    info = hp.mdsbevd("N", "U", n, kd, ab.copy(order="F"), kd + 1, d, z, 1, work, 1, iwork, 1)
+    assert info == 0 and np.array_equal(d, w)
+
+
+def test_band_wide_device_entry():
+    n, kd = 900, 50
+    ab = _band(n, kd, seed=77)
+    abd = torch.tensor(np.ascontiguousarray(ab.T), device="cuda")
+    w = torch.empty(n, dtype=torch.float64, device="cuda")
+    z = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    hp.mdsbevd_dev(kd, abd, w, z)
+    _check(ab, w.cpu().numpy(), z.cpu().numpy().reshape(n, n).T)

@@ -7,6 +7,8 @@ restated MDLAED3/CauchylikeEig.
 
 Tolerances: the HSS products within 1e-11 (relative Frobenius) of the dense
 products at HSS tolerance 1e-14; orthogonality of Q C within 1e-12 * n."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -16,6 +18,8 @@ import hsspack_gb300 as hp
 from helpers import interlace_grid
 
 pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def _dev(a):
@@ -79,10 +83,17 @@ def test_cauchy_merge_8192_secular_vs_dlaed4(merge_8192):
     n, d, z, dd, lam, difl, difr, zh, al = merge_8192
     lam_o, difl_o, difr_o = oracle.secular(d, z, 1.0)
     lam_g, difl_g, difr_g = (t.cpu().numpy() for t in (lam, difl, difr))
-    # the secular tests' bar: roots within 1e-13 * max|d|, gaps to 1e-11
-    assert np.max(np.abs(lam_g - lam_o)) <= 1e-13 * max(1.0, np.abs(d).max())
-    assert np.max(np.abs(difl_g - difl_o) / np.abs(difl_o)) <= 1e-11
+    # the secular tests' bar: roots within 1e-13 * max|d|, gaps to 1e-11; the
+    # last root against 50 digits instead (DLAED4's is 1.5e-13 off there)
+    assert np.max(np.abs(lam_g[:-1] - lam_o[:-1])) <= 1e-13 * max(1.0, np.abs(d).max())
+    assert np.max(np.abs(difl_g[:-1] - difl_o[:-1]) / np.abs(difl_o[:-1])) <= 1e-11
     assert np.max(np.abs(difr_g[:-1] - difr_o[:-1]) / np.abs(difr_o[:-1])) <= 1e-11
+    g = np.load(os.path.join(GOLD, "merge8192_mp.npz"))
+    i = g["idx"]
+    assert np.max(np.abs(lam_g[i] - g["lam"])) <= 1e-15 * max(1.0, np.abs(g["lam"]).max())
+    assert np.max(np.abs(difl_g[i] - g["difl"]) / np.abs(g["difl"])) <= 1e-13
+    m = i < n - 1
+    assert np.max(np.abs(difr_g[i[m]] - g["difr"][m]) / np.abs(g["difr"][m])) <= 1e-13
     # Loewner z-hat and alpha from the oracle's roots (the restated MDLAED3)
     zh_o, al_o = oracle.lowner(d, difl_o, difr_o, z)
     assert np.max(np.abs(zh.cpu().numpy() - zh_o) / np.abs(zh_o)) <= 1e-12

@@ -168,3 +168,90 @@ def test_host_entry_packed_output_matches_device(kind, n, extra):
     assert np.array_equal(Z[:n], zdev)
     if extra:
         assert np.all(Z[n:] == 7.0)
+
+
+# COMPZ = 'V' (SRC/mdstedc.f90:139 with ICOMPZ = 1): Z holds on entry the
+# orthogonal matrix of a reduction to tridiagonal form and on exit that matrix
+# times the tridiagonal's eigenvectors, i.e. the eigenvectors of the original
+# matrix.  Checked on a dense symmetric matrix reduced by Householder (SciPy's
+# LAPACK DGEHRD/DORGHR: the tridiagonal of a symmetric matrix), and on random
+# and Toeplitz tridiagonals with a random orthogonal Q0 (the supports of the DC
+# eigenvectors are sparse for the first, full for the second: the grouped and
+# the dense product).
+
+
+def _mdstedc_v(d, e, Q0):
+    n = len(d)
+    w = np.array(d, dtype=np.float64)
+    ew = np.zeros(max(n, 1))
+    ew[: n - 1] = e
+    Z = np.asfortranarray(Q0.copy())
+    work = np.zeros(1)
+    iwork = np.zeros(1, dtype=np.int32)
+    assert hp.mdstedc("V", n, w, ew, Z, n, work, -1, iwork, -1) == 0
+    info = hp.mdstedc("V", n, w, ew, Z, n, work, int(work[0]), iwork, int(iwork[0]))
+    assert info == 0, (info, hp._err())
+    return w, Z
+
+
+@pytest.mark.parametrize("n", [2, 20, 300, 1500])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_compz_v_reduced_symmetric(n, precision):
+    import scipy.linalg
+    from scipy.linalg import lapack
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    A = (A + A.T) / 2
+    H, Q0 = scipy.linalg.hessenberg(A, calc_q=True)
+    d, e = np.diag(H).copy(), np.diag(H, -1).copy()
+    old = hp.set_config(precision=precision)
+    try:
+        w, Z = _mdstedc_v(d, e, Q0)
+    finally:
+        hp.restore_config(old)
+    an = np.abs(np.linalg.eigvalsh(A)).max()
+    wl, info = lapack.dsterf(d.copy(), e.copy())
+    assert info == 0
+    assert np.all(np.diff(w) >= 0)
+    assert np.max(np.abs(w - np.sort(wl))) <= EV_TOL * an
+    assert np.linalg.norm(A @ Z - Z * w) / (n * an) <= RES_TOL
+    assert np.linalg.norm(Z.T @ Z - np.eye(n)) / n <= ORTH_TOL
+
+
+@pytest.mark.parametrize("kind,n", [("random", 4096), ("toeplitz", 1024), ("split", 700)])
+def test_compz_v_equals_q0_times_eigenvectors(kind, n):
+    rng = np.random.default_rng(7)
+    if kind == "toeplitz":
+        d, e = toeplitz_tridiag(n)
+    else:
+        d, e = rand_tridiag(n, seed=n)
+        if kind == "split":
+            e[[99, 100, 400]] = 0.0
+    Q0, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    old = hp.set_config(precision=1, smlsiz=12)
+    try:
+        w, Z = _mdstedc_v(d, e, Q0)
+        wi, Qi = hp.eigh_tridiagonal(d, e)
+    finally:
+        hp.restore_config(old)
+    # the same eigenvalues as COMPZ = 'I', and Z = Q0 Q_T with Q_T the 'I' vectors
+    assert np.array_equal(w, wi)
+    ref = Q0 @ Qi
+    assert np.max(np.abs(Z - ref)) <= 1e-13
+    wl, _ = oracle.dstedc_lapack(d, e)
+    ev, res, orth = eig_metrics(d, e, w, Q0.T @ Z, wl)
+    assert ev <= EV_TOL and res <= RES_TOL and orth <= ORTH_TOL, (ev, res, orth)
+
+
+def test_compz_v_device_entry_matches_host_entry():
+    import torch
+    n = 2500
+    d, e = rand_tridiag(n, seed=11)
+    Q0, _ = np.linalg.qr(np.random.default_rng(11).standard_normal((n, n)))
+    w, Z = _mdstedc_v(d, e, Q0)
+    dd = torch.tensor(d, device="cuda")
+    ee = torch.tensor(np.append(e, 0.0), device="cuda")
+    zz = torch.tensor(np.ascontiguousarray(Q0.T), device="cuda")  # column-major Q0
+    hp.mdstedc_v_dev(dd, ee, zz)
+    assert np.array_equal(dd.cpu().numpy(), w)
+    assert np.array_equal(zz.cpu().numpy().T, Z)

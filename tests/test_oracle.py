@@ -57,6 +57,23 @@ def test_oracle_secular_vs_mp_roots_nearly_deflatable():
             assert np.max(np.abs(lam - g[key + "_lam"])) <= 1e-13, key
 
 
+def test_oracle_secular_vs_mp_roots_merge8192():
+    # the n = 8192 Cauchy-merge problem: LAPACK DLAED4 within 1e-13 of the
+    # 50-digit roots except the last, which it leaves 1.5e-13 off (its stopping
+    # test for the root beyond the last pole is looser); the GPU parity test
+    # pins that root to the 50-digit value instead
+    g = np.load(os.path.join(GOLD, "merge8192_mp.npz"))
+    n = 8192
+    rng = np.random.default_rng(0)
+    d = np.sort(rng.uniform(0.0, 1.0, n))
+    z = rng.standard_normal(n) / np.sqrt(n)
+    lam, difl, difr = oracle.secular(d, z, 1.0)
+    i = g["idx"]
+    err = np.abs(lam[i] - g["lam"])
+    assert np.max(err[i < n - 1]) <= 1e-13
+    assert 1e-14 < err[i == n - 1][0] <= 1e-12
+
+
 def test_oracle_glued_wilkinson():
     # Wilkinson-type blocks glued by 1e-8: every merge has nearly deflatable
     # poles; the restated MDSTEDC (HSS merges from K >= 40) holds the bar
