@@ -94,10 +94,12 @@ def test_cauchy_merge_8192_secular_vs_dlaed4(merge_8192):
     assert np.max(np.abs(difl_g[i] - g["difl"]) / np.abs(g["difl"])) <= 1e-13
     m = i < n - 1
     assert np.max(np.abs(difr_g[i[m]] - g["difr"][m]) / np.abs(g["difr"][m])) <= 1e-13
-    # Loewner z-hat and alpha from the oracle's roots (the restated MDLAED3)
+    # Loewner z-hat and alpha from the oracle's roots (the restated MDLAED3):
+    # each z-hat is a product of 2k - 1 = 16383 factors, so the two orders of
+    # multiplication differ by up to ~k eps relative (1.6e-12 measured); bar 1e-11
     zh_o, al_o = oracle.lowner(d, difl_o, difr_o, z)
-    assert np.max(np.abs(zh.cpu().numpy() - zh_o) / np.abs(zh_o)) <= 1e-12
-    assert np.max(np.abs(al.cpu().numpy() - al_o) / np.abs(al_o)) <= 1e-12
+    assert np.max(np.abs(zh.cpu().numpy() - zh_o) / np.abs(zh_o)) <= 1e-11
+    assert np.max(np.abs(al.cpu().numpy() - al_o) / np.abs(al_o)) <= 1e-11
 
 
 @pytest.mark.parametrize("precision", [0, 1])
