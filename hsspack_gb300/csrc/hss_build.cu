@@ -118,7 +118,7 @@ __device__ __forceinline__ double warp_prod(double v) {
 template <bool ROW>
 __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, double *W, int *PL,
                          int *PQ, double *V, int *PU, int M, int N, double tol, int rmax,
-                         int *overflow, int *nswap) {
+                         int *overflow, int *nswap, double rho) {
   __shared__ ArgMax red[HT / 32];
   __shared__ int s_rk;
   const int tid = threadIdx.x;
@@ -261,7 +261,9 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
       if (tid == 0) W[k] = (den(PL[k], PU[k]) / A[k]) * pr;
     }
     __syncthreads();
-    // strong swaps every 10 steps (searchMax2Eig[m], rho = 1.5)
+    // strong swaps every 10 steps when an interpolation entry exceeds rho
+    // (searchMax2Eig[m] with rho = 1.5, CauchyHssEig.f90:98-99; searchMax2 with
+    // rho = 1.02 for generic Cauchy matrices, CauchyHss_VP2.f90:70-71)
     if ((k + 1) % 10 == 0) {
       for (int guard = 0; guard < M + 8; ++guard) {
         ArgMax best{-1.0, INT_MAX};
@@ -283,7 +285,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
         if (r.i != INT_MAX && best.i == r.i && best.v == r.v) s_jj = ii_loc;
         __syncthreads();
         const int ii = r.i == INT_MAX ? 0 : r.i, jj = s_jj;
-        if (!(r.v > 1.5) || jj >= M) break;
+        if (!(r.v > rho) || jj >= M) break;
         if (tid == 0) atomicAdd(nswap, 1);
         for (int j = k + 1 + tid; j < N; j += HT)
           V[j] *= ROW ? (-P.fd(PL[ii], PU[j])) / (-P.fd(PL[jj], PU[j]))
@@ -369,7 +371,8 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   }
   __syncthreads();
   PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
-  int Rk = rrlu_node<true>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1);
+  int Rk = rrlu_node<true>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1,
+                           h.rho);
   __syncthreads();
   for (int i = tid; i < M; i += HT) { h.U[r0 + i] = A[i]; h.PL[r0 + i] = PL[i]; INV[PQ[i]] = i; }
   __syncthreads();
@@ -421,7 +424,8 @@ k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   }
   __syncthreads();
   PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
-  int Rk = rrlu_node<false>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1);
+  int Rk = rrlu_node<false>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1,
+                            h.rho);
   __syncthreads();
   for (int i = tid; i < M; i += HT) { h.V[c0 + i] = A[i]; h.PU[c0 + i] = PL[i]; INV[PQ[i]] = i; }
   __syncthreads();
@@ -550,7 +554,7 @@ static T *up(const char *name, const std::vector<T> &v, cudaStream_t st) {
 // Build the HSS generators on the device; on return the ranks are on the host.
 static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F, const double *u,
                          const double *v, const double *difl, const double *difr, cudaStream_t st,
-                         bool sq = false) {
+                         bool sq = false, double rho = 1.5) {
   int launches = 0;
   pl.t = make_tree(K, ni);
   const HostTree &t = pl.t;
@@ -558,7 +562,7 @@ static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F
   const int rmax = std::max(HSS_RMIN, t.mmax);
   HssDev &h = pl.h;
   h.FF = F; h.DIFL = difl; h.DIFR = difr; h.sq = sq;
-  h.K = K; h.ltr = ltr; h.rmax = rmax;
+  h.K = K; h.ltr = ltr; h.rmax = rmax; h.rho = rho;
   h.U = pool<double>("hs_U", K); h.V = pool<double>("hs_V", K);
   h.PL = pool<int>("hs_PL", K); h.PU = pool<int>("hs_PU", K);
   h.Ut = pool<double>("hs_Ut", K); h.Vt = pool<double>("hs_Vt", K);
@@ -810,7 +814,8 @@ int svd_hss_merge(const SvdHssArgs &a, int *rank, cudaStream_t st) {
     const double *v = side == 0 ? alpha : beta;
     HssPlan pl;
     stage_begin(HSS_ST_HSS_BUILD, st);
-    launches += hss_construct(pl, a.K, a.leaf, a.tol, a.dl, u, v, a.difl, a.difr, st, true);
+    // the SVD module's swap threshold (rrluCauchysvd, CauchyHssvd_VPS.f90:110)
+    launches += hss_construct(pl, a.K, a.leaf, a.tol, a.dl, u, v, a.difl, a.difr, st, true, 1.1);
     stage_end(HSS_ST_HSS_BUILD, st, 0, 0.0);
     if (pl.ok) {
       stage_begin(HSS_ST_HSS_MM, st);
@@ -881,7 +886,8 @@ int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *
   HCK(cudaEventRecord(e0, st));
   k_cauchy_repr<<<(n + 255) / 256, 256, 0, st>>>(n, D, F, u, difl, difr, mu);
   HssPlan pl;
-  int launches = 1 + hss_construct(pl, n, ni, tol, F, v, mu, difl, difr, st);
+  // the generic Cauchy module's swap threshold (rrluCauchy, CauchyHss_VP2.f90:70)
+  int launches = 1 + hss_construct(pl, n, ni, tol, F, v, mu, difl, difr, st, false, 1.02);
   HCK(cudaEventRecord(e1, st));
   transpose(n, ncb, B, ldb, X, ncb, st);
   if (pl.ok) {

@@ -25,6 +25,7 @@ struct HssDev {
   const double *FF, *DIFL, *DIFR;  // poles and root gaps (length K)
   bool sq;                         // singular-value mode (differences of squares)
   int K, ltr, rmax;
+  double rho;                      // strong-swap threshold of the RRLU (1.5 eigen/SVD, 1.02 VP2)
   // current compressed generators (row side: U, PL; column side: V, PU)
   double *U, *V;
   int *PL, *PU;

@@ -62,6 +62,9 @@ def lib():
                                   _D, _D, _D, _D, ctypes.c_int, ctypes.c_int, _I]
         L.hso_cauchylike.argtypes = [_D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int]
         L.hso_get_stats.argtypes = [ctypes.POINTER(HsoStats)]
+        L.hso_cauchyhssmm.argtypes = [ctypes.c_int, _D, _D, _D, _D, ctypes.c_int,
+                                      ctypes.c_double, _D, ctypes.c_int, ctypes.c_int]
+        L.hso_cauchyhssmm.restype = ctypes.c_int
         rc = L.hso_init(openblas_path().encode())
         if rc != 0:
             raise RuntimeError("oracle: cannot load LAPACK (rc=%d)" % rc)
@@ -159,3 +162,14 @@ def dhssevc(F, u, v, difl, difr, Q, ni=200, tol=1e-17):
     if rc != 0:
         raise RuntimeError("dhssevc rc=%d" % rc)
     return Q, mr.value
+
+
+def cauchyhssmm(D, F, U, V, B, ni, tol):
+    """CauchyHssMM (SRC/cauchyhssmm.f90) restated with the VP2 module: returns
+    (C @ B, max generator rank) for C(i,j) = U_i V_j / (D_i - F_j)."""
+    n = len(D)
+    args = [np.array(a, dtype=np.float64, copy=True) for a in (D, F, U, V)]
+    Bf = np.array(B, dtype=np.float64, order="F", copy=True)
+    r = lib().hso_cauchyhssmm(n, *[_p(a) for a in args], int(ni), float(tol), _p(Bf),
+                              Bf.shape[0], Bf.shape[1])
+    return Bf, r

@@ -1039,6 +1039,285 @@ int laed0(int n, double *d, double *e, double *Q, int ldq, const hso_config &cfg
   return 0;
 }
 
+// ---------------------------------------------- generic Cauchy HSS (VP2) ---
+// Module CauchyHss_VP2 (SRC/CauchyHss_VP2.f90) for C(i,j) = u_i v_j / (D_i - F_j)
+// with plain pole differences (no DIFL/DIFR), as SRC/cauchyhssmm.f90 uses it.
+// Indices are 0-based; k below is the 0-based step (Fortran k - 1).
+
+// CauchyMax (:166-185): largest |u_i / (D_i - F)|, i < n, first index on ties.
+void vp2_cmax(const double *D, double F, const double *u, int n, double &junk, int &jj) {
+  junk = -1.0;
+  jj = 0;
+  for (int i = 0; i < n; ++i) {
+    const double t = std::fabs(u[i] / (D[i] - F));
+    if (t > junk) { junk = t; jj = i; }
+  }
+}
+
+// CauchyPivtG (:187-236): alternate row / column maxima until the pivot is
+// the largest entry of its row and its column.  Fortran's `continue` after the
+// row swap is a no-op, so a row swap is always followed by a column swap.
+void vp2_pivt(double *D, double *F, double *u, double *v, int *PL, int *PU, int k, double *A,
+              int M, int N) {
+  double junkL, junkU;
+  int jjL, jjU;
+  vp2_cmax(D + k, F[k], u + k, M - k, junkL, jjL);
+  vp2_cmax(F + k, D[k], v + k, N - k, junkU, jjU);
+  junkL *= std::fabs(v[k]);
+  junkU *= std::fabs(u[k]);
+  const double piv = std::fabs(u[k] * v[k] / (D[k] - F[k]));
+  if (junkL <= piv && junkU <= piv) return;
+  bool flg = junkL > junkU;
+  for (int guard = 0; guard < 4 * (M + N) + 8; ++guard) {  // the Fortran loop is unbounded
+    if (flg) {
+      const int jj = jjL;
+      swp(D, k, jj + k); swp(u, k, jj + k); swp(A, k, jj + k); swp(PL, k, jj + k);
+      vp2_cmax(F + k, D[k], v + k, N - k, junkU, jjU);
+      if (jjU == 0) return;
+    }
+    const int jj = jjU;
+    swp(F, k, jj + k); swp(v, k, jj + k); swp(PU, k, jj + k);
+    vp2_cmax(D + k, F[k], u + k, M - k, junkL, jjL);
+    if (jjL == 0) return;
+    flg = true;
+  }
+}
+
+// CauchyPivtG_CP (:239-290): complete pivoting over the Schur complement.
+void vp2_pivt_cp(double *D, double *F, double *u, double *v, int *PL, int *PU, int k, double *A,
+                 int M, int N) {
+  double best = -1.0;
+  int ii = 0, jj = 0;
+  for (int j = 0; j < N - k; ++j) {
+    double t;
+    int a;
+    vp2_cmax(D + k, F[k + j], u + k, M - k, t, a);
+    t = std::fabs(t * v[k + j]);
+    if (j == 0 || t > best) { best = t; ii = a; jj = j; }
+  }
+  swp(D, k, ii + k); swp(u, k, ii + k); swp(A, k, ii + k); swp(PL, k, ii + k);
+  swp(F, k, jj + k); swp(v, k, jj + k); swp(PU, k, jj + k);
+}
+
+// searchMax2 (:135-163): the largest |U2_i W_j / (D2_i - D1_j)| over i < ldu,
+// j < ldw; ii = column j, jj = row i (relative to U2/D2).
+void vp2_search(const double *U2, const double *W, const double *D2, const double *D1, int ldu,
+                int ldw, int &ii, int &jj, double &nmax) {
+  double junk;
+  int jjl;
+  vp2_cmax(D2, D1[0], U2, ldu, junk, jjl);
+  nmax = junk * std::fabs(W[0]);
+  ii = 0;
+  jj = jjl;
+  for (int j = 1; j < ldw; ++j) {
+    vp2_cmax(D2, D1[j], U2, ldu, junk, jjl);
+    junk *= std::fabs(W[j]);
+    if (junk > nmax) { nmax = junk; ii = j; jj = jjl; }
+  }
+}
+
+// rrluCauchy (:7-134): structured strong RRLU with rho = 1.02, swaps checked
+// every 10 steps.  A (row generators) and D are permuted in place; U receives
+// the Schur row generators (last M - Rk used), W the first Rk column
+// generators of Mat_N; PL / PU the row / column permutations.
+int vp2_rrlu(double *D, double *F, double *A, double *V, double tol, double *U, double *W,
+             int *PL, int *PU, int M, int N, long long &nswap) {
+  for (int i = 0; i < M; ++i) { U[i] = A[i]; PL[i] = i; }
+  for (int j = 0; j < N; ++j) PU[j] = j;
+  int Rk = std::min(M, N);
+  const int mn = Rk;
+  double Amax = 0.0;
+  const double rho = 1.02;
+  const int prd = 10;
+  for (int k = 0; k < mn; ++k) {
+    vp2_pivt(D, F, U, V, PL, PU, k, A, M, N);
+    double Ukk = U[k] * V[k] / (D[k] - F[k]);
+    Amax = std::max(Amax, std::fabs(Ukk));
+    if (std::fabs(Ukk) < tol * Amax) {
+      vp2_pivt_cp(D, F, U, V, PL, PU, k, A, M, N);
+      Ukk = U[k] * V[k] / (D[k] - F[k]);
+      Amax = std::max(Amax, std::fabs(Ukk));
+      if (std::fabs(Ukk) < tol * Amax) { Rk = k; break; }
+    }
+    for (int i = k + 1; i < M; ++i) U[i] = U[i] * (D[i] - D[k]) / (D[i] - F[k]);
+    for (int j = k + 1; j < N; ++j) V[j] = V[j] * (F[j] - F[k]) / (F[j] - D[k]);
+    for (int j = 0; j < k; ++j) W[j] = W[j] * ((F[k] - D[j]) / (D[k] - D[j]));
+    W[k] = (D[k] - F[k]) / A[k];
+    for (int j = 0; j < k; ++j) W[k] = W[k] * (F[j] - D[k]) / (D[j] - D[k]);
+    bool again = ((k + 1) % prd) == 0;
+    while (again) {
+      again = false;
+      int ii, jj;
+      double nmax;
+      vp2_search(U + k + 1, W, D + k + 1, D, M - k - 1, k + 1, ii, jj, nmax);
+      if (M - k - 1 > 0 && nmax > rho) {
+        ++nswap;
+        again = true;
+        jj += k + 1;
+        for (int j = k + 1; j < N; ++j) V[j] = V[j] * ((F[j] - D[ii]) / (F[j] - D[jj]));
+        for (int i = k + 1; i < jj; ++i) U[i] = U[i] * ((D[i] - D[jj]) / (D[i] - D[ii]));
+        for (int i = jj + 1; i < M; ++i) U[i] = U[i] * ((D[i] - D[jj]) / (D[i] - D[ii]));
+        for (int j = 0; j < ii; ++j) W[j] = W[j] * ((D[j] - D[ii]) / (D[j] - D[jj]));
+        for (int j = ii + 1; j <= k; ++j) W[j] = W[j] * ((D[j] - D[ii]) / (D[j] - D[jj]));
+        U[jj] = A[ii] * ((D[ii] - D[jj]) / (D[ii] - F[ii]));
+        W[ii] = (D[jj] - F[ii]) / A[jj];
+        for (int j = 0; j <= k; ++j) {
+          if (j == ii) continue;
+          U[jj] = U[jj] * ((D[ii] - D[j]) / (D[ii] - F[j]));
+          W[ii] = W[ii] * ((F[j] - D[jj]) / (D[j] - D[jj]));
+        }
+        swp(PL, ii, jj); swp(D, ii, jj); swp(A, ii, jj);
+      }
+    }
+  }
+  return Rk;
+}
+
+// comprcauchy (:616-725) + Cauchylike2 (:743-778).  Row case: the node's rows
+// (poles Dn, generators Un, M of them) against the other columns (Fo, Vo, N):
+// returns U_node (M x Rk) in the node's original row order; Dn / Un permuted
+// so that their first Rk entries are the skeleton.  Column case: the node's
+// columns (poles Fn, generators Vn, M) against the other rows (Do, Uo, N):
+// returns V_node (Rk x M) in the node's original column order.
+int vp2_compress(bool row, double *Pn, double *Gn, double *Po, double *Go, double tol, int M,
+                 int N, std::vector<double> &Q, long long &nswap) {
+  std::vector<double> Z(M, 0.0), W(std::max(std::min(M, N), 1), 0.0);
+  std::vector<int> PL(M), PU(std::max(N, 1)), inv(M);
+  // row: rrluCauchy(D, F, U, V); column: rrluCauchy(F, D, V, U)
+  const int Rk = vp2_rrlu(Pn, Po, Gn, Go, tol, Z.data(), W.data(), PL.data(), PU.data(), M, N,
+                          nswap);
+  for (int i = 0; i < M; ++i) inv[PL[i]] = i;
+  if (Rk < M) {
+    Q.assign((size_t)M * Rk, 0.0);
+    for (int r = 0; r < M; ++r) {
+      const int p = inv[r];
+      for (int j = 0; j < Rk; ++j) {
+        const double v = p < Rk ? (p == j ? 1.0 : 0.0) : Z[p] * W[j] / (Pn[p] - Pn[j]);
+        // Cauchylike2's two branches (:763-775) give the same entry
+        // Z_p W_j / (P_p - P_j); the column case stores it transposed (Rk x M)
+        if (row) Q[r + (size_t)j * M] = v;
+        else Q[j + (size_t)r * Rk] = v;
+      }
+    }
+  } else {
+    Q.assign((size_t)M * M, 0.0);
+    for (int r = 0; r < M; ++r) {
+      if (row) Q[r + (size_t)inv[r] * M] = 1.0;
+      else Q[inv[r] + (size_t)r * M] = 1.0;
+    }
+  }
+  return Rk;
+}
+
+// cauchy2hss (:387-613): post-order traversal with a stack of compressed
+// skeletons; every node's rows are compressed against the skeleton columns
+// of the nodes to its left and the full columns to its right, then its
+// columns likewise.  D, F, U, V are overwritten (as in the Fortran).
+void cauchy2hss_vp2(const Tree &t, int n, double *D, double *F, double *U, double *V, double tol,
+                    Gen &g, long long &nswap) {
+  g.init(t.ltr);
+  const int ltr = t.ltr;
+  std::vector<int> l0(ltr + 1), l1(ltr + 1);
+  for (int i = 1, lt = 0, it = 0; i <= ltr; ++i) {
+    if (t.leaf(i)) { l0[i] = lt; l1[i] = lt + t.m[it] - 1; lt = l1[i] + 1; ++it; }
+    else { l0[i] = l0[t.c1[i]]; l1[i] = l1[t.c2[i]]; }
+  }
+  std::vector<int> lsr(t.lvl + 3, 0), lsc(t.lvl + 3, 0);
+  int ns = 0;  // stack depth; lsr[ns] / lsc[ns]: next free skeleton position
+  std::vector<double> Di, Fi, Ui, Vi;
+  auto row_compress = [&](int node, int r0, int mi, int ncolL) {
+    // rows D/U[r0 .. r0+mi) against skeleton columns [0, ncolL) and columns right of the node
+    const int ni = n - (l1[node] + 1);
+    const int nt = ncolL + ni;
+    Di.assign(D + r0, D + r0 + mi); Ui.assign(U + r0, U + r0 + mi);
+    Fi.resize(std::max(nt, 1)); Vi.resize(std::max(nt, 1));
+    for (int j = 0; j < ncolL; ++j) { Fi[j] = F[j]; Vi[j] = V[j]; }
+    for (int j = 0; j < ni; ++j) { Fi[ncolL + j] = F[l1[node] + 1 + j]; Vi[ncolL + j] = V[l1[node] + 1 + j]; }
+    const int Rk = vp2_compress(true, Di.data(), Ui.data(), Fi.data(), Vi.data(), tol, mi, nt,
+                                g.U[node], nswap);
+    g.Ur[node] = mi; g.Uc[node] = Rk;
+    return Rk;
+  };
+  auto col_compress = [&](int node, int c0, int mi, int nrowL) {
+    const int ni = n - (l1[node] + 1);
+    const int nt = nrowL + ni;
+    Fi.assign(F + c0, F + c0 + mi); Vi.assign(V + c0, V + c0 + mi);
+    Di.resize(std::max(nt, 1)); Ui.resize(std::max(nt, 1));
+    for (int j = 0; j < nrowL; ++j) { Di[j] = D[j]; Ui[j] = U[j]; }
+    for (int j = 0; j < ni; ++j) { Di[nrowL + j] = D[l1[node] + 1 + j]; Ui[nrowL + j] = U[l1[node] + 1 + j]; }
+    const int Rk = vp2_compress(false, Fi.data(), Vi.data(), Di.data(), Ui.data(), tol, mi, nt,
+                                g.V[node], nswap);
+    g.Vr[node] = Rk; g.Vc[node] = mi;
+    return Rk;
+  };
+  for (int i = 1; i <= ltr; ++i) {
+    if (t.leaf(i)) {
+      const int mi = l1[i] - l0[i] + 1;
+      g.Dm[i] = mi;
+      g.D[i].assign((size_t)mi * mi, 0.0);
+      for (int c = 0; c < mi; ++c)
+        for (int r = 0; r < mi; ++r)
+          g.D[i][r + (size_t)c * mi] = U[l0[i] + r] * V[l0[i] + c] / (D[l0[i] + r] - F[l0[i] + c]);
+      if (i == ltr) break;  // a single leaf: no off-diagonal blocks
+      int Rk = row_compress(i, l0[i], mi, lsc[ns]);
+      for (int j = 0; j < Rk; ++j) { D[lsr[ns] + j] = Di[j]; U[lsr[ns] + j] = Ui[j]; }
+      lsr[ns + 1] = lsr[ns] + Rk;
+      Rk = col_compress(i, l0[i], mi, lsr[ns]);
+      for (int j = 0; j < Rk; ++j) { F[lsc[ns] + j] = Fi[j]; V[lsc[ns] + j] = Vi[j]; }
+      lsc[ns + 1] = lsc[ns] + Rk;
+      ++ns;
+    } else {
+      // B generators between the two children (top two stack entries)
+      const int c1 = t.c1[i], c2 = t.c2[i];
+      const int r1 = lsr[ns - 1] - lsr[ns - 2], r2 = lsr[ns] - lsr[ns - 1];
+      const int k1 = lsc[ns - 1] - lsc[ns - 2], k2 = lsc[ns] - lsc[ns - 1];
+      g.Br[c1] = r1; g.Bc[c1] = k2;
+      g.B[c1].assign((size_t)std::max(r1 * k2, 1), 0.0);
+      for (int c = 0; c < k2; ++c)
+        for (int r = 0; r < r1; ++r)
+          g.B[c1][r + (size_t)c * r1] = U[lsr[ns - 2] + r] * V[lsc[ns - 1] + c] /
+                                        (D[lsr[ns - 2] + r] - F[lsc[ns - 1] + c]);
+      g.Br[c2] = r2; g.Bc[c2] = k1;
+      g.B[c2].assign((size_t)std::max(r2 * k1, 1), 0.0);
+      for (int c = 0; c < k1; ++c)
+        for (int r = 0; r < r2; ++r)
+          g.B[c2][r + (size_t)c * r2] = U[lsr[ns - 1] + r] * V[lsc[ns - 2] + c] /
+                                        (D[lsr[ns - 1] + r] - F[lsc[ns - 2] + c]);
+      if (i == ltr) break;
+      // the children's skeleton rows (then columns) merged and compressed again
+      int mi = lsr[ns] - lsr[ns - 2];
+      int Rk = row_compress(i, lsr[ns - 2], mi, lsc[ns - 2]);
+      for (int j = 0; j < Rk; ++j) { D[lsr[ns - 2] + j] = Di[j]; U[lsr[ns - 2] + j] = Ui[j]; }
+      lsr[ns - 1] = lsr[ns - 2] + Rk;
+      mi = lsc[ns] - lsc[ns - 2];
+      Rk = col_compress(i, lsc[ns - 2], mi, lsr[ns - 2]);
+      for (int j = 0; j < Rk; ++j) { F[lsc[ns - 2] + j] = Fi[j]; V[lsc[ns - 2] + j] = Vi[j]; }
+      lsc[ns - 1] = lsc[ns - 2] + Rk;
+      --ns;
+    }
+  }
+}
+
+// The generators of C^T from those of C: U <-> V^T, D^T, and B of a node is
+// the transposed B of its sibling (C^T(rows i, cols j) = (U_j B_j V_i)^T).
+void transpose_gen(const Tree &t, const Gen &g, Gen &h) {
+  h.init(t.ltr);
+  auto tr = [](const std::vector<double> &a, int r, int c) {
+    std::vector<double> b((size_t)std::max(r * c, 1), 0.0);
+    for (int j = 0; j < c; ++j)
+      for (int i = 0; i < r; ++i) b[j + (size_t)i * c] = a[i + (size_t)j * r];
+    return b;
+  };
+  for (int i = 1; i <= t.ltr; ++i) {
+    if (t.leaf(i) && g.Dm[i] > 0) { h.Dm[i] = g.Dm[i]; h.D[i] = tr(g.D[i], g.Dm[i], g.Dm[i]); }
+    if (i == t.ltr) continue;
+    h.Ur[i] = g.Vc[i]; h.Uc[i] = g.Vr[i]; h.U[i] = tr(g.V[i], g.Vr[i], g.Vc[i]);
+    h.Vr[i] = g.Uc[i]; h.Vc[i] = g.Ur[i]; h.V[i] = tr(g.U[i], g.Ur[i], g.Uc[i]);
+    const int s = t.sibling(i);
+    h.Br[i] = g.Bc[s]; h.Bc[i] = g.Br[s]; h.B[i] = tr(g.B[s], g.Br[s], g.Bc[s]);
+  }
+}
+
 }  // namespace
 
 // =================================================================== C API ==
@@ -1193,6 +1472,30 @@ int hso_dhssevc(int k, int ni, double tol, const double *F, const double * /*D*/
                 const double *u, const double *v, const double *difl,
                 const double *difr, double *Q, int ldq, int nrows, int *mr) {
   return dhssevc(k, ni, tol, F, u, v, difl, difr, Q, ldq, nrows, mr);
+}
+
+// CauchyHssMM (SRC/cauchyhssmm.f90:1-123): B (n x ncb, ldb) <- C B with
+// C(i,j) = U_i V_j / (D_i - F_j) compressed by the VP2 module (leaf ni, tol);
+// the product is (B^T C^T)^T through fastHssmmL's restatement.  D, F, U, V are
+// overwritten as in the Fortran.  Returns the largest generator rank.
+int hso_cauchyhssmm(int n, double *D, double *F, double *U, double *V, int ni, double tol,
+                    double *B, int ldb, int ncb) {
+  Tree t = make_tree(n, ni);
+  Gen g, h;
+  long long sw = 0;
+  cauchy2hss_vp2(t, n, D, F, U, V, tol, g, sw);
+  g_stats.n_swaps += sw;
+  transpose_gen(t, g, h);
+  std::vector<double> X((size_t)ncb * n);
+  for (int c = 0; c < n; ++c)
+    for (int r = 0; r < ncb; ++r) X[r + (size_t)c * ncb] = B[c + (size_t)r * ldb];
+  hss_mm_left(t, h, X.data(), ncb, ncb);
+  for (int c = 0; c < n; ++c)
+    for (int r = 0; r < ncb; ++r) B[c + (size_t)r * ldb] = X[r + (size_t)c * ncb];
+  int r = 0;
+  for (int i = 1; i < t.ltr; ++i) r = std::max(r, std::max(g.Uc[i], g.Vr[i]));
+  g_stats.max_rank = std::max(g_stats.max_rank, r);
+  return r;
 }
 
 void hso_cauchylike(double *A, const double *D, const double *F, const double *u,

@@ -159,3 +159,20 @@ def test_hssmm_oracle_tree_and_accuracy():
     assert np.abs(Y - A @ B).max() <= 2e-11 and 20 <= rank <= 45
     Y2, _ = hssmm_ref.dhssmml(A, B.T, 64, 1e-11)
     assert np.abs(Y2 - B.T @ A).max() <= 2e-11
+
+
+@pytest.mark.parametrize("n,ni,tol", [(300, 32, 1e-14), (1024, 64, 1e-14), (2000, 64, 1e-11)])
+def test_oracle_cauchyhssmm_vp2_vs_dense(n, ni, tol):
+    # CauchyHssMM restated with the VP2 module (post-order cauchy2hss, rrluCauchy
+    # with rho = 1.02) on the interlacing grid of TEST/testCauchyHss_serial.f90:
+    # the HSS product agrees with the dense one to the compression tolerance
+    from helpers import interlace_grid
+    F, D = interlace_grid(n)
+    rng = np.random.default_rng(n)
+    u, v = rng.standard_normal(n), rng.standard_normal(n)
+    B = rng.standard_normal((n, 64))
+    C = u[:, None] * v[None, :] / (D[:, None] - F[None, :])
+    ref = C @ B
+    out, r = oracle.cauchyhssmm(D, F, u, v, B, ni, tol)
+    assert np.linalg.norm(out - ref) / np.linalg.norm(ref) <= 100 * tol
+    assert 0 < r < n // 4
