@@ -142,13 +142,21 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     pos += __popc(m);
   }
   __syncthreads();
-  // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371): a
-  //      sequential chain over the candidates, run by one thread on a shared-
-  //      memory copy of their z, d, type (global memory when there are many)
+  // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371).  The
+  //      chain always pairs candidate t-1 with candidate t, and a rotation
+  //      changes only the values of its own pair, so the test of pair t on the
+  //      original values holds unless pair t-1 rotated.  All pairs are tested
+  //      in parallel first (the chain's quick test: clearly above the tolerance
+  //      means no rotation); one thread then runs the exact DLAED2 test on the
+  //      pairs that may rotate, in order, and after every rotation on the next
+  //      pair too (its left value has changed) -- the rotations, their order
+  //      and the values are those of the sequential chain.  The candidates' z,
+  //      d and type sit in shared memory when they fit, else in global memory.
   constexpr int NCS = 1536;
   __shared__ double c_z[NCS], c_d[NCS];
   __shared__ unsigned char c_t[NCS];
-  __shared__ int s_ng;
+  __shared__ int c_l[NCS];
+  __shared__ int s_ng, s_nl;
   const bool in_smem = nc <= NCS;
   if (in_smem) {
     for (int t = tid; t < nc; t += MT) {
@@ -159,59 +167,79 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     }
     __syncthreads();
   }
-  if (tid == 0) {
-    int ng = 0;
-    if (in_smem) {
-      int pj = 0;
-      for (int t = 1; t < nc; ++t) {
-        const int nj = t;
-        const double zp = c_z[pj], zn = c_z[nj];
-        const double tt = c_d[nj] - c_d[pj];
-        // |tt c s| = |tt zn zp| / (zn^2 + zp^2): pairs clearly above tol skip the
-        // hypot and divides of the exact test (decisions unchanged)
-        if (fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp)) { pj = nj; continue; }
-        const double tau = hypot(zn, zp);
-        const double c = zn / tau, sn = -zp / tau;
-        if (fabs(tt * c * sn) <= tol) {
-          c_z[nj] = tau;
-          c_z[pj] = 0.0;
-          if (c_t[nj] != c_t[pj]) c_t[nj] = 2;
-          c_t[pj] = 5;  // deflated by rotation: value changes, order fixed below
-          w.gvp[s + ng] = w.srt[s + w.cand[s + pj]];
-          w.gvq[s + ng] = w.srt[s + w.cand[s + nj]];
-          w.gvc[s + ng] = c;
-          w.gvs[s + ng] = sn;
-          ++ng;
-          const double dp = c_d[pj], dn = c_d[nj];
-          c_d[pj] = dp * c * c + dn * sn * sn;
-          c_d[nj] = dp * sn * sn + dn * c * c;
-        }
-        pj = nj;
+  auto zr = [&](int t) -> double & { return in_smem ? c_z[t] : w.zs[s + w.cand[s + t]]; };
+  auto dr = [&](int t) -> double & { return in_smem ? c_d[t] : w.ds[s + w.cand[s + t]]; };
+  auto tr = [&](int t) -> unsigned char & {
+    return in_smem ? c_t[t] : w.typ[s + w.cand[s + t]];
+  };
+  // pairs t = 1 .. nc-1 that may rotate, compacted in order (warp segments as above)
+  int *lst = w.l1slot + s;  // free until the deflated lists are written below
+  {
+    const int np = max(nc - 1, 0);
+    const int pseg = (((np + NW - 1) / NW) + 31) & ~31;
+    const int p0 = min(np, wid * pseg), p1 = min(np, p0 + pseg);
+    auto maybe = [&](int t) -> bool {  // t = 1 .. nc-1, original values
+      const double zp = zr(t - 1), zn = zr(t);
+      const double tt = dr(t) - dr(t - 1);
+      return !(fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp));
+    };
+    int cntp = 0;
+    for (int a0 = p0; a0 < p1; a0 += 32) {
+      const int a = a0 + lane;
+      cntp += __popc(__ballot_sync(HSS_FULL, a < p1 && maybe(a + 1)));
+    }
+    unsigned long long ptot;
+    int ppos = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)cntp : 0ull, &ptot);
+    ppos = __shfl_sync(HSS_FULL, ppos, 0);
+    for (int a0 = p0; a0 < p1; a0 += 32) {
+      const int a = a0 + lane;
+      const bool mb = a < p1 && maybe(a + 1);
+      const unsigned mk = __ballot_sync(HSS_FULL, mb);
+      if (mb) {
+        const int r = ppos + __popc(mk & below);
+        if ((int)ptot <= NCS) c_l[r] = a + 1; else lst[r] = a + 1;
       }
-    } else {
-      int pj = w.cand[s];
-      for (int t = 1; t < nc; ++t) {
-        const int nj = w.cand[s + t];
-        const double zp = w.zs[s + pj], zn = w.zs[s + nj];
-        const double tt = w.ds[s + nj] - w.ds[s + pj];
-        if (fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp)) { pj = nj; continue; }
-        const double tau = hypot(zn, zp);
-        const double c = zn / tau, sn = -zp / tau;
-        if (fabs(tt * c * sn) <= tol) {
-          w.zs[s + nj] = tau;
-          w.zs[s + pj] = 0.0;
-          if (w.typ[s + nj] != w.typ[s + pj]) w.typ[s + nj] = 2;
-          w.typ[s + pj] = 5;
-          w.gvp[s + ng] = w.srt[s + pj];
-          w.gvq[s + ng] = w.srt[s + nj];
-          w.gvc[s + ng] = c;
-          w.gvs[s + ng] = sn;
-          ++ng;
-          const double dp = w.ds[s + pj], dn = w.ds[s + nj];
-          w.ds[s + pj] = dp * c * c + dn * sn * sn;
-          w.ds[s + nj] = dp * sn * sn + dn * c * c;
-        }
-        pj = nj;
+      ppos += __popc(mk);
+    }
+    if (tid == 0) s_nl = (int)ptot;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const int nl = s_nl;
+    const int *L = nl <= NCS ? c_l : lst;
+    int ng = 0, done = 0;  // pairs up to `done` have been visited
+    // the exact test of pair (t-1, t) on the current values; true if it rotated
+    auto visit = [&](int t) -> bool {
+      const int pj = t - 1, nj = t;
+      const double zp = zr(pj), zn = zr(nj);
+      const double tt = dr(nj) - dr(pj);
+      if (fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp)) return false;
+      const double tau = hypot(zn, zp);
+      const double c = zn / tau, sn = -zp / tau;
+      if (!(fabs(tt * c * sn) <= tol)) return false;
+      zr(nj) = tau;
+      zr(pj) = 0.0;
+      if (tr(nj) != tr(pj)) tr(nj) = 2;
+      tr(pj) = 5;  // deflated by rotation: value changes, order fixed below
+      w.gvp[s + ng] = w.srt[s + w.cand[s + pj]];
+      w.gvq[s + ng] = w.srt[s + w.cand[s + nj]];
+      w.gvc[s + ng] = c;
+      w.gvs[s + ng] = sn;
+      ++ng;
+      const double dp = dr(pj), dn = dr(nj);
+      dr(pj) = dp * c * c + dn * sn * sn;
+      dr(nj) = dp * sn * sn + dn * c * c;
+      return true;
+    };
+    for (int a = 0; a < nl; ++a) {
+      int t = L[a];
+      if (t <= done) continue;  // already visited after a rotation
+      bool rot = visit(t);
+      done = t;
+      while (rot && t + 1 < nc) {
+        ++t;
+        rot = visit(t);
+        done = t;
       }
     }
     s_ng = ng;
