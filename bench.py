@@ -394,9 +394,14 @@ def run_extra(torch, hp, full_cfg):
         Q = torch.randn(n * n, dtype=torch.float64, device="cuda")
         for prec in (0, 1):
             hp.set_config(precision=prec)
-            out["cauchy_hss_multiply_n8192_%s_ms" % ("fp64" if prec == 0 else "split_bf16")] = \
+            key = "fp64" if prec == 0 else "split_bf16"
+            out["cauchy_hss_multiply_n8192_%s_ms" % key] = \
                 _timed_ms(torch, lambda: hp.dhssevc_dev(dd, zh, al, difl, difr, Q, n, n, ni=128,
                                                         tol=1e-14))
+            # the last call's construction and product (CUDA events in the library)
+            stt = hp.get_stats()["stage_ms"]
+            out["cauchy_hss_n8192_%s_build_ms" % key] = stt["hss_build"]
+            out["cauchy_hss_n8192_%s_product_ms" % key] = stt["hss_multiply"]
         out["cauchy_hss_max_rank"] = hp.get_stats()["max_rank"]
         del Q
         # DHSSMM: the Cauchy-like matrix of TEST/testfmm.f90 (interlaced points,

@@ -2026,10 +2026,15 @@ int hss_dhssevc_dev(int k, int ni, double tol, const double *F, const double *u,
   cudaStream_t st = (cudaStream_t)stream;
   try {
     int rank = 0;
-    hss_dhssevc_core(k, ni, tol, c.cfg.precision, F, u, v, difl, difr, Q, ldq, nrows, &rank, st);
+    float t2[2] = {0.f, 0.f};
+    hss_dhssevc_core(k, ni, tol, c.cfg.precision, F, u, v, difl, difr, Q, ldq, nrows, &rank, st,
+                     t2);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     c.stats.max_rank = rank;
+    // construction and product times of this call (CUDA events)
+    c.stats.stage_ms[HSS_ST_HSS_BUILD] = t2[0];
+    c.stats.stage_ms[HSS_ST_HSS_MM] = t2[1];
     return 0;
   } catch (CudaError &ex) {
     c.err = ex.msg;

@@ -910,10 +910,16 @@ int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *
 
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
-                     long long ldq, int nrows, int *rank, cudaStream_t st) {
+                     long long ldq, int nrows, int *rank, cudaStream_t st, float *times) {
   double *T = pool<double>("hss_T", (size_t)nrows * K);
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  if (times) {
+    HCK(cudaEventCreate(&e0)); HCK(cudaEventCreate(&e1)); HCK(cudaEventCreate(&e2));
+    HCK(cudaEventRecord(e0, st));
+  }
   HssPlan pl;
   int launches = hss_construct(pl, K, ni, tol, F, u, v, difl, difr, st);
+  if (times) HCK(cudaEventRecord(e1, st));
   if (pl.ok) {
     launches += hss_multiply(pl, Q, ldq, nrows, T, nrows, precision, st);
     *rank = pl.max_rank;
@@ -923,6 +929,13 @@ int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, 
   }
   HCK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), T, nrows * sizeof(double), nrows * sizeof(double), K,
                         cudaMemcpyDeviceToDevice, st));
+  if (times) {  // construction / product (with the copy back) in ms
+    HCK(cudaEventRecord(e2, st));
+    HCK(cudaEventSynchronize(e2));
+    HCK(cudaEventElapsedTime(&times[0], e0, e1));
+    HCK(cudaEventElapsedTime(&times[1], e1, e2));
+    cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  }
   return launches + 1;
 }
 

@@ -53,7 +53,8 @@ int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *
 // DHSSEVC on caller arrays: Q(0:nrows, 0:K) <- Q * C.
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
-                     long long ldq, int nrows, int *rank, cudaStream_t st);
+                     long long ldq, int nrows, int *rank, cudaStream_t st,
+                     float *times = nullptr);
 
 // DHSSMM / DHSSMML on device arrays (mat2hss.cu): A (n x n, lda) compressed to
 // HSS by truncated SVD (leaf ni, absolute tolerance tol); side 0: B (n x k,
