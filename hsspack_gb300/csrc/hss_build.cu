@@ -378,7 +378,7 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   __syncthreads();
   const int mn = min(M, N);
   double *G = h.Ug + (long long)node * h.ucap;
-  if (Rk < mn) {
+  if (Rk < (h.vp2 ? M : mn)) {
     for (int idx = tid; idx < M * Rk; idx += HT) {
       const int r = idx % M, j = idx / M, p = INV[r];
       G[idx] = (p < Rk) ? (p == j ? 1.0 : 0.0) : Z[p] * W[j] / P.fv(F[p], F[j]);
@@ -431,7 +431,7 @@ k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   __syncthreads();
   const int mn = min(M, N);
   double *G = h.Vg + (long long)node * h.vcap;
-  if (Rk < mn) {
+  if (Rk < (h.vp2 ? M : mn)) {
     for (int idx = tid; idx < Rk * M; idx += HT) {
       const int i = idx % Rk, c = idx / Rk, p = INV[c];
       G[idx] = (p < Rk) ? (p == i ? 1.0 : 0.0) : -W[i] * Z[p] / P.dd(PL[i], PL[p]);
@@ -554,7 +554,7 @@ static T *up(const char *name, const std::vector<T> &v, cudaStream_t st) {
 // Build the HSS generators on the device; on return the ranks are on the host.
 static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F, const double *u,
                          const double *v, const double *difl, const double *difr, cudaStream_t st,
-                         bool sq = false, double rho = 1.5) {
+                         bool sq = false, double rho = 1.5, bool vp2 = false) {
   int launches = 0;
   pl.t = make_tree(K, ni);
   const HostTree &t = pl.t;
@@ -562,7 +562,7 @@ static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F
   const int rmax = std::max(HSS_RMIN, t.mmax);
   HssDev &h = pl.h;
   h.FF = F; h.DIFL = difl; h.DIFR = difr; h.sq = sq;
-  h.K = K; h.ltr = ltr; h.rmax = rmax; h.rho = rho;
+  h.K = K; h.ltr = ltr; h.rmax = rmax; h.rho = rho; h.vp2 = vp2;
   h.U = pool<double>("hs_U", K); h.V = pool<double>("hs_V", K);
   h.PL = pool<int>("hs_PL", K); h.PU = pool<int>("hs_PU", K);
   h.Ut = pool<double>("hs_Ut", K); h.Vt = pool<double>("hs_Vt", K);
@@ -886,8 +886,9 @@ int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *
   HCK(cudaEventRecord(e0, st));
   k_cauchy_repr<<<(n + 255) / 256, 256, 0, st>>>(n, D, F, u, difl, difr, mu);
   HssPlan pl;
-  // the generic Cauchy module's swap threshold (rrluCauchy, CauchyHss_VP2.f90:70)
-  int launches = 1 + hss_construct(pl, n, ni, tol, F, v, mu, difl, difr, st, false, 1.02);
+  // the generic Cauchy module's swap threshold and full-rank rule (rrluCauchy,
+  // CauchyHss_VP2.f90:70; comprcauchy, :650)
+  int launches = 1 + hss_construct(pl, n, ni, tol, F, v, mu, difl, difr, st, false, 1.02, true);
   HCK(cudaEventRecord(e1, st));
   transpose(n, ncb, B, ldb, X, ncb, st);
   if (pl.ok) {

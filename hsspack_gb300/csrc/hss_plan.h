@@ -26,6 +26,11 @@ struct HssDev {
   bool sq;                         // singular-value mode (differences of squares)
   int K, ltr, rmax;
   double rho;                      // strong-swap threshold of the RRLU (1.5 eigen/SVD, 1.02 VP2)
+  // full-rank rule: false as ComprcauchyEig (an identity generator once the
+  // rank reaches min(M, N), CauchyHssEig.f90:2380); true as the generic
+  // module's comprcauchy (the interpolation generator whenever Rk < M,
+  // CauchyHss_VP2.f90:650)
+  bool vp2;
   // current compressed generators (row side: U, PL; column side: V, PU)
   double *U, *V;
   int *PL, *PU;

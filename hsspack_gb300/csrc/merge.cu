@@ -122,24 +122,45 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   const int seg = (((n + NW - 1) / NW) + 31) & ~31;
   const int w0 = min(n, wid * seg), w1 = min(n, w0 + seg);
   const unsigned below = (1u << lane) - 1u;  // lanes ahead of this one
+  // (position passes load four iterations ahead: the loads of one batch are
+  // in flight together instead of one latency per 32 positions)
+  constexpr int PB = 4;
   int cnt = 0;
-  for (int i0 = w0; i0 < w1; i0 += 32) {
-    const int i = i0 + lane;
-    const bool in = i < w1;
-    const bool big = in && rho * fabs(w.zs[s + i]) > tol;
-    if (in && !big) w.typ[s + i] = 4;  // deflated, small z
-    cnt += __popc(__ballot_sync(HSS_FULL, big));
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    double zv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      zv[b] = i < w1 ? w.zs[s + i] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool in = i < w1;
+      const bool big = in && rho * fabs(zv[b]) > tol;
+      if (in && !big) w.typ[s + i] = 4;  // deflated, small z
+      cnt += __popc(__ballot_sync(HSS_FULL, big));
+    }
   }
   unsigned long long tot;
   int pos = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)cnt : 0ull, &tot);
   pos = __shfl_sync(HSS_FULL, pos, 0);
   const int nc = (int)tot;
-  for (int i0 = w0; i0 < w1; i0 += 32) {
-    const int i = i0 + lane;
-    const bool big = i < w1 && w.typ[s + i] != 4;
-    const unsigned m = __ballot_sync(HSS_FULL, big);
-    if (big) w.cand[s + pos + __popc(m & below)] = i;
-    pos += __popc(m);
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    double zv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      zv[b] = i < w1 ? w.zs[s + i] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool big = i < w1 && rho * fabs(zv[b]) > tol;  // the test of the pass above
+      const unsigned m = __ballot_sync(HSS_FULL, big);
+      if (big) w.cand[s + pos + __popc(m & below)] = i;
+      pos += __popc(m);
+    }
   }
   __syncthreads();
   // ---- close poles deflate by Givens rotations (mdlaed2.f90:314-371).  The
@@ -155,7 +176,7 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   constexpr int NCS = 1536;
   __shared__ double c_z[NCS], c_d[NCS];
   __shared__ unsigned char c_t[NCS];
-  __shared__ int c_l[NCS];
+  __shared__ int c_l[NCS], c_l2[NCS];
   __shared__ int s_ng, s_nl;
   const bool in_smem = nc <= NCS;
   if (in_smem) {
@@ -258,13 +279,21 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   //      and deflated (slots, values) lists; same warp segments and ranks
   unsigned long long pk = 0;  // types 1, 2, 3 counted in 21-bit fields
   int n5 = 0;
-  for (int i0 = w0; i0 < w1; i0 += 32) {
-    const int i = i0 + lane;
-    const int t = i < w1 ? w.typ[s + i] : 0;
-    pk += (unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 1)) +
-          ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 2)) << 21) +
-          ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 3)) << 42);
-    n5 += __popc(__ballot_sync(HSS_FULL, t == 5));
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    int tv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      tv[b] = i < w1 ? w.typ[s + i] : 0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int t = tv[b];
+      pk += (unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 1)) +
+            ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 2)) << 21) +
+            ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 3)) << 42);
+      n5 += __popc(__ballot_sync(HSS_FULL, t == 5));
+    }
   }
   unsigned long long ptot, t5;
   unsigned long long pre = block_scan64<MT>(lane == 0 ? pk : 0ull, &ptot);
@@ -277,12 +306,25 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   const int nrot = (int)t5;
   int r1 = (int)(pre & 0x1fffff), r2 = (int)((pre >> 21) & 0x1fffff),
       r3 = (int)((pre >> 42) & 0x1fffff);
-  for (int i0 = w0; i0 < w1; i0 += 32) {
-    const int i = i0 + lane;
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    int tb[PB], sb[PB];
+    double db[PB], zb[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool in = i < w1;
+      tb[b] = in ? w.typ[s + i] : 0;
+      db[b] = in ? w.ds[s + i] : 0.0;
+      zb[b] = in ? w.zs[s + i] : 0.0;
+      sb[b] = in ? w.srt[s + i] : 0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+    const int i = i0 + 32 * b + lane;
     const bool in = i < w1;
-    const int t = in ? w.typ[s + i] : 0;
-    const double dv = in ? w.ds[s + i] : 0.0, zv = in ? w.zs[s + i] : 0.0;
-    const int sv = in ? w.srt[s + i] : 0;
+    const int t = tb[b];
+    const double dv = db[b], zv = zb[b];
+    const int sv = sb[b];
     const unsigned m1 = __ballot_sync(HSS_FULL, t == 1), m2 = __ballot_sync(HSS_FULL, t == 2),
                    m3 = __ballot_sync(HSS_FULL, t == 3), m5 = __ballot_sync(HSS_FULL, t == 5);
     if (in) {
@@ -307,18 +349,26 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
       }
     }
     r1 += __popc(m1); r2 += __popc(m2); r3 += __popc(m3); r5 += __popc(m5);
+    }
   }
   __syncthreads();
   // The small-z list is ascending; rotated poles moved inside their gap
   // (mdlaed2.f90:340-356 inserts them in order), so sort those and merge.
-  if (nrot > 1) block_sort_pairs(w.l2val + s, w.l2slot + s, w.ds + s, w.cand + s, nrot);
   const int n1l = (n - K) - nrot;
-  // the (short) rotated list in shared memory for the searches of the long one
+  // the (short) rotated list sorted in shared memory (the chain's arrays are
+  // free now) and kept there for the searches of the long one
   const bool l2s = nrot <= NCS;
   const double *l2 = l2s ? c_z : w.l2val + s;
   if (l2s) {
-    for (int i = tid; i < nrot; i += MT) c_z[i] = w.l2val[s + i];
+    for (int i = tid; i < nrot; i += MT) { c_z[i] = w.l2val[s + i]; c_l[i] = w.l2slot[s + i]; }
     __syncthreads();
+    if (nrot > 1) {
+      block_sort_pairs(c_z, c_l, c_d, c_l2, nrot);
+      for (int i = tid; i < nrot; i += MT) { w.l2val[s + i] = c_z[i]; w.l2slot[s + i] = c_l[i]; }
+      __syncthreads();
+    }
+  } else if (nrot > 1) {
+    block_sort_pairs(w.l2val + s, w.l2slot + s, w.ds + s, w.cand + s, nrot);
   }
   for (int i = tid; i < n1l; i += MT) {  // L1 element: count L2 < v
     const double v = w.l1val[s + i];
