@@ -91,91 +91,27 @@ k_gemm_f64(int nprob, const GemmDesc *__restrict__ probs) {
 
 int gemm_tiles(int M, int N) { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN); }
 
-// Small products (N, K <= 128: the lowest DC levels and the products the
-// tensor cores do not take): 32 x 32 output tiles, 64 threads with a 4 x 4
-// register tile each, 32-deep inner slices double-buffered in shared memory
-// (a 64 x 64 tile would be mostly empty for M or N of 16 .. 64).  Problems and
-// their tiles are flattened; a CTA finds its problem by binary search on the
-// tile prefix, once.  FP64 FMA bound: 16 FMAs per 8 shared-memory loads.
-constexpr int SM_T = 32, SK = 32, ST = 64;
-
-int gemm_small_tiles(int M, int N) { return ((M + SM_T - 1) / SM_T) * ((N + SM_T - 1) / SM_T); }
-
-__global__ void __launch_bounds__(ST)
-k_gemm_small(int nprob, const GemmDesc *__restrict__ probs) {
-  __shared__ double As[2][SK][SM_T + 1];
-  __shared__ double Bs[2][SK][SM_T + 1];
+// Small products (N, K <= 32: the lowest DC levels): one thread per output
+// element, the K-term dot product from L1 (a 64 x 64 tile would be mostly
+// empty).  Problem p owns outputs [eoff[p], eoff[p+1]).
+__global__ void __launch_bounds__(256)
+k_gemm_small(int nprob, const GemmDesc *__restrict__ probs, const long long *__restrict__ eoff) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= eoff[nprob]) return;
   int lo = 0, hi = nprob;
-  const int b = blockIdx.x;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (probs[mid].tile0 <= b) lo = mid; else hi = mid;
-  }
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (eoff[mid] <= idx) lo = mid; else hi = mid; }
   const GemmDesc P = probs[lo];
-  const int t = b - P.tile0;
-  const int tm = (P.M + SM_T - 1) / SM_T;
-  const int m0 = (t % tm) * SM_T, n0 = (t / tm) * SM_T;
-  const int tid = threadIdx.x;
-  const int tx = tid & 7, ty = tid >> 3;  // rows tx*4 .. tx*4+3, columns ty*4 .. ty*4+3
-  double acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-  const int nk = (P.K + SK - 1) / SK;
-  auto load = [&](int buf, int kb) {
-    const int k0 = kb * SK;
-#pragma unroll
-    for (int r = 0; r < (SM_T * SK) / ST; ++r) {  // A: row fastest (coalesced columns)
-      const int idx = tid + r * ST;
-      const int row = idx % SM_T, kk = idx / SM_T;
-      const int gr = m0 + row, gk = k0 + kk;
-      As[buf][kk][row] = (gr < P.M && gk < P.K) ? __ldg(P.A + (long long)gk * P.lda + gr) : 0.0;
-    }
-#pragma unroll
-    for (int r = 0; r < (SM_T * SK) / ST; ++r) {  // B: inner index fastest
-      const int idx = tid + r * ST;
-      const int kk = idx % SK, col = idx / SK;
-      const int gk = k0 + kk, gc = n0 + col;
-      Bs[buf][kk][col] = (gk < P.K && gc < P.N) ? __ldg(P.B + (long long)gc * P.ldb + gk) : 0.0;
-    }
-  };
-  if (nk > 0) load(0, 0);
-  __syncthreads();
-  for (int kb = 0; kb < nk; ++kb) {
-    const int cur = kb & 1;
-    if (kb + 1 < nk) load(cur ^ 1, kb + 1);
-    // slices past K hold zeros: run to the next multiple of 4
-    const int kend = (min(SK, P.K - kb * SK) + 3) & ~3;
-#pragma unroll 4
-    for (int kk = 0; kk < kend; ++kk) {
-      double a[4], bb[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[cur][kk][tx * 4 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) bb[j] = Bs[cur][kk][ty * 4 + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int gc = n0 + ty * 4 + j;
-    if (gc >= P.N) continue;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int gr = m0 + tx * 4 + i;
-      if (gr >= P.M) continue;
-      double *c = P.C + (long long)gc * P.ldc + gr;
-      *c = P.beta ? *c + acc[i][j] : acc[i][j];
-    }
-  }
+  const long long e = idx - eoff[lo];
+  const int i = (int)(e % P.M), j = (int)(e / P.M);
+  const double *a = P.A + i, *b = P.B + (long long)j * P.ldb;
+  double acc = 0.0;
+  for (int k = 0; k < P.K; ++k) acc = fma(__ldg(a + (long long)k * P.lda), __ldg(b + k), acc);
+  double *c = P.C + (long long)j * P.ldc + i;
+  *c = P.beta ? *c + acc : acc;
 }
 
-// largest N and K taken by the 32 x 32 tile kernel (hss_config.small_nk; 0: 128)
+// largest N and K taken by the element kernel (hss_config.small_nk; 0: 128,
+// measured faster than 64 x 64 FP64 tiles for the DC merges' K <= 128)
 static int g_small_nk = 128;
 void set_small_nk(int v) { g_small_nk = v > 0 ? v : 128; }
 
@@ -200,7 +136,7 @@ void launch_gemm(const std::vector<GemmDesc> &probs, int precision, cudaStream_t
   if (probs.empty()) return;
   // one pass: tensor-core splitting pays off once a product has enough MACs
   // per operand byte (precision 1); the rest stay on the FP64 pipe, small
-  // ones (N, K <= g_small_nk) in 32 x 32 tiles, others in 64 x 64 tiles
+  // ones (N, K <= g_small_nk) by the element kernel, others by 64 x 64 tiles
   const double big_macs = ldexp(1.0, g_split_log2);
   std::vector<GemmDesc> big, tiny, tiled;
   tiny.reserve(probs.size());
@@ -215,11 +151,15 @@ void launch_gemm(const std::vector<GemmDesc> &probs, int precision, cudaStream_t
     else launch_gemm_split(big, err, st);
   }
   if (!tiny.empty()) {
-    long long tiles = 0;
-    for (auto &p : tiny) { p.tile0 = (int)tiles; tiles += gemm_small_tiles(p.M, p.N); }
+    std::vector<long long> eoff(tiny.size() + 1);
+    eoff[0] = 0;
+    for (size_t i = 0; i < tiny.size(); ++i) eoff[i + 1] = eoff[i] + (long long)tiny[i].M * tiny[i].N;
     GemmDesc *d = pool<GemmDesc>("gemm_small_probs", tiny.size());
+    long long *de = pool<long long>("gemm_small_eoff", eoff.size());
     stage_h2d(d, tiny.data(), tiny.size() * sizeof(GemmDesc), st);
-    if (tiles > 0) k_gemm_small<<<(unsigned)tiles, ST, 0, st>>>((int)tiny.size(), d);
+    stage_h2d(de, eoff.data(), eoff.size() * sizeof(long long), st);
+    if (eoff.back() > 0)
+      k_gemm_small<<<(unsigned)((eoff.back() + 255) / 256), 256, 0, st>>>((int)tiny.size(), d, de);
   }
   if (tiled.empty()) return;
   int tiles = 0;
