@@ -185,6 +185,12 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq,
   }
 }
 
+// a / b within 1.5 ulp through the one-ulp reciprocal (four FP64 instructions
+// instead of a correctly rounded divide): the step of one root runs on one lane
+// but takes a whole warp's FP64 issue slots, so its divides matter.  b = 0
+// gives NaN, which fails every bracket test below and falls back to bisection.
+__device__ __forceinline__ double qdiv(double a, double b) { return a * rcp_nr(b); }
+
 // Consume one evaluation at (o, tau).
 __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   if (r.phase == 2) return;
@@ -257,10 +263,10 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   if (!r.fw) {  // middle way: each side's sum on its own pole
     c = w - gl * s.dpsi - gr * s.dphi;
   } else if (r.oi == r.j) {  // fixed weight: origin pole exact, the rest on the other
-    const double q = (__ldg(r.z + r.jl) / gl) * (__ldg(r.z + r.jl) / gl);
+    const double t = qdiv(__ldg(r.z + r.jl), gl), q = t * t;
     c = w - gr * dw - (gl - gr) * q;
   } else {
-    const double q = (__ldg(r.z + r.jr) / gr) * (__ldg(r.z + r.jr) / gr);
+    const double t = qdiv(__ldg(r.z + r.jr), gr), q = t * t;
     c = w - gl * dw - (gr - gl) * q;
   }
   double eta;
@@ -273,16 +279,16 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
     } else {
       double disc = a * a - 4.0 * b * c;
       if (disc < 0.0) disc = 0.0;
-      eta = (a >= 0.0) ? (a + sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a - sqrt(disc));
+      eta = (a >= 0.0) ? qdiv(a + sqrt(disc), 2.0 * c) : qdiv(2.0 * b, a - sqrt(disc));
     }
   } else if (c == 0.0) {
-    eta = (a != 0.0) ? b / a : -w / dw;
+    eta = (a != 0.0) ? qdiv(b, a) : -qdiv(w, dw);
   } else {  // the root between the two poles
     double disc = a * a - 4.0 * b * c;
     if (disc < 0.0) disc = 0.0;
-    eta = (a <= 0.0) ? (a - sqrt(disc)) / (2.0 * c) : (2.0 * b) / (a + sqrt(disc));
+    eta = (a <= 0.0) ? qdiv(a - sqrt(disc), 2.0 * c) : qdiv(2.0 * b, a + sqrt(disc));
   }
-  if (w * eta >= 0.0) eta = -w / dw;  // model went the wrong way: Newton step
+  if (w * eta >= 0.0) eta = -qdiv(w, dw);  // model went the wrong way: Newton step
   double tn = r.tau + eta;
   const bool bisect = !(tn > r.lo && tn < r.hi);
   if (bisect) {
@@ -309,7 +315,7 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   // distance to the origin pole, and at most 100 x the square of the
   // previous relative step): the new iterate's error is below 1e-18 of that
   // distance, so it is final without another evaluation.
-  const double rel = fabs(step) / fmax(fabs(r.tau), 1e-300);
+  const double rel = qdiv(fabs(step), fmax(fabs(r.tau), 1e-300));
   if (!bisect && r.prel >= 0.0 && rel <= 1e-10 && rel <= 100.0 * r.prel * r.prel) {
     r.phase = 2;
     return;
