@@ -110,7 +110,10 @@ __device__ __forceinline__ double warp_prod(double v) {
 }
 
 // Structured strong RRLU of one node (row or column case).  Node side (length
-// M) in shared memory, other side (length N) in global scratch.
+// M) in shared memory, other side (length N) in global scratch.  The scans and
+// generator updates over the N other-side entries are FP64-pipe bound, so their
+// divides go through qdiv (within 1.5 ulp); the pivot values and the generator
+// entries written out use correctly rounded divides.
 //   ROW:  C(i,j) = A_i V_j / (F_{PL_i} - lam_{PU_j})
 //   COL:  C(i,j) = A_i V_j / (lam_{PL_i} - F_{PU_j})
 // Returns Rk; on exit A/PL/F are permuted, Z holds the Schur row generators,
@@ -137,7 +140,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
   auto colmax = [&](int k) -> int {
     ArgMax a{-1.0, INT_MAX};
     for (int i = k + tid; i < M; i += HT) {
-      const double t = fabs(Z[i] / den(PL[i], PU[k]));
+      const double t = fabs(qdiv(Z[i], den(PL[i], PU[k])));
       if (t > a.v) { a.v = t; a.i = i; }
     }
     a = block_argmax(a, red);
@@ -146,7 +149,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
   auto colmax_v = [&](int k, int &arg) -> double {
     ArgMax a{-1.0, INT_MAX};
     for (int i = k + tid; i < M; i += HT) {
-      const double t = fabs(Z[i] / den(PL[i], PU[k]));
+      const double t = fabs(qdiv(Z[i], den(PL[i], PU[k])));
       if (t > a.v) { a.v = t; a.i = i; }
     }
     a = block_argmax(a, red);
@@ -156,7 +159,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
   auto rowmax_v = [&](int k, int &arg) -> double {
     ArgMax a{-1.0, INT_MAX};
     for (int j = k + tid; j < N; j += HT) {
-      const double t = fabs(V[j] / den(PL[k], PU[j]));
+      const double t = fabs(qdiv(V[j], den(PL[k], PU[j])));
       if (t > a.v) { a.v = t; a.i = j; }
     }
     a = block_argmax(a, red);
@@ -224,7 +227,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
         double cm = -1.0;
         int a = k;
         for (int i = k; i < M; ++i) {
-          const double t = fabs(Z[i] / den(PL[i], PU[j]));
+          const double t = fabs(qdiv(Z[i], den(PL[i], PU[j])));
           if (t > cm) { cm = t; a = i; }
         }
         const double t = fabs(cm * V[j]);
@@ -247,12 +250,13 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
     // Schur-complement generator updates
     const double Fk = ROW ? F[k] : 0.0;
     for (int j = k + 1 + tid; j < M; j += HT)
-      Z[j] *= rowdiff(j, k) / den(PL[j], PU[k]);
+      Z[j] *= qdiv(rowdiff(j, k), den(PL[j], PU[k]));
     for (int j = k + 1 + tid; j < N; j += HT)
-      V[j] *= ROW ? P.dd(PU[j], PU[k]) / (-P.fd(PL[k], PU[j]))
-                  : P.fv(__ldg(P.F + PU[j]), __ldg(P.F + PU[k])) / P.fd(PU[j], PL[k]);
+      V[j] *= ROW ? qdiv(P.dd(PU[j], PU[k]), -P.fd(PL[k], PU[j]))
+                  : qdiv(P.fv(__ldg(P.F + PU[j]), __ldg(P.F + PU[k])), P.fd(PU[j], PL[k]));
     for (int j = tid; j < k; j += HT)
-      W[j] *= ROW ? (-P.fd(PL[j], PU[k])) / P.fv(Fk, F[j]) : P.fd(PU[k], PL[j]) / P.dd(PL[k], PL[j]);
+      W[j] *= ROW ? qdiv(-P.fd(PL[j], PU[k]), P.fv(Fk, F[j]))
+                  : qdiv(P.fd(PU[k], PL[j]), P.dd(PL[k], PL[j]));
     if (tid < 32) {  // W[k] = den(k,k)/A[k] * prod_{j<k} ...
       double pr = 1.0;
       for (int j = tid; j < k; j += 32)
@@ -272,7 +276,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
           double cm = -1.0;
           int a = k + 1;
           for (int i = k + 1; i < M; ++i) {
-            const double t = fabs(Z[i] / rowdiff(i, j));
+            const double t = fabs(qdiv(Z[i], rowdiff(i, j)));
             if (t > cm) { cm = t; a = i; }
           }
           const double t = cm * fabs(W[j]);
@@ -288,8 +292,8 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
         if (!(r.v > rho) || jj >= M) break;
         if (tid == 0) atomicAdd(nswap, 1);
         for (int j = k + 1 + tid; j < N; j += HT)
-          V[j] *= ROW ? (-P.fd(PL[ii], PU[j])) / (-P.fd(PL[jj], PU[j]))
-                      : P.fd(PU[j], PL[ii]) / P.fd(PU[j], PL[jj]);
+          V[j] *= ROW ? qdiv(-P.fd(PL[ii], PU[j]), -P.fd(PL[jj], PU[j]))
+                      : qdiv(P.fd(PU[j], PL[ii]), P.fd(PU[j], PL[jj]));
         double ujj = 0.0, wii = 0.0;
         if (tid < 32) {
           double pu = 1.0, pw = 1.0;

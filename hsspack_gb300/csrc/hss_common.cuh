@@ -38,6 +38,10 @@ __device__ __forceinline__ double rcp_nr(double x) {
   return fma(y, fma(e, e, e), y);
 }
 
+// a / b within 1.5 ulp through rcp_nr (four FP64 instructions instead of a
+// correctly rounded divide) for the FP64-pipe bound loops; b = 0 gives NaN.
+__device__ __forceinline__ double qdiv(double a, double b) { return a * rcp_nr(b); }
+
 // (value, index) argmax with "first index wins" ties -- Fortran MAXLOC order.
 struct ArgMax {
   double v;

@@ -185,12 +185,9 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq,
   }
 }
 
-// a / b within 1.5 ulp through the one-ulp reciprocal (four FP64 instructions
-// instead of a correctly rounded divide): the step of one root runs on one lane
-// but takes a whole warp's FP64 issue slots, so its divides matter.  b = 0
-// gives NaN, which fails every bracket test below and falls back to bisection.
-__device__ __forceinline__ double qdiv(double a, double b) { return a * rcp_nr(b); }
-
+// The step of one root runs on one lane but takes a whole warp's FP64 issue
+// slots, so its divides go through qdiv; a zero denominator gives NaN, which
+// fails every bracket test below and falls back to bisection.
 // Consume one evaluation at (o, tau).
 __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   if (r.phase == 2) return;
