@@ -23,6 +23,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "hss_common.cuh"
 #include "hss_gemm.h"
 #include "hss_hss.h"
@@ -32,6 +34,8 @@
 #include "../../include/hsspack_gb300.h"
 
 namespace hss {
+
+namespace cg = cooperative_groups;
 
 #define HCK(x)                                                                              \
   do {                                                                                      \
@@ -109,6 +113,42 @@ __device__ __forceinline__ double warp_prod(double v) {
   return v;
 }
 
+// ---- cluster cooperation of one node's RRLU --------------------------------
+// A node's RRLU may run on a cluster of G CTAs (G = 1, 2, 4, 8): every CTA holds
+// the same node-side arrays in its shared memory and repeats the node-side work
+// identically; the other-side positions (the long side, up to K) are split
+// between the CTAs, their partial argmaxes combined through distributed shared
+// memory, and swaps of other-side entries done by rank 0 between cluster
+// barriers.  Other-side entries are read through L2 (ld.global.cg) so that a
+// CTA never sees a stale L1 copy of an entry another CTA of the cluster wrote.
+struct ArgMax3 {
+  double v;
+  int i;  // position (first wins on ties)
+  int a;  // auxiliary index carried with the winner
+};
+
+__device__ __forceinline__ void csync(int G) {
+  if (G > 1) cg::this_cluster().sync();
+  else __syncthreads();
+}
+
+// the cluster-wide best of each CTA's (value, position, aux), identical in every
+// CTA; slot: two shared slots used alternately (a slot is rewritten only after
+// the next cluster barrier, by which time every CTA has read it)
+__device__ __forceinline__ ArgMax3 cluster_best(ArgMax3 x, int G, ArgMax3 *slot, int &phase) {
+  if (G == 1) return x;
+  cg::cluster_group cl = cg::this_cluster();
+  if (threadIdx.x == 0) slot[phase] = x;
+  cl.sync();
+  ArgMax3 r{-1.0, INT_MAX, 0};
+  for (int q = 0; q < G; ++q) {
+    const ArgMax3 y = *cl.map_shared_rank(slot + phase, q);
+    if (y.v > r.v || (y.v == r.v && y.i < r.i)) r = y;
+  }
+  phase ^= 1;
+  return r;
+}
+
 // Structured strong RRLU of one node (row or column case).  Node side (length
 // M) in shared memory, other side (length N) in global scratch.  The scans and
 // generator updates over the N other-side entries are FP64-pipe bound, so their
@@ -118,13 +158,19 @@ __device__ __forceinline__ double warp_prod(double v) {
 //   COL:  C(i,j) = A_i V_j / (lam_{PL_i} - F_{PU_j})
 // Returns Rk; on exit A/PL/F are permuted, Z holds the Schur row generators,
 // W the column generators of the interpolation block, PQ the row permutation.
+// G, crank: the cluster size and this CTA's rank in it (1, 0 without a cluster).
 template <bool ROW>
 __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, double *W, int *PL,
                          int *PQ, double *V, int *PU, int M, int N, double tol, int rmax,
-                         int *overflow, int *nswap, double rho) {
+                         int *overflow, int *nswap, double rho, int G, int crank) {
   __shared__ ArgMax red[HT / 32];
+  __shared__ ArgMax3 cslot[2];
   __shared__ int s_rk;
+  int cphase = 0;
   const int tid = threadIdx.x;
+  const int jstep = G * HT, joff = crank * HT;  // this CTA's share of the other side
+  auto Vr = [&](int j) -> double { return __ldcg(V + j); };
+  auto PUr = [&](int j) -> int { return __ldcg(PU + j); };
   // row poles: ROW -> F values (old poles); COL -> lam values (index PL)
   auto den = [&](int pl, int pu) -> double {  // C denominator for pole indices
     return ROW ? P.fd(pl, pu) : -P.fd(pu, pl);
@@ -139,8 +185,9 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
   double Amax = 0.0;
   auto colmax = [&](int k) -> int {
     ArgMax a{-1.0, INT_MAX};
+    const int puk = PUr(k);
     for (int i = k + tid; i < M; i += HT) {
-      const double t = fabs(qdiv(Z[i], den(PL[i], PU[k])));
+      const double t = fabs(qdiv(Z[i], den(PL[i], puk)));
       if (t > a.v) { a.v = t; a.i = i; }
     }
     a = block_argmax(a, red);
@@ -148,8 +195,9 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
   };
   auto colmax_v = [&](int k, int &arg) -> double {
     ArgMax a{-1.0, INT_MAX};
+    const int puk = PUr(k);
     for (int i = k + tid; i < M; i += HT) {
-      const double t = fabs(qdiv(Z[i], den(PL[i], PU[k])));
+      const double t = fabs(qdiv(Z[i], den(PL[i], puk)));
       if (t > a.v) { a.v = t; a.i = i; }
     }
     a = block_argmax(a, red);
@@ -158,13 +206,14 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
   };
   auto rowmax_v = [&](int k, int &arg) -> double {
     ArgMax a{-1.0, INT_MAX};
-    for (int j = k + tid; j < N; j += HT) {
-      const double t = fabs(qdiv(V[j], den(PL[k], PU[j])));
+    for (int j = k + joff + tid; j < N; j += jstep) {
+      const double t = fabs(qdiv(Vr(j), den(PL[k], PUr(j))));
       if (t > a.v) { a.v = t; a.i = j; }
     }
     a = block_argmax(a, red);
-    arg = a.i == INT_MAX ? k : a.i;
-    return a.v;
+    const ArgMax3 c = cluster_best(ArgMax3{a.v, a.i, 0}, G, cslot, cphase);
+    arg = c.i == INT_MAX ? k : c.i;
+    return c.v;
   };
   auto swap_row = [&](int a, int b) {
     __syncthreads();
@@ -179,17 +228,17 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
     __syncthreads();
   };
   auto swap_col = [&](int a, int b) {
-    __syncthreads();
-    if (tid == 0 && a != b) {
-      double t = V[a]; V[a] = V[b]; V[b] = t;
-      int ti = PU[a]; PU[a] = PU[b]; PU[b] = ti;
+    csync(G);
+    if (crank == 0 && tid == 0 && a != b) {
+      const double t = Vr(a); V[a] = Vr(b); V[b] = t;
+      const int ti = PUr(a); PU[a] = PUr(b); PU[b] = ti;
     }
-    __syncthreads();
+    csync(G);
   };
   int Rk = mn;
   for (int k = 0; k < mn; ++k) {
     if (k >= rmax) {  // would exceed the generator capacity
-      if (tid == 0) atomicOr(overflow, 1);
+      if (tid == 0 && crank == 0) atomicOr(overflow, 1);
       Rk = k;
       break;
     }
@@ -197,9 +246,9 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
       int jl, ju;
       double jkL = colmax_v(k, jl);
       double jkU = rowmax_v(k, ju);
-      jkL *= fabs(V[k]);
+      jkL *= fabs(Vr(k));
       jkU *= fabs(Z[k]);
-      const double piv = fabs(Z[k] * V[k] / den(PL[k], PU[k]));
+      const double piv = fabs(Z[k] * Vr(k) / den(PL[k], PUr(k)));
       if (!(jkL <= piv && jkU <= piv)) {
         bool fromcol = jkL > jkU;
         for (int guard = 0; guard < 4 * (M + N) + 8; ++guard) {
@@ -217,54 +266,61 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
       }
     }
     __syncthreads();
-    double Ukk = Z[k] * V[k] / den(PL[k], PU[k]);
+    double Ukk = Z[k] * Vr(k) / den(PL[k], PUr(k));
     Amax = fmax(Amax, fabs(Ukk));
     if (fabs(Ukk) < tol * Amax) {
       // complete pivoting over the Schur complement (CauchyPivtEig_CP)
       ArgMax best{-1.0, INT_MAX};
       int bi_loc = k;
-      for (int j = k + tid; j < N; j += HT) {
+      for (int j = k + joff + tid; j < N; j += jstep) {
         double cm = -1.0;
         int a = k;
+        const int puj = PUr(j);
         for (int i = k; i < M; ++i) {
-          const double t = fabs(qdiv(Z[i], den(PL[i], PU[j])));
+          const double t = fabs(qdiv(Z[i], den(PL[i], puj)));
           if (t > cm) { cm = t; a = i; }
         }
-        const double t = fabs(cm * V[j]);
+        const double t = fabs(cm * Vr(j));
         if (t > best.v) { best.v = t; best.i = j; bi_loc = a; }
       }
       __shared__ int s_bi;
       ArgMax r = block_argmax(best, red);
-      const int bj = r.i == INT_MAX ? k : r.i;
       if (tid == 0 && r.i == INT_MAX) s_bi = k;
       __syncthreads();
       if (r.i != INT_MAX && best.i == r.i && best.v == r.v) s_bi = bi_loc;
       __syncthreads();
-      const int bi = s_bi;
+      const ArgMax3 c = cluster_best(ArgMax3{r.v, r.i, s_bi}, G, cslot, cphase);
+      const int bj = c.i == INT_MAX ? k : c.i;
+      const int bi = c.i == INT_MAX ? k : c.a;
       swap_row(k, bi);
       swap_col(k, bj);
-      Ukk = Z[k] * V[k] / den(PL[k], PU[k]);
+      Ukk = Z[k] * Vr(k) / den(PL[k], PUr(k));
       Amax = fmax(Amax, fabs(Ukk));
       if (fabs(Ukk) < tol * Amax) { Rk = k; break; }
     }
     // Schur-complement generator updates
     const double Fk = ROW ? F[k] : 0.0;
+    const int puk = PUr(k);
     for (int j = k + 1 + tid; j < M; j += HT)
-      Z[j] *= qdiv(rowdiff(j, k), den(PL[j], PU[k]));
-    for (int j = k + 1 + tid; j < N; j += HT)
-      V[j] *= ROW ? qdiv(P.dd(PU[j], PU[k]), -P.fd(PL[k], PU[j]))
-                  : qdiv(P.fv(__ldg(P.F + PU[j]), __ldg(P.F + PU[k])), P.fd(PU[j], PL[k]));
+      Z[j] *= qdiv(rowdiff(j, k), den(PL[j], puk));
+    for (int j = k + 1 + joff + tid; j < N; j += jstep) {
+      const int puj = PUr(j);
+      V[j] = Vr(j) * (ROW ? qdiv(P.dd(puj, puk), -P.fd(PL[k], puj))
+                          : qdiv(P.fv(__ldg(P.F + puj), __ldg(P.F + puk)), P.fd(puj, PL[k])));
+    }
     for (int j = tid; j < k; j += HT)
-      W[j] *= ROW ? qdiv(-P.fd(PL[j], PU[k]), P.fv(Fk, F[j]))
-                  : qdiv(P.fd(PU[k], PL[j]), P.dd(PL[k], PL[j]));
+      W[j] *= ROW ? qdiv(-P.fd(PL[j], puk), P.fv(Fk, F[j]))
+                  : qdiv(P.fd(puk, PL[j]), P.dd(PL[k], PL[j]));
     if (tid < 32) {  // W[k] = den(k,k)/A[k] * prod_{j<k} ...
       double pr = 1.0;
-      for (int j = tid; j < k; j += 32)
-        pr *= ROW ? (-P.fd(PL[k], PU[j])) / P.fv(F[j], Fk) : P.fd(PU[j], PL[k]) / P.dd(PL[j], PL[k]);
+      for (int j = tid; j < k; j += 32) {
+        const int puj = PUr(j);
+        pr *= ROW ? (-P.fd(PL[k], puj)) / P.fv(F[j], Fk) : P.fd(puj, PL[k]) / P.dd(PL[j], PL[k]);
+      }
       pr = warp_prod(pr);
-      if (tid == 0) W[k] = (den(PL[k], PU[k]) / A[k]) * pr;
+      if (tid == 0) W[k] = (den(PL[k], puk) / A[k]) * pr;
     }
-    __syncthreads();
+    csync(G);  // every CTA reads the updated V[k+1] next
     // strong swaps every 10 steps when an interpolation entry exceeds rho
     // (searchMax2Eig[m] with rho = 1.5, CauchyHssEig.f90:98-99; searchMax2 with
     // rho = 1.02 for generic Cauchy matrices, CauchyHss_VP2.f90:70-71)
@@ -290,27 +346,31 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
         __syncthreads();
         const int ii = r.i == INT_MAX ? 0 : r.i, jj = s_jj;
         if (!(r.v > rho) || jj >= M) break;
-        if (tid == 0) atomicAdd(nswap, 1);
-        for (int j = k + 1 + tid; j < N; j += HT)
-          V[j] *= ROW ? qdiv(-P.fd(PL[ii], PU[j]), -P.fd(PL[jj], PU[j]))
-                      : qdiv(P.fd(PU[j], PL[ii]), P.fd(PU[j], PL[jj]));
+        if (tid == 0 && crank == 0) atomicAdd(nswap, 1);
+        for (int j = k + 1 + joff + tid; j < N; j += jstep) {
+          const int puj = PUr(j);
+          V[j] = Vr(j) * (ROW ? qdiv(-P.fd(PL[ii], puj), -P.fd(PL[jj], puj))
+                              : qdiv(P.fd(puj, PL[ii]), P.fd(puj, PL[jj])));
+        }
         double ujj = 0.0, wii = 0.0;
         if (tid < 32) {
           double pu = 1.0, pw = 1.0;
           for (int j = tid; j <= k; j += 32) {
             if (j == ii) continue;
+            const int puj = PUr(j);
             if (ROW) {
-              pu *= P.fv(F[ii], F[j]) / P.fd(PL[ii], PU[j]);
-              pw *= (-P.fd(PL[jj], PU[j])) / P.fv(F[j], F[jj]);
+              pu *= P.fv(F[ii], F[j]) / P.fd(PL[ii], puj);
+              pw *= (-P.fd(PL[jj], puj)) / P.fv(F[j], F[jj]);
             } else {
-              pu *= P.dd(PL[ii], PL[j]) / (-P.fd(PU[j], PL[ii]));
-              pw *= P.fd(PU[j], PL[jj]) / P.dd(PL[j], PL[jj]);
+              pu *= P.dd(PL[ii], PL[j]) / (-P.fd(puj, PL[ii]));
+              pw *= P.fd(puj, PL[jj]) / P.dd(PL[j], PL[jj]);
             }
           }
           pu = warp_prod(pu);
           pw = warp_prod(pw);
-          ujj = A[ii] * (rowdiff(ii, jj) / den(PL[ii], PU[ii])) * pu;
-          wii = (ROW ? P.fd(PL[jj], PU[ii]) : -P.fd(PU[ii], PL[jj])) / A[jj] * pw;
+          const int puii = PUr(ii);
+          ujj = A[ii] * (rowdiff(ii, jj) / den(PL[ii], puii)) * pu;
+          wii = (ROW ? P.fd(PL[jj], puii) : -P.fd(puii, PL[jj])) / A[jj] * pw;
         }
         __syncthreads();
         // Z, W updates use the pre-swap poles
@@ -340,8 +400,11 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
         }
         __syncthreads();
       }
+      csync(G);  // the swaps' other-side updates before the next step's scans
     }
   }
+  // no CTA leaves while another may still read its shared slots
+  if (G > 1) csync(G);
   return Rk;
 }
 
@@ -350,10 +413,11 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
 constexpr int MMAXS = 512;  // max rows of a node handled in shared memory
 
 __global__ void __launch_bounds__(HT)
-k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
+k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol, int csz) {
   __shared__ double F[MMAXS], A[MMAXS], Z[MMAXS], W[MMAXS];
   __shared__ int PL[MMAXS], PQ[MMAXS], INV[MMAXS];
-  const int a = blockIdx.x;
+  const int a = blockIdx.x / csz;  // the node; a cluster of G CTAs shares it
+  const int crank = csz > 1 ? (int)cg::this_cluster().block_rank() : 0;
   if (a >= nn) return;
   const int node = nodes[a];
   const int tid = threadIdx.x;
@@ -363,7 +427,7 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   if (M > MMAXS) { if (tid == 0) atomicOr(h.flag, 2); return; }
   double *V = h.oval + (long long)a * h.K;
   int *PU = h.oidx + (long long)a * h.K;
-  for (int j = tid; j < lca; j += HT) {
+  for (int j = crank * HT + tid; j < lca; j += csz * HT) {  // this CTA's share of the copy
     if (j < c0) { V[j] = h.V[j]; PU[j] = h.PU[j]; }
     else if (j > h.lc1[node]) { V[j - nc] = h.V[j]; PU[j - nc] = h.PU[j]; }
   }
@@ -373,10 +437,11 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
     F[i] = h.FF[PL[i]];
     W[i] = 0.0;
   }
-  __syncthreads();
+  csync(csz);
   PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
   int Rk = rrlu_node<true>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1,
-                           h.rho);
+                           h.rho, csz, crank);
+  if (crank != 0) return;  // rank 0 writes the node's results
   __syncthreads();
   for (int i = tid; i < M; i += HT) { h.U[r0 + i] = A[i]; h.PL[r0 + i] = PL[i]; INV[PQ[i]] = i; }
   __syncthreads();
@@ -403,10 +468,11 @@ k_hss_rows(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
 // (ComprcauchyEig 'c', :2382-2430).  The transposed block has the node's
 // roots as row poles.
 __global__ void __launch_bounds__(HT)
-k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
+k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol, int csz) {
   __shared__ double F[MMAXS], A[MMAXS], Z[MMAXS], W[MMAXS];
   __shared__ int PL[MMAXS], PQ[MMAXS], INV[MMAXS];
-  const int a = blockIdx.x;
+  const int a = blockIdx.x / csz;  // the node; a cluster of G CTAs shares it
+  const int crank = csz > 1 ? (int)cg::this_cluster().block_rank() : 0;
   if (a >= nn) return;
   const int node = nodes[a];
   const int tid = threadIdx.x;
@@ -416,7 +482,7 @@ k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
   if (M > MMAXS) { if (tid == 0) atomicOr(h.flag, 2); return; }
   double *V = h.oval + (long long)a * h.K;
   int *PU = h.oidx + (long long)a * h.K;
-  for (int j = tid; j < lda; j += HT) {
+  for (int j = crank * HT + tid; j < lda; j += csz * HT) {  // this CTA's share of the copy
     if (j < r0) { V[j] = h.U[j]; PU[j] = h.PL[j]; }
     else if (j > h.lr1[node]) { V[j - nr] = h.U[j]; PU[j - nr] = h.PL[j]; }
   }
@@ -426,10 +492,11 @@ k_hss_cols(HssDev h, const int *__restrict__ nodes, int nn, double tol) {
     F[i] = 0.0;
     W[i] = 0.0;
   }
-  __syncthreads();
+  csync(csz);
   PoleDiff P{h.FF, h.DIFL, h.DIFR, h.sq};
   int Rk = rrlu_node<false>(P, F, A, Z, W, PL, PQ, V, PU, M, N, tol, h.rmax, h.flag, h.flag + 1,
-                            h.rho);
+                            h.rho, csz, crank);
+  if (crank != 0) return;  // rank 0 writes the node's results
   __syncthreads();
   for (int i = tid; i < M; i += HT) { h.V[c0 + i] = A[i]; h.PU[c0 + i] = PL[i]; INV[PQ[i]] = i; }
   __syncthreads();
@@ -548,6 +615,38 @@ __global__ void k_init_gens(int K, const double *__restrict__ u, const double *_
 }
 
 // --------------------------------------------------------------- host ----
+// CTAs per node of a level (a thread-block cluster): doubled while the level
+// stays within HSS_CLUSTER_CTAS CTAs, up to a portable cluster of 8.  Levels of
+// 8 nodes or fewer run one CTA per node: their other side (the skeletons of the
+// remaining nodes) is short, and the cluster barriers of every pivot step cost
+// more than the split scans save (measured on the 8192-point Cauchy merge).
+constexpr int HSS_CLUSTER_MAX = 8;
+constexpr int HSS_CLUSTER_CTAS = 304;  // two CTAs per SM
+static int hss_cluster_size(int nn) {
+  int G = 1;
+  if (nn <= 8) return 1;
+  while (G < HSS_CLUSTER_MAX && (long long)nn * G * 2 <= HSS_CLUSTER_CTAS) G *= 2;
+  return G;
+}
+
+static void launch_node_rrlu(void (*kern)(HssDev, const int *, int, double, int),
+                             const HssDev &h, const int *dn, int nn, double tol,
+                             cudaStream_t st) {
+  const int G = hss_cluster_size(nn);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nn * G));
+  cfg.blockDim = dim3(HT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  HCK(cudaLaunchKernelEx(&cfg, kern, h, dn, nn, tol, G));
+}
 template <class T>
 static T *up(const char *name, const std::vector<T> &v, cudaStream_t st) {
   T *d = pool<T>(name, std::max<size_t>(v.size(), 1));
@@ -639,9 +738,9 @@ static int hss_construct(HssPlan &pl, int K, int ni, double tol, const double *F
     snprintf(nm, sizeof nm, "hs_pairs%d", LL);
     int *dpr = up(nm, pairs, st);
     const int nn = (int)nodes.size();
-    k_hss_rows<<<nn, HT, 0, st>>>(h, dn, nn, tol);
+    launch_node_rrlu(k_hss_rows, h, dn, nn, tol, st);
     k_hss_compact<<<1, 512, 0, st>>>(h, dn, nn, da, (int)above.size(), dp, 0, 1);
-    k_hss_cols<<<nn, HT, 0, st>>>(h, dn, nn, tol);
+    launch_node_rrlu(k_hss_cols, h, dn, nn, tol, st);
     k_hss_compact<<<1, 512, 0, st>>>(h, dn, nn, da, (int)above.size(), dp, (int)parents.size() / 3, 0);
     k_hss_B<<<nn, 256, 0, st>>>(h, dpr, nn);
     launches += 5;
