@@ -236,6 +236,11 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
     csync(G);
   };
   int Rk = mn;
+  // the other-side update pass of step k also finds row k+1's maximum over the
+  // updated entries (the scan step k+1 would start with), unless a strong swap
+  // changes the rows or entries in between
+  bool have_next = false;
+  ArgMax next_best{-1.0, INT_MAX};
   for (int k = 0; k < mn; ++k) {
     if (k >= rmax) {  // would exceed the generator capacity
       if (tid == 0 && crank == 0) atomicOr(overflow, 1);
@@ -245,7 +250,15 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
     {  // Gu's variant of complete pivoting (CauchyPivtEig, :571-680)
       int jl, ju;
       double jkL = colmax_v(k, jl);
-      double jkU = rowmax_v(k, ju);
+      double jkU;
+      if (have_next) {  // row k's maximum was found during step k-1's update pass
+        const ArgMax3 c = cluster_best(ArgMax3{next_best.v, next_best.i, 0}, G, cslot, cphase);
+        ju = c.i == INT_MAX ? k : c.i;
+        jkU = c.v;
+      } else {
+        jkU = rowmax_v(k, ju);
+      }
+      have_next = false;
       jkL *= fabs(Vr(k));
       jkU *= fabs(Z[k]);
       const double piv = fabs(Z[k] * Vr(k) / den(PL[k], PUr(k)));
@@ -303,10 +316,22 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
     const int puk = PUr(k);
     for (int j = k + 1 + tid; j < M; j += HT)
       Z[j] *= qdiv(rowdiff(j, k), den(PL[j], puk));
+    const bool fuse = k + 1 < mn && k + 1 < M;
+    const int pln = fuse ? PL[k + 1] : 0;
+    ArgMax nb{-1.0, INT_MAX};
     for (int j = k + 1 + joff + tid; j < N; j += jstep) {
       const int puj = PUr(j);
-      V[j] = Vr(j) * (ROW ? qdiv(P.dd(puj, puk), -P.fd(PL[k], puj))
-                          : qdiv(P.fv(__ldg(P.F + puj), __ldg(P.F + puk)), P.fd(puj, PL[k])));
+      const double vj = Vr(j) * (ROW ? qdiv(P.dd(puj, puk), -P.fd(PL[k], puj))
+                                     : qdiv(P.fv(__ldg(P.F + puj), __ldg(P.F + puk)), P.fd(puj, PL[k])));
+      V[j] = vj;
+      if (fuse) {  // |C(k+1, j)| / |A(k+1)| of the next step's Schur complement
+        const double t = fabs(qdiv(vj, den(pln, puj)));
+        if (t > nb.v) { nb.v = t; nb.i = j; }
+      }
+    }
+    if (fuse) {
+      next_best = block_argmax(nb, red);
+      have_next = true;
     }
     for (int j = tid; j < k; j += HT)
       W[j] *= ROW ? qdiv(-P.fd(PL[j], puk), P.fv(Fk, F[j]))
@@ -346,6 +371,7 @@ __device__ int rrlu_node(const PoleDiff &P, double *F, double *A, double *Z, dou
         __syncthreads();
         const int ii = r.i == INT_MAX ? 0 : r.i, jj = s_jj;
         if (!(r.v > rho) || jj >= M) break;
+        have_next = false;  // rows and other-side entries change
         if (tid == 0 && crank == 0) atomicAdd(nswap, 1);
         for (int j = k + 1 + joff + tid; j < N; j += jstep) {
           const int puj = PUr(j);
