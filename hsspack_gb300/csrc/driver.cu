@@ -669,29 +669,67 @@ static int solve_core(Ctx &c, const std::vector<Problem> &pr, cudaStream_t st) {
   std::vector<double> bscale;
   std::vector<int> nblocks(np, 0);
   const int smlsiz = std::max(1, std::min(c.cfg.smlsiz, 32));
-  for (int p = 0; p < np; ++p) {
-    const int n = pr[p].n, o = (int)P[p];
-    for (int i = 0; i < n; ++i) hd[o + i] = pr[p].hd[i];
-    for (int i = 0; i + 1 < n; ++i) he[o + i] = pr[p].he[i];
-    int start = o;
-    while (start < o + n) {
-      int finish = start;
-      while (finish < o + n - 1 && !negligible(he[finish], hd[finish], hd[finish + 1])) ++finish;
-      he[finish] = 0.0;
-      double nrm = 0.0;
-      for (int i = start; i <= finish; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
-      for (int i = start; i < finish; ++i) nrm = std::max(nrm, std::fabs(he[i]));
-      const int m = finish - start + 1;
-      double scl = 1.0;
-      if (m > smlsiz && nrm > 0.0) {
-        scl = nrm;
-        const double mul = 1.0 / nrm;
-        for (int i = start; i <= finish; ++i) hd[i] *= mul;
-        for (int i = start; i < finish; ++i) he[i] *= mul;
+  struct Blocks {
+    std::vector<int> start, size, prob;
+    std::vector<double> scale;
+  };
+  // problems p0 .. p1 - 1 into their own block lists (problems touch disjoint
+  // ranges of hd, he and nblocks, so ranges of problems run on separate threads)
+  auto split = [&](int p0, int p1, Blocks &out) {
+    for (int p = p0; p < p1; ++p) {
+      const int n = pr[p].n, o = (int)P[p];
+      for (int i = 0; i < n; ++i) hd[o + i] = pr[p].hd[i];
+      for (int i = 0; i + 1 < n; ++i) he[o + i] = pr[p].he[i];
+      int start = o;
+      while (start < o + n) {
+        int finish = start;
+        while (finish < o + n - 1 && !negligible(he[finish], hd[finish], hd[finish + 1])) ++finish;
+        he[finish] = 0.0;
+        double nrm = 0.0;
+        for (int i = start; i <= finish; ++i) nrm = std::max(nrm, std::fabs(hd[i]));
+        for (int i = start; i < finish; ++i) nrm = std::max(nrm, std::fabs(he[i]));
+        const int m = finish - start + 1;
+        double scl = 1.0;
+        if (m > smlsiz && nrm > 0.0) {
+          scl = nrm;
+          const double mul = 1.0 / nrm;
+          for (int i = start; i <= finish; ++i) hd[i] *= mul;
+          for (int i = start; i < finish; ++i) he[i] *= mul;
+        }
+        out.start.push_back(start); out.size.push_back(m); out.scale.push_back(scl);
+        out.prob.push_back(p);
+        nblocks[p]++;
+        start = finish + 1;
       }
-      bstart.push_back(start); bsize.push_back(m); bscale.push_back(scl); bprob.push_back(p);
-      nblocks[p]++;
-      start = finish + 1;
+    }
+  };
+  {
+    // a batch of many positions splits on host threads, each taking a run of
+    // whole problems of about N / nt positions; the lists join in problem order
+    const int nt = N >= (1 << 17) && np > 1 ? std::min(host_threads(), np) : 1;
+    std::vector<Blocks> part(nt);
+    std::vector<int> cut(nt + 1, np);
+    cut[0] = 0;
+    for (int t = 1, p = 0; t < nt; ++t) {
+      const long long goal = (long long)N * t / nt;
+      while (p < np && P[p] < goal) ++p;
+      cut[t] = std::max(p, cut[t - 1]);
+    }
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) {
+      try {
+        th.emplace_back(split, cut[t], cut[t + 1], std::ref(part[t]));
+      } catch (...) {
+        split(cut[t], cut[t + 1], part[t]);  // no thread available: run it here
+      }
+    }
+    split(cut[0], cut[1], part[0]);
+    for (auto &x : th) x.join();
+    for (const Blocks &b : part) {
+      bstart.insert(bstart.end(), b.start.begin(), b.start.end());
+      bsize.insert(bsize.end(), b.size.begin(), b.size.end());
+      bscale.insert(bscale.end(), b.scale.begin(), b.scale.end());
+      bprob.insert(bprob.end(), b.prob.begin(), b.prob.end());
     }
   }
   CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
