@@ -107,6 +107,10 @@ SIGNATURES = {
     "hss_dhssmm_dev": (ctypes.c_int, [ctypes.c_int, _V, ctypes.c_int, _V, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                       _V, _V]),
+    "svdhssupdat_": (None, [_D, _D, _D, _D, _I, _D, _I]),
+    "hss_svdhssupdat_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_int, _V, _V]),
+    "hss_svdupd_deflate": (ctypes.c_int, [ctypes.c_int, _D, _D, _I, _I]),
     "hss_rcp_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V]),
     "hss_fp64_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, _V, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
@@ -373,6 +377,52 @@ def cauchyhssmm_dev(D, F, u, v, B, ni, tol, stream=None):
     if rc != 0:
         raise HssError("hss_cauchyhssmm_dev rc=%d: %s" % (rc, _err()))
     return t[0], t[1]
+
+
+def svdhssupdat(F, Z, V, tol, ni):
+    """SvdHssUpdat (SRC/SvdHssUpdat.f90:1) through the Fortran entry point.
+    F (n, ascending) and Z = V^T a are copied; V (n x n, Fortran-ordered, rows =
+    right singular vectors) is updated in place.  Returns (D, F, Z) as the
+    routine leaves them (D[:K] the new singular values, ascending)."""
+    F = np.array(F, dtype=np.float64)
+    Z = np.array(Z, dtype=np.float64)
+    n = len(F)
+    if V.dtype != np.float64 or not V.flags.f_contiguous or V.shape != (n, n):
+        raise ValueError("V must be a Fortran-ordered float64 n x n array")
+    D = np.zeros(n)
+    ints = [ctypes.c_int(int(x)) for x in (n, ni)]
+    load().svdhssupdat_(_pd(D), _pd(F), _pd(Z), _pd(V), ctypes.byref(ints[0]),
+                        ctypes.byref(ctypes.c_double(tol)), ctypes.byref(ints[1]))
+    msg = _err()  # the entry point clears it on entry; non-empty means it failed
+    if msg:
+        raise HssError(msg)
+    return D, F, Z
+
+
+def svdhssupdat_dev(d, f, z, vt, tol, ni, stream=None):
+    """SvdHssUpdat on device tensors (vt: memory column-major n x n, rows = right
+    singular vectors); returns K."""
+    n = f.numel()
+    k = ctypes.c_int(0)
+    rc = load().hss_svdhssupdat_dev(n, _ptr(d), _ptr(f), _ptr(z), _ptr(vt), max(1, n), float(tol),
+                                    int(ni), ctypes.cast(ctypes.pointer(k), ctypes.c_void_p),
+                                    _stream(stream))
+    if rc != 0:
+        raise HssError("hss_svdhssupdat_dev rc=%d: %s" % (rc, _err()))
+    return k.value
+
+
+def svdupd_deflate(f, z):
+    """MDLASD20's deflation on the host (no GPU): returns (K, f, z, idxp, nrot)."""
+    f = np.array(f, dtype=np.float64)
+    z = np.array(z, dtype=np.float64)
+    n = len(f)
+    idxp = np.zeros(n, dtype=np.int32)
+    nrot = ctypes.c_int(0)
+    K = load().hss_svdupd_deflate(n, _pd(f), _pd(z),
+                                  idxp.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                  ctypes.byref(nrot))
+    return K, f, z, idxp, nrot.value
 
 
 def _dhssmm_call(fn, A, B, ni, tol, prank, ncol, m=None):

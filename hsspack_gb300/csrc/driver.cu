@@ -2148,6 +2148,95 @@ void cauchyhssmm_(const double *D, const double *F, const double *U, const doubl
   }
 }
 
+// SvdHssUpdat (SRC/SvdHssUpdat.f90:1) on device arrays.
+int hss_svdhssupdat_dev(int n, double *d, double *f, double *z, double *vt, int ldvt, double tol,
+                        int ni, int *k, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (k) *k = 0;
+  if (n < 0) return -1;
+  if (ldvt < std::max(1, n)) return -6;
+  if (ni < 1) return -8;
+  if (n == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    memset(&c.stats, 0, sizeof c.stats);
+    int *status = buf<int>(c, "su_status", 8);
+    CK(cudaMemsetAsync(status, 0, 8 * sizeof(int), st));
+    int rank = 0;
+    float t2[2] = {0.f, 0.f};
+    const int K = svd_update_core(n, d, f, z, vt, ldvt, tol, ni, c.cfg.precision, &rank, status,
+                                  t2, st);
+    int hst[8];
+    CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    if (k) *k = K;
+    c.stats.max_rank = rank;
+    c.stats.total_k = K;
+    c.stats.secular_roots = K;
+    c.stats.secular_iters = (long long)(((unsigned long long)(unsigned)hst[3] << 32) | (unsigned)hst[2]);
+    c.stats.stage_ms[HSS_ST_HSS_BUILD] = t2[0];
+    c.stats.stage_ms[HSS_ST_HSS_MM] = t2[1];
+    return hst[0] ? hst[0] : 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+// SvdHssUpdat(D,F,Z,V,N0,TOL,ni) with host arrays (V: N0 x N0, leading dimension
+// N0, rows = right singular vectors).  The reference has no INFO argument:
+// failures leave the outputs untouched and set hss_last_error().
+void svdhssupdat_(double *D, double *F, double *Z, double *V, const int *n0_, const double *tol_,
+                  const int *ni_) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  const int n = *n0_, ni = *ni_;
+  c.err.clear();  // without INFO, an empty hss_last_error() reports success
+  if (n <= 0 || ni < 1) {
+    c.err = "SvdHssUpdat: bad N0 or ni";
+    return;
+  }
+  try {
+    cudaStream_t st = nullptr;
+    double *dv = buf<double>(c, "su_in", 3 * (size_t)n);
+    double *dV = buf<double>(c, "su_V", (size_t)n * n);
+    CK(cudaMemcpyAsync(dv + n, F, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv + 2 * n, Z, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dV, V, sizeof(double) * n * n, cudaMemcpyHostToDevice, st));
+    int k = 0;
+    const int info = hss_svdhssupdat_dev(n, dv, dv + n, dv + 2 * n, dV, n, *tol_, ni, &k, st);
+    if (info != 0) {
+      if (info < 1000000) c.err = "SvdHssUpdat: a secular root did not converge";
+      return;
+    }
+    CK(cudaMemcpyAsync(D, dv, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(F, dv + n, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Z, dv + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(V, dV, sizeof(double) * n * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c.stats.host_h2d_bytes = 8LL * n * (n + 2);
+    c.stats.host_d2h_bytes = 8LL * n * (n + 3);
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+  }
+}
+
+// MDLASD20's deflation alone (host code, no GPU): for the CPU tests.
+int hss_svdupd_deflate(int n, double *f, double *z, int *idxp, int *nrot) {
+  if (n < 0) return -1;
+  const SvdUpdDeflation df = svdupd_deflate(n, f, z);
+  for (int j = 0; j < n; ++j) idxp[j] = df.idxp[j];
+  if (nrot) *nrot = (int)df.rot.size();
+  return df.K;
+}
+
 int hss_rcp_dev(int n, const double *x, double *y, void *stream) {
   Ctx &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);

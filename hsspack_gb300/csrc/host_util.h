@@ -34,6 +34,74 @@ inline bool negligible(double e, double a, double b) {
   return !(ae > HSS_EPS * std::sqrt(aa) * std::sqrt(ab));
 }
 
+// MDLASD20 (SRC/mdlasd20.f90:122-300): deflation of the updating problem
+// M = [diag(f); z^T] (f ascending).  A small z_j deflates f_j; two poles closer
+// than the tolerance are rotated so that the first one's z vanishes (the
+// rotation acts on rows p, q of V^T: x <- c x + s y, y <- c y - s x).  On return
+// f[0..K) holds the non-deflated poles and f[K..n) the deflated values in the
+// reference's order (last deflated first); z[0..K) the non-deflated weights
+// (z[K..n) as the rotations left them at their original positions); idxp[j] is
+// the original position of new position j (V^T row j of the output is row
+// idxp[j] of the rotated input).  Deviations, both readings of undefined
+// behaviour in the Fortran: the local ALPHA and BETA that enter the tolerance
+// are never set there and count as 0 here, and HFLAG (uninitialised in
+// SvdHssUpdat, set .FALSE. only when K > 10) is always .FALSE., i.e. all rows
+// are permuted.
+struct SvdUpdRot {
+  int p, q;
+  double c, s;
+};
+struct SvdUpdDeflation {
+  int K = 0;
+  double tol = 0.0;
+  std::vector<int> idxp;
+  std::vector<SvdUpdRot> rot;
+};
+inline SvdUpdDeflation svdupd_deflate(int n, double *f, double *z) {
+  SvdUpdDeflation r;
+  r.idxp.assign(n, 0);
+  if (n <= 0) return r;
+  const double tol = 8.0 * HSS_EPS * std::max(std::fabs(f[n - 1]), std::fabs(f[0]));
+  r.tol = tol;
+  std::vector<double> ww(n, 0.0);
+  int K = 0, K2 = n, jprev = -1;
+  for (int j = 0; j < n; ++j) {
+    if (std::fabs(z[j]) <= tol) {
+      r.idxp[--K2] = j;  // deflated by a small z
+    } else {
+      jprev = j;
+      break;
+    }
+  }
+  if (jprev >= 0) {
+    for (int j = jprev + 1; j < n; ++j) {
+      if (std::fabs(z[j]) <= tol) {
+        r.idxp[--K2] = j;
+      } else if (std::fabs(f[j] - f[jprev]) <= tol) {  // close poles: rotate
+        const double tau = std::hypot(z[j], z[jprev]);
+        const double c = z[j] / tau, s = -z[jprev] / tau;
+        z[j] = tau;
+        z[jprev] = 0.0;
+        r.rot.push_back(SvdUpdRot{jprev, j, c, s});
+        r.idxp[--K2] = jprev;
+        jprev = j;
+      } else {
+        ww[K] = z[jprev];
+        r.idxp[K++] = jprev;
+        jprev = j;
+      }
+    }
+    ww[K] = z[jprev];
+    r.idxp[K++] = jprev;
+  }
+  for (int j = 0; j < K; ++j) z[j] = ww[j];
+  for (int j = 0; j < n; ++j) ww[j] = f[r.idxp[j]];
+  for (int j = 0; j < n; ++j) f[j] = ww[j];
+  if (std::fabs(z[0]) <= tol) z[0] = tol;
+  r.K = K;
+  return r;
+}
+
 // Eigenvectors bound for host memory (mdstedc_): when the columns' supports
 // cover little of Z, the solve leaves them packed on the device (the
 // supported rows of every output column back to back) instead of writing the

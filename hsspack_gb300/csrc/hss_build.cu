@@ -1040,7 +1040,8 @@ int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *
 
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
-                     long long ldq, int nrows, int *rank, cudaStream_t st, float *times) {
+                     long long ldq, int nrows, int *rank, cudaStream_t st, float *times, bool sq,
+                     double swap_rho) {
   double *T = pool<double>("hss_T", (size_t)nrows * K);
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
   if (times) {
@@ -1048,13 +1049,13 @@ int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, 
     HCK(cudaEventRecord(e0, st));
   }
   HssPlan pl;
-  int launches = hss_construct(pl, K, ni, tol, F, u, v, difl, difr, st);
+  int launches = hss_construct(pl, K, ni, tol, F, u, v, difl, difr, st, sq, swap_rho);
   if (times) HCK(cudaEventRecord(e1, st));
   if (pl.ok) {
     launches += hss_multiply(pl, Q, ldq, nrows, T, nrows, precision, st);
     *rank = pl.max_rank;
   } else {
-    dense_product(K, F, u, v, difl, difr, Q, ldq, nrows, T, nrows, st);
+    dense_product(K, F, u, v, difl, difr, Q, ldq, nrows, T, nrows, st, sq);
     *rank = K;
   }
   HCK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), T, nrows * sizeof(double), nrows * sizeof(double), K,

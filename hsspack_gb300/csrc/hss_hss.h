@@ -50,11 +50,26 @@ int hss_cauchyhssmm_core(int n, const double *D, const double *F, const double *
                          const double *v, int ni, double tol, int precision, double *B,
                          long long ldb, int ncb, int *rank, float *times, cudaStream_t st);
 
-// DHSSEVC on caller arrays: Q(0:nrows, 0:K) <- Q * C.
+// DHSSEVC on caller arrays: Q(0:nrows, 0:K) <- Q * C.  sq: singular-value
+// mode, C(i,j) = u_i v_j / (F_i^2 - sigma_j^2) with sigma_j = F_j + DIFL_j;
+// swap_rho: the RRLU's strong-swap threshold (the eigen module's 1.5, the SVD
+// module's 1.1).
 int hss_dhssevc_core(int K, int ni, double tol, int precision, const double *F, const double *u,
                      const double *v, const double *difl, const double *difr, double *Q,
                      long long ldq, int nrows, int *rank, cudaStream_t st,
-                     float *times = nullptr);
+                     float *times = nullptr, bool sq = false, double swap_rho = 1.5);
+
+// SvdHssUpdat (SRC/SvdHssUpdat.f90:1-178) on device arrays: the singular values
+// and right singular vectors of [A; a^T] from A's.  f (n, ascending): A's
+// singular values; z (n): V^T a; vt (n x n, ldvt): V^T (rows are the right
+// singular vectors).  On return d[0..K) holds the K new singular values of the
+// non-deflated problem (ascending) and d[K..n) the deflated ones, f and z are
+// as MDLASD20 / MDLASD31 leave them, and vt's rows are the updated right
+// singular vectors in the order of d.  Returns K (the secular equation's
+// order); *rank: the largest HSS rank (K when the product ran densely).
+int svd_update_core(int n, double *d, double *f, double *z, double *vt, long long ldvt, double tol,
+                    int ni, int precision, int *rank, int *status, float *times,
+                    cudaStream_t st);
 
 // DHSSMM / DHSSMML on device arrays (mat2hss.cu): A (n x n, lda) compressed to
 // HSS by truncated SVD (leaf ni, absolute tolerance tol); side 0: B (n x k,

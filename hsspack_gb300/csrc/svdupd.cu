@@ -1,0 +1,148 @@
+// svdupd.cu -- SVD updating on sm_103a (SvdHssUpdat, SRC/SvdHssUpdat.f90:1-178).
+//
+// A = U diag(f) V^T gains a row a^T.  With z = V^T a, [A; a^T] = diag(U, 1) M V^T
+// for the broken-arrow matrix M = [diag(f); z^T], so the updated singular values
+// are M's and the updated right singular vectors are V times M's.  The reference
+// deflates M (MDLASD20, SRC/mdlasd20.f90), solves the K-term secular equation
+// and recomputes z by Loewner's formula (MDLASD31, SRC/mdlasd31.f90), compresses
+// the Cauchy-like matrix of M's right singular vectors,
+//   A(i,j) = alpha_i zhat_j / (sigma_i^2 - f_j^2)   (Cauchy2hssvd,
+//   SRC/CauchyHssvd_VPS.f90:2762-2790),
+// to HSS form and multiplies it into the first K rows of the permuted V^T
+// (fastHssmm in 200-column panels, SRC/SvdHssUpdat.f90:145-165).
+//
+// Here the deflation runs on the host (O(n) scalar work, host_util.h); the rest
+// stays in HBM.  V^T is transposed once so that every right singular vector is
+// a contiguous column: the deflating rotations and the permutation then move
+// whole columns (coalesced), and the product is the eigen merge's
+// W(:, 0:K) <- W(:, 0:K) C with the singular-value mode Cauchy-like matrix
+// C(i,j) = zhat_i (-alpha_j) / (f_i^2 - sigma_j^2) = A(j,i): the secular solver
+// and Loewner kernels in singular-value mode, the structured RRLU with the SVD
+// module's swap threshold (rho = 1.1) and the level-batched HSS multiply.
+// Negating alpha leaves every pivot decision unchanged (they compare |C|).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "hss_common.cuh"
+#include "hss_gemm.h"
+#include "hss_hss.h"
+#include "hss_kernels.h"
+#include "hss_plan.h"
+#include "hss_pool.h"
+#include "host_util.h"
+
+namespace hss {
+
+#define SCK(x)                                                                              \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess) throw HssError{std::string(#x) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+
+// The deflating rotations in order, DROT on column pairs of W (n rows, ld):
+// (x, y) <- (c x + s y, c y - s x) for x = W(:, p_t), y = W(:, q_t).  A pair
+// shares a column with the next one, so one thread owns one row and applies
+// all of them in sequence; the threads of a warp read consecutive rows.
+__global__ void k_cols_rotate(int n, int nrot, const int2 *__restrict__ pq,
+                              const double2 *__restrict__ cs, double *__restrict__ W,
+                              long long ld) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int t = 0; t < nrot; ++t) {
+    const int2 p = __ldg(pq + t);
+    const double2 g = __ldg(cs + t);
+    double *x = W + (long long)p.x * ld + r, *y = W + (long long)p.y * ld + r;
+    const double xv = *x, yv = *y;
+    *x = g.x * xv + g.y * yv;
+    *y = g.x * yv - g.y * xv;
+  }
+}
+
+// W2(:, j) = W(:, idx[j]) for the n columns (n rows each); grid (row tiles,
+// column groups).
+__global__ void k_permute_cols(int n, const int *__restrict__ idx, const double *__restrict__ W,
+                               long long ldw, double *__restrict__ W2, long long ld2) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int j = blockIdx.y; j < n; j += gridDim.y)
+    W2[(long long)j * ld2 + r] = W[(long long)__ldg(idx + j) * ldw + r];
+}
+
+__global__ void k_negate(int n, double *__restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = -x[i];
+}
+
+template <class T>
+static T *upload(const char *name, const std::vector<T> &v, cudaStream_t st) {
+  T *d = pool<T>(name, std::max<size_t>(v.size(), 1));
+  if (!v.empty()) stage_h2d(d, v.data(), v.size() * sizeof(T), st);
+  return d;
+}
+
+int svd_update_core(int n, double *d, double *f, double *z, double *vt, long long ldvt, double tol,
+                    int ni, int precision, int *rank, int *status, float *times,
+                    cudaStream_t st) {
+  *rank = 0;
+  if (times) times[0] = times[1] = 0.f;
+  std::vector<double> hf(n), hz(n);
+  SCK(cudaMemcpyAsync(hf.data(), f, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  SCK(cudaMemcpyAsync(hz.data(), z, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  SCK(cudaStreamSynchronize(st));
+  const SvdUpdDeflation df = svdupd_deflate(n, hf.data(), hz.data());
+  const int K = df.K;
+  // right singular vectors as columns, rotated and permuted
+  double *W = pool<double>("su_W", (size_t)n * n), *W2 = pool<double>("su_W2", (size_t)n * n);
+  transpose(n, n, vt, ldvt, W, n, st);
+  const int nrot = (int)df.rot.size();
+  if (nrot > 0) {
+    std::vector<int2> pq(nrot);
+    std::vector<double2> cs(nrot);
+    for (int t = 0; t < nrot; ++t) {
+      pq[t] = make_int2(df.rot[t].p, df.rot[t].q);
+      cs[t] = make_double2(df.rot[t].c, df.rot[t].s);
+    }
+    int2 *dpq = upload("su_pq", pq, st);
+    double2 *dcs = upload("su_cs", cs, st);
+    k_cols_rotate<<<(n + 127) / 128, 128, 0, st>>>(n, nrot, dpq, dcs, W, n);
+  }
+  int *didx = upload("su_idxp", df.idxp, st);
+  k_permute_cols<<<dim3((n + 255) / 256, std::min(n, 8192)), 256, 0, st>>>(n, didx, W, n, W2, n);
+  SCK(cudaMemcpyAsync(f, hf.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  SCK(cudaMemcpyAsync(z, hz.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  // the deflated values keep their places; the non-deflated ones are replaced below
+  SCK(cudaMemcpyAsync(d, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (K >= 1) {
+    std::vector<int> hv{0, K, 0, K};
+    int *v = upload("su_view", hv, st);
+    std::vector<double> one{1.0};
+    double *rho = upload("su_rho", one, st);  // z unnormalised: 1 + sum z_j^2 / (f_j^2 - s^2)
+    LevelView lv{v, v + 1, rho, v + 2, 1};
+    double *lam = pool<double>("su_lam", K), *difl = pool<double>("su_difl", K),
+           *difr = pool<double>("su_difr", K), *zhat = pool<double>("su_zhat", K),
+           *alpha = pool<double>("su_alpha", K);
+    launch_secular(lv, K, K, f, z, lam, difl, difr, nullptr, status,
+                   (unsigned long long *)(status + 2), nullptr, st, true);
+    launch_lowner(lv, K, f, difl, difr, z, zhat, st, true, K);
+    launch_alpha(lv, K, f, difl, difr, zhat, alpha, st, true);
+    k_negate<<<(K + 255) / 256, 256, 0, st>>>(K, alpha);
+    if (K >= 2 * ni) {
+      hss_dhssevc_core(K, ni, tol, precision, f, zhat, alpha, difl, difr, W2, n, n, rank, st,
+                       times, true, 1.1);
+    } else {  // a single leaf: the product is one dense block
+      double *C = pool<double>("su_C", (size_t)K * K), *T = pool<double>("su_T", (size_t)n * K);
+      launch_cauchy_eig(K, f, zhat, alpha, difl, difr, C, st, true);
+      std::vector<GemmDesc> g{{W2, C, T, n, K, n, n, K, K, 0, 0}};
+      launch_gemm(g, 0, st);
+      SCK(cudaMemcpyAsync(W2, T, sizeof(double) * n * K, cudaMemcpyDeviceToDevice, st));
+      *rank = K;
+    }
+    SCK(cudaMemcpyAsync(d, lam, sizeof(double) * K, cudaMemcpyDeviceToDevice, st));
+    SCK(cudaMemcpyAsync(z, zhat, sizeof(double) * K, cudaMemcpyDeviceToDevice, st));
+  }
+  transpose(n, n, W2, n, vt, ldvt, st);
+  return K;
+}
+
+}  // namespace hss

@@ -238,6 +238,21 @@ int hss_lowner_noalloc_dev(int k, const double *dlamda, const double *difl,
                            const double *difr, double *z, double *alpha,
                            void *stream);
 
+/* SvdHssUpdat(D,F,Z,V,N0,TOL,ni) replaces SRC/SvdHssUpdat.f90:1: the SVD of
+ * A = U diag(F) V^T with one row a^T appended, given F (N0, ascending), Z = V^T a
+ * and V (N0 x N0, leading dimension N0, the right singular vectors as ROWS, as
+ * the reference's MDLASD20 reads it).  On return D(1:K) holds the K new
+ * singular values of the non-deflated problem (ascending) and D(K+1:N0) the
+ * deflated ones (the reference leaves D(K+1:N0) undefined), F and Z are as
+ * MDLASD20 / MDLASD31 leave them (F(1:K) the poles, F(K+1:N0) the deflated
+ * values; Z(1:K) recomputed by Loewner's formula), and the rows of V are the
+ * updated right singular vectors in the order of D.  The Cauchy-like matrix of
+ * the new vectors is compressed to HSS (leaf ni, tolerance TOL) on the GPU.
+ * No INFO argument (as the reference): every call clears hss_last_error() on
+ * entry, and a failure leaves the outputs untouched and sets it. */
+void svdhssupdat_(double *D, double *F, double *Z, double *V, const int *n0, const double *tol,
+                  const int *ni);
+
 /* DHSSEVC (SRC/CauchyHssEig.f90:2444): Q(0:nrows, 0:K) <- Q * C where
  * C(i,j) = u_i v_j / (F_i - lam_j), lam_j = F_j + difl_j, compressed to HSS
  * with leaf ni and tolerance tol.  Q is column-major with leading dim ldq. */
@@ -260,6 +275,20 @@ int hss_cauchyhssmm_dev(int n, const double *D, const double *F, const double *u
  * Returns 0, -i for a bad i-th argument, or 1000000 / 1000001. */
 int hss_dhssmm_dev(int n, const double *A, int lda, double *B, int ldb, int k, double tol,
                    int ni, int side, float *times, void *stream);
+
+/* SvdHssUpdat on device arrays: d, f, z (n), vt (n x n, ldvt; rows = right
+ * singular vectors), as svdhssupdat_; *k (may be NULL) receives K, the order of
+ * the secular equation after deflation.  hss_get_stats(): max_rank (the
+ * largest HSS rank; K when the product ran as one dense block), stage_ms of
+ * HSS_ST_HSS_BUILD / HSS_ST_HSS_MM.  Returns 0, -i for a bad i-th argument, a
+ * positive status (a secular root did not converge), or 1000000 / 1000001. */
+int hss_svdhssupdat_dev(int n, double *d, double *f, double *z, double *vt, int ldvt,
+                        double tol, int ni, int *k, void *stream);
+
+/* MDLASD20's deflation alone (host code; needs no GPU): f, z (n) modified as
+ * MDLASD20 leaves them, idxp[j] (n) the original position of new position j;
+ * *nrot (may be NULL) the number of deflating rotations.  Returns K. */
+int hss_svdupd_deflate(int n, double *f, double *z, int *idxp, int *nrot);
 
 /* Dense Cauchy-like eigenvector block C(i,j) = u_i v_j / (F_i - lam_j) through
  * DIFL/DIFR (SRC/CauchyHssEig.f90:1688, CauchylikeEig), k-by-k column-major. */
