@@ -19,6 +19,7 @@ memory and streams): :func:`mdstedc_dev`, :func:`mdstedc_batch_dev`
 :func:`lowner_dev`, :func:`dhssevc_dev`, :func:`cauchy_eig_dev`.
 """
 import ctypes
+import math
 import os
 
 import numpy as np
@@ -111,6 +112,15 @@ SIGNATURES = {
     "hss_svdhssupdat_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_int, _V, _V]),
     "hss_svdupd_deflate": (ctypes.c_int, [ctypes.c_int, _D, _D, _I, _I]),
+    "hsscholsolver_": (None, [ctypes.c_char_p, ctypes.c_char_p, _D, _I, _D, _I, _D, _I, _I, _D,
+                              _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
+    "hss_chol_factor_dev": (ctypes.c_int, [ctypes.c_int, _V, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_int, ctypes.c_int, _V, _V]),
+    "hss_chol_solve_dev": (ctypes.c_int, [_V, _V, ctypes.c_int, ctypes.c_int, _V]),
+    "hss_chol_pcg_dev": (ctypes.c_int, [_V, ctypes.c_int, _V, ctypes.c_int, _V, _V,
+                                        ctypes.c_double, ctypes.c_int, _V, _V, _V]),
+    "hss_chol_info": (ctypes.c_int, [_V, _V, _V, _V, _V, _V]),
+    "hss_chol_free": (None, [_V]),
     "hss_rcp_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V]),
     "hss_fp64_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, _V, _V]),
     "hss_mdstedc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V]),
@@ -410,6 +420,77 @@ def svdhssupdat_dev(d, f, z, vt, tol, ni, stream=None):
     if rc != 0:
         raise HssError("hss_svdhssupdat_dev rc=%d: %s" % (rc, _err()))
     return k.value
+
+
+def hsscholsolver(rs, wpcg, A, b, ni, tol, prank, pp=5, tau=1e-13, maxit=30):
+    """HssCholSolver (SRC/HssCholSolver.f90:1) through the Fortran entry point:
+    returns (x, INFO) for the SPD matrix A (n x n, any float64 layout; symmetric)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    x = np.array(b, dtype=np.float64)
+    n = A.shape[0]
+    info = ctypes.c_int(0)
+    ints = [ctypes.c_int(int(v)) for v in (n, ni, prank, pp, maxit)]
+    load().hsscholsolver_(rs.encode(), wpcg.encode(), _pd(A), ctypes.byref(ints[0]), _pd(x),
+                          ctypes.byref(ints[1]), ctypes.byref(ctypes.c_double(tol)),
+                          ctypes.byref(ints[2]), ctypes.byref(ints[3]),
+                          ctypes.byref(ctypes.c_double(tau)), ctypes.byref(ints[4]),
+                          ctypes.byref(info), 1, 1)
+    return x, info.value
+
+
+class HssChol:
+    """An HSS Cholesky factor of a device matrix (hss_chol_factor_dev)."""
+
+    def __init__(self, A, ni, tol, prank, ps=0, stream=None):
+        """A: device tensor holding the n x n matrix column-major (any shape)."""
+        n = math.isqrt(A.numel())
+        if n * n != A.numel():
+            raise ValueError("A must hold an n x n matrix")
+        h = ctypes.c_void_p()
+        rc = load().hss_chol_factor_dev(n, _ptr(A), n, int(ni), float(tol), int(prank), int(ps),
+                                        ctypes.cast(ctypes.pointer(h), ctypes.c_void_p),
+                                        _stream(stream))
+        if rc != 0:
+            raise HssError("hss_chol_factor_dev rc=%d: %s" % (rc, _err()))
+        self.h, self.n = h, n
+
+    def info(self):
+        v = [ctypes.c_int(0) for _ in range(4)]
+        b = ctypes.c_longlong(0)
+        load().hss_chol_info(self.h, *[ctypes.cast(ctypes.pointer(x), ctypes.c_void_p) for x in v],
+                             ctypes.cast(ctypes.pointer(b), ctypes.c_void_p))
+        return {"n": v[0].value, "max_rank": v[1].value, "levels": v[2].value,
+                "root": v[3].value, "bytes": b.value}
+
+    def solve(self, B, stream=None):
+        """B: device tensor whose memory is column-major n x nrhs (solved in place)."""
+        nrhs = B.numel() // self.n
+        rc = load().hss_chol_solve_dev(self.h, _ptr(B), self.n, nrhs, _stream(stream))
+        if rc != 0:
+            raise HssError("hss_chol_solve_dev rc=%d: %s" % (rc, _err()))
+
+    def pcg(self, A, b, x, tau, maxit, precondition=True, stream=None):
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        rc = load().hss_chol_pcg_dev(self.h if precondition else None, self.n, _ptr(A), self.n,
+                                     _ptr(b), _ptr(x), float(tau), int(maxit),
+                                     ctypes.cast(ctypes.pointer(it), ctypes.c_void_p),
+                                     ctypes.cast(ctypes.pointer(rr), ctypes.c_void_p),
+                                     _stream(stream))
+        if rc != 0:
+            raise HssError("hss_chol_pcg_dev rc=%d: %s" % (rc, _err()))
+        return it.value, rr.value
+
+    def free(self):
+        if self.h:
+            load().hss_chol_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def svdupd_deflate(f, z):

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -26,6 +27,7 @@
 #include "../../include/hsspack_gb300.h"
 #include "hss_common.cuh"
 #include "hss_gemm.h"
+#include "hss_chol.h"
 #include "hss_hss.h"
 #include "hss_kernels.h"
 #include "hss_pool.h"
@@ -2225,6 +2227,179 @@ void svdhssupdat_(double *D, double *F, double *Z, double *V, const int *n0_, co
     c.err = ex.msg;
   } catch (HssError &ex) {
     c.err = ex.msg;
+  }
+}
+
+// ------------------------------------------------------- HSS Cholesky ----
+struct hss_chol {
+  CholFactor F;
+};
+
+int hss_chol_factor_dev(int n, const double *A, int lda, int ni, double tol, int prank, int ps,
+                        hss_chol **out, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (out) *out = nullptr;
+  if (n < 1) return -1;
+  if (lda < n) return -3;
+  if (ni < 1 || ni > CH_MAXM) return -4;
+  if (prank < 1) return -6;
+  if (ps < 0) return -7;
+  if (!out) return -8;
+  cudaStream_t st = (cudaStream_t)stream;
+  hss_chol *h = new (std::nothrow) hss_chol;
+  if (!h) return -8;
+  try {
+    memset(&c.stats, 0, sizeof c.stats);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, st));
+    const int info = hss_chol_factor_core(n, A, lda, ni, tol, prank, ps, 0x5eedull, h->F, st);
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.stats.ms_total = ms;
+    c.stats.max_rank = h->F.max_rank;
+    c.stats.n_levels = (int)h->F.lv.size();
+    if (info != 0) {
+      c.err = info == 1 ? "HSS Cholesky: a diagonal block is not positive definite"
+                        : "HSS Cholesky: a node has more than 128 rows";
+      delete h;
+      return info;
+    }
+    *out = h;
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    delete h;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    delete h;
+    return 1000001;
+  }
+}
+
+int hss_chol_solve_dev(const hss_chol *f, double *B, int ldb, int nrhs, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (!f) return -1;
+  if (ldb < f->F.n) return -3;
+  if (nrhs < 0) return -4;
+  if (nrhs == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    hss_chol_solve_core(f->F, B, ldb, nrhs, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+int hss_chol_pcg_dev(const hss_chol *f, int n, const double *A, int lda, const double *b,
+                     double *x, double tau, int maxit, int *iters, double *relres, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 1) return -2;
+  if (f && f->F.n != n) return -2;
+  if (lda < n) return -4;
+  if (maxit < 0) return -8;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    double rr = 0.0;
+    const int it = hss_chol_pcg_core(f ? &f->F : nullptr, n, A, lda, b, x, tau, maxit, &rr, st);
+    CK(cudaGetLastError());
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return 0;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+int hss_chol_info(const hss_chol *f, int *n, int *max_rank, int *levels, int *root,
+                  long long *bytes) {
+  if (!f) return -1;
+  if (n) *n = f->F.n;
+  if (max_rank) *max_rank = f->F.max_rank;
+  if (levels) *levels = (int)f->F.lv.size();
+  if (root) *root = f->F.Nroot;
+  if (bytes) *bytes = f->F.fac_bytes;
+  return 0;
+}
+
+void hss_chol_free(hss_chol *f) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  delete f;
+}
+
+// HssCholSolver(RS,WPCG,A,LDA,b,ni,tol,prank,pp,tau,MaxIt,info) with host
+// arrays: N = LDA (as the reference); b (N) is replaced by the solution.
+void hsscholsolver_(const char *rs, const char *wpcg, double *A, const int *lda_, double *b,
+                    const int *ni_, const double *tol_, const int *prank_, const int *pp_,
+                    const double *tau_, const int *maxit_, int *info, size_t rs_len,
+                    size_t wpcg_len) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  *info = 0;
+  (void)rs_len;
+  (void)wpcg_len;
+  const char r = (char)toupper((unsigned char)rs[0]), w = (char)toupper((unsigned char)wpcg[0]);
+  if (r != 'R' && r != 'S') { *info = -1; return; }
+  if (w != 'Y' && w != 'N') { *info = -2; return; }
+  const int n = *lda_, ni = *ni_, prank = *prank_, pp = *pp_;
+  if (n < 1) { *info = -4; return; }
+  if (ni < 1 || ni > CH_MAXM) { *info = -6; return; }
+  if (prank < 1) { *info = -8; return; }
+  if (r == 'R' && pp < 0) { *info = -9; return; }
+  if (*maxit_ < 0) { *info = -11; return; }
+  try {
+    cudaStream_t st = nullptr;
+    double *dA = buf<double>(c, "hc_hostA", (size_t)n * n);
+    double *dv = buf<double>(c, "hc_hostv", 2 * (size_t)n);
+    CK(cudaMemcpyAsync(dA, A, sizeof(double) * n * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv, b, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    hss_chol *f = nullptr;
+    const int ps = r == 'R' ? prank + pp : 0;
+    const int fi = hss_chol_factor_dev(n, dA, n, ni, *tol_, prank, ps, &f, st);
+    if (fi != 0) { *info = fi; return; }
+    if (w == 'N') {
+      const int si = hss_chol_solve_dev(f, dv, n, 1, st);
+      if (si != 0) { *info = si; hss_chol_free(f); return; }
+      CK(cudaMemcpyAsync(b, dv, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    } else {
+      int it = 0;
+      double rr = 0.0;
+      const int pi = hss_chol_pcg_dev(f, n, dA, n, dv, dv + n, *tau_, *maxit_, &it, &rr, st);
+      if (pi != 0) { *info = pi; hss_chol_free(f); return; }
+      CK(cudaMemcpyAsync(b, dv + n, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+      c.stats.secular_iters = it;  // the CG steps taken
+    }
+    CK(cudaStreamSynchronize(st));
+    hss_chol_free(f);
+    c.stats.host_h2d_bytes = 8LL * n * (n + 1);
+    c.stats.host_d2h_bytes = 8LL * n;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    *info = 1000001;
   }
 }
 

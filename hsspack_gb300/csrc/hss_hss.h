@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 namespace hss {
 
@@ -79,5 +80,12 @@ int svd_update_core(int n, double *d, double *f, double *z, double *vt, long lon
 int hss_dhssmm_core(int n, const double *A, long long lda, double *B, long long ldb, int k,
                     double tol, int ni, int side, int precision, int *rank, float *times,
                     cudaStream_t st);
+
+// Right singular vectors (singular value > tol, decreasing) of column-major
+// tall matrices by TSQR, pivoted QR and one-sided Jacobi (mat2hss.cu).
+std::vector<int> tall_right_bases(const std::vector<const double *> &X,
+                                  const std::vector<int> &rows, const std::vector<int> &ncol,
+                                  const std::vector<long long> &ld, const std::vector<double *> &P,
+                                  const std::vector<double *> &PT, double tol, cudaStream_t st);
 
 }  // namespace hss

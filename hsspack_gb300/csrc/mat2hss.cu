@@ -551,6 +551,23 @@ static std::vector<int> tall_bases(const std::vector<TallDesc> &ds, const std::v
   return rk;
 }
 
+// Right singular vectors with singular value above tol of column-major tall
+// matrices X[i] (rows[i] x ncol[i], leading dimension ld[i], ncol <= 128), in
+// decreasing order, into P[i] (ncol x k, ld ncol) and PT[i] (k x ncol, ld k);
+// returns the ranks k (one host synchronisation).
+std::vector<int> tall_right_bases(const std::vector<const double *> &X,
+                                  const std::vector<int> &rows, const std::vector<int> &ncol,
+                                  const std::vector<long long> &ld, const std::vector<double *> &P,
+                                  const std::vector<double *> &PT, double tol, cudaStream_t st) {
+  std::vector<TallDesc> ds;
+  for (size_t i = 0; i < X.size(); ++i) {
+    if (ncol[i] > QR_MAXC) throw HssError{"tall_right_bases: more than 128 columns"};
+    ds.push_back(TallDesc{X[i], 1, ld[i], rows[i], ncol[i], INT_MAX, 0});
+  }
+  int launches = 0;
+  return tall_bases(ds, P, PT, tol, launches, st);
+}
+
 struct Front {
   int node, ra, rb, ca, cb;
 };

@@ -253,6 +253,22 @@ int hss_lowner_noalloc_dev(int k, const double *dlamda, const double *difl,
 void svdhssupdat_(double *D, double *F, double *Z, double *V, const int *n0, const double *tol,
                   const int *ni);
 
+/* HssCholSolver(RS,WPCG,A,LDA,b,ni,tol,prank,pp,tau,MaxIt,info) replaces
+ * SRC/HssCholSolver.f90:1: solves A x = b for the dense SPD matrix A (N = LDA,
+ * as the reference) through an HSS Cholesky factorisation (leaves of ni rows,
+ * ni <= 128; singular values of the scaled off-diagonal block columns above
+ * tol kept, at most prank per node; RS = 'S' exact singular vectors, 'R' a
+ * sketch of prank + pp rows).  WPCG = 'N' returns the factorisation's solve,
+ * 'Y' the preconditioned CG solution (relative residual below tau or MaxIt + 1
+ * steps).  b (N) is replaced by the solution; A is not modified.  INFO: -1 / -2
+ * bad RS / WPCG (as the reference), -4, -6, -8, -9, -11 for LDA, ni, prank, pp,
+ * MaxIt; 1 a diagonal block not positive definite, 2 a node of more than 128
+ * rows, 1000000 / 1000001 CUDA / construction failures (hss_last_error()). */
+void hsscholsolver_(const char *rs, const char *wpcg, double *A, const int *lda, double *b,
+                    const int *ni, const double *tol, const int *prank, const int *pp,
+                    const double *tau, const int *maxit, int *info, size_t rs_len,
+                    size_t wpcg_len);
+
 /* DHSSEVC (SRC/CauchyHssEig.f90:2444): Q(0:nrows, 0:K) <- Q * C where
  * C(i,j) = u_i v_j / (F_i - lam_j), lam_j = F_j + difl_j, compressed to HSS
  * with leaf ni and tolerance tol.  Q is column-major with leading dim ldq. */
@@ -289,6 +305,25 @@ int hss_svdhssupdat_dev(int n, double *d, double *f, double *z, double *vt, int 
  * MDLASD20 leaves them, idxp[j] (n) the original position of new position j;
  * *nrot (may be NULL) the number of deflating rotations.  Returns K. */
 int hss_svdupd_deflate(int n, double *f, double *z, int *idxp, int *nrot);
+
+/* HSS Cholesky on device arrays (the pieces of HssCholSolver).  The factor
+ * owns its device memory until hss_chol_free.
+ * hss_chol_factor_dev: A (n x n, lda; read only); ni leaf rows (<= 128); tol;
+ *   prank the largest rank kept per node; ps = 0 exact singular vectors of the
+ *   scaled block columns, ps > 0 those of a ps-row uniform [0,1) sketch.
+ *   Returns 0 (*out set), -i for a bad i-th argument, 1 / 2 as INFO above.
+ * hss_chol_solve_dev: B (n x nrhs, ldb) <- the factorisation's solve.
+ * hss_chol_pcg_dev: x <- CG solution of A x = b preconditioned by the factor
+ *   (f = NULL: unpreconditioned); *iters, *relres as the loop ends. */
+typedef struct hss_chol hss_chol;
+int hss_chol_factor_dev(int n, const double *A, int lda, int ni, double tol, int prank, int ps,
+                        hss_chol **out, void *stream);
+int hss_chol_solve_dev(const hss_chol *f, double *B, int ldb, int nrhs, void *stream);
+int hss_chol_pcg_dev(const hss_chol *f, int n, const double *A, int lda, const double *b,
+                     double *x, double tau, int maxit, int *iters, double *relres, void *stream);
+int hss_chol_info(const hss_chol *f, int *n, int *max_rank, int *levels, int *root,
+                  long long *bytes);
+void hss_chol_free(hss_chol *f);
 
 /* Dense Cauchy-like eigenvector block C(i,j) = u_i v_j / (F_i - lam_j) through
  * DIFL/DIFR (SRC/CauchyHssEig.f90:1688, CauchylikeEig), k-by-k column-major. */
