@@ -429,6 +429,61 @@ def run_extra(torch, hp, full_cfg):
                 "max_rank": hp.get_stats()["max_rank"],
                 "max_abs_err_vs_dense": float((Bd - ref).abs().max())}
             del A, B0, Bd, ref
+        # SVD updating (SvdHssUpdat) n = 10000, the reference's test case
+        # (TEST/testUpsvdCauchy.f90): F evenly spaced in (0.1, 9), Z iid U(0, 1)
+        # with Z(10) = 1e-16 and Z(200) = 1e-17, V = I; leaf 64, tol 1e-14
+        n = 10000
+        f0 = torch.tensor(0.1 + (2 * np.arange(1, n + 1) - 1) * (8.9 / (2 * n)), device="cuda")
+        zh = np.random.default_rng(0).uniform(0.0, 1.0, n)
+        zh[9], zh[199] = 1e-16, 1e-17
+        z0 = torch.tensor(zh, device="cuda")
+        v0 = torch.eye(n, dtype=torch.float64, device="cuda").reshape(-1)
+        fw, zw, vw = f0.clone(), z0.clone(), v0.clone()
+        dw = torch.zeros(n, dtype=torch.float64, device="cuda")
+        for prec in (0, 1):
+            hp.set_config(precision=prec)
+            key = "fp64" if prec == 0 else "split_bf16"
+
+            def upd():
+                fw.copy_(f0)
+                zw.copy_(z0)
+                vw.copy_(v0)
+                hp.svdhssupdat_dev(dw, fw, zw, vw, 1e-14, 64)
+
+            out["svd_update_n10000_%s_ms" % key] = _timed_ms(torch, upd)
+            out["svd_update_n10000_max_rank"] = hp.get_stats()["max_rank"]
+        del v0, vw
+        # HSS Cholesky (HssCholSolver) n = 8192: Gaussian kernel (length 0.01) on
+        # sorted uniform points plus 1e-2 I; leaves of 32, tol 1e-8, at most 20
+        # per node; factor, solve, CG preconditioned by it and plain CG (tau 1e-13)
+        hp.set_config(precision=0)
+        n = 8192
+        xs = torch.sort(torch.rand(n, dtype=torch.float64, device="cuda",
+                                   generator=torch.Generator("cuda").manual_seed(0)))[0]
+        Ak = torch.exp(-0.5 * ((xs[:, None] - xs[None, :]) / 0.01) ** 2)
+        Ak += 1e-2 * torch.eye(n, dtype=torch.float64, device="cuda")
+        Ak = Ak.reshape(-1)
+        bk = Ak.view(n, n).sum(1)
+        xk = torch.zeros_like(bk)
+        fac = [None]
+
+        def factor():
+            if fac[0] is not None:
+                fac[0].free()
+            fac[0] = hp.HssChol(Ak, 32, 1e-8, 20)
+
+        out["hss_cholesky_n8192_factor_ms"] = _timed_ms(torch, factor)
+        out["hss_cholesky_n8192_max_rank"] = fac[0].info()["max_rank"]
+        yk = bk.clone()
+        out["hss_cholesky_n8192_solve_ms"] = _timed_ms(torch, lambda: (yk.copy_(bk), fac[0].solve(yk)))
+        t0 = time.perf_counter()
+        it, rr = fac[0].pcg(Ak, bk, xk, 1e-13, 30)
+        out["hss_cholesky_n8192_pcg"] = {"steps": it, "relres": rr,
+                                         "ms": (time.perf_counter() - t0) * 1e3}
+        it0, rr0 = fac[0].pcg(Ak, bk, xk, 1e-13, 30, precondition=False)
+        out["hss_cholesky_n8192_plain_cg"] = {"steps": it0, "relres": rr0}
+        fac[0].free()
+        del Ak
     finally:
         hp.restore_config(old)
     return out
