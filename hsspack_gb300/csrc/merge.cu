@@ -9,6 +9,8 @@
 // they are, modified in place only by deflating Givens rotations.  This is the
 // reference's INDXQ indirection (mdlaed0.f90:221, mdlaed2.f90:229-233) carried
 // through to the end, so no level copies the whole n x n block.
+#include <cooperative_groups.h>
+
 #include "hss_block.cuh"
 #include "hss_common.cuh"
 #include "hss_kernels.h"
@@ -389,6 +391,336 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   }
 }
 
+// ---- the same bookkeeping for merges of more than PCL_MIN_N positions, on a
+// thread-block cluster of PCL_G CTAs per merge.  One CTA's position passes are
+// bound by the memory-level parallelism of its SM (the loads of a 32768-position
+// merge take ~140 us on one SM whatever its thread count), so every pass is
+// split between the cluster's CTAs: each owns a contiguous range of positions
+// (or of candidates), and its block-wide totals are combined with the other
+// CTAs' through distributed shared memory, so every list keeps the position
+// order of the one-CTA kernel.  The chain of Givens tests stays serial, on
+// thread 0 of the first CTA (it visits only the pairs that may rotate), and
+// the rotated list is sorted by that CTA; the results are those of
+// k_merge_prepare.  Data another CTA wrote in this launch is read through L2
+// (ld.global.cg); cluster barriers order the phases.  Requires PREP_FRONT (the
+// merged order and z come from k_merge_front).
+namespace cg = cooperative_groups;
+constexpr int PCL_G = 8;
+constexpr int PCL_T = 512;
+constexpr int PCL_MIN_N = 8192;
+
+// cluster-wide exclusive scan of each CTA's 64-bit total; two shared slots used
+// alternately (a slot is rewritten only after the next cluster barrier)
+__device__ __forceinline__ unsigned long long cl_scan(unsigned long long v,
+                                                      unsigned long long *slot, int &ph,
+                                                      unsigned long long *tot) {
+  cg::cluster_group cl = cg::this_cluster();
+  if (threadIdx.x == 0) slot[ph] = v;
+  cl.sync();
+  const unsigned r = cl.block_rank(), G = cl.num_blocks();
+  unsigned long long base = 0, t = 0;
+  for (unsigned q = 0; q < G; ++q) {
+    const unsigned long long x = *cl.map_shared_rank(slot + ph, q);
+    if (q < r) base += x;
+    t += x;
+  }
+  ph ^= 1;
+  *tot = t;
+  return base;
+}
+__device__ __forceinline__ double cl_max(double v, double *slot, int &ph) {
+  cg::cluster_group cl = cg::this_cluster();
+  if (threadIdx.x == 0) slot[ph] = v;
+  cl.sync();
+  double r = 0.0;
+  for (unsigned q = 0; q < cl.num_blocks(); ++q) r = fmax(r, *cl.map_shared_rank(slot + ph, q));
+  ph ^= 1;
+  return r;
+}
+
+template <int MT>
+__global__ void __launch_bounds__(MT)
+k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn,
+                   const int *__restrict__ mn1, const double *__restrict__ e,
+                   double *__restrict__ Dp, int *__restrict__ perm, LevelScratch w,
+                   int *__restrict__ out, double *__restrict__ orho,
+                   const double *__restrict__ rsrc) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int G = (int)cl.num_blocks(), crank = (int)cl.block_rank();
+  const int m = blockIdx.x / G;
+  if (m >= P) return;  // whole clusters only (the grid is P * G)
+  const int s = ms[m], n = mn[m], n1 = mn1[m];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  constexpr int NW = MT / 32, PB = 4;
+  const unsigned below = (1u << lane) - 1u;
+  __shared__ unsigned long long s_sl[2];
+  __shared__ double s_sd[2];
+  __shared__ int s_ng;
+  int ph = 0, phd = 0;
+  const double rho_in = rsrc ? rsrc[m] : e[s + n1 - 1];
+  // this CTA's positions, split into warp segments as in k_merge_prepare
+  const int a0 = (int)((long long)n * crank / G), a1 = (int)((long long)n * (crank + 1) / G);
+  const int seg = ((((a1 - a0) + NW - 1) / NW) + 31) & ~31;
+  const int w0 = min(a1, a0 + wid * seg), w1 = min(a1, w0 + seg);
+  // ---- maxima of |d| and |z| (mdlaed2.f90:265-267)
+  double dmax = 0.0, zmax = 0.0;
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    double zv[PB], dv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      zv[b] = i < w1 ? w.zs[s + i] : 0.0;
+      dv[b] = i < w1 ? w.ds[s + i] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) { zmax = fmax(zmax, fabs(zv[b])); dmax = fmax(dmax, fabs(dv[b])); }
+  }
+  dmax = cl_max(block_max<MT>(dmax), s_sd, phd);
+  zmax = cl_max(block_max<MT>(zmax), s_sd, phd);
+  const double rho = fabs(2.0 * rho_in);
+  const double tol = 8.0 * HSS_EPS * fmax(dmax, zmax);
+  if (rho * zmax <= tol) {  // nothing couples the halves
+    for (int i = a0 + tid; i < a1; i += MT) perm[s + i] = w.srt[s + i];
+    if (crank == 0 && tid == 0) {
+      out[5 * m] = 0; out[5 * m + 1] = 0; out[5 * m + 2] = 0; out[5 * m + 3] = 0;
+      out[5 * m + 4] = 0;
+      orho[m] = rho;
+    }
+    cl.sync();
+    return;
+  }
+  // ---- candidates (deflation by small z, mdlaed2.f90:304-313), in position order
+  int cnt = 0;
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    double zv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      zv[b] = i < w1 ? w.zs[s + i] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool in = i < w1;
+      const bool big = in && rho * fabs(zv[b]) > tol;
+      if (in && !big) w.typ[s + i] = 4;
+      cnt += __popc(__ballot_sync(HSS_FULL, big));
+    }
+  }
+  unsigned long long tot, ctot;
+  int pos = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)cnt : 0ull, &tot);
+  pos = __shfl_sync(HSS_FULL, pos, 0) + (int)cl_scan(tot, s_sl, ph, &ctot);
+  const int nc = (int)ctot;
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    double zv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      zv[b] = i < w1 ? w.zs[s + i] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool big = i < w1 && rho * fabs(zv[b]) > tol;
+      const unsigned mk = __ballot_sync(HSS_FULL, big);
+      if (big) w.cand[s + pos + __popc(mk & below)] = i;
+      pos += __popc(mk);
+    }
+  }
+  cl.sync();  // every candidate written
+  // ---- pairs t = 1 .. nc-1 that may rotate (the chain's quick test on the
+  //      original values), compacted in order into l1slot (free until the
+  //      deflated lists are written)
+  int *lst = w.l1slot + s;
+  auto cz = [&](int t) { return w.zs[s + __ldcg(w.cand + s + t)]; };
+  auto cd = [&](int t) { return w.ds[s + __ldcg(w.cand + s + t)]; };
+  {
+    const int np = max(nc - 1, 0);
+    const int b0 = (int)((long long)np * crank / G), b1 = (int)((long long)np * (crank + 1) / G);
+    const int pseg = ((((b1 - b0) + NW - 1) / NW) + 31) & ~31;
+    const int p0 = min(b1, b0 + wid * pseg), p1 = min(b1, p0 + pseg);
+    auto maybe = [&](int t) -> bool {
+      const double zp = cz(t - 1), zn = cz(t);
+      const double tt = cd(t) - cd(t - 1);
+      return !(fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp));
+    };
+    int cntp = 0;
+    for (int q0 = p0; q0 < p1; q0 += 32) {
+      const int a = q0 + lane;
+      cntp += __popc(__ballot_sync(HSS_FULL, a < p1 && maybe(a + 1)));
+    }
+    unsigned long long ptot, pctot;
+    int ppos = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)cntp : 0ull, &ptot);
+    ppos = __shfl_sync(HSS_FULL, ppos, 0) + (int)cl_scan(ptot, s_sl, ph, &pctot);
+    for (int q0 = p0; q0 < p1; q0 += 32) {
+      const int a = q0 + lane;
+      const bool mb = a < p1 && maybe(a + 1);
+      const unsigned mk = __ballot_sync(HSS_FULL, mb);
+      if (mb) lst[ppos + __popc(mk & below)] = a + 1;
+      ppos += __popc(mk);
+    }
+    if (tid == 0) s_ng = (int)pctot;  // the list's length, until the chain sets ng
+  }
+  cl.sync();  // the pair list complete
+  // ---- the chain (mdlaed2.f90:314-371) on thread 0 of the first CTA
+  if (crank == 0 && tid == 0) {
+    const int nl = s_ng;
+    auto zr = [&](int t) -> double & { return w.zs[s + __ldcg(w.cand + s + t)]; };
+    auto dr = [&](int t) -> double & { return w.ds[s + __ldcg(w.cand + s + t)]; };
+    auto tr = [&](int t) -> unsigned char & { return w.typ[s + __ldcg(w.cand + s + t)]; };
+    int ng = 0, done = 0;
+    auto visit = [&](int t) -> bool {
+      const int pj = t - 1, nj = t;
+      const double zp = zr(pj), zn = zr(nj);
+      const double tt = dr(nj) - dr(pj);
+      if (fabs(tt * zn * zp) > 1.000000000001 * tol * fma(zn, zn, zp * zp)) return false;
+      const double tau = hypot(zn, zp);
+      const double c = zn / tau, sn = -zp / tau;
+      if (!(fabs(tt * c * sn) <= tol)) return false;
+      zr(nj) = tau;
+      zr(pj) = 0.0;
+      if (tr(nj) != tr(pj)) tr(nj) = 2;
+      tr(pj) = 5;
+      w.gvp[s + ng] = w.srt[s + __ldcg(w.cand + s + pj)];
+      w.gvq[s + ng] = w.srt[s + __ldcg(w.cand + s + nj)];
+      w.gvc[s + ng] = c;
+      w.gvs[s + ng] = sn;
+      ++ng;
+      const double dp = dr(pj), dn = dr(nj);
+      dr(pj) = dp * c * c + dn * sn * sn;
+      dr(nj) = dp * sn * sn + dn * c * c;
+      return true;
+    };
+    for (int a = 0; a < nl; ++a) {
+      int t = __ldcg(lst + a);
+      if (t <= done) continue;
+      bool rot = visit(t);
+      done = t;
+      while (rot && t + 1 < nc) {
+        ++t;
+        rot = visit(t);
+        done = t;
+      }
+    }
+    s_ng = ng;
+    __threadfence();
+  }
+  cl.sync();  // the chain's values and types visible
+  // ---- compact non-deflated and deflated lists (reads through L2: the chain
+  //      may have changed any candidate)
+  unsigned long long pk = 0;
+  int n5 = 0;
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    int tv[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      tv[b] = i < w1 ? __ldcg(w.typ + s + i) : 0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int t = tv[b];
+      pk += (unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 1)) +
+            ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 2)) << 21) +
+            ((unsigned long long)__popc(__ballot_sync(HSS_FULL, t == 3)) << 42);
+      n5 += __popc(__ballot_sync(HSS_FULL, t == 5));
+    }
+  }
+  unsigned long long ptot, t5, cptot, ct5;
+  unsigned long long pre = block_scan64<MT>(lane == 0 ? pk : 0ull, &ptot);
+  int r5 = (int)block_scan64<MT>(lane == 0 ? (unsigned long long)n5 : 0ull, &t5);
+  pre = __shfl_sync(HSS_FULL, pre, 0) + cl_scan(ptot, s_sl, ph, &cptot);
+  r5 = __shfl_sync(HSS_FULL, r5, 0) + (int)cl_scan(t5, s_sl, ph, &ct5);
+  const int c1 = (int)(cptot & 0x1fffff), c2 = (int)((cptot >> 21) & 0x1fffff),
+            c3 = (int)((cptot >> 42) & 0x1fffff);
+  const int K = c1 + c2 + c3;
+  const int nrot = (int)ct5;
+  int r1 = (int)(pre & 0x1fffff), r2 = (int)((pre >> 21) & 0x1fffff),
+      r3 = (int)((pre >> 42) & 0x1fffff);
+  for (int i0 = w0; i0 < w1; i0 += 32 * PB) {
+    int tb[PB], sb[PB];
+    double db[PB], zb[PB];
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool in = i < w1;
+      tb[b] = in ? __ldcg(w.typ + s + i) : 0;
+      db[b] = in ? __ldcg(w.ds + s + i) : 0.0;
+      zb[b] = in ? __ldcg(w.zs + s + i) : 0.0;
+      sb[b] = in ? w.srt[s + i] : 0;
+    }
+#pragma unroll
+    for (int b = 0; b < PB; ++b) {
+      const int i = i0 + 32 * b + lane;
+      const bool in = i < w1;
+      const int t = tb[b];
+      const unsigned m1 = __ballot_sync(HSS_FULL, t == 1), m2 = __ballot_sync(HSS_FULL, t == 2),
+                     m3 = __ballot_sync(HSS_FULL, t == 3), m5 = __ballot_sync(HSS_FULL, t == 5);
+      if (in) {
+        const int e1 = r1 + __popc(m1 & below), e2 = r2 + __popc(m2 & below),
+                  e3 = r3 + __popc(m3 & below), e5 = r5 + __popc(m5 & below);
+        const int j = e1 + e2 + e3;
+        if (t <= 3) {
+          w.dl[s + j] = db[b];
+          w.zw[s + j] = zb[b];
+          w.ndslot[s + j] = sb[b];
+          w.grp[s + j] = (t == 1) ? e1 : (t == 2) ? c1 + e2 : c1 + c2 + e3;
+        } else {
+          const int a = i - j;
+          Dp[sb[b]] = db[b];
+          if (t == 5) {
+            w.l2slot[s + e5] = sb[b]; w.l2val[s + e5] = db[b];
+          } else {
+            const int a1d = a - e5;
+            w.l1slot[s + a1d] = sb[b]; w.l1val[s + a1d] = db[b];
+          }
+        }
+      }
+      r1 += __popc(m1); r2 += __popc(m2); r3 += __popc(m3); r5 += __popc(m5);
+    }
+  }
+  cl.sync();  // the lists complete
+  const int n1l = (n - K) - nrot;
+  // ---- the rotated list sorted by the first CTA (usually short)
+  if (crank == 0 && nrot > 1) {
+    constexpr int NCS = 1536;
+    __shared__ double c_v[NCS], c_tv[NCS];
+    __shared__ int c_p[NCS], c_tp[NCS];
+    if (nrot <= NCS) {
+      for (int i = tid; i < nrot; i += MT) { c_v[i] = __ldcg(w.l2val + s + i); c_p[i] = __ldcg(w.l2slot + s + i); }
+      __syncthreads();
+      block_sort_pairs(c_v, c_p, c_tv, c_tp, nrot);
+      for (int i = tid; i < nrot; i += MT) { w.l2val[s + i] = c_v[i]; w.l2slot[s + i] = c_p[i]; }
+    } else {
+      block_sort_pairs(w.l2val + s, w.l2slot + s, w.ds + s, w.cand + s, nrot);
+    }
+    __threadfence();
+  }
+  cl.sync();  // the sorted rotated list visible
+  // ---- merge the two deflated lists (mdlaed2.f90:340-356), split between CTAs
+  {
+    const int q0 = (int)((long long)n1l * crank / G), q1 = (int)((long long)n1l * (crank + 1) / G);
+    for (int i = q0 + tid; i < q1; i += MT) {  // L1 element: count L2 < v
+      const double v = __ldcg(w.l1val + s + i);
+      int lo = 0, hi = nrot;
+      while (lo < hi) { int md = (lo + hi) >> 1; if (__ldcg(w.l2val + s + md) < v) lo = md + 1; else hi = md; }
+      w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = __ldcg(w.l1slot + s + i);
+    }
+    const int u0 = (int)((long long)nrot * crank / G), u1 = (int)((long long)nrot * (crank + 1) / G);
+    for (int i = u0 + tid; i < u1; i += MT) {  // L2 element: count L1 <= v
+      const double v = __ldcg(w.l2val + s + i);
+      int lo = 0, hi = n1l;
+      while (lo < hi) { int md = (lo + hi) >> 1; if (__ldcg(w.l1val + s + md) <= v) lo = md + 1; else hi = md; }
+      w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = __ldcg(w.l2slot + s + i);
+    }
+  }
+  if (crank == 0 && tid == 0) {
+    out[5 * m] = K; out[5 * m + 1] = s_ng; out[5 * m + 2] = c1; out[5 * m + 3] = c2;
+    out[5 * m + 4] = c3;
+    orho[m] = rho;
+  }
+}
+
 // Apply each merge's Givens rotations, in order, to its slot pairs: one thread
 // per row (rows of a block are independent; columns are read coalesced).
 // Front half of the prepare for all merges of a level, one thread per
@@ -753,6 +1085,24 @@ void launch_merge_prepare(int P, int maxn, const int *ms, const int *mn, const i
                           const LevelScratch &w, int *out, double *orho, cudaStream_t st,
                           const double *zsrc, const double *rsrc, int flags, const int2 *sup) {
   if (P <= 0) return;
+  if ((flags & PREP_FRONT) && maxn > PCL_MIN_N) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(P * PCL_G));
+    cfg.blockDim = dim3(PCL_T);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = PCL_G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_merge_prepare_cl<PCL_T>, P, ms, mn, mn1, e, Dp, perm, w, out,
+                           orho, rsrc) == cudaSuccess)
+      return;
+    (void)cudaGetLastError();  // no cluster launch here: the one-CTA kernel below
+  }
 #define PREP_CASE(T)                                                                        \
   case T:                                                                                  \
     k_merge_prepare<T><<<P, T, 0, st>>>(P, ms, mn, mn1, e, Q, ldq, Dp, perm, w, out, orho, \
