@@ -342,7 +342,9 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
       } else {
         const int a = i - j;  // deflated before position i
         Dp[sv] = dv;
-        if (t == 5) {
+        if (nrot == 0) {  // no rotated poles: the small-z list is the deflated list
+          w.dfslot[s + a] = sv; w.dfval[s + a] = dv;
+        } else if (t == 5) {
           w.l2slot[s + e5] = sv; w.l2val[s + e5] = dv;
         } else {
           const int a1 = a - e5;  // small-z deflated before position i
@@ -357,6 +359,7 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
   // The small-z list is ascending; rotated poles moved inside their gap
   // (mdlaed2.f90:340-356 inserts them in order), so sort those and merge.
   const int n1l = (n - K) - nrot;
+  if (nrot > 0) {  // else the compaction wrote the deflated list directly
   // the (short) rotated list sorted in shared memory (the chain's arrays are
   // free now) and kept there for the searches of the long one
   const bool l2s = nrot <= NCS;
@@ -384,6 +387,7 @@ k_merge_prepare(int P, const int *__restrict__ ms, const int *__restrict__ mn,
     while (lo < hi) { int md = (lo + hi) >> 1; if (w.l1val[s + md] <= v) lo = md + 1; else hi = md; }
     w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = w.l2slot[s + i];
   }
+  }  // nrot > 0
   if (tid == 0) {
     out[5 * m] = K; out[5 * m + 1] = s_ng; out[5 * m + 2] = c1; out[5 * m + 3] = c2;
     out[5 * m + 4] = c3;
@@ -428,13 +432,17 @@ __device__ __forceinline__ unsigned long long cl_scan(unsigned long long v,
   *tot = t;
   return base;
 }
-__device__ __forceinline__ double cl_max(double v, double *slot, int &ph) {
+// cluster-wide maxima of two values (one exchange)
+__device__ __forceinline__ double2 cl_max2(double2 v, double2 *slot) {
   cg::cluster_group cl = cg::this_cluster();
-  if (threadIdx.x == 0) slot[ph] = v;
+  if (threadIdx.x == 0) *slot = v;
   cl.sync();
-  double r = 0.0;
-  for (unsigned q = 0; q < cl.num_blocks(); ++q) r = fmax(r, *cl.map_shared_rank(slot + ph, q));
-  ph ^= 1;
+  double2 r = make_double2(0.0, 0.0);
+  for (unsigned q = 0; q < cl.num_blocks(); ++q) {
+    const double2 x = *cl.map_shared_rank(slot, q);
+    r.x = fmax(r.x, x.x);
+    r.y = fmax(r.y, x.y);
+  }
   return r;
 }
 
@@ -454,9 +462,9 @@ k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn
   constexpr int NW = MT / 32, PB = 4;
   const unsigned below = (1u << lane) - 1u;
   __shared__ unsigned long long s_sl[2];
-  __shared__ double s_sd[2];
+  __shared__ double2 s_sd;
   __shared__ int s_ng;
-  int ph = 0, phd = 0;
+  int ph = 0;
   const double rho_in = rsrc ? rsrc[m] : e[s + n1 - 1];
   // this CTA's positions, split into warp segments as in k_merge_prepare
   const int a0 = (int)((long long)n * crank / G), a1 = (int)((long long)n * (crank + 1) / G);
@@ -475,8 +483,13 @@ k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn
 #pragma unroll
     for (int b = 0; b < PB; ++b) { zmax = fmax(zmax, fabs(zv[b])); dmax = fmax(dmax, fabs(dv[b])); }
   }
-  dmax = cl_max(block_max<MT>(dmax), s_sd, phd);
-  zmax = cl_max(block_max<MT>(zmax), s_sd, phd);
+  dmax = block_max<MT>(dmax);
+  zmax = block_max<MT>(zmax);
+  {
+    const double2 mx = cl_max2(make_double2(dmax, zmax), &s_sd);
+    dmax = mx.x;
+    zmax = mx.y;
+  }
   const double rho = fabs(2.0 * rho_in);
   const double tol = 8.0 * HSS_EPS * fmax(dmax, zmax);
   if (rho * zmax <= tol) {  // nothing couples the halves
@@ -668,7 +681,9 @@ k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn
         } else {
           const int a = i - j;
           Dp[sb[b]] = db[b];
-          if (t == 5) {
+          if (nrot == 0) {  // no rotated poles: the small-z list is the deflated list
+            w.dfslot[s + a] = sb[b]; w.dfval[s + a] = db[b];
+          } else if (t == 5) {
             w.l2slot[s + e5] = sb[b]; w.l2val[s + e5] = db[b];
           } else {
             const int a1d = a - e5;
@@ -679,8 +694,9 @@ k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn
       r1 += __popc(m1); r2 += __popc(m2); r3 += __popc(m3); r5 += __popc(m5);
     }
   }
-  cl.sync();  // the lists complete
+  cl.sync();  // the lists complete (and no CTA leaves while another reads its slots)
   const int n1l = (n - K) - nrot;
+  if (nrot > 0) {  // uniform: nrot is the cluster's count
   // ---- the rotated list sorted by the first CTA (usually short)
   if (crank == 0 && nrot > 1) {
     constexpr int NCS = 1536;
@@ -696,7 +712,7 @@ k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn
     }
     __threadfence();
   }
-  cl.sync();  // the sorted rotated list visible
+  if (nrot > 1) cl.sync();  // the sorted rotated list visible
   // ---- merge the two deflated lists (mdlaed2.f90:340-356), split between CTAs
   {
     const int q0 = (int)((long long)n1l * crank / G), q1 = (int)((long long)n1l * (crank + 1) / G);
@@ -714,6 +730,7 @@ k_merge_prepare_cl(int P, const int *__restrict__ ms, const int *__restrict__ mn
       w.dfval[s + i + lo] = v; w.dfslot[s + i + lo] = __ldcg(w.l2slot + s + i);
     }
   }
+  }  // nrot > 0
   if (crank == 0 && tid == 0) {
     out[5 * m] = K; out[5 * m + 1] = s_ng; out[5 * m + 2] = c1; out[5 * m + 3] = c2;
     out[5 * m + 4] = c3;
