@@ -99,6 +99,9 @@ SIGNATURES = {
                         _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
     "hss_mdbdsdc_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, ctypes.c_int, _V, ctypes.c_int,
                                        _V]),
+    "mdbdsvd_": (None, [_I, _I, _D, _I, _D, _D, _D, _I, _D, _I, _I, _D, _I, _I, _I]),
+    "hss_mdbdsvd_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _V, ctypes.c_int, _V, _V,
+                                       ctypes.c_int, _V, ctypes.c_int, ctypes.c_int, _V]),
     "cauchyhssmm_": (None, [_D, _D, _D, _D, _I, _I, _D, _I, _D, _I, _D]),
     "hss_cauchyhssmm_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, ctypes.c_int,
                                            ctypes.c_double, _V, ctypes.c_int, ctypes.c_int, _V,
@@ -357,6 +360,53 @@ def mdbdsdc_dev(d, e, u, vt, stream=None):
                                   _stream(stream))
     if info != 0:
         raise HssError("hss_mdbdsdc_dev INFO=%d: %s" % (info, _err()))
+    return info
+
+
+def mdbdsvd(n, sb, ab, ldab, a, s, u, ldu, vt, ldvt, smlsiz, work, lwork, iwork):
+    """MDBDSVD with the Fortran argument list (SRC/mdbdsvd.f90:1); numpy arrays,
+    ab (LDAB x N), u and vt Fortran ordered.  Returns (INFO, SMLSIZ on exit)."""
+    for x, dt in ((ab, np.float64), (a, np.float64), (s, np.float64), (u, np.float64),
+                  (vt, np.float64), (work, np.float64), (iwork, np.int32)):
+        if x.dtype != dt:
+            raise TypeError("array dtype must be %s" % dt)
+    for x in (ab, u, vt):
+        if x.ndim == 2 and not x.flags.f_contiguous:
+            raise ValueError("ab, u and vt must be Fortran ordered")
+    info = ctypes.c_int(0)
+    ints = [ctypes.c_int(int(x)) for x in (n, sb, ldab, ldu, ldvt, smlsiz, lwork)]
+    load().mdbdsvd_(ctypes.byref(ints[0]), ctypes.byref(ints[1]), _pd(ab), ctypes.byref(ints[2]),
+                    _pd(a), _pd(s), _pd(u), ctypes.byref(ints[3]), _pd(vt), ctypes.byref(ints[4]),
+                    ctypes.byref(ints[5]), _pd(work), ctypes.byref(ints[6]),
+                    iwork.ctypes.data_as(_I), ctypes.byref(info))
+    return info.value, ints[5].value
+
+
+def svd_banded(ab, sb, smlsiz=25):
+    """(s descending, U, VT) of the upper banded n x n matrix in upper band
+    storage ab ((sb + 1) x n, row sb the diagonal) through MDBDSVD."""
+    ab = np.asfortranarray(ab, dtype=np.float64)
+    n = ab.shape[1]
+    s = np.zeros(n)
+    U = np.zeros((n, n), order="F")
+    VT = np.zeros((n, n), order="F")
+    one = np.zeros(1)
+    info, _ = mdbdsvd(n, sb, ab, ab.shape[0], one, s, U, max(1, n), VT, max(1, n), smlsiz, one, 1,
+                      np.zeros(1, dtype=np.int32))
+    if info != 0:
+        raise HssError("MDBDSVD INFO=%d: %s" % (info, _err()))
+    return s, U, VT
+
+
+def mdbdsvd_dev(sb, ab, s, u, vt, smlsiz=25, stream=None):
+    """Device banded SVD: ab a tensor whose memory is the column-major
+    (sb + 1) x n upper band storage; s (n,) singular values descending, u and vt
+    (n, n) column-major storage."""
+    n = s.numel()
+    info = load().hss_mdbdsvd_dev(n, sb, _ptr(ab), sb + 1, _ptr(s), _ptr(u), max(1, n), _ptr(vt),
+                                  max(1, n), int(smlsiz), _stream(stream))
+    if info != 0:
+        raise HssError("hss_mdbdsvd_dev INFO=%d: %s" % (info, _err()))
     return info
 
 

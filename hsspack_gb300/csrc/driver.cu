@@ -1024,38 +1024,21 @@ __global__ void k_scale(int n, double *x, double a) {
 }
 
 // ------------------------------------------------------------- SVD DC ----
-// One level of bidiagonal SVD merges (MDLASD1, SRC/mdlasd1.f90): deflation
-// (MDLASD2), the secular equation and the z rebuild in squared mode, the K x K
-// U and V blocks, the products U2 Ub and V2 Vb (DLASD3's products), the new
-// ascending order.  Merge m covers rows ms[m] .. ms[m] + N - 1, N = nl+1+nr.
-static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int> &mnl,
-                           const std::vector<int> &mnr, const std::vector<int> &msq,
-                           const double *d, const double *e, double *U, double *V, long long ld,
-                           double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st) {
+// The part of a level of SVD merges after their deflation (shared by the
+// bidiagonal merges and the banded row appends): the deflating rotations of U
+// and V columns, the secular equation and the z rebuild in squared mode, the
+// K x K U and V blocks, the products U2 Ub and V2 Vb (DLASD3's products) or the
+// HSS products (DHSSVCS), sigma back to scale and the new ascending order.
+// hout: the prepare's 5 ints per merge (pinned); mpos: positions per merge
+// (the arrow's size, the pole first); mN / mM: rows of U / V in its window
+// [ms, ms + mN) / [ms, ms + mM); dms / dpos: ms and mpos on the device.
+static void svd_merge_tail(Ctx &c, const std::vector<int> &ms, const std::vector<int> &mpos,
+                           const std::vector<int> &mN, const std::vector<int> &mM,
+                           const int *dms, const int *dpos, const int *hout, const double *dnrm,
+                           double *U, double *V, long long ld, double *Dp, int *perm,
+                           LevelArrays &L, int *status, cudaStream_t st) {
   const int P = (int)ms.size();
-  if (P == 0) return;
-  std::vector<int> mN(P), mM(P);
-  for (int m = 0; m < P; ++m) { mN[m] = mnl[m] + 1 + mnr[m]; mM[m] = mN[m] + msq[m]; }
-  const int maxN = *std::max_element(mN.begin(), mN.end());
-  const int maxM = *std::max_element(mM.begin(), mM.end());
-  int *dms = buf<int>(c, "sv_s", P), *dnl = buf<int>(c, "sv_nl", P), *dnr = buf<int>(c, "sv_nr", P),
-      *dsq = buf<int>(c, "sv_sq", P), *dN = buf<int>(c, "sv_N", P), *dM = buf<int>(c, "sv_M", P);
-  h2d(dms, ms, st); h2d(dnl, mnl, st); h2d(dnr, mnr, st); h2d(dsq, msq, st); h2d(dN, mN, st);
-  h2d(dM, mM, st);
-  int *dout = buf<int>(c, "g_out", 5 * P);
-  double *dnrm = buf<double>(c, "sv_nrm", P);
-  stage_begin(HSS_ST_PREPARE, st);
-  launch_svd_prepare(P, maxN, dms, dnl, dnr, dsq, d, e, U, ld, V, ld, Dp, perm, L.w, dout, dnrm,
-                     st);
-  {
-    long long nn = 0;
-    for (int x : mN) nn += x;
-    stage_end(HSS_ST_PREPARE, st, 64 * nn, 0.0);
-  }
-  c.launches++;
-  int *hout = (int *)pinned(c, (size_t)P * 5 * sizeof(int));
-  CK(cudaMemcpyAsync(hout, dout, (size_t)P * 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+  const int maxPos = *std::max_element(mpos.begin(), mpos.end());
   std::vector<int> aK(P), aoff(P + 1, 0), gs, gN, gM, gng;
   std::vector<double> ones(P, 1.0);
   int maxK = 1, maxNg = 0, maxMg = 0;
@@ -1175,9 +1158,41 @@ static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector
   // ---- sigma back to scale, new ascending order
   stage_begin(HSS_ST_FINISH, st);
   launch_svd_unscale(lv, total, dnrm, L.lam, st);
-  launch_merge_finish(P, maxN, dms, dN, vK, L.lam, L.w, perm, Dp, st);
+  launch_merge_finish(P, maxPos, dms, dpos, vK, L.lam, L.w, perm, Dp, st);
   stage_end(HSS_ST_FINISH, st, 0, 0.0);
   c.launches += 2;
+}
+
+// One level of bidiagonal SVD merges (MDLASD1, SRC/mdlasd1.f90): deflation
+// (MDLASD2) by k_svd_prepare, then svd_merge_tail.  Merge m covers rows
+// ms[m] .. ms[m] + N - 1, N = nl + 1 + nr.
+static void run_svd_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int> &mnl,
+                           const std::vector<int> &mnr, const std::vector<int> &msq,
+                           const double *d, const double *e, double *U, double *V, long long ld,
+                           double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st) {
+  const int P = (int)ms.size();
+  if (P == 0) return;
+  std::vector<int> mN(P), mM(P);
+  for (int m = 0; m < P; ++m) { mN[m] = mnl[m] + 1 + mnr[m]; mM[m] = mN[m] + msq[m]; }
+  const int maxN = *std::max_element(mN.begin(), mN.end());
+  int *dms = buf<int>(c, "sv_s", P), *dnl = buf<int>(c, "sv_nl", P), *dnr = buf<int>(c, "sv_nr", P),
+      *dsq = buf<int>(c, "sv_sq", P), *dN = buf<int>(c, "sv_N", P);
+  h2d(dms, ms, st); h2d(dnl, mnl, st); h2d(dnr, mnr, st); h2d(dsq, msq, st); h2d(dN, mN, st);
+  int *dout = buf<int>(c, "g_out", 5 * P);
+  double *dnrm = buf<double>(c, "sv_nrm", P);
+  stage_begin(HSS_ST_PREPARE, st);
+  launch_svd_prepare(P, maxN, dms, dnl, dnr, dsq, d, e, U, ld, V, ld, Dp, perm, L.w, dout, dnrm,
+                     st);
+  {
+    long long nn = 0;
+    for (int x : mN) nn += x;
+    stage_end(HSS_ST_PREPARE, st, 64 * nn, 0.0);
+  }
+  c.launches++;
+  int *hout = (int *)pinned(c, (size_t)P * 5 * sizeof(int));
+  CK(cudaMemcpyAsync(hout, dout, (size_t)P * 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  svd_merge_tail(c, ms, mN, mN, mM, dms, dN, hout, dnrm, U, V, ld, Dp, perm, L, status, st);
 }
 
 // MDBDSDC('U', COMPQ) (SRC/mdbdsdc.f90:1) of the upper bidiagonal (d, e) in
@@ -1329,6 +1344,207 @@ static int svd_solve(Ctx &c, bool lower, int n, std::vector<double> hd, std::vec
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
   return info;
+}
+
+// ------------------------------------------------------ banded SVD DC ----
+// MDBDSVDT (SRC/mdbdsvdt.f90): a node of X rows keeps nl = X / 2 rows on the
+// left, sb center rows and nr = X - nl - sb rows on the right; the left child
+// has sb extra columns, the right child those of its parent (the root none).
+// lv[0 .. depth - 1] are the merge levels (root first), lv[depth] the leaves.
+struct BNode {
+  int s, X, sq;  // rows [s, s + X), sq extra columns (0 or sb)
+  int nl;        // rows of the left child (merge nodes)
+};
+
+// balanced: nl = (X - sb + 1) / 2 instead of X / 2 (both sides within one row)
+static bool bsvd_levels(int n, int sb, int depth, bool balanced,
+                        std::vector<std::vector<BNode>> &lv) {
+  lv.assign(1, std::vector<BNode>{BNode{0, n, 0, 0}});
+  for (int d = 0; d < depth; ++d) {
+    std::vector<BNode> nx;
+    for (BNode &x : lv.back()) {
+      const int nl = balanced ? (x.X - sb + 1) / 2 : x.X / 2, nr = x.X - nl - sb;
+      if (nl < 1 || nr < 1) return false;
+      x.nl = nl;
+      nx.push_back(BNode{x.s, nl, sb, 0});
+      nx.push_back(BNode{x.s + nl + sb, nr, x.sq, 0});
+    }
+    lv.push_back(nx);
+  }
+  return true;
+}
+
+// The reference's depth floor(log2(n / (msub + 1))) (at least 1), made valid
+// (every node keeps rows on both sides), then deepened until every leaf fits
+// one CTA's shared memory (bsvd_rows_max() rows).  The reference's halving
+// shrinks right children by sb at every level; when no depth of it fits (wide
+// bands), balanced cuts are used instead.  Returns the depth, or -1.
+static int bsvd_tree(int n, int sb, int msub, std::vector<std::vector<BNode>> &lv) {
+  if (n <= bsvd_rows_max()) {
+    lv.assign(1, std::vector<BNode>{BNode{0, n, 0, 0}});
+    return 0;
+  }
+  auto largest = [&lv]() {
+    int mx = 0;
+    for (const BNode &x : lv.back()) mx = std::max(mx, x.X);
+    return mx;
+  };
+  for (int balanced = 0; balanced < 2; ++balanced) {
+    int depth = balanced ? 1 : std::max(1, (int)std::floor(std::log2((double)n / (double)(msub + 1))));
+    while (depth > 1 && !bsvd_levels(n, sb, depth, balanced, lv)) --depth;
+    if (!bsvd_levels(n, sb, depth, balanced, lv)) continue;
+    bool fits = true;
+    while (fits && largest() > bsvd_rows_max()) {
+      std::vector<std::vector<BNode>> t;
+      fits = bsvd_levels(n, sb, depth + 1, balanced, t);
+      if (fits) {
+        lv.swap(t);
+        ++depth;
+      }
+    }
+    if (fits) return depth;
+  }
+  return -1;
+}
+
+// Append k (0 .. sb - 1) of every merge of one level (MDBDSVD1's loop over the
+// inserted rows, SRC/mdbdsvd1.f90:259-354): z = V^T b for row c_k = s + nl + k,
+// the fold of the null vectors, the deflation, then the shared merge tail.
+static void run_bsvd_append(Ctx &c, const std::vector<BNode> &nodes, int k, int sb, int n,
+                            const double *ab, long long ldab, double *U, double *V, long long ld,
+                            double *Dp, int *perm, LevelArrays &L, int *status, cudaStream_t st) {
+  const int P = (int)nodes.size();
+  std::vector<int> ms(P), mrow(P), mN(P), mM(P), mnl(P), mna(P), mb0(P), mnb(P), mpos(P),
+      poff(P + 1, 0);
+  for (int m = 0; m < P; ++m) {
+    const BNode &x = nodes[m];
+    const int nl = x.nl, nr = x.X - nl - sb;
+    ms[m] = x.s;
+    mN[m] = x.X;
+    mM[m] = x.X + x.sq;
+    mnl[m] = nl;
+    mrow[m] = x.s + nl + k;
+    mna[m] = k == 0 ? nl : nl + nr + k;  // the first append merges both children's lists
+    mb0[m] = k == 0 ? x.s + nl + sb : 0;
+    mnb[m] = k == 0 ? nr : 0;
+    mpos[m] = nl + nr + k + 1;
+    poff[m + 1] = poff[m] + mM[m];
+  }
+  const int maxM = *std::max_element(mM.begin(), mM.end());
+  const int maxPos = *std::max_element(mpos.begin(), mpos.end());
+  int *dms = buf<int>(c, "bs_s", P), *drow = buf<int>(c, "bs_row", P), *dN = buf<int>(c, "bs_N", P),
+      *dM = buf<int>(c, "bs_M", P), *dnl = buf<int>(c, "bs_nl", P), *dna = buf<int>(c, "bs_na", P),
+      *db0 = buf<int>(c, "bs_b0", P), *dnb = buf<int>(c, "bs_nb", P), *dpos = buf<int>(c, "bs_pos", P),
+      *dpoff = buf<int>(c, "bs_poff", P + 1);
+  h2d(dms, ms, st); h2d(drow, mrow, st); h2d(dN, mN, st); h2d(dM, mM, st); h2d(dnl, mnl, st);
+  h2d(dna, mna, st); h2d(db0, mb0, st); h2d(dnb, mnb, st); h2d(dpos, mpos, st); h2d(dpoff, poff, st);
+  double *z = buf<double>(c, "bs_z", n);
+  double *amax = buf<double>(c, "bs_amax", P);
+  int *dout = buf<int>(c, "g_out", 5 * P);
+  double *dnrm = buf<double>(c, "sv_nrm", P);
+  stage_begin(HSS_ST_PREPARE, st);
+  launch_bsvd_z(P, poff[P], dpoff, dms, drow, sb, n, ab, ldab, V, ld, z, st);
+  launch_bsvd_fold(P, maxM, dms, dN, dM, dnl, drow, sb, n, ab, ldab, V, ld, z, amax, st);
+  launch_bsvd_prepare(P, maxPos, dms, drow, dna, db0, dnb, amax, z, U, ld, Dp, perm, L.w, dout,
+                      dnrm, st);
+  {
+    long long bytes = 0;
+    for (int m = 0; m < P; ++m)
+      bytes += 8LL * mM[m] * (sb + 2) + 16LL * mM[m] * (2 * sb) + 64LL * mpos[m];
+    stage_end(HSS_ST_PREPARE, st, bytes, 0.0);
+  }
+  c.launches += 3;
+  int *hout = (int *)pinned(c, (size_t)P * 5 * sizeof(int));
+  CK(cudaMemcpyAsync(hout, dout, (size_t)P * 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  svd_merge_tail(c, ms, mpos, mN, mM, dms, dpos, hout, dnrm, U, V, ld, Dp, perm, L, status, st);
+}
+
+// MDBDSVD (SRC/mdbdsvd.f90:1) of the n x n upper banded matrix in HBM (upper
+// band storage, ldab >= sb + 1): singular values descending into w, U (ldu),
+// VT (ldvt).  The leaves' dense SVDs, then per merge level the sb row appends.
+static int bsvd_core(Ctx &c, int n, int sb, const double *ab, long long ldab, int msub,
+                     double *Uo, long long ldu, double *VT, long long ldvt, double *w,
+                     cudaStream_t st) {
+  memset(&c.stats, 0, sizeof c.stats);
+  c.launches = 0;
+  std::vector<std::vector<BNode>> lv;
+  const int depth = bsvd_tree(n, sb, msub, lv);
+  if (depth < 0) {
+    c.err = "MDBDSVD: no cut of the band leaves every block within the leaf size";
+    return -2;
+  }
+  cudaEvent_t ev0, ev1;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  CK(cudaEventRecord(ev0, st));
+  double *U = buf<double>(c, "sv_U", (size_t)n * n);
+  double *V = buf<double>(c, "sv_V", (size_t)n * n);
+  double *Dp = buf<double>(c, "Dp", n);
+  int *perm = buf<int>(c, "perm", n);
+  int *status = buf<int>(c, "status", 8);
+  CK(cudaMemsetAsync(status, 0, 8 * sizeof(int), st));
+  CK(cudaMemsetAsync(gemm_flag(c), 0, sizeof(int), st));
+  CK(cudaMemsetAsync(U, 0, sizeof(double) * (size_t)n * n, st));
+  CK(cudaMemsetAsync(V, 0, sizeof(double) * (size_t)n * n, st));
+  {
+    std::vector<int> la, lr, lc;
+    double flops = 0.0;
+    for (const BNode &x : lv.back()) {
+      la.push_back(x.s);
+      lr.push_back(x.X);
+      lc.push_back(x.X + x.sq);
+      const double cc = x.X + x.sq;
+      flops += 10.0 * 3.0 * cc * cc * (x.X + cc);  // ~10 sweeps of c^2/2 rotations
+    }
+    const int nl = (int)la.size();
+    int *dla = buf<int>(c, "bl_a", nl), *dlr = buf<int>(c, "bl_r", nl), *dlc = buf<int>(c, "bl_c", nl);
+    h2d(dla, la, st); h2d(dlr, lr, st); h2d(dlc, lc, st);
+    stage_begin(HSS_ST_LEAF, st);
+    launch_bsvd_leaf(nl, dla, dlr, dlc, sb, ab, ldab, U, n, V, n, Dp, perm, status, st);
+    stage_end(HSS_ST_LEAF, st, 8LL * n * (sb + 1) + 16LL * n * 96, flops);
+    c.launches++;
+  }
+  if (depth > 0) {
+    LevelArrays L = level_arrays(c, n);
+    for (int d = depth - 1; d >= 0; --d) {  // merges bottom-up
+      c.stats.n_levels++;
+      for (int k = 0; k < sb; ++k)
+        run_bsvd_append(c, lv[d], k, sb, n, ab, ldab, U, V, n, Dp, perm, L, status, st);
+    }
+  }
+  stage_begin(HSS_ST_FINAL, st);
+  launch_svd_outputs(n, perm, Dp, U, n, V, n, Uo, ldu, VT, ldvt, w, true, st);
+  stage_end(HSS_ST_FINAL, st, 32LL * n * n, 0.0);
+  c.launches += 2;
+  CK(cudaEventRecord(ev1, st));
+  int hst[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  CK(cudaMemcpyAsync(hst, status, sizeof hst, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hst + 1, gemm_flag(c), sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  unsigned long long its, terms;
+  memcpy(&its, hst + 2, sizeof its);
+  memcpy(&terms, hst + 6, sizeof terms);
+  c.stats.secular_iters = (long long)its;
+  c.stats.stage_flops[HSS_ST_SECULAR] = 15.0 * (double)terms;
+  float ms_ = 0.f;
+  CK(cudaEventElapsedTime(&ms_, ev0, ev1));
+  c.stats.ms_total = ms_;
+  c.stats.kernel_launches = c.launches;
+  collect_stage_times(c);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  CK(cudaGetLastError());
+  if (hst[1]) {
+    c.err = "tensor-core product: bounded wait timed out";
+    return 1;
+  }
+  if (hst[0] != 0) {
+    c.err = hst[0] == HSS_SECULAR_NOCONV ? "secular iteration did not converge"
+                                          : "leaf Jacobi iteration did not converge";
+    return 1;
+  }
+  return 0;
 }
 
 // Symmetric band eigensolve from device arrays: ab upper band storage
@@ -1753,6 +1969,94 @@ void mdbdsdc_(const char *uplo, const char *compq, const int *n_, double *d, dou
   } catch (CudaError &ex) {
     c.err = ex.msg;
     *info = 1000000;
+  }
+}
+
+// MDBDSVD (SRC/mdbdsvd.f90:1) on device arrays.  The band's leaves are at most
+// 64 rows and 96 columns, so sb <= 32.
+int hss_mdbdsvd_dev(int n, int sb, const double *ab, int ldab, double *s, double *u, int ldu,
+                    double *vt, int ldvt, int smlsiz, void *stream) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (n < 0) return -1;
+  if (sb < 1 || sb > n || sb > 32) {
+    c.err = "hss_mdbdsvd_dev: sb must be in 1 .. min(n, 32)";
+    return -2;
+  }
+  if (ldab < sb + 1) return -4;
+  if (ldu < std::max(1, n)) return -7;
+  if (ldvt < std::max(1, n)) return -9;
+  if (smlsiz < 3) return -10;
+  if (n == 0) return 0;
+  try {
+    return bsvd_core(c, n, sb, ab, ldab, std::max(smlsiz, 3 * sb), u, ldu, vt, ldvt, s,
+                     (cudaStream_t)stream);
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    return 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    return 1000001;
+  }
+}
+
+// MDBDSVD(N, SB, AB, LDAB, A, S, U, LDU, VT, LDVT, SMLSIZ, WORK, LWORK, IWORK,
+// INFO) with host arrays.  Argument checks as mdbdsvd.f90:120-137 (the second
+// group overrides the first), plus LDAB >= SB + 1 (-4) and SB <= 32 (-3).  A,
+// WORK, LWORK and IWORK are not used (the reference's workspaces); SMLSIZ is
+// raised to 3 SB as MDBDSVDT does.
+void mdbdsvd_(const int *n_, const int *sb_, double *ab, const int *ldab_, double *a, double *s,
+              double *u, const int *ldu_, double *vt, const int *ldvt_, int *smlsiz_, double *work,
+              int *lwork_, int *iwork, int *info) {
+  Ctx &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  (void)a; (void)work; (void)lwork_; (void)iwork;
+  const int n = *n_, sb = *sb_, ldab = *ldab_, ldu = *ldu_, ldvt = *ldvt_;
+  *info = 0;
+  if (n < 0 || n < sb) *info = -2;
+  else if (sb < 1) *info = -3;
+  if (ldu < n) *info = -9;
+  else if (ldvt < n) *info = -10;
+  else if (*smlsiz_ < 3) *info = -11;
+  if (*info == 0 && ldab < sb + 1) *info = -4;
+  if (*info == 0 && sb > 32) {
+    *info = -3;
+    c.err = "MDBDSVD: semibandwidths above 32 are not supported";
+    return;
+  }
+  if (*info != 0) {
+    c.err = "MDBDSVD: illegal argument " + std::to_string(-*info);
+    return;
+  }
+  if (n > *smlsiz_ && *smlsiz_ < 3 * sb) *smlsiz_ = 3 * sb;
+  if (n == 0) return;
+  try {
+    cudaStream_t st = nullptr;
+    const long long lda = sb + 1;
+    std::vector<double> hb((size_t)lda * n);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i <= sb; ++i) hb[(size_t)j * lda + i] = ab[(size_t)j * ldab + i];  // AB(SB+1+I-J, J)
+    double *dab = buf<double>(c, "band_ab", hb.size());
+    double *dU = buf<double>(c, "z_out", (size_t)n * n);
+    double *dVT = buf<double>(c, "vt_out", (size_t)n * n);
+    double *dw = buf<double>(c, "w_out", n);
+    CK(cudaMemcpyAsync(dab, hb.data(), sizeof(double) * hb.size(), cudaMemcpyHostToDevice, st));
+    *info = bsvd_core(c, n, sb, dab, lda, std::max(*smlsiz_, 3 * sb), dU, n, dVT, n, dw, st);
+    if (*info != 0) return;
+    CK(cudaMemcpy2DAsync(u, sizeof(double) * ldu, dU, sizeof(double) * n, sizeof(double) * n, n,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpy2DAsync(vt, sizeof(double) * ldvt, dVT, sizeof(double) * n, sizeof(double) * n, n,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c.stats.host_h2d_bytes = 8LL * lda * n;
+    c.stats.host_d2h_bytes = 16LL * n * n + 8LL * n;
+  } catch (CudaError &ex) {
+    c.err = ex.msg;
+    *info = 1000000;
+  } catch (HssError &ex) {
+    c.err = ex.msg;
+    *info = 1000001;
   }
 }
 

@@ -198,6 +198,25 @@ void launch_svd_outputs(int n, const int *perm, const double *Dp, const double *
 void launch_rows_rotate_back(int n, int ncols, const double *cs, const double *sn, double *A,
                              long long lda, cudaStream_t st);
 
+// bsvd.cu: banded SVD divide and conquer (leaves, row coefficients z = V^T b,
+// the fold of the null vectors, the deflation of a row append)
+size_t bsvd_leaf_smem();
+int bsvd_rows_max();
+int bsvd_cols_max();
+void launch_bsvd_leaf(int nleaf, const int *la, const int *lr, const int *lc, int sb,
+                      const double *AB, long long ldab, double *U, long long ldu, double *V,
+                      long long ldv, double *Dp, int *perm, int *status, cudaStream_t st);
+void launch_bsvd_z(int P, int total, const int *poff, const int *ms, const int *mrow, int sb, int n,
+                   const double *AB, long long ldab, const double *V, long long ldv, double *z,
+                   cudaStream_t st);
+void launch_bsvd_fold(int P, int maxm, const int *ms, const int *mN, const int *mM, const int *mnl,
+                      const int *mrow, int sb, int n, const double *AB, long long ldab, double *V,
+                      long long ldv, double *z, double *amax, cudaStream_t st);
+void launch_bsvd_prepare(int P, int maxn, const int *ms, const int *mrow, const int *mna,
+                         const int *mb0, const int *mnb, const double *amax, const double *zslot,
+                         double *U, long long ldu, const double *Dp, const int *perm,
+                         const LevelScratch &w, int *out, double *onrm, cudaStream_t st);
+
 // driver.cu: set the message hss_last_error() returns
 void set_last_error(const std::string &msg);
 

@@ -105,6 +105,21 @@ void mdbdsdc_(const char *uplo, const char *compq, const int *n, double *d, doub
               double *u, const int *ldu, double *vt, const int *ldvt, double *q, int *iq,
               double *work, int *iwork, int *info, size_t uplo_len, size_t compq_len);
 
+/* MDBDSVD(N,SB,AB,LDAB,A,S,U,LDU,VT,LDVT,SMLSIZ,WORK,LWORK,IWORK,INFO) replaces
+ * SRC/mdbdsvd.f90:1: SVD of the N x N upper banded matrix with SB
+ * superdiagonals, AB(LDAB, N) in upper band storage (AB(SB+1+I-J, J) =
+ * A(I, J)); S returns the singular values in decreasing order, U the left and
+ * VT the (transposed) right singular vectors.  Structured banded divide and
+ * conquer: dense leaf SVDs, then at every merge the SB center rows appended
+ * one at a time.  INFO as the reference (-2: N < 0 or N < SB, -3: SB < 1,
+ * -9 / -10: LDU / LDVT < N, -11: SMLSIZ < 3; the later test wins), plus
+ * -4 for LDAB < SB + 1 and -3 for SB > 32 (leaves of at most 64 rows and 96
+ * columns in one CTA's shared memory).  SMLSIZ is raised to 3 SB when N > SMLSIZ,
+ * as MDBDSVDT does; A, WORK, LWORK and IWORK (workspaces) are not touched. */
+void mdbdsvd_(const int *n, const int *sb, double *ab, const int *ldab, double *a, double *s,
+              double *u, const int *ldu, double *vt, const int *ldvt, int *smlsiz, double *work,
+              int *lwork, int *iwork, int *info);
+
 /* CauchyHssMM(D,F,U,V,N,ni,tol,ncol,B,LDB,time) replaces SRC/cauchyhssmm.f90:1:
  * B(1:N, 1:N) <- C * B for the Cauchy-like C(i,j) = U(i) V(j) / (D(i) - F(j)),
  * compressed to HSS with leaf ni and tolerance tol; time(1) / time(2) return
@@ -192,6 +207,14 @@ int hss_mdstedc_v_dev(int n, double *d, double *e, double *z, int ldz, void *str
  * failure. */
 int hss_mdbdsdc_dev(int n, double *d, double *e, double *u, int ldu, double *vt, int ldvt,
                     void *stream);
+
+/* SVD of the upper banded n x n matrix in HBM (the MDBDSVD path): ab(ldab, n)
+ * upper band storage with 1 <= sb <= min(n, 32) superdiagonals; s(n) singular
+ * values descending, u(ldu, n), vt(ldvt, n) out; smlsiz >= 3 as MDBDSVD's
+ * (the tree depth before the leaves are cut to 64 rows).  Returns 0, -i for a
+ * bad i-th argument, > 0 on failure. */
+int hss_mdbdsvd_dev(int n, int sb, const double *ab, int ldab, double *s, double *u, int ldu,
+                    double *vt, int ldvt, int smlsiz, void *stream);
 
 /* Symmetric band eigensolve in HBM (the MDSBEVD path): ab(ldab, n) upper band
  * storage, kd >= 0 (band divide and conquer up to HSS_BAND_KD_MAX, device
