@@ -152,44 +152,75 @@ __device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 *dig
   }
 }
 
-// exponent e with max|x| <= 2^e (frexp convention), 0 for an all-zero vector
-__device__ __forceinline__ int exp_of(double amax) {
-  if (amax == 0.0) return 0;
-  int e;
-  frexp(amax, &e);
-  return e;
+// frexp exponent of the largest |x| from its bit pattern (0 for zero)
+__device__ __forceinline__ int bits_exp(unsigned long long b) {
+  if (b == 0) return 0;
+  const int ex = (int)(b >> 52);
+  return ex ? ex - 1022 : (64 - __clzll((long long)b)) - 1074;
 }
 
-// A: M x K (lda) -> planes [tile_m][tile_k][s] of TM x TK, row exponents.
-// One CTA per 128-row panel; pass 1 row max, pass 2 digits.
-__device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
-  __shared__ double smax[8][TM];
-  __shared__ int sexp[TM];
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  // pass 1: each warp takes columns k = w, w+8, ...; lanes cover 4 x 32 rows
-  double mx[4] = {0, 0, 0, 0};
-  for (int k = w; k < P.inner; k += 8)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int r = tm * TM + q * 32 + lane;
-      if (r < P.rows) mx[q] = fmax(mx[q], fabs(P.src[(long long)k * P.ld + r]));
+
+// The split runs over work items (operand, panel, chunk of SPLIT_KC k values):
+// k_split_amax / k_split_bmax record the largest |x| of every row of A /
+// column of B as its bit pattern (atomicMax on the sign-cleared bits, which
+// order like |x|), then k_split_a / k_split_b write the digits of their chunk
+// with the row / column exponents frexp(max|x|).  Many items per panel keep
+// enough loads in flight for the long K of the large products.
+constexpr int SPLIT_KC = 128;
+constexpr int SPLIT_KT = SPLIT_KC / TK;  // k tiles per item
+
+// the operand whose items contain flattened item b (operands sorted by w0)
+__device__ __forceinline__ int split_operand(const SplitProb *__restrict__ probs, int nprob, int b) {
+  int lo = 0, hi = nprob;
+  while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (probs[mid].w0 <= b) lo = mid; else hi = mid; }
+  return lo;
+}
+
+// A (M x K, lda): item = (row panel tm, chunk kc), tm fastest
+__global__ void __launch_bounds__(256)
+k_split_amax(const SplitProb *__restrict__ probs, int nprob) {
+  const SplitProb P = probs[split_operand(probs, nprob, blockIdx.x)];
+  const int t = blockIdx.x - P.w0, ntm = (P.rows + TM - 1) / TM;
+  const int tm = t % ntm, kc = t / ntm;
+  const int tid = threadIdx.x, half = tid >> 7, r = tm * TM + (tid & 127);
+  const int k1 = min(P.inner, (kc + 1) * SPLIT_KC);
+  unsigned long long m = 0;
+  if (r < P.rows) {
+#pragma unroll 4
+    for (int k = kc * SPLIT_KC + half; k < k1; k += 2) {
+      const unsigned long long b =
+          (unsigned long long)__double_as_longlong(P.src[(long long)k * P.ld + r]) & 0x7FFFFFFFFFFFFFFFull;
+      m = b > m ? b : m;
     }
-#pragma unroll
-  for (int q = 0; q < 4; ++q) smax[w][q * 32 + lane] = mx[q];
+  }
+  __shared__ unsigned long long sm[128];
+  if (half) sm[tid & 127] = m;
   __syncthreads();
+  if (!half && r < P.rows) {
+    const unsigned long long o = sm[tid];
+    atomicMax(P.mbits + r, o > m ? o : m);
+  }
+}
+
+// A: planes [tile_m][tile_k][s] of TM x TK for the k tiles of chunk kc; the
+// thread handles (row, 8 consecutive k) -> 16-byte rows of core matrices
+__global__ void __launch_bounds__(256)
+k_split_a(const SplitProb *__restrict__ probs, int nprob) {
+  const SplitProb P = probs[split_operand(probs, nprob, blockIdx.x)];
+  const int t = blockIdx.x - P.w0, ntm = (P.rows + TM - 1) / TM;
+  const int tm = t % ntm, kc = t / ntm;
+  const int tid = threadIdx.x;
+  __shared__ int sexp[TM];
   if (tid < TM) {
-    double m = 0.0;
-    for (int i = 0; i < 8; ++i) m = fmax(m, smax[i][tid]);
-    const int e = exp_of(m);
     const int r = tm * TM + tid;
-    if (r < P.rows) P.expo[r] = e;
+    const int e = r < P.rows ? bits_exp(P.mbits[r]) : 0;
     sexp[tid] = e;
+    if (kc == 0 && r < P.rows) P.expo[r] = e;
   }
   __syncthreads();
-  // pass 2: thread handles (row, 8 consecutive k) -> 16-byte rows of core matrices
-  const int nkt = (P.inner + TK - 1) / TK;
+  const int kt0 = kc * SPLIT_KT, nkt = min(P.ktiles, kt0 + SPLIT_KT) - kt0;
   for (int v = tid; v < nkt * TM * (TK / 8); v += 256) {
-    const int kt = v / (TM * (TK / 8)), u = v % (TM * (TK / 8));
+    const int kt = kt0 + v / (TM * (TK / 8)), u = v % (TM * (TK / 8));
     char *tile = (char *)P.dst + ((long long)tm * P.ktiles + kt) * SP * ATILE;
     const int r = u % TM, k8 = u / TM;
     const int gr = tm * TM + r;
@@ -210,29 +241,53 @@ __device__ __forceinline__ void split_a_panel(const SplitProb &P, int tm) {
   }
 }
 
-// B: K x N (ldb) -> one K-major tile per (tile_n, tile_k) holding the SP
-// planes stacked along N (plane p in rows p TN .. p TN + TN - 1, so the
-// planes 0..P-1 form one operand of N = P TN rows), column exponents.  One
-// CTA per TN-column panel.
-__device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
-  __shared__ int sexp[TN];
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  for (int c = w; c < TN; c += 8) {  // warp per column: max over k
+// B (K x N, ldb; column gc holds k contiguously): item = (column panel tn,
+// chunk kc); warp per column, lanes along k
+__global__ void __launch_bounds__(256)
+k_split_bmax(const SplitProb *__restrict__ probs, int nprob) {
+  const SplitProb P = probs[split_operand(probs, nprob, blockIdx.x)];
+  const int t = blockIdx.x - P.w0, ntn = (P.rows + TN - 1) / TN;
+  const int tn = t % ntn, kc = t / ntn;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k1 = min(P.inner, (kc + 1) * SPLIT_KC);
+  for (int c = w; c < TN; c += 8) {
     const int gc = tn * TN + c;
-    double m = 0.0;
-    if (gc < P.rows)
-      for (int k = lane; k < P.inner; k += 32) m = fmax(m, fabs(P.src[(long long)gc * P.ld + k]));
-    m = warp_max(m);
-    if (lane == 0) {
-      const int e = exp_of(m);
-      if (gc < P.rows) P.expo[gc] = e;
-      sexp[c] = e;
+    if (gc >= P.rows) break;
+    unsigned long long m = 0;
+    for (int k = kc * SPLIT_KC + lane; k < k1; k += 32) {
+      const unsigned long long b =
+          (unsigned long long)__double_as_longlong(P.src[(long long)gc * P.ld + k]) & 0x7FFFFFFFFFFFFFFFull;
+      m = b > m ? b : m;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long v = __shfl_xor_sync(HSS_FULL, m, o);
+      m = v > m ? v : m;
+    }
+    if (lane == 0) atomicMax(P.mbits + gc, m);
+  }
+}
+
+// B: one K-major tile per (tile_n, tile_k) holding the SP planes stacked along
+// N (plane p in rows p TN .. p TN + TN - 1, so the planes 0..P-1 form one
+// operand of N = P TN rows), for the k tiles of chunk kc
+__global__ void __launch_bounds__(256)
+k_split_b(const SplitProb *__restrict__ probs, int nprob) {
+  const SplitProb P = probs[split_operand(probs, nprob, blockIdx.x)];
+  const int t = blockIdx.x - P.w0, ntn = (P.rows + TN - 1) / TN;
+  const int tn = t % ntn, kc = t / ntn;
+  const int tid = threadIdx.x;
+  __shared__ int sexp[TN];
+  if (tid < TN) {
+    const int gc = tn * TN + tid;
+    const int e = gc < P.rows ? bits_exp(P.mbits[gc]) : 0;
+    sexp[tid] = e;
+    if (kc == 0 && gc < P.rows) P.expo[gc] = e;
   }
   __syncthreads();
-  const int nkt = (P.inner + TK - 1) / TK;
+  const int kt0 = kc * SPLIT_KT, nkt = min(P.ktiles, kt0 + SPLIT_KT) - kt0;
   for (int v = tid; v < nkt * TN * (TK / 8); v += 256) {
-    const int kt = v / (TN * (TK / 8)), u = v % (TN * (TK / 8));
+    const int kt = kt0 + v / (TN * (TK / 8)), u = v % (TN * (TK / 8));
     char *tile = (char *)P.dst + ((long long)tn * P.ktiles + kt) * SP * BTILE;
     const int c = u / (TK / 8), k8 = u % (TK / 8);
     const int gc = tn * TN + c;
@@ -250,24 +305,6 @@ __device__ __forceinline__ void split_b_panel(const SplitProb &P, int tn) {
     for (int s = 0; s < SP; ++s)
       *reinterpret_cast<uint4 *>(tile + tile_off(s * TN + c, k8 * 8, SP * TN)) =
           *reinterpret_cast<uint4 *>(dg[s]);
-  }
-}
-
-// One CTA per (panel, problem), problems strided over gridDim.y (<= 65535).
-__global__ void __launch_bounds__(256)
-k_split_a(const SplitProb *__restrict__ probs, int nprob) {
-  for (int pi = blockIdx.y; pi < nprob; pi += gridDim.y) {
-    const SplitProb P = probs[pi];
-    if ((int)blockIdx.x * TM < P.rows) split_a_panel(P, blockIdx.x);
-    __syncthreads();
-  }
-}
-__global__ void __launch_bounds__(256)
-k_split_b(const SplitProb *__restrict__ probs, int nprob) {
-  for (int pi = blockIdx.y; pi < nprob; pi += gridDim.y) {
-    const SplitProb P = probs[pi];
-    if ((int)blockIdx.x * TN < P.rows) split_b_panel(P, blockIdx.x);
-    __syncthreads();
   }
 }
 
@@ -602,12 +639,6 @@ struct ExpJob {  // rows of A (stride = lda between k) or columns of B (contiguo
   int off;       // first flattened item of this job
 };
 
-// frexp exponent of the largest |x| from its bit pattern (0 for zero)
-__device__ __forceinline__ int bits_exp(unsigned long long b) {
-  if (b == 0) return 0;
-  const int ex = (int)(b >> 52);
-  return ex ? ex - 1022 : (64 - __clzll((long long)b)) - 1074;
-}
 
 // the SP digits of q (|q| <= 2^60) as BF16 bit patterns, packed into the
 // 16-byte core-matrix rows (element c of the 8 at half-word c)
@@ -815,21 +846,23 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   // split every A and B operand
   std::vector<SplitProb> sa, sb;
   std::vector<TcProb> tc;
-  long long abytes = 0, bbytes = 0, ea = 0, eb = 0;
-  int maxtm = 0, maxtn = 0, tiles = 0;
+  long long abytes = 0, bbytes = 0, ea = 0, eb = 0, wa = 0, wb = 0;
+  int tiles = 0;
   for (const auto &p : probs) {
     const int kt = (p.K + TK - 1) / TK;
     const int ntm = (p.M + TM - 1) / TM, ntn = (p.N + TN - 1) / TN;
-    SplitProb a{p.A, p.lda, p.M, p.K, kt, nullptr, nullptr};
-    SplitProb bb{p.B, p.ldb, p.N, p.K, kt, nullptr, nullptr};
-    a.dst = (void *)abytes; a.expo = (int *)ea;
-    bb.dst = (void *)bbytes; bb.expo = (int *)eb;
+    const int nkc = (kt + SPLIT_KT - 1) / SPLIT_KT;
+    SplitProb a{p.A, p.lda, p.M, p.K, kt, nullptr, nullptr, nullptr, (int)wa};
+    SplitProb bb{p.B, p.ldb, p.N, p.K, kt, nullptr, nullptr, nullptr, (int)wb};
+    a.dst = (void *)abytes; a.expo = (int *)ea; a.mbits = (unsigned long long *)ea;
+    bb.dst = (void *)bbytes; bb.expo = (int *)eb; bb.mbits = (unsigned long long *)eb;
     abytes += (long long)ntm * kt * SP * ATILE;
     bbytes += (long long)ntn * kt * SP * BTILE;
     ea += ntm * TM;
     eb += ntn * TN;
+    wa += (long long)ntm * nkc;
+    wb += (long long)ntn * nkc;
     sa.push_back(a); sb.push_back(bb);
-    maxtm = std::max(maxtm, ntm); maxtn = std::max(maxtn, ntn);
     TcProb t{nullptr, nullptr, nullptr, nullptr, p.C, p.ldc, p.M, p.N, kt, p.beta, tiles};
     tiles += ntm * ntn;
     tc.push_back(t);
@@ -837,9 +870,12 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   if (tiles == 0) return;  // every product is empty
   char *A = pool<char>("gs_A", abytes + 1024), *B = pool<char>("gs_B", bbytes + 1024);
   int *EA = pool<int>("gs_ea", ea + 1), *EB = pool<int>("gs_eb", eb + 1);
+  unsigned long long *MA = pool<unsigned long long>("gs_ma", ea + 1),
+                     *MB = pool<unsigned long long>("gs_mb", eb + 1);
   for (size_t i = 0; i < probs.size(); ++i) {
     sa[i].dst = A + (long long)sa[i].dst; sa[i].expo = EA + (long long)sa[i].expo;
     sb[i].dst = B + (long long)sb[i].dst; sb[i].expo = EB + (long long)sb[i].expo;
+    sa[i].mbits = MA + (long long)sa[i].mbits; sb[i].mbits = MB + (long long)sb[i].mbits;
     tc[i].a_planes = (const char *)sa[i].dst; tc[i].b_planes = (const char *)sb[i].dst;
     tc[i].ea = sa[i].expo; tc[i].eb = sb[i].expo;
   }
@@ -856,9 +892,19 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   stage_h2d(dsb, sb.data(), sb.size() * sizeof(SplitProb), st);
   stage_h2d(dtc, tc.data(), tc.size() * sizeof(TcProb), st);
   stage_h2d(dtp, tp.data(), tp.size() * sizeof(int), st);
-  const unsigned gy = (unsigned)std::min<size_t>(sa.size(), 65535);
-  k_split_a<<<dim3(maxtm, gy), 256, 0, st>>>(dsa, (int)sa.size());
-  k_split_b<<<dim3(maxtn, gy), 256, 0, st>>>(dsb, (int)sb.size());
+  // exponents default to 0 (operands with K = 0 have no work item)
+  cudaMemsetAsync(EA, 0, sizeof(int) * (ea + 1), st);
+  cudaMemsetAsync(EB, 0, sizeof(int) * (eb + 1), st);
+  cudaMemsetAsync(MA, 0, sizeof(unsigned long long) * (ea + 1), st);
+  cudaMemsetAsync(MB, 0, sizeof(unsigned long long) * (eb + 1), st);
+  if (wa > 0) {
+    k_split_amax<<<(unsigned)wa, 256, 0, st>>>(dsa, (int)sa.size());
+    k_split_a<<<(unsigned)wa, 256, 0, st>>>(dsa, (int)sa.size());
+  }
+  if (wb > 0) {
+    k_split_bmax<<<(unsigned)wb, 256, 0, st>>>(dsb, (int)sb.size());
+    k_split_b<<<(unsigned)wb, 256, 0, st>>>(dsb, (int)sb.size());
+  }
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);

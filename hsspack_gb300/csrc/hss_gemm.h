@@ -24,6 +24,8 @@ struct SplitProb {
   int ld, rows, inner, ktiles;
   void *dst;   // digit planes, pre-tiled
   int *expo;   // per row / column exponent
+  unsigned long long *mbits;  // per row / column largest |x| as bits (zeroed)
+  int w0;      // first flattened work item (panel x k chunk) of this operand
 };
 
 int gemm_tiles(int M, int N);
