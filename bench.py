@@ -370,7 +370,9 @@ def run_extra(torch, hp, full_cfg):
             ew.copy_(e)
             hp.mdbdsdc_dev(dw, ew, u, vt)
 
+        hp.set_config(predictor=2)  # FP32 pre-solved secular starts (squared mode)
         out["bidiagonal_svd_n16384_ms"] = _timed_ms(torch, svd)
+        hp.set_config(predictor=0)
         del u, vt
         # banded n = 16384, kd = 4, entries iid U[-1, 1] (seed 0)
         kd = 4
@@ -493,9 +495,10 @@ def run_extra(torch, hp, full_cfg):
         uv = torch.empty(n * n, dtype=torch.float64, device="cuda")
         vv = torch.empty(n * n, dtype=torch.float64, device="cuda")
         for prec, key in ((1, "split"), (0, "fp64")):
-            hp.set_config(precision=prec)
+            hp.set_config(precision=prec, predictor=2)
             out["banded_svd_n5000_sb5_%s_ms" % key] = _timed_ms(
                 torch, lambda: hp.mdbdsvd_dev(sb, abt, sv, uv, vv, smlsiz=75))
+        hp.set_config(predictor=0)
         st = hp.get_stats()
         out["banded_svd_n5000_sb5_stats"] = {"levels": st["n_levels"], "appends": st["n_merges"],
                                              "max_k": st["max_k"], "total_k": st["total_k"]}

@@ -1075,9 +1075,18 @@ static void svd_merge_tail(Ctx &c, const std::vector<int> &ms, const std::vector
   c.stats.secular_roots += total;
   double k2 = 0.0;
   for (int K : aK) k2 += (double)K * K;
+  float *guess = nullptr;
+  if (c.cfg.predictor == 2) {  // starts from an FP32 pre-solve in squared mode
+    guess = buf<float>(c, "guess", L.n);
+    float *d32 = buf<float>(c, "pole_f32", L.n), *z32 = buf<float>(c, "z_f32", L.n);
+    stage_begin(HSS_ST_PREDICT, st);
+    launch_secular_guess32(lv, total, maxK, L.n, L.w.dl, L.w.zw, d32, z32, guess, st, true);
+    stage_end(HSS_ST_PREDICT, st, 0, 0.0);
+    c.launches += 2;
+  }
   stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
-                 (unsigned long long *)(status + 2), nullptr, st, true);
+                 (unsigned long long *)(status + 2), guess, st, true, guess != nullptr);
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 0.0);  // flops from the pole-term count
   stage_begin(HSS_ST_LOWNER, st);
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true, maxK);

@@ -48,10 +48,10 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
                     unsigned long long *itsum, const float *guess, cudaStream_t st,
                     bool sq = false, bool full = false);
 // starts for the FP64 iteration from an FP32 pre-solve (npos: positions of the
-// level arrays, d32 / z32 their FP32 copies)
+// level arrays, d32 / z32 their FP32 copies; sq: singular-value mode)
 void launch_secular_guess32(const LevelView &lv, int total, int maxk, int npos,
                             const double *dl, const double *zw, float *d32, float *z32,
-                            float *guess, cudaStream_t st);
+                            float *guess, cudaStream_t st, bool sq = false);
 // maxk: the largest K of the launch (lanes per root as the secular kernel;
 // the default keeps a full warp per root)
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,

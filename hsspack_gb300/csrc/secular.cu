@@ -598,7 +598,9 @@ __device__ __forceinline__ float group_sum_f(float v) {
 // origin pole.  The result (a few 1e-6 of the interval at
 // best) only starts the FP64 iteration, which decides convergence as before;
 // guess[s + j] = signed distance to the nearer pole / interval, 0 for none.
-template <int L>
+// SQ: singular-value mode, the variable tau = sigma^2 - d_o^2 and the pole gaps
+// (d_i - d_o)(d_i + d_o), as the FP64 kernel's squared mode.
+template <int L, bool SQ>
 __global__ void __launch_bounds__(256)
 k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__restrict__ d32,
                   const float *__restrict__ z32, float *__restrict__ guess) {
@@ -624,7 +626,12 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
 #pragma unroll
     for (int q = 0; q < 2 * GR; ++q) {
       const int i = n0 + q;
-      gn[q] = (active && i >= 0 && i < K) ? (float)(__ldg(dl + s + i) - dorg) : 0.f;
+      if (active && i >= 0 && i < K) {
+        const double di = __ldg(dl + s + i);
+        gn[q] = SQ ? (float)((di - dorg) * (di + dorg)) : (float)(di - dorg);
+      } else {
+        gn[q] = 0.f;
+      }
     }
   };
   near_gaps(j);
@@ -641,7 +648,9 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
       for (int i = gl; i < Ka; i += L) {
         if (i >= n0 && i < n0 + 2 * GR) continue;  // the near poles follow
         const float zi = __ldg(z32 + s + i);
-        const float t = __fdividef(zi, (__ldg(d32 + s + i) - do32) - tau);
+        const float di = __ldg(d32 + s + i);
+        const float gi = SQ ? (di - do32) * (di + do32) : di - do32;
+        const float t = __fdividef(zi, gi - tau);
         if (i <= j) { a0 = fmaf(zi, t, a0); a1 = fmaf(t, t, a1); }
         else { b0 = fmaf(zi, t, b0); b1 = fmaf(t, t, b1); }
       }
@@ -817,15 +826,18 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
 }
 void launch_secular_guess32(const LevelView &lv, int total, int maxk, int npos,
                             const double *dl, const double *zw, float *d32, float *z32,
-                            float *guess, cudaStream_t st) {
+                            float *guess, cudaStream_t st, bool sq) {
   if (total <= 0) return;
   k_to_f32<<<(npos + 255) / 256, 256, 0, st>>>(npos, dl, zw, d32, z32);
   const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
   const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
   switch (L) {
-#define G32_CASE(LL) \
-  case LL: k_secular_guess32<LL><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess); break;
+#define G32_CASE(LL)                                                                   \
+  case LL:                                                                             \
+    if (sq) k_secular_guess32<LL, true><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess);  \
+    else k_secular_guess32<LL, false><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess);    \
+    break;
     G32_CASE(1) G32_CASE(2) G32_CASE(4) G32_CASE(8) G32_CASE(16) G32_CASE(32)
 #undef G32_CASE
   }

@@ -62,6 +62,26 @@ def test_svd_lower_signed_graded_and_restatement():
     assert np.max(np.abs(sr - s2)) <= SV_TOL * 2.0
 
 
+@pytest.mark.parametrize("n", [100, 1000, 4000])
+def test_svd_fp32_presolved_starts(n):
+    # predictor = 2: the secular iteration starts from an FP32 pre-solve in
+    # squared mode; random, graded and deflating cases
+    old = hp.set_config(predictor=2, precision=1)
+    try:
+        d, e = _bidiag(n, seed=100 + n)
+        _check(d, e, *hp.svd_bidiagonal(d, e))
+        dg, eg = d * np.logspace(0, -10, n), e * np.logspace(0, -10, n - 1)
+        _check(dg, eg, *hp.svd_bidiagonal(dg, eg))
+        d2, e2 = d.copy(), e.copy()
+        d2[::7] = 0.0
+        d2[10:50] = 0.5
+        e2[10:50] = 0.0
+        _check(d2, e2, *hp.svd_bidiagonal(d2, e2))
+        assert hp.get_stats()["secular_iters"] > 0
+    finally:
+        hp.restore_config(old)
+
+
 def test_svd_deflation_cases():
     # repeated and zero entries: small z, equal singular values, zero diagonals
     n = 400
