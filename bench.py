@@ -350,6 +350,22 @@ def _timed_ms(torch, fn, reps=3):
     return t0.elapsed_time(t1) / reps
 
 
+def run_extra_child(full_cfg):
+    """run_extra in a child process with its own CUDA context: a failure there
+    (a device error included) cannot take this run's line with it."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--extra-only", "--extra-cfg",
+           json.dumps(full_cfg)]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+    except subprocess.TimeoutExpired:
+        return {"error": "secondary figures: no result within 900 s"}
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    if r.returncode != 0 or not lines:
+        tail = (r.stderr or r.stdout).strip().splitlines()
+        return {"error": "secondary figures: exit %d: %s" % (r.returncode, tail[-1] if tail else "")}
+    return json.loads(lines[-1])
+
+
 def run_extra(torch, hp, full_cfg):
     """Secondary figures (not the metric): the other configurations' device
     times through the library's device entry points."""
@@ -431,30 +447,6 @@ def run_extra(torch, hp, full_cfg):
                 "max_rank": hp.get_stats()["max_rank"],
                 "max_abs_err_vs_dense": float((Bd - ref).abs().max())}
             del A, B0, Bd, ref
-        # SVD updating (SvdHssUpdat) n = 10000, the reference's test case
-        # (TEST/testUpsvdCauchy.f90): F evenly spaced in (0.1, 9), Z iid U(0, 1)
-        # with Z(10) = 1e-16 and Z(200) = 1e-17, V = I; leaf 64, tol 1e-14
-        n = 10000
-        f0 = torch.tensor(0.1 + (2 * np.arange(1, n + 1) - 1) * (8.9 / (2 * n)), device="cuda")
-        zh = np.random.default_rng(0).uniform(0.0, 1.0, n)
-        zh[9], zh[199] = 1e-16, 1e-17
-        z0 = torch.tensor(zh, device="cuda")
-        v0 = torch.eye(n, dtype=torch.float64, device="cuda").reshape(-1)
-        fw, zw, vw = f0.clone(), z0.clone(), v0.clone()
-        dw = torch.zeros(n, dtype=torch.float64, device="cuda")
-        for prec in (0,):  # the update's product runs in FP64 (svdupd.cu)
-            hp.set_config(precision=prec)
-            key = "fp64"
-
-            def upd():
-                fw.copy_(f0)
-                zw.copy_(z0)
-                vw.copy_(v0)
-                hp.svdhssupdat_dev(dw, fw, zw, vw, 1e-14, 64)
-
-            out["svd_update_n10000_%s_ms" % key] = _timed_ms(torch, upd)
-            out["svd_update_n10000_max_rank"] = hp.get_stats()["max_rank"]
-        del v0, vw
         # HSS Cholesky (HssCholSolver) n = 8192: Gaussian kernel (length 0.01) on
         # sorted uniform points plus 1e-2 I; leaves of 32, tol 1e-8, at most 20
         # per node; factor, solve, CG preconditioned by it and plain CG (tau 1e-13)
@@ -696,7 +688,7 @@ def run_ours(args):
 
     extra = None
     if not args.no_extra and rank == 0:
-        extra = run_extra(torch, hp, full_cfg)
+        extra = run_extra_child(full_cfg)
 
     # dominant stage -> roofline (contract object), plus every stage against
     # the bound that applies to it
@@ -800,6 +792,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batch figures")
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
+    ap.add_argument("--extra-only", action="store_true",
+                    help="only the other configurations' figures (one JSON dict; the child "
+                         "process of a full run)")
+    ap.add_argument("--extra-cfg", default="{}", help="the library configuration for --extra-only")
     ap.add_argument("--smlsiz", type=int, default=0,
                     help="fixed DC leaf size instead of the autotuner (profiling runs)")
     ap.add_argument("--predictor", type=int, default=2, choices=[0, 1, 2],
@@ -810,7 +806,12 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warmup + timed solves (for ncu launch lists)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.extra_only:
+        import torch
+        import hsspack_gb300 as hp
+        torch.cuda.set_device(0)
+        print(json.dumps(run_extra(torch, hp, json.loads(args.extra_cfg))), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -38,6 +38,19 @@ constexpr int BSVD_ROWS_MAX = 64;   // leaf rows (one CTA's shared-memory Jacobi
 constexpr int BSVD_COLS_MAX = 96;   // leaf columns (rows + sb)
 constexpr int BSVD_SWEEPS = 40;
 
+// Sum over the warp, valid in lane 0 only: a halving tree whose adds run on
+// the lanes that need them (31 lane additions instead of the butterfly's 160;
+// this part's FP64 pipe is charged per active lane).
+__device__ __forceinline__ double warp_sum0(double v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(HSS_FULL, v, o);
+    if (lane < o) v += t;
+  }
+  return v;
+}
+
 __device__ __forceinline__ double bsvd_at(const double *__restrict__ AB, long long ldab, int sb,
                                           int i, int j) {
   const int d = j - i;
@@ -97,7 +110,7 @@ k_bsvd_leaf(int nleaf, const int *__restrict__ la, const int *__restrict__ lr,
   const double tolr = 4.0 * c * HSS_EPS;
   // columns below 4 c eps |B|_F are rounding residue (a wide block has c - r
   // of them); their mutual angles are noise, so they are never rotated
-  const double small2 = tolr * tolr * nb2;
+  const double tolr2 = tolr * tolr, small2 = tolr2 * nb2;
   bool conv = c < 2;
   for (int sweep = 0; sweep < BSVD_SWEEPS && !conv; ++sweep) {
     if (tid == 0) s_rot = 0;
@@ -113,11 +126,32 @@ k_bsvd_leaf(int nleaf, const int *__restrict__ la, const int *__restrict__ lr,
           const double x = Bs[p * RP + i], y = Bs[q * RP + i];
           al += x * x; be += y * y; ga += x * y;
         }
-        al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
-        if (al <= small2 || be <= small2 || fabs(ga) <= tolr * sqrt(al * be)) continue;
-        const double ze = (be - al) / (2.0 * ga);
-        const double t = copysign(1.0, ze) / (fabs(ze) + sqrt(1.0 + ze * ze));
-        const double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
+        al = warp_sum0(al); be = warp_sum0(be); ga = warp_sum0(ga);
+        // the test and the rotation on lane 0 only, cs and sn broadcast
+        double cs = 1.0, sn = 0.0;
+        int go = 0;
+        if (lane == 0 && al > small2 && be > small2 && ga * ga > tolr2 * (al * be)) {
+          // the angle in FP32 (any t gives an exactly orthogonal rotation once
+          // cs and sn are formed in FP64; an angle good to 1e-7 still removes
+          // all but 1e-7 of ga).  With both norms above small2 and ga above the
+          // test, |ze| < 1 / (2 tolr^2) fits FP32; beyond 1e18 (where ze^2
+          // would overflow) t = 1 / (2 |ze|).
+          const float zf = (float)qdiv(be - al, 2.0 * ga), az = fabsf(zf);
+          const float w1 = fmaf(zf, zf, 1.f);
+          const float tf = az > 1e18f ? __fdividef(0.5f, az) : __fdividef(1.f, az + w1 * rsqrtf(w1));
+          const double t = (double)copysignf(tf, zf);
+          // cs = 1 / sqrt(1 + t^2), 1 + t^2 in [1, 2]: FP32 estimate (rel.
+          // 1e-7) and two Newton steps y (3/2 - x y^2 / 2) in FP64
+          const double hx = 0.5 * fma(t, t, 1.0);
+          cs = (double)rsqrtf((float)(2.0 * hx));
+          cs *= fma(-hx, cs * cs, 1.5);
+          cs *= fma(-hx, cs * cs, 1.5);
+          sn = cs * t;
+          go = 1;
+        }
+        if (!__shfl_sync(HSS_FULL, go, 0)) continue;
+        cs = __shfl_sync(HSS_FULL, cs, 0);
+        sn = __shfl_sync(HSS_FULL, sn, 0);
         for (int i = lane; i < r; i += 32) {
           const double x = Bs[p * RP + i], y = Bs[q * RP + i];
           Bs[p * RP + i] = cs * x - sn * y;

@@ -1384,34 +1384,38 @@ static bool bsvd_levels(int n, int sb, int depth, bool balanced,
 }
 
 // The reference's depth floor(log2(n / (msub + 1))) (at least 1), made valid
-// (every node keeps rows on both sides), then deepened until every leaf fits
-// one CTA's shared memory (bsvd_rows_max() rows).  The reference's halving
-// shrinks right children by sb at every level; when no depth of it fits (wide
-// bands), balanced cuts are used instead.  Returns the depth, or -1.
+// (every node keeps rows on both sides), then deepened until every leaf has at
+// most 32 rows (the leaf Jacobi's cost grows as c^2 (r + c) and its warps work
+// along the rows), or, where no tree gets there (sb near 32), 64 rows (one
+// CTA's shared memory, bsvd_rows_max()).  The reference's halving shrinks
+// right children by sb at every level; when no depth of it fits, balanced cuts
+// are used instead.  Returns the depth, or -1.
 static int bsvd_tree(int n, int sb, int msub, std::vector<std::vector<BNode>> &lv) {
-  if (n <= bsvd_rows_max()) {
-    lv.assign(1, std::vector<BNode>{BNode{0, n, 0, 0}});
-    return 0;
-  }
   auto largest = [&lv]() {
     int mx = 0;
     for (const BNode &x : lv.back()) mx = std::max(mx, x.X);
     return mx;
   };
-  for (int balanced = 0; balanced < 2; ++balanced) {
-    int depth = balanced ? 1 : std::max(1, (int)std::floor(std::log2((double)n / (double)(msub + 1))));
-    while (depth > 1 && !bsvd_levels(n, sb, depth, balanced, lv)) --depth;
-    if (!bsvd_levels(n, sb, depth, balanced, lv)) continue;
-    bool fits = true;
-    while (fits && largest() > bsvd_rows_max()) {
-      std::vector<std::vector<BNode>> t;
-      fits = bsvd_levels(n, sb, depth + 1, balanced, t);
-      if (fits) {
-        lv.swap(t);
-        ++depth;
-      }
+  for (const int cap : {std::min(32, bsvd_rows_max()), bsvd_rows_max()}) {
+    if (n <= cap) {
+      lv.assign(1, std::vector<BNode>{BNode{0, n, 0, 0}});
+      return 0;
     }
-    if (fits) return depth;
+    for (int balanced = 0; balanced < 2; ++balanced) {
+      int depth = balanced ? 1 : std::max(1, (int)std::floor(std::log2((double)n / (double)(msub + 1))));
+      while (depth > 1 && !bsvd_levels(n, sb, depth, balanced, lv)) --depth;
+      if (!bsvd_levels(n, sb, depth, balanced, lv)) continue;
+      bool fits = true;
+      while (fits && largest() > cap) {
+        std::vector<std::vector<BNode>> t;
+        fits = bsvd_levels(n, sb, depth + 1, balanced, t);
+        if (fits) {
+          lv.swap(t);
+          ++depth;
+        }
+      }
+      if (fits) return depth;
+    }
   }
   return -1;
 }

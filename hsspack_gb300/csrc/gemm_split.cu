@@ -180,6 +180,7 @@ __device__ __forceinline__ int split_operand(const SplitProb *__restrict__ probs
 __global__ void __launch_bounds__(256)
 k_split_amax(const SplitProb *__restrict__ probs, int nprob) {
   const SplitProb P = probs[split_operand(probs, nprob, blockIdx.x)];
+  if (P.ktiles <= SPLIT_KT) return;  // one chunk: k_split_a takes the maxima itself
   const int t = blockIdx.x - P.w0, ntm = (P.rows + TM - 1) / TM;
   const int tm = t % ntm, kc = t / ntm;
   const int tid = threadIdx.x, half = tid >> 7, r = tm * TM + (tid & 127);
@@ -211,9 +212,34 @@ k_split_a(const SplitProb *__restrict__ probs, int nprob) {
   const int tm = t % ntm, kc = t / ntm;
   const int tid = threadIdx.x;
   __shared__ int sexp[TM];
+  __shared__ unsigned long long smx[8][TM];
+  const bool single = P.ktiles <= SPLIT_KT;
+  if (single) {  // one chunk: the row maxima here (warps over k, lanes over rows)
+    const int lane = tid & 31, w = tid >> 5;
+    unsigned long long mx[4] = {0, 0, 0, 0};
+    for (int k = w; k < P.inner; k += 8)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = tm * TM + q * 32 + lane;
+        if (r < P.rows) {
+          const unsigned long long b =
+              (unsigned long long)__double_as_longlong(P.src[(long long)k * P.ld + r]) & 0x7FFFFFFFFFFFFFFFull;
+          mx[q] = b > mx[q] ? b : mx[q];
+        }
+      }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) smx[w][q * 32 + lane] = mx[q];
+    __syncthreads();
+  }
   if (tid < TM) {
     const int r = tm * TM + tid;
-    const int e = r < P.rows ? bits_exp(P.mbits[r]) : 0;
+    unsigned long long m = 0;
+    if (single) {
+      for (int i = 0; i < 8; ++i) m = smx[i][tid] > m ? smx[i][tid] : m;
+    } else if (r < P.rows) {
+      m = P.mbits[r];
+    }
+    const int e = r < P.rows ? bits_exp(m) : 0;
     sexp[tid] = e;
     if (kc == 0 && r < P.rows) P.expo[r] = e;
   }
@@ -246,6 +272,7 @@ k_split_a(const SplitProb *__restrict__ probs, int nprob) {
 __global__ void __launch_bounds__(256)
 k_split_bmax(const SplitProb *__restrict__ probs, int nprob) {
   const SplitProb P = probs[split_operand(probs, nprob, blockIdx.x)];
+  if (P.ktiles <= SPLIT_KT) return;  // one chunk: k_split_b takes the maxima itself
   const int t = blockIdx.x - P.w0, ntn = (P.rows + TN - 1) / TN;
   const int tn = t % ntn, kc = t / ntn;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -278,7 +305,29 @@ k_split_b(const SplitProb *__restrict__ probs, int nprob) {
   const int tn = t % ntn, kc = t / ntn;
   const int tid = threadIdx.x;
   __shared__ int sexp[TN];
-  if (tid < TN) {
+  if (P.ktiles <= SPLIT_KT) {  // one chunk: warp per column, max over k here
+    const int lane = tid & 31, w = tid >> 5;
+    for (int c = w; c < TN; c += 8) {
+      const int gc = tn * TN + c;
+      unsigned long long m = 0;
+      if (gc < P.rows)
+        for (int k = lane; k < P.inner; k += 32) {
+          const unsigned long long b =
+              (unsigned long long)__double_as_longlong(P.src[(long long)gc * P.ld + k]) & 0x7FFFFFFFFFFFFFFFull;
+          m = b > m ? b : m;
+        }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(HSS_FULL, m, o);
+        m = v > m ? v : m;
+      }
+      if (lane == 0) {
+        const int e = bits_exp(m);
+        sexp[c] = e;
+        if (gc < P.rows) P.expo[gc] = e;
+      }
+    }
+  } else if (tid < TN) {
     const int gc = tn * TN + tid;
     const int e = gc < P.rows ? bits_exp(P.mbits[gc]) : 0;
     sexp[tid] = e;
@@ -848,10 +897,12 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   std::vector<TcProb> tc;
   long long abytes = 0, bbytes = 0, ea = 0, eb = 0, wa = 0, wb = 0;
   int tiles = 0;
+  bool multi = false;  // some operand has more than one k chunk
   for (const auto &p : probs) {
     const int kt = (p.K + TK - 1) / TK;
     const int ntm = (p.M + TM - 1) / TM, ntn = (p.N + TN - 1) / TN;
     const int nkc = (kt + SPLIT_KT - 1) / SPLIT_KT;
+    multi = multi || nkc > 1;
     SplitProb a{p.A, p.lda, p.M, p.K, kt, nullptr, nullptr, nullptr, (int)wa};
     SplitProb bb{p.B, p.ldb, p.N, p.K, kt, nullptr, nullptr, nullptr, (int)wb};
     a.dst = (void *)abytes; a.expo = (int *)ea; a.mbits = (unsigned long long *)ea;
@@ -892,19 +943,18 @@ void launch_gemm_split(const std::vector<GemmDesc> &probs, int *d_err, cudaStrea
   stage_h2d(dsb, sb.data(), sb.size() * sizeof(SplitProb), st);
   stage_h2d(dtc, tc.data(), tc.size() * sizeof(TcProb), st);
   stage_h2d(dtp, tp.data(), tp.size() * sizeof(int), st);
-  // exponents default to 0 (operands with K = 0 have no work item)
-  cudaMemsetAsync(EA, 0, sizeof(int) * (ea + 1), st);
-  cudaMemsetAsync(EB, 0, sizeof(int) * (eb + 1), st);
-  cudaMemsetAsync(MA, 0, sizeof(unsigned long long) * (ea + 1), st);
-  cudaMemsetAsync(MB, 0, sizeof(unsigned long long) * (eb + 1), st);
-  if (wa > 0) {
-    k_split_amax<<<(unsigned)wa, 256, 0, st>>>(dsa, (int)sa.size());
-    k_split_a<<<(unsigned)wa, 256, 0, st>>>(dsa, (int)sa.size());
+  // operands of one k chunk (the DC's small products) take their maxima in
+  // the digit kernels; the maxima pass (zeroed, then atomicMax) only runs when
+  // some operand has several chunks.  Operands with K = 0 have no work item and
+  // an unwritten exponent, which their all-zero sums never use.
+  if (multi) {
+    cudaMemsetAsync(MA, 0, sizeof(unsigned long long) * (ea + 1), st);
+    cudaMemsetAsync(MB, 0, sizeof(unsigned long long) * (eb + 1), st);
+    if (wa > 0) k_split_amax<<<(unsigned)wa, 256, 0, st>>>(dsa, (int)sa.size());
+    if (wb > 0) k_split_bmax<<<(unsigned)wb, 256, 0, st>>>(dsb, (int)sb.size());
   }
-  if (wb > 0) {
-    k_split_bmax<<<(unsigned)wb, 256, 0, st>>>(dsb, (int)sb.size());
-    k_split_b<<<(unsigned)wb, 256, 0, st>>>(dsb, (int)sb.size());
-  }
+  if (wa > 0) k_split_a<<<(unsigned)wa, 256, 0, st>>>(dsa, (int)sa.size());
+  if (wb > 0) k_split_b<<<(unsigned)wb, 256, 0, st>>>(dsb, (int)sb.size());
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TC);

@@ -304,18 +304,22 @@ __global__ void k_svd_vectors(LevelView lv, const double *__restrict__ dl,
   const int s = __ldg(lv.s + m);
   const int K = __ldg(lv.K + m);
   PoleDiff P{dl + s, difl + s, difr + s, true};
+  double *vc = Vb + boff[m] + (long long)j * K, *uc = Ub + boff[m] + (long long)j * K;
+  // each entry is formed once (FP64 issue slots are the scarce resource): the
+  // unnormalised V column goes out first and is rescaled from L2 by the same
+  // lanes; the divide through the one-ulp reciprocal
   double sv = 0.0, su = 0.0;
   for (int i = lane; i < K; i += HSS_WARP) {
-    const double v = __ldg(zhat + s + i) / P.fd(i, j);
+    const double v = qdiv(__ldg(zhat + s + i), P.fd(i, j));
+    vc[i] = v;
     sv += v * v;
     if (i > 0) { const double u = __ldg(dl + s + i) * v; su += u * u; }
   }
   sv = warp_sum(sv);
   su = warp_sum(su);
   const double av = 1.0 / sqrt(sv), au = 1.0 / sqrt(1.0 + su);
-  double *vc = Vb + boff[m] + (long long)j * K, *uc = Ub + boff[m] + (long long)j * K;
   for (int i = lane; i < K; i += HSS_WARP) {
-    const double v = __ldg(zhat + s + i) / P.fd(i, j);
+    const double v = vc[i];
     vc[i] = v * av;
     uc[i] = i == 0 ? -au : __ldg(dl + s + i) * v * au;
   }
