@@ -390,8 +390,25 @@ def run_extra(torch, hp, full_cfg):
         out["bidiagonal_svd_n16384_ms"] = _timed_ms(torch, svd)
         hp.set_config(predictor=0)
         del u, vt
+        # banded SVD (MDBDSVD) n = 5000, SB = 5, AB iid U[0, 1), SMLSIZ = 75: the
+        # reference's test case (TEST/test_bdc1.f90); products split-BF16 and FP64
+        n, sb = 5000, 5
+        abh = np.random.default_rng(2013).uniform(0.0, 1.0, (sb + 1, n))
+        abt = torch.tensor(np.asfortranarray(abh).ravel(order="F"), device="cuda")
+        sv = torch.empty(n, dtype=torch.float64, device="cuda")
+        uv = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        vv = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        for prec, key in ((1, "split"), (0, "fp64")):
+            hp.set_config(precision=prec, predictor=2)
+            out["banded_svd_n5000_sb5_%s_ms" % key] = _timed_ms(
+                torch, lambda: hp.mdbdsvd_dev(sb, abt, sv, uv, vv, smlsiz=75))
+        hp.set_config(predictor=0)
+        st = hp.get_stats()
+        out["banded_svd_n5000_sb5_stats"] = {"levels": st["n_levels"], "appends": st["n_merges"],
+                                             "max_k": st["max_k"], "total_k": st["total_k"]}
+        del uv, vv
         # banded n = 16384, kd = 4, entries iid U[-1, 1] (seed 0)
-        kd = 4
+        n, kd = 16384, 4
         ab = rng.uniform(-1.0, 1.0, (kd + 1, n))
         abd = torch.tensor(np.ascontiguousarray(ab.T), device="cuda")
         w = torch.empty(n, dtype=torch.float64, device="cuda")
@@ -478,23 +495,6 @@ def run_extra(torch, hp, full_cfg):
         out["hss_cholesky_n8192_plain_cg"] = {"steps": it0, "relres": rr0}
         fac[0].free()
         del Ak
-        # banded SVD (MDBDSVD) n = 5000, SB = 5, AB iid U[0, 1), SMLSIZ = 75: the
-        # reference's test case (TEST/test_bdc1.f90); products split-BF16 and FP64
-        n, sb = 5000, 5
-        abh = np.random.default_rng(2013).uniform(0.0, 1.0, (sb + 1, n))
-        abt = torch.tensor(np.asfortranarray(abh).ravel(order="F"), device="cuda")
-        sv = torch.empty(n, dtype=torch.float64, device="cuda")
-        uv = torch.empty(n * n, dtype=torch.float64, device="cuda")
-        vv = torch.empty(n * n, dtype=torch.float64, device="cuda")
-        for prec, key in ((1, "split"), (0, "fp64")):
-            hp.set_config(precision=prec, predictor=2)
-            out["banded_svd_n5000_sb5_%s_ms" % key] = _timed_ms(
-                torch, lambda: hp.mdbdsvd_dev(sb, abt, sv, uv, vv, smlsiz=75))
-        hp.set_config(predictor=0)
-        st = hp.get_stats()
-        out["banded_svd_n5000_sb5_stats"] = {"levels": st["n_levels"], "appends": st["n_merges"],
-                                             "max_k": st["max_k"], "total_k": st["total_k"]}
-        del uv, vv
     finally:
         hp.restore_config(old)
     return out
