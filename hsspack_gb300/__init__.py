@@ -115,6 +115,7 @@ SIGNATURES = {
     "hss_svdhssupdat_dev": (ctypes.c_int, [ctypes.c_int, _V, _V, _V, _V, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_int, _V, _V]),
     "hss_svdupd_deflate": (ctypes.c_int, [ctypes.c_int, _D, _D, _I, _I]),
+    "hss_bsvd_tree": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _I, _I]),
     "hsscholsolver_": (None, [ctypes.c_char_p, ctypes.c_char_p, _D, _I, _D, _I, _D, _I, _I, _D,
                               _I, _I, ctypes.c_size_t, ctypes.c_size_t]),
     "hss_chol_factor_dev": (ctypes.c_int, [ctypes.c_int, _V, ctypes.c_int, ctypes.c_int,
@@ -396,6 +397,19 @@ def svd_banded(ab, sb, smlsiz=25):
     if info != 0:
         raise HssError("MDBDSVD INFO=%d: %s" % (info, _err()))
     return s, U, VT
+
+
+def bsvd_tree(n, sb, smlsiz=25):
+    """The banded SVD's leaves (host logic, no GPU): (merge levels, [(first row,
+    rows, columns), ...]); raises HssError for arguments the library rejects."""
+    st, rw, cl = (np.zeros(max(n, 1), dtype=np.int32) for _ in range(3))
+    nl = ctypes.c_int(0)
+    depth = load().hss_bsvd_tree(int(n), int(sb), int(smlsiz), st.ctypes.data_as(_I),
+                                 rw.ctypes.data_as(_I), cl.ctypes.data_as(_I), ctypes.byref(nl))
+    if depth < 0:
+        raise HssError("hss_bsvd_tree rc=%d" % depth)
+    return depth, [(int(a), int(b), int(c)) for a, b, c in zip(st[:nl.value], rw[:nl.value],
+                                                              cl[:nl.value])]
 
 
 def mdbdsvd_dev(sb, ab, s, u, vt, smlsiz=25, stream=None):

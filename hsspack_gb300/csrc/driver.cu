@@ -2729,6 +2729,22 @@ int hss_svdupd_deflate(int n, double *f, double *z, int *idxp, int *nrot) {
   return df.K;
 }
 
+int hss_bsvd_tree(int n, int sb, int smlsiz, int *leaf_start, int *leaf_rows, int *leaf_cols,
+                  int *nleaves) {
+  if (n < 1 || sb < 1 || sb > 32 || sb > n || smlsiz < 3) return -1;
+  std::vector<std::vector<BNode>> lv;
+  const int depth = bsvd_tree(n, sb, std::max(smlsiz, 3 * sb), lv);
+  if (depth < 0) return -2;
+  const std::vector<BNode> &leaves = lv.back();
+  for (size_t i = 0; i < leaves.size(); ++i) {
+    leaf_start[i] = leaves[i].s;
+    leaf_rows[i] = leaves[i].X;
+    leaf_cols[i] = leaves[i].X + leaves[i].sq;
+  }
+  *nleaves = (int)leaves.size();
+  return depth;
+}
+
 int hss_rcp_dev(int n, const double *x, double *y, void *stream) {
   Ctx &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);

@@ -329,6 +329,14 @@ int hss_svdhssupdat_dev(int n, double *d, double *f, double *z, double *vt, int 
  * *nrot (may be NULL) the number of deflating rotations.  Returns K. */
 int hss_svdupd_deflate(int n, double *f, double *z, int *idxp, int *nrot);
 
+/* The banded SVD's tree (host logic of the MDBDSVD path, no GPU): the leaves of
+ * the n-row band with sb superdiagonals, in row order -- first row, rows, and
+ * columns (rows + the sb extra columns, none for the last leaf); the arrays hold
+ * n entries.  Returns the number of merge levels, -1 for bad arguments, -2 when
+ * no tree fits the leaf limit. */
+int hss_bsvd_tree(int n, int sb, int smlsiz, int *leaf_start, int *leaf_rows, int *leaf_cols,
+                  int *nleaves);
+
 /* HSS Cholesky on device arrays (the pieces of HssCholSolver).  The factor
  * owns its device memory until hss_chol_free.
  * hss_chol_factor_dev: A (n x n, lda; read only); ni leaf rows (<= 128); tol;

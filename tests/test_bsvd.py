@@ -74,6 +74,42 @@ def test_oracle_tree_is_mdbdsvdt():
     assert all(c == r + 5 for _, r, c in leaves[:-1])
 
 
+@pytest.mark.parametrize("sb", [1, 2, 5, 8, 12, 16, 20, 31, 32])
+def test_library_tree_tiles_the_band(sb):
+    # the library's cut of the band (host logic): leaves in row order separated
+    # by exactly one center block of sb rows, 2^depth leaves, extra columns on
+    # all but the last, at most 64 rows (32 whenever the band allows it); where
+    # MDBDSVDT's own tree is valid and its leaves already have at most 32 rows,
+    # the library's leaves are exactly MDBDSVDT's
+    for n in [sb, sb + 1, 33, 64, 65, 100, 257, 1000, 1500, 5000, 16384]:
+        if n < sb:
+            continue
+        depth, leaves = hp.bsvd_tree(n, sb, 25)
+        assert len(leaves) == 2 ** depth
+        pos = 0
+        for i, (a, r, c) in enumerate(leaves):
+            assert a == pos and r >= 1
+            assert c == r + (sb if i < len(leaves) - 1 else 0)
+            assert r <= 64
+            pos = a + r + sb
+        assert pos - sb == n
+        if sb <= 16:
+            assert max(r for _, r, _ in leaves) <= 32, (n, sb)
+        if n > 32:
+            try:
+                _, ref_leaves = ref.tree(n, sb, 25)
+            except AssertionError:  # the reference's halving leaves a side empty
+                continue
+            if max(r for _, r, _ in ref_leaves) <= 32:
+                assert [(a, r, c) for a, r, c in ref_leaves] == leaves
+
+
+def test_library_tree_rejects_bad_arguments():
+    for args in [(0, 1), (10, 0), (10, 11), (100, 33)]:
+        with pytest.raises(hp.HssError):
+            hp.bsvd_tree(*args)
+
+
 def _call(n, sb, ldab, ldu, ldvt, smlsiz):
     ab = np.zeros((max(ldab, 1), max(n, 1)), order="F")
     u = np.zeros((max(ldu, 1), max(n, 1)), order="F")
