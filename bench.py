@@ -267,6 +267,12 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
         for sml in (8, 12, 16):
             tune_ms[str(sml)] = timed(batched, 1, 1, dict(full_cfg, smlsiz=sml))[0]
         bcfg["smlsiz"] = int(min(tune_ms, key=tune_ms.get))
+        # products of 64 to 127 rows on the tensor cores (128-row tiles, the rest
+        # zero) instead of the FP64 element kernel
+        key = "%d+m64" % bcfg["smlsiz"]
+        tune_ms[key] = timed(batched, 1, 1, dict(bcfg, split_min_m=64))[0]
+        if tune_ms[key] < tune_ms[str(bcfg["smlsiz"])]:
+            bcfg["split_min_m"] = 64
     steps = max(1, min(args.steps, 5))
     ms, launches = timed(batched, steps, max(3, args.warmup), bcfg)
     # every problem's residual ||TQ - QW||_F / (n ||T||) from the last solve
@@ -299,7 +305,8 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
            "plain_solves_per_s": len(sizes_all) * 1000.0 / ms_plain,
            "full_vs_plain": ms_plain / ms, "full_vs_batched_fp64": ms_fp64 / ms,
            "full_vs_standard_start": ms_std / ms, "batched_vs_loop": ms_loop / ms,
-           "resid_max": res, "smlsiz": bcfg.get("smlsiz"), "autotune_ms": tune_ms or None}
+           "resid_max": res, "smlsiz": bcfg.get("smlsiz"),
+           "split_min_m": bcfg.get("split_min_m", 128), "autotune_ms": tune_ms or None}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_s = batch_cpu_solve(probs_all, threads)
