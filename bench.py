@@ -409,7 +409,7 @@ def run_extra(torch, hp, full_cfg):
             hp.set_config(precision=prec, predictor=2)
             out["banded_svd_n5000_sb5_%s_ms" % key] = _timed_ms(
                 torch, lambda: hp.mdbdsvd_dev(sb, abt, sv, uv, vv, smlsiz=75))
-        hp.set_config(predictor=0)
+        hp.set_config(precision=full_cfg.get("precision", 1), predictor=0)
         st = hp.get_stats()
         out["banded_svd_n5000_sb5_stats"] = {"levels": st["n_levels"], "appends": st["n_merges"],
                                              "max_k": st["max_k"], "total_k": st["total_k"]}
