@@ -1,7 +1,8 @@
 """Autotuner for the divide-and-conquer configuration.
 
-Chooses, per problem-size bucket (powers of two), the DC leaf size SMLSIZ and
-the secular start (standard, learned or FP32 pre-solve), by timing the
+Chooses, per problem-size bucket (powers of two), the DC leaf size SMLSIZ, the
+secular start (standard, learned or FP32 pre-solve) and, with split-BF16
+products, whether products of 64-127 rows go to the tensor cores, by timing the
 candidate settings on a seeded random tridiagonal of that size (device time
 from the library's CUDA events).  Results are cached in ``_lib/autotune.json``
 next to the library and applied with :func:`apply`.
@@ -61,7 +62,25 @@ def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None, predictor=(
             finally:
                 hp.restore_config(old)
     key = min(results, key=results.get)
-    sml = cfgs[key]["smlsiz"]
+    if int((base or {}).get("precision", 0)) == 1:
+        # the winner once more with the products of 64-127 rows on the tensor
+        # cores (128-row tiles) instead of the FP64 element kernel
+        k64 = key + "+m64"
+        cfg = dict(base, **cfgs[key], split_min_m=64)
+        old = hp.set_config(**cfg)
+        try:
+            best = float("inf")
+            for _ in range(reps + 1):
+                dw.copy_(d0)
+                ew.copy_(e0)
+                hp.mdstedc_dev(dw, ew, z)
+                best = min(best, hp.get_stats()["ms_total"])
+            results[k64] = best
+            cfgs[k64] = dict(cfgs[key], split_min_m=64)
+        finally:
+            hp.restore_config(old)
+        if results[k64] < results[key]:
+            key = k64
     cache = load_cache()
     cache[_bucket(n)] = dict(cfgs[key], ms=results)
     try:
@@ -76,7 +95,7 @@ def lookup(n):
     ent = load_cache().get(_bucket(n))
     if not ent:
         return None
-    return {k: ent[k] for k in ("smlsiz", "predictor") if k in ent}
+    return {k: ent[k] for k in ("smlsiz", "predictor", "split_min_m") if k in ent}
 
 
 def apply(n):
