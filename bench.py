@@ -271,8 +271,16 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
         # zero) instead of the FP64 element kernel
         key = "%d+m64" % bcfg["smlsiz"]
         tune_ms[key] = timed(batched, 1, 1, dict(bcfg, split_min_m=64))[0]
-        if tune_ms[key] < tune_ms[str(bcfg["smlsiz"])]:
+        best = tune_ms[str(bcfg["smlsiz"])]
+        if tune_ms[key] < best:
             bcfg["split_min_m"] = 64
+            best = tune_ms[key]
+        # the FP32 pre-solve refined by one float-float step (predictor 3)
+        if int(bcfg.get("predictor", 0)) == 2:
+            key = "%d+ff" % bcfg["smlsiz"]
+            tune_ms[key] = timed(batched, 1, 1, dict(bcfg, predictor=3))[0]
+            if tune_ms[key] < best:
+                bcfg["predictor"] = 3
     steps = max(1, min(args.steps, 5))
     ms, launches = timed(batched, steps, max(3, args.warmup), bcfg)
     # every problem's residual ||TQ - QW||_F / (n ||T||) from the last solve
@@ -306,7 +314,8 @@ def run_batch(args, torch, hp, full_cfg, plain_cfg, world, rank, dist):
            "full_vs_plain": ms_plain / ms, "full_vs_batched_fp64": ms_fp64 / ms,
            "full_vs_standard_start": ms_std / ms, "batched_vs_loop": ms_loop / ms,
            "resid_max": res, "smlsiz": bcfg.get("smlsiz"),
-           "split_min_m": bcfg.get("split_min_m", 128), "autotune_ms": tune_ms or None}
+           "split_min_m": bcfg.get("split_min_m", 128), "predictor": bcfg.get("predictor"),
+           "autotune_ms": tune_ms or None}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_s = batch_cpu_solve(probs_all, threads)
@@ -618,7 +627,7 @@ def run_ours(args):
         tuned, tune_ms = {"smlsiz": args.smlsiz, "predictor": args.predictor}, None
     else:
         tuned, tune_ms = autotune.tune(n, reps=1, base=full_cfg,
-                                       predictor=(0, 1, 2) if have_pred else (0, 2))
+                                       predictor=(0, 1, 2, 3) if have_pred else (0, 2, 3))
     full_cfg.update(tuned)
     if args.profile_batch:  # the batch's solves only (ncu launch lists)
         if rank == 0:
@@ -642,9 +651,11 @@ def run_ours(args):
     ms_fp64, _, _, _ = timed(max(1, min(3, args.steps)), 1, False,
                              dict(full_cfg, precision=0))
     # the secular start A/B at the tuned leaf size: standard (midpoint), learned
-    # MLP, FP32 pre-solve; time per solve and FP64 evaluations per root
+    # MLP, FP32 pre-solve, the pre-solve refined in float-float; time per solve
+    # and FP64 evaluations per root
     start_ab = {}
-    for pred, name in ((0, "standard"), (1, "learned"), (2, "fp32_presolve")):
+    for pred, name in ((0, "standard"), (1, "learned"), (2, "fp32_presolve"),
+                       (3, "fp32_presolve_ff")):
         if pred == 1 and not have_pred:
             continue
         m_ab, _, _, st_ab = timed(max(1, min(3, args.steps)), 1, False,

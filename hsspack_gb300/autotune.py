@@ -1,7 +1,8 @@
 """Autotuner for the divide-and-conquer configuration.
 
 Chooses, per problem-size bucket (powers of two), the DC leaf size SMLSIZ, the
-secular start (standard, learned or FP32 pre-solve) and, with split-BF16
+secular start (standard, learned, FP32 pre-solve or the pre-solve refined in
+float-float) and, with split-BF16
 products, whether products of 64-127 rows go to the tensor cores, by timing the
 candidate settings on a seeded random tridiagonal of that size (device time
 from the library's CUDA events).  Results are cached in ``_lib/autotune.json``
@@ -33,9 +34,10 @@ def load_cache():
 
 def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None, predictor=(0,)):
     """Time MDSTEDC('I') at size n for each DC leaf size and secular start
-    (predictor 0 standard, 1 learned, 2 FP32 pre-solve); return the best
-    config dict (and all timings, keyed "smlsiz", "smlsiz+learned" or
-    "smlsiz+fp32") and cache it under the size bucket."""
+    (predictor 0 standard, 1 learned, 2 FP32 pre-solve, 3 FP32 pre-solve
+    refined in float-float); return the best config dict (and all timings,
+    keyed "smlsiz", "smlsiz+learned", "smlsiz+fp32" or "smlsiz+ff") and cache
+    it under the size bucket."""
     import torch
     import hsspack_gb300 as hp
     rng = np.random.default_rng(seed)
@@ -47,7 +49,7 @@ def tune(n, candidates=SMLSIZ_CANDIDATES, reps=2, seed=0, base=None, predictor=(
     results, cfgs = {}, {}
     for pred in predictor:
         for sml in candidates:
-            key = "%d%s" % (sml, ("", "+learned", "+fp32")[int(pred)])
+            key = "%d%s" % (sml, ("", "+learned", "+fp32", "+ff")[int(pred)])
             cfg = dict(base or {}, smlsiz=int(sml), predictor=int(pred))
             old = hp.set_config(**cfg)
             try:

@@ -432,12 +432,22 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   for (int K : aK) k2 += (double)K * K;
   float *guess = nullptr;
   const int maxK = *std::max_element(aK.begin(), aK.end());
-  if (c.cfg.predictor == 2) {
-    // starts from an FP32 pre-solve of every root
+  float4 *gref = nullptr;
+  if (c.cfg.predictor >= 2) {
+    // starts from an FP32 pre-solve of every root (3: refined by one
+    // float-float step, exact starts in gref)
     guess = buf<float>(c, "guess", L.n);
     float *d32 = buf<float>(c, "pole_f32", L.n), *z32 = buf<float>(c, "z_f32", L.n);
+    float *d32lo = nullptr, *z2h = nullptr, *z2l = nullptr;
+    if (c.cfg.predictor == 3) {
+      d32lo = buf<float>(c, "pole_f32lo", L.n);
+      z2h = buf<float>(c, "z2_f32", L.n);
+      z2l = buf<float>(c, "z2_f32lo", L.n);
+      gref = buf<float4>(c, "guess_ref", L.n);
+    }
     stage_begin(HSS_ST_PREDICT, st);
-    launch_secular_guess32(lv, total, maxK, L.n, L.w.dl, L.w.zw, d32, z32, guess, st);
+    launch_secular_guess32(lv, total, maxK, L.n, L.w.dl, L.w.zw, d32, z32, guess, st, false,
+                           d32lo, z2h, z2l, gref);
     stage_end(HSS_ST_PREDICT, st, 0, 0.0);
     c.launches += 2;
   } else if (c.cfg.predictor && c.pred_ready) {
@@ -454,7 +464,7 @@ static void run_merges(Ctx &c, const std::vector<int> &ms, const std::vector<int
   }
   stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
-                 (unsigned long long *)(status + 2), guess, st, false, c.cfg.predictor == 2);
+                 (unsigned long long *)(status + 2), guess, st, false, c.cfg.predictor >= 2, gref);
   // per pole term per evaluation: 2 sub, 1 div, 2 mul, 3 add (x ~4 evaluations)
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 0.0);  // flops from the pole-term count
   stage_begin(HSS_ST_LOWNER, st);
@@ -1076,17 +1086,26 @@ static void svd_merge_tail(Ctx &c, const std::vector<int> &ms, const std::vector
   double k2 = 0.0;
   for (int K : aK) k2 += (double)K * K;
   float *guess = nullptr;
-  if (c.cfg.predictor == 2) {  // starts from an FP32 pre-solve in squared mode
+  float4 *gref = nullptr;
+  if (c.cfg.predictor >= 2) {  // starts from an FP32 pre-solve in squared mode
     guess = buf<float>(c, "guess", L.n);
     float *d32 = buf<float>(c, "pole_f32", L.n), *z32 = buf<float>(c, "z_f32", L.n);
+    float *d32lo = nullptr, *z2h = nullptr, *z2l = nullptr;
+    if (c.cfg.predictor == 3) {
+      d32lo = buf<float>(c, "pole_f32lo", L.n);
+      z2h = buf<float>(c, "z2_f32", L.n);
+      z2l = buf<float>(c, "z2_f32lo", L.n);
+      gref = buf<float4>(c, "guess_ref", L.n);
+    }
     stage_begin(HSS_ST_PREDICT, st);
-    launch_secular_guess32(lv, total, maxK, L.n, L.w.dl, L.w.zw, d32, z32, guess, st, true);
+    launch_secular_guess32(lv, total, maxK, L.n, L.w.dl, L.w.zw, d32, z32, guess, st, true,
+                           d32lo, z2h, z2l, gref);
     stage_end(HSS_ST_PREDICT, st, 0, 0.0);
     c.launches += 2;
   }
   stage_begin(HSS_ST_SECULAR, st);
   launch_secular(lv, total, maxK, L.w.dl, L.w.zw, L.lam, L.difl, L.difr, L.iters, status,
-                 (unsigned long long *)(status + 2), guess, st, true, guess != nullptr);
+                 (unsigned long long *)(status + 2), guess, st, true, guess != nullptr, gref);
   stage_end(HSS_ST_SECULAR, st, 40LL * total, 0.0);  // flops from the pole-term count
   stage_begin(HSS_ST_LOWNER, st);
   launch_lowner(lv, total, L.w.dl, L.difl, L.difr, L.w.zw, L.zhat, st, true, maxK);
@@ -2299,7 +2318,7 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     CK(cudaMemsetAsync(status, 0, sizeof(int), st));
     LevelView lv{vs, vK, vr, vo, 1};
     float *guess = nullptr;
-    if (c.cfg.predictor == 2) {
+    if (c.cfg.predictor >= 2) {  // (3 runs the plain pre-solve here)
       guess = buf<float>(c, "x_guess", k);
       launch_secular_guess32(lv, k, k, k, dlamda, z, buf<float>(c, "x_d32", k),
                              buf<float>(c, "x_z32", k), guess, st);
@@ -2312,7 +2331,7 @@ int hss_secular_dev(int k, const double *dlamda, const double *z, double rho, do
     unsigned long long *cnt = (unsigned long long *)buf<char>(c, "x_counts", 24);
     CK(cudaMemsetAsync(cnt, 0, 24, st));
     launch_secular(lv, k, k, dlamda, z, lam, difl, difr, iters, status, cnt, guess, st, false,
-                   c.cfg.predictor == 2);
+                   c.cfg.predictor >= 2);
     unsigned long long hc[2];
     CK(cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
     int hs = 0;

@@ -43,15 +43,20 @@ void set_secular_terms(int t);
 void set_secular_threads(int t);
 // sq: singular-value mode (poles d_i^2, outputs sigma and DIFL/DIFR = sigma - d)
 // guess: per root start (see root_init), full: its bracket is the whole interval
+// gref: exact starts of the refined pre-solve (launch_secular_guess32 with gref)
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st,
-                    bool sq = false, bool full = false);
+                    bool sq = false, bool full = false, const float4 *gref = nullptr);
 // starts for the FP64 iteration from an FP32 pre-solve (npos: positions of the
 // level arrays, d32 / z32 their FP32 copies; sq: singular-value mode)
+// gref (with d32lo, z2h, z2l, npos floats each): the refined pre-solve, one
+// float-float evaluation and step after the FP32 iteration
 void launch_secular_guess32(const LevelView &lv, int total, int maxk, int npos,
                             const double *dl, const double *zw, float *d32, float *z32,
-                            float *guess, cudaStream_t st, bool sq = false);
+                            float *guess, cudaStream_t st, bool sq = false,
+                            float *d32lo = nullptr, float *z2h = nullptr, float *z2l = nullptr,
+                            float4 *gref = nullptr);
 // maxk: the largest K of the launch (lanes per root as the secular kernel;
 // the default keeps a full warp per root)
 void launch_lowner(const LevelView &lv, int total, const double *dl, const double *difl,

@@ -150,7 +150,8 @@ __device__ __forceinline__ double gap(const RootState &r, int i) { return pdiff(
 // full: the start's side is not known (an FP32 pre-solve) -- the bracket is
 // the whole interval; otherwise (a learned start after the FP64 midpoint
 // evaluation) the half interval.
-__device__ __forceinline__ void root_init(RootState &r, float guess, double zsq, bool full) {
+__device__ __forceinline__ void root_init(RootState &r, float guess, double zsq, bool full,
+                                          float4 ref = make_float4(0.f, 0.f, 0.f, 0.f)) {
   r.rhoinv = 1.0 / r.rho;
   r.iters = 0;
   r.status = HSS_OK;
@@ -174,6 +175,13 @@ __device__ __forceinline__ void root_init(RootState &r, float guess, double zsq,
       const double half = full ? r.delta : 0.5 * r.delta;
       if (guess > 0.0f) { r.oi = r.j; r.tau = (double)guess * r.delta; r.lo = 0.0; r.hi = half; }
       else { r.oi = r.j + 1; r.tau = (double)guess * r.delta; r.lo = -half; r.hi = 0.0; }
+      if (ref.x != 0.0f) {
+        // a refined pre-solve: the start tau = x + y exactly (origin as the
+        // guess's sign), and z its last step / tau, which counts as the
+        // previous step of the quadratic-convergence acceptance
+        r.tau = (double)ref.x + (double)ref.y;
+        r.prel = (double)ref.z;
+      }
       r.phase = 1;
       r.learned = true;
       r.iters = full ? 0 : 1;  // the learned start spent one evaluation on the midpoint
@@ -330,7 +338,7 @@ __global__ void __launch_bounds__(256)
 k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
           double *__restrict__ lam, double *__restrict__ difl, double *__restrict__ difr,
           int *__restrict__ iters, int *__restrict__ status, unsigned long long *__restrict__ itsum,
-          const float *__restrict__ guess, bool full) {
+          const float *__restrict__ guess, bool full, const float4 *__restrict__ gref) {
   const int lane = threadIdx.x & 31, gl = lane & (L - 1);
   const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
   const int total = __ldg(lv.rootoff + lv.P);
@@ -350,11 +358,16 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
   st.z = zw + s;
   st.sq = SQ;
   st.oi = 0;
+  // sum z^2 bounds the last root only (the root beyond every pole): the other
+  // roots skip that pass over the poles (the group sum still runs on every lane)
   double zsq = 0.0;
-  for (int i = gl; i < st.K; i += L) zsq += __ldg(st.z + i) * __ldg(st.z + i);
+  const int kz = (valid && st.j == st.K - 1) ? st.K : 0;
+  for (int i = gl; i < kz; i += L) zsq += __ldg(st.z + i) * __ldg(st.z + i);
   zsq = group_sum<L>(zsq);
   const bool trivial = !valid || st.K == 1;
-  if (!trivial) root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq, full);
+  if (!trivial)
+    root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq, full,
+              gref ? gref[s + st.j] : make_float4(0.f, 0.f, 0.f, 0.f));
   else st.phase = 2;
   while (__any_sync(HSS_FULL, st.phase != 2)) {
     const SecSums sm = sec_eval<L, SQ>(st.d, st.z, st.phase == 2 ? 0 : st.K, st.oi, st.tau, st.jl,
@@ -582,6 +595,55 @@ __global__ void k_to_f32(int n, const double *__restrict__ a, const double *__re
   if (i < n) { fa[i] = (float)a[i]; fb[i] = (float)b[i]; }
 }
 
+// Float-float arithmetic (value = hi + lo, |lo| <= ulp(hi) / 2; Dekker 1971,
+// Knuth's TwoSum): about 48 significant bits from FP32 instructions.
+__device__ __forceinline__ void ff_two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, float &sh,
+                                       float &sl) {
+  float s1, e1;
+  ff_two_sum(ah, bh, s1, e1);
+  e1 += al + bl;
+  sh = s1 + e1;
+  sl = e1 - (sh - s1);
+}
+__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float &ph,
+                                       float &pl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);  // the exact error of the product
+  e += ah * bl + al * bh;
+  ph = p + e;
+  pl = e - (ph - p);
+}
+__device__ __forceinline__ void ff_div(float ah, float al, float bh, float bl, float &qh,
+                                       float &ql) {
+  const float q1 = ah / bh;
+  const float p = q1 * bh, pe = fmaf(q1, bh, -p);
+  const float r = (((ah - p) - pe) + al) - q1 * bl;  // a - q1 b
+  const float q2 = r / bh;
+  qh = q1 + q2;
+  ql = q2 - (qh - q1);
+}
+
+// FP32 copies plus the float-float splits the refined pre-solve needs: poles
+// d = dh + dl, and z^2 = z2h + z2l (z^2 formed in FP64), once per level.
+__global__ void k_to_ff(int n, const double *__restrict__ a, const double *__restrict__ b,
+                        float *__restrict__ fa, float *__restrict__ fb, float *__restrict__ fal,
+                        float *__restrict__ z2h, float *__restrict__ z2l) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = a[i], z = b[i], z2 = z * z;
+  const float dh = (float)d, zh2 = (float)z2;
+  fa[i] = dh;
+  fal[i] = (float)(d - (double)dh);
+  fb[i] = (float)z;
+  z2h[i] = zh2;
+  z2l[i] = (float)(z2 - (double)zh2);
+}
+
 template <int L>
 __device__ __forceinline__ float group_sum_f(float v) {
 #pragma unroll
@@ -600,22 +662,32 @@ __device__ __forceinline__ float group_sum_f(float v) {
 // guess[s + j] = signed distance to the nearer pole / interval, 0 for none.
 // SQ: singular-value mode, the variable tau = sigma^2 - d_o^2 and the pole gaps
 // (d_i - d_o)(d_i + d_o), as the FP64 kernel's squared mode.
-template <int L, bool SQ>
+// FF (refined pre-solve): after the FP32 iteration has converged, one more
+// evaluation of the secular function in float-float arithmetic (every term, from
+// the splits d32 + d32lo and z2h + z2l: no FP64 instruction per term) and one
+// step from it; gref[s + j] = (tau, step, |step / tau|, 0), 0 when not refined.
+// The FP64 iteration then starts at tau + step exactly, usually accepting after
+// one evaluation (its first step shows quadratic convergence).
+template <int L, bool SQ, bool FF>
 __global__ void __launch_bounds__(256)
 k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__restrict__ d32,
-                  const float *__restrict__ z32, float *__restrict__ guess) {
+                  const float *__restrict__ z32, float *__restrict__ guess,
+                  const float *__restrict__ d32lo, const float *__restrict__ z2h,
+                  const float *__restrict__ z2l, float4 *__restrict__ gref) {
   constexpr int GR = 4;
   const int lane = threadIdx.x & 31, gl = lane & (L - 1);
   const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
   const int total = __ldg(lv.rootoff + lv.P);
   int s = 0, j = 0, K = 0;
   float rhoinv = 1.f;
+  double rhoinv_d = 1.0;
   if (r < total) {
     const int m = find_merge(lv.rootoff, lv.P, r);
     s = __ldg(lv.s + m);
     j = r - __ldg(lv.rootoff + m);
     K = __ldg(lv.K + m);
-    rhoinv = (float)(1.0 / __ldg(lv.rho + m));
+    rhoinv_d = 1.0 / __ldg(lv.rho + m);
+    rhoinv = (float)rhoinv_d;
   }
   const bool active = r < total && K >= 2 && j < K - 1;
   const int n0 = j - GR + 1;  // first near pole
@@ -640,7 +712,7 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
   float do32 = active ? __ldg(d32 + s + j) : 0.f;
   const int Ka = active ? K : 0;
   float tau = 0.5f * delta, lo = 0.f, hi = delta;
-  bool done = !active;
+  bool done = !active, conv32 = false;
 #pragma unroll 1
   for (int it = 0; it < 10; ++it) {
     float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
@@ -687,6 +759,7 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
         if (fabsf(eta) <= 4e-6f * fabsf(tau)) {  // FP32 resolution reached
           tau += eta;
           done = true;
+          conv32 = true;
         } else {
           float tn = tau + eta;
           if (!(tn > lo && tn < hi)) tn = 0.5f * (lo + hi);
@@ -703,15 +776,67 @@ k_secular_guess32(LevelView lv, const double *__restrict__ dl, const float *__re
       }
     }
   }
+  float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (FF) {
+    const bool go = active && conv32 && tau != 0.f;
+    float wh = 0.f, wl = 0.f, a1 = 0.f, b1 = 0.f;
+    if (go) {
+      const float dho = __ldg(d32 + s + o), dlo = __ldg(d32lo + s + o);
+      for (int i = gl; i < Ka; i += L) {
+        const float dhi = __ldg(d32 + s + i), dli = __ldg(d32lo + s + i);
+        float gh, glo;  // d_i - d_o (squared mode: (d_i - d_o)(d_i + d_o))
+        ff_add(dhi, dli, -dho, -dlo, gh, glo);
+        if (SQ) {
+          float ph, pl;
+          ff_add(dhi, dli, dho, dlo, ph, pl);
+          ff_mul(gh, glo, ph, pl, gh, glo);
+        }
+        float eh, el;  // gap - tau
+        ff_add(gh, glo, -tau, 0.f, eh, el);
+        float th, tl;
+        ff_div(__ldg(z2h + s + i), __ldg(z2l + s + i), eh, el, th, tl);
+        ff_add(wh, wl, th, tl, wh, wl);
+        const float t = __fdividef(__ldg(z32 + s + i), eh);
+        if (i <= j) a1 = fmaf(t, t, a1); else b1 = fmaf(t, t, b1);
+      }
+    }
+#pragma unroll
+    for (int q = L / 2; q > 0; q >>= 1) {  // group sums (every lane ends with the same bits)
+      const float oh = __shfl_xor_sync(HSS_FULL, wh, q), ol = __shfl_xor_sync(HSS_FULL, wl, q);
+      ff_add(wh, wl, oh, ol, wh, wl);
+    }
+    a1 = group_sum_f<L>(a1);
+    b1 = group_sum_f<L>(b1);
+    if (go) {
+      const float rh = (float)rhoinv_d, rl = (float)(rhoinv_d - (double)rh);
+      ff_add(wh, wl, rh, rl, wh, wl);
+      const float w = wh, dw = a1 + b1;
+      const float gL = gn[GR - 1] - tau, gR = gn[GR] - tau;  // the poles j, j + 1
+      const float A = (gL + gR) * w - gL * gR * dw;
+      const float B = gL * gR * w;
+      const float C = w - gL * a1 - gR * b1;
+      float eta;
+      if (C == 0.f) {
+        eta = A != 0.f ? B / A : -w / dw;
+      } else {
+        const float disc = fmaxf(A * A - 4.f * B * C, 0.f);
+        eta = A <= 0.f ? (A - sqrtf(disc)) / (2.f * C) : (2.f * B) / (A + sqrtf(disc));
+      }
+      if (!(w * eta < 0.f)) eta = -w / dw;
+      // only a correction well inside FP32's resolution is used
+      if (fabsf(eta) <= 1e-4f * fabsf(tau)) rf = make_float4(tau, eta, fabsf(eta / tau), 0.f);
+    }
+  }
   if (r < total && gl == 0) {
     float g = 0.f;
     if (active) {
       g = tau / delta;  // from the origin pole: positive from d_j, negative from d_{j+1}
-      if (g > 0.5f) g -= 1.f;
-      else if (g < -0.5f) g += 1.f;
-      if (!(fabsf(g) > 0.f && fabsf(g) <= 0.5f)) g = 0.f;
+      if (g > 0.5f) { g -= 1.f; rf.x = 0.f; }
+      else if (g < -0.5f) { g += 1.f; rf.x = 0.f; }
+      if (!(fabsf(g) > 0.f && fabsf(g) <= 0.5f)) { g = 0.f; rf.x = 0.f; }
     }
     guess[s + j] = g;
+    if (FF) gref[s + j] = rf;
   }
 }
 
@@ -808,7 +933,7 @@ static int lanes_per_root(int total, int maxk) {
 void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, const double *zw,
                     double *lam, double *difl, double *difr, int *iters, int *status,
                     unsigned long long *itsum, const float *guess, cudaStream_t st, bool sq,
-                    bool full) {
+                    bool full, const float4 *gref) {
   if (total <= 0) return;
   const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
@@ -817,7 +942,7 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
 #define SEC_CASE(LL, SQ)                                                                     \
   case LL * 2 + SQ:                                                                          \
     k_secular<LL, SQ><<<grid, tb, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,     \
-                                            itsum, guess, full);                             \
+                                            itsum, guess, full, gref);                       \
     break;
     SEC_CASE(1, 0) SEC_CASE(2, 0) SEC_CASE(4, 0) SEC_CASE(8, 0) SEC_CASE(16, 0) SEC_CASE(32, 0)
     SEC_CASE(1, 1) SEC_CASE(2, 1) SEC_CASE(4, 1) SEC_CASE(8, 1) SEC_CASE(16, 1) SEC_CASE(32, 1)
@@ -826,19 +951,26 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
 }
 void launch_secular_guess32(const LevelView &lv, int total, int maxk, int npos,
                             const double *dl, const double *zw, float *d32, float *z32,
-                            float *guess, cudaStream_t st, bool sq) {
+                            float *guess, cudaStream_t st, bool sq, float *d32lo, float *z2h,
+                            float *z2l, float4 *gref) {
   if (total <= 0) return;
-  k_to_f32<<<(npos + 255) / 256, 256, 0, st>>>(npos, dl, zw, d32, z32);
+  const bool ff = gref != nullptr;
+  if (ff) k_to_ff<<<(npos + 255) / 256, 256, 0, st>>>(npos, dl, zw, d32, z32, d32lo, z2h, z2l);
+  else k_to_f32<<<(npos + 255) / 256, 256, 0, st>>>(npos, dl, zw, d32, z32);
   const int L = lanes_per_root(total, maxk);
   const int tb = root_block((long long)total * L);
   const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
-  switch (L) {
-#define G32_CASE(LL)                                                                   \
-  case LL:                                                                             \
-    if (sq) k_secular_guess32<LL, true><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess);  \
-    else k_secular_guess32<LL, false><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess);    \
+  const int mode = (sq ? 1 : 0) + (ff ? 2 : 0);
+  switch (L * 4 + mode) {
+#define G32_CASE(LL, SQ, FF)                                                         \
+  case LL * 4 + (SQ ? 1 : 0) + (FF ? 2 : 0):                                         \
+    k_secular_guess32<LL, SQ, FF><<<grid, tb, 0, st>>>(lv, dl, d32, z32, guess, d32lo, \
+                                                       z2h, z2l, gref);                \
     break;
-    G32_CASE(1) G32_CASE(2) G32_CASE(4) G32_CASE(8) G32_CASE(16) G32_CASE(32)
+#define G32_ALL(LL) G32_CASE(LL, false, false) G32_CASE(LL, true, false) \
+                    G32_CASE(LL, false, true) G32_CASE(LL, true, true)
+    G32_ALL(1) G32_ALL(2) G32_ALL(4) G32_ALL(8) G32_ALL(16) G32_ALL(32)
+#undef G32_ALL
 #undef G32_CASE
   }
 }

@@ -28,7 +28,8 @@ typedef struct hss_config {
   double tol;     /* HSS low-rank tolerance (reference: 1e-17, CauchyHssEig.f90:2523) */
   int smlsiz;     /* DC leaf size, ILAENV(9) = 25 (mdlaed0.f90:188)                  */
   int precision;  /* 0: FP64 products; 1: split-BF16 tensor-core products           */
-  int predictor;  /* secular start: 0 standard; 1 learned (MLP); 2 FP32 pre-solve  */
+  int predictor;  /* secular start: 0 standard; 1 learned (MLP); 2 FP32 pre-solve;
+                    3 FP32 pre-solve refined by one float-float step */
   int batched;    /* 1: one launch per stage per DC level; 0: launches per merge    */
   int profile;    /* 1: time every stage with CUDA events (hss_stats.stage_ms)      */
   int sec_terms;  /* secular solver: at most this many lanes' worth of work per  */

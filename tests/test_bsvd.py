@@ -171,12 +171,13 @@ def test_vs_lapack(n, sb, kind):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pred", [2, 3])
 @pytest.mark.parametrize("n,sb,kind", [(3000, 5, "uniform"), (1600, 6, "zero_rows"),
                                        (2000, 4, "toeplitz"), (1500, 32, "normal")])
-def test_fp32_presolved_starts(n, sb, kind):
-    # predictor = 2: every append's secular equation starts from the FP32
-    # pre-solve in squared mode
-    old = hp.set_config(predictor=2, precision=1)
+def test_fp32_presolved_starts(n, sb, kind, pred):
+    # predictor = 2 / 3: every append's secular equation starts from the FP32
+    # pre-solve in squared mode (3: refined by one float-float step)
+    old = hp.set_config(predictor=pred, precision=1)
     try:
         ab = _band(n, sb, 3 * n + sb, kind)
         s, U, VT = hp.svd_banded(ab, sb, 25)

@@ -85,20 +85,23 @@ def test_stats_counts():
 # FP64 evaluations per root
 
 
+@pytest.mark.parametrize("pred", [2, 3])
 @pytest.mark.parametrize("n", [3, 26, 257, 2048, 6000])
-def test_fp32_start_random(n):
+def test_fp32_start_random(n, pred):
     d, e = rand_tridiag(n, seed=n + 7)
-    _check(d, e, predictor=2)
+    _check(d, e, predictor=pred)
 
 
+@pytest.mark.parametrize("pred", [2, 3])
 @pytest.mark.parametrize("n", [500, 2048])
-def test_fp32_start_toeplitz(n):
+def test_fp32_start_toeplitz(n, pred):
     d, e = toeplitz_tridiag(n)
-    w, _ = _check(d, e, predictor=2)
+    w, _ = _check(d, e, predictor=pred)
     assert np.max(np.abs(w - toeplitz_eigs(n))) <= 4 * EV_TOL
 
 
-def test_fp32_start_clustered_spectrum():
+@pytest.mark.parametrize("pred", [2, 3])
+def test_fp32_start_clustered_spectrum(pred):
     # eigenvalues in tight clusters (poles closer than FP32 resolves):
     # diagonal 1 + 1e-9 noise with weak coupling, plus a few outliers
     n = 3000
@@ -106,10 +109,10 @@ def test_fp32_start_clustered_spectrum():
     d = 1.0 + 1e-9 * rng.standard_normal(n)
     d[::500] += 3.0
     e = 1e-4 * rng.uniform(0.5, 1.0, n - 1)
-    _check(d, e, predictor=2)
+    _check(d, e, predictor=pred)
 
 
-@pytest.mark.parametrize("pred", [0, 2])
+@pytest.mark.parametrize("pred", [0, 2, 3])
 @pytest.mark.parametrize("smlsiz", [12, 25])
 def test_glued_wilkinson(pred, smlsiz):
     # Wilkinson-type blocks (pairs of nearly equal eigenvalues) glued weakly:
@@ -135,6 +138,22 @@ def test_fp32_start_saves_evaluations():
             hp.restore_config(old)
         evals[pred] = st["secular_iters"] / max(st["secular_roots"], 1)
     assert evals[2] < evals[0] - 0.5, evals
+
+
+def test_refined_start_saves_evaluations():
+    # predictor = 3: the FP32 pre-solve refined by one float-float step; most
+    # roots are accepted after one FP64 evaluation
+    d, e = rand_tridiag(4096, seed=6)
+    evals = {}
+    for pred in (2, 3):
+        old = hp.set_config(predictor=pred)
+        try:
+            hp.eigh_tridiagonal(d, e)
+            st = hp.get_stats()
+        finally:
+            hp.restore_config(old)
+        evals[pred] = st["secular_iters"] / max(st["secular_roots"], 1)
+    assert evals[3] < evals[2] - 0.4, evals
 
 
 # The host entry (MDSTEDC) zero-fills Z on host threads during the solve and

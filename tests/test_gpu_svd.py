@@ -62,11 +62,13 @@ def test_svd_lower_signed_graded_and_restatement():
     assert np.max(np.abs(sr - s2)) <= SV_TOL * 2.0
 
 
+@pytest.mark.parametrize("pred", [2, 3])
 @pytest.mark.parametrize("n", [100, 1000, 4000])
-def test_svd_fp32_presolved_starts(n):
-    # predictor = 2: the secular iteration starts from an FP32 pre-solve in
-    # squared mode; random, graded and deflating cases
-    old = hp.set_config(predictor=2, precision=1)
+def test_svd_fp32_presolved_starts(n, pred):
+    # predictor = 2 / 3: the secular iteration starts from an FP32 pre-solve in
+    # squared mode (3: refined by one float-float step); random, graded and
+    # deflating cases
+    old = hp.set_config(predictor=pred, precision=1)
     try:
         d, e = _bidiag(n, seed=100 + n)
         _check(d, e, *hp.svd_bidiagonal(d, e))
