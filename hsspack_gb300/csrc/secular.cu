@@ -328,6 +328,111 @@ __device__ __forceinline__ void root_step(RootState &r, const SecSums &s) {
   r.prel = bisect ? -1.0 : rel;
 }
 
+// Outputs of one finished root (lam, DIFL, DIFR, iteration counts, status);
+// K = 1 is solved here in closed form.
+template <bool SQ>
+__device__ __forceinline__ void secular_out(RootState &st, int s, double *__restrict__ lam,
+                                            double *__restrict__ difl, double *__restrict__ difr,
+                                            int *__restrict__ iters, int *__restrict__ status,
+                                            unsigned long long *__restrict__ itsum) {
+  double lm, dfl, dfr;
+  if (st.K == 1) {
+    const double zz = __ldg(st.z) * __ldg(st.z);
+    const double d0 = __ldg(st.d);
+    if (SQ) {  // sigma^2 = d_0^2 + rho z^2
+      lm = d0 + st.rho * zz / (d0 + sqrt(d0 * d0 + st.rho * zz));
+      dfl = lm - d0;
+    } else {
+      lm = d0 + st.rho * zz; dfl = st.rho * zz;
+    }
+    dfr = 0.0;
+    st.iters = 0; st.status = HSS_OK; st.fell_back = false;
+  } else if (SQ) {
+    // sigma = sqrt(d_o^2 + tau) = d_o + tau / (d_o + sigma); DIFL / DIFR as
+    // sigma - d from (sigma^2 - d^2) / (sigma + d)
+    const double o = pole(st, st.oi);
+    lm = o + st.tau / (o + sqrt(o * o + st.tau));
+    dfl = (st.tau - gap(st, st.j)) / (lm + pole(st, st.j));
+    dfr = st.last ? 0.0 : (st.tau - gap(st, st.j + 1)) / (lm + pole(st, st.j + 1));
+  } else {
+    lm = pole(st, st.oi) + st.tau;
+    dfl = -(gap(st, st.j) - st.tau);
+    dfr = st.last ? 0.0 : -(gap(st, st.j + 1) - st.tau);
+  }
+  lam[s + st.j] = lm;
+  difl[s + st.j] = dfl;
+  difr[s + st.j] = dfr;
+  if (iters) iters[s + st.j] = st.iters;
+  if (itsum) {
+    atomicAdd(itsum, (unsigned long long)st.iters);
+    if (st.fell_back) atomicAdd(itsum + 1, 1ull);
+    atomicAdd(itsum + 2, (unsigned long long)st.iters * (unsigned long long)st.K);  // pole terms
+  }
+  if (st.status) atomicMax(status, st.status);
+}
+
+// One lane per root with a sequence of roots per lane (wide levels): lane l of
+// the T launched takes roots l, l + T, l + 2T, ..., starting the next as soon as
+// its current one has converged.  A warp then costs the largest per-lane sum
+// of evaluations instead of, root after root, the largest evaluation count of
+// its 32 roots (the FP64 pipe is charged per warp instruction, idle lanes
+// included).
+template <bool SQ>
+__device__ __forceinline__ void secular_lanes(const LevelView &lv, const double *__restrict__ dl,
+                                              const double *__restrict__ zw,
+                                              double *__restrict__ lam, double *__restrict__ difl,
+                                              double *__restrict__ difr, int *__restrict__ iters,
+                                              int *__restrict__ status,
+                                              unsigned long long *__restrict__ itsum,
+                                              const float *__restrict__ guess, bool full,
+                                              const float4 *__restrict__ gref) {
+  const int total = __ldg(lv.rootoff + lv.P);
+  const long long T = (long long)gridDim.x * blockDim.x;
+  long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  RootState st;
+  st.K = 0; st.j = 0; st.jl = 0; st.oi = 0; st.tau = 0.0; st.phase = 2;
+  st.d = dl; st.z = zw;
+  int s = 0;
+  bool act = false;
+  auto next = [&]() {  // the lane's next root that needs the iteration
+    act = false;
+    for (; r < total; r += T) {
+      const int m = find_merge(lv.rootoff, lv.P, (int)r);
+      s = __ldg(lv.s + m);
+      st.j = (int)r - __ldg(lv.rootoff + m);
+      st.K = __ldg(lv.K + m);
+      st.rho = __ldg(lv.rho + m);
+      st.d = dl + s;
+      st.z = zw + s;
+      st.sq = SQ;
+      st.oi = 0;
+      if (st.K == 1) {
+        secular_out<SQ>(st, s, lam, difl, difr, iters, status, itsum);
+        continue;
+      }
+      double zsq = 0.0;  // the last root's bound only
+      if (st.j == st.K - 1)
+        for (int i = 0; i < st.K; ++i) zsq += __ldg(st.z + i) * __ldg(st.z + i);
+      root_init(st, guess ? __ldg(guess + s + st.j) : 2.0f, zsq, full,
+                gref ? gref[s + st.j] : make_float4(0.f, 0.f, 0.f, 0.f));
+      act = true;
+      return;
+    }
+  };
+  next();
+  while (__any_sync(HSS_FULL, act)) {
+    const SecSums sm = sec_eval<1, SQ>(st.d, st.z, act ? st.K : 0, st.oi, st.tau, st.jl, 0);
+    if (act) {
+      root_step(st, sm);
+      if (st.phase == 2) {
+        secular_out<SQ>(st, s, lam, difl, difr, iters, status, itsum);
+        r += T;
+        next();
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------- kernels -----
 // Batched over the merges of one DC level (find_merge: hss_common.cuh).
 
@@ -338,7 +443,12 @@ __global__ void __launch_bounds__(256)
 k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict__ zw,
           double *__restrict__ lam, double *__restrict__ difl, double *__restrict__ difr,
           int *__restrict__ iters, int *__restrict__ status, unsigned long long *__restrict__ itsum,
-          const float *__restrict__ guess, bool full, const float4 *__restrict__ gref) {
+          const float *__restrict__ guess, bool full, const float4 *__restrict__ gref,
+          bool lanes) {
+  if (L == 1 && lanes) {
+    secular_lanes<SQ>(lv, dl, zw, lam, difl, difr, iters, status, itsum, guess, full, gref);
+    return;
+  }
   const int lane = threadIdx.x & 31, gl = lane & (L - 1);
   const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) / L);
   const int total = __ldg(lv.rootoff + lv.P);
@@ -382,42 +492,7 @@ k_secular(LevelView lv, const double *__restrict__ dl, const double *__restrict_
       st.phase = __shfl_sync(HSS_FULL, st.phase, lead);
     }
   }
-  if (valid && gl == 0) {
-    double lm, dfl, dfr;
-    if (st.K == 1) {
-      const double zz = __ldg(st.z) * __ldg(st.z);
-      const double d0 = __ldg(st.d);
-      if (SQ) {  // sigma^2 = d_0^2 + rho z^2
-        lm = d0 + st.rho * zz / (d0 + sqrt(d0 * d0 + st.rho * zz));
-        dfl = lm - d0;
-      } else {
-        lm = d0 + st.rho * zz; dfl = st.rho * zz;
-      }
-      dfr = 0.0;
-      st.iters = 0; st.status = HSS_OK;
-    } else if (SQ) {
-      // sigma = sqrt(d_o^2 + tau) = d_o + tau / (d_o + sigma); DIFL / DIFR as
-      // sigma - d from (sigma^2 - d^2) / (sigma + d)
-      const double o = pole(st, st.oi);
-      lm = o + st.tau / (o + sqrt(o * o + st.tau));
-      dfl = (st.tau - gap(st, st.j)) / (lm + pole(st, st.j));
-      dfr = st.last ? 0.0 : (st.tau - gap(st, st.j + 1)) / (lm + pole(st, st.j + 1));
-    } else {
-      lm = pole(st, st.oi) + st.tau;
-      dfl = -(gap(st, st.j) - st.tau);
-      dfr = st.last ? 0.0 : -(gap(st, st.j + 1) - st.tau);
-    }
-    lam[s + st.j] = lm;
-    difl[s + st.j] = dfl;
-    difr[s + st.j] = dfr;
-    if (iters) iters[s + st.j] = st.iters;
-    if (itsum) {
-      atomicAdd(itsum, (unsigned long long)st.iters);
-      if (st.fell_back) atomicAdd(itsum + 1, 1ull);
-      atomicAdd(itsum + 2, (unsigned long long)st.iters * (unsigned long long)st.K);  // pole terms
-    }
-    if (st.status) atomicMax(status, st.status);
-  }
+  if (valid && gl == 0) secular_out<SQ>(st, s, lam, difl, difr, iters, status, itsum);
 }
 
 // Loewner: z_hat_i^2 = prod_j (d_i - lam_j) / prod_{j != i} (d_i - d_j)
@@ -936,13 +1011,18 @@ void launch_secular(const LevelView &lv, int total, int maxk, const double *dl, 
                     bool full, const float4 *gref) {
   if (total <= 0) return;
   const int L = lanes_per_root(total, maxk);
-  const int tb = root_block((long long)total * L);
-  const unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
+  int tb = root_block((long long)total * L);
+  unsigned grid = (unsigned)(((long long)total * L + tb - 1) / tb);
+  // wide levels at one root per lane: 152 x 512 lanes, each with a sequence of
+  // roots (secular_lanes), once there are at least two roots per lane
+  constexpr long long SEC_LANES = 152LL * 512;
+  const bool lanes = L == 1 && total >= 2 * SEC_LANES;
+  if (lanes) { tb = 256; grid = (unsigned)(SEC_LANES / tb); }
   switch (L * 2 + (sq ? 1 : 0)) {
 #define SEC_CASE(LL, SQ)                                                                     \
   case LL * 2 + SQ:                                                                          \
     k_secular<LL, SQ><<<grid, tb, 0, st>>>(lv, dl, zw, lam, difl, difr, iters, status,     \
-                                            itsum, guess, full, gref);                       \
+                                            itsum, guess, full, gref, lanes);                \
     break;
     SEC_CASE(1, 0) SEC_CASE(2, 0) SEC_CASE(4, 0) SEC_CASE(8, 0) SEC_CASE(16, 0) SEC_CASE(32, 0)
     SEC_CASE(1, 1) SEC_CASE(2, 1) SEC_CASE(4, 1) SEC_CASE(8, 1) SEC_CASE(16, 1) SEC_CASE(32, 1)
