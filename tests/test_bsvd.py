@@ -187,6 +187,17 @@ def test_fp32_presolved_starts(n, sb, kind, pred):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n,sb", [(1, 1), (2, 1), (2, 2), (7, 3), (7, 7), (64, 32), (65, 32),
+                                  (66, 32), (97, 31)])
+def test_small_and_edge_shapes(n, sb):
+    # a single element, sb = n, the widest band as one leaf (n = 64, sb = 32:
+    # 64 x 64) and the smallest trees with a one-row leaf (n = 65, 66)
+    ab = _band(n, sb, 100 * n + sb, "normal")
+    s, U, VT = hp.svd_banded(ab, sb, 25)
+    _check(ref.band_to_dense(ab, sb), s, U, VT)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("sb", [2, 7])
 def test_vs_oracle(sb):
     n = 700
